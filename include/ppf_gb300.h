@@ -1,0 +1,238 @@
+/*
+ * ppf_gb300.h -- C ABI of libppf_gb300.so, the GB300 (sm_103a) explicit
+ * time-stepping engine behind pyphasefield's Simulation/engine plugin API.
+ *
+ * Conventions
+ *  - Every function returns int32_t: PPF_OK (0) or a negative PPF_ERR_* code;
+ *    ppf_last_error() gives a one-line message for the calling thread.
+ *  - The library owns no field buffers. Callers pass device pointers, the
+ *    grid geometry and a cudaStream_t (passed as void*, NULL = legacy default
+ *    stream). Work is stream-ordered; no function synchronises the device.
+ *  - Grids are C order, interior cells only (no ghost layers): axis ndim-1 is
+ *    contiguous, rows are `pitch` elements apart, planes pitch*shape[ndim-2]
+ *    elements apart. A 1-D grid is passed as 2-D with shape[0] = 1 and a
+ *    periodic axis 0. Ghost cells of the reference's Field (pyphasefield
+ *    field.py:6-20) are never stored: the boundary rule of
+ *    Simulation.apply_boundary_conditions (simulation.py:560-618) is applied
+ *    while each tile is loaded.
+ *  - Input and output buffers of a step must not overlap.
+ *  - *_f32 entry points store and compute in float, *_f64 in double. The
+ *    physical parameters are always passed as double and folded on the host.
+ */
+#ifndef PPF_GB300_H
+#define PPF_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PPF_ABI_VERSION 1
+
+#define PPF_OK 0
+#define PPF_ERR_INVALID (-1)     /* bad argument (shape, pitch, pointer, depth) */
+#define PPF_ERR_CUDA (-2)        /* a CUDA runtime call failed */
+#define PPF_ERR_UNSUPPORTED (-3) /* valid request this build does not implement */
+#define PPF_ERR_TIMEOUT (-4)     /* a bounded device-side wait gave up */
+#define PPF_ERR_NONFINITE (-5)   /* a field produced NaN/Inf (status flag) */
+
+/* Boundary condition types, per axis. Spelled as in the reference
+ * (Simulation.init_boundary_conditions, simulation.py:109-123). */
+#define PPF_BC_PERIODIC 0
+#define PPF_BC_NEUMANN 1
+#define PPF_BC_DIRCHLET 2
+
+/* Status-flag bits written by kernels into a caller-provided int32. */
+#define PPF_STATUS_NONFINITE 1
+#define PPF_STATUS_TIMEOUT 2
+#define PPF_STATUS_RANGE 4
+
+typedef struct PpfGrid {
+  int32_t ndim;     /* 2 or 3 */
+  int32_t reserved; /* must be 0 */
+  int64_t shape[3]; /* interior cells per axis, C order (first ndim used) */
+  int64_t pitch;    /* elements between rows; >= shape[ndim-1], multiple of 4 */
+} PpfGrid;
+
+/* Ghost-cell rule per axis (C order, same as PpfGrid.shape). value holds,
+ * per field (up to 2), axis and side (0 = low, 1 = high), the Neumann
+ * gradient (ghost = edge -/+ dx*value, simulation.py:583-584) or the
+ * Dirichlet ghost value (simulation.py:591-592). The reference keeps these
+ * in Simulation._boundary_conditions_array; this ABI takes one constant per
+ * face. Corner ghosts compose axis by axis in the reference's fill order. */
+typedef struct PpfBoundary {
+  int32_t type[3];
+  int32_t reserved;
+  double value[2][3][2];
+} PpfBoundary;
+
+/* Diffusion explicit step: c += dt*D*lap(c)
+ * (engine_ExplicitDiffusion, Engines/Diffusion.py:198-208). */
+typedef struct PpfDiffusionParams {
+  double dx, dt, D;
+} PpfDiffusionParams;
+
+/* Allen-Cahn ("CahnAllen") explicit step:
+ * phi += dt*M*(eps^2 lap(phi) - 16 W (4phi^3 - 6phi^2 + 2phi))
+ * (engine_CahnAllenExplicit, Engines/CahnAllen.py:128-135). */
+typedef struct PpfAllenCahnParams {
+  double dx, dt, M, epsilon, W;
+} PpfAllenCahnParams;
+
+/* Cahn-Hilliard explicit step:
+ * mu = -eps^2 lap(c) + (4c^3 - 6c^2 + 2c);  c += dt*M*lap(mu)
+ * (engine_CahnHilliardExplicit, Engines/CahnHilliard.py:134-146; the
+ * reference omits dt, this ABI applies it), written in flux form: every
+ * face flux dt*M*(mu_nbr - mu)/dx^2 is added to one cell and subtracted
+ * from the other.
+ * centered = 1: the buffers hold u = c - 1/2 (the double well's midpoint)
+ *   and mu's bulk term is evaluated as 4u^3 - u (the same polynomial).
+ * quantum > 0 (a power of two, float path only): every face flux is rounded
+ *   to a multiple of quantum. With field values that are multiples of
+ *   quantum below 2^24*quantum in magnitude, every float add is exact and
+ *   the field's sum is conserved exactly (centered storage with
+ *   quantum = 2^-24 covers c in (-1/2, 3/2)). 0 disables rounding. */
+typedef struct PpfCahnHilliardParams {
+  double dx, dt, M, epsilon, quantum;
+  int32_t centered;
+  int32_t reserved;
+} PpfCahnHilliardParams;
+
+/* Warren-Boettinger 1995 Ni-Cu isothermal solidification
+ * (engine_Warren1995, Engines/Warren1995.py:50-92). Material constants are
+ * the Warren1995 engine's user_data keys (Warren1995.py:138-169); ebar, W_A,
+ * W_B, M_A, M_B are the derived values of just_before_simulating
+ * (Warren1995.py:193-203). Noise uniform numbers come from Philox4x32-10
+ * keyed by (seed, step) with the cell index as counter. */
+typedef struct PpfWarren1995Params {
+  double dx, dt;
+  double T_mA, T_mB, L_A, L_B, D_L, D_S, v_m, R, y_e, T, alpha;
+  double ebar, W_A, W_B, M_A, M_B;
+} PpfWarren1995Params;
+
+/* Launch shape of one explicit-step call. NULL selects the defaults
+ * (depth 1, library-chosen tile). depth = time steps advanced per HBM pass
+ * (temporal blocking, 1..8, 2-D Diffusion/Allen-Cahn only); tile_x/tile_y =
+ * output tile per CTA (0 = default); pdl = 1 launches with programmatic
+ * dependent launch so back-to-back steps overlap their launch latency. */
+typedef struct PpfTiling {
+  int32_t depth;
+  int32_t tile_x;
+  int32_t tile_y;
+  int32_t pdl;
+} PpfTiling;
+
+/* ---- library ---------------------------------------------------------- */
+
+/* ABI version (PPF_ABI_VERSION) and build string. */
+int32_t ppf_version(int32_t* abi_version, char* buf, size_t len);
+/* Message of the last failed call on this thread (empty if none). */
+int32_t ppf_last_error(char* buf, size_t len);
+/* Device properties the host side uses for tiling: SM count, max shared
+ * memory per block (opt-in) and compute capability. */
+int32_t ppf_device_info(int32_t device, int32_t* sm_count, int32_t* smem_optin,
+                        int32_t* cc_major, int32_t* cc_minor);
+
+/* ---- explicit steps (one HBM pass) ------------------------------------ */
+
+/* Advance tiling->depth time steps in one pass. Replaces Simulation.simulation_loop() +
+ * apply_boundary_conditions() of the Diffusion engine
+ * (simulation.py:262-266, Engines/Diffusion.py:198-208). */
+int32_t ppf_diffusion_step_f32(const PpfDiffusionParams* p, const PpfGrid* g,
+                               const PpfBoundary* bc, const float* in,
+                               float* out, const PpfTiling* tiling,
+                               void* stream);
+int32_t ppf_diffusion_step_f64(const PpfDiffusionParams* p, const PpfGrid* g,
+                               const PpfBoundary* bc, const double* in,
+                               double* out, const PpfTiling* tiling,
+                               void* stream);
+
+/* Same contract for the Allen-Cahn engine (Engines/CahnAllen.py:128-135). */
+int32_t ppf_allen_cahn_step_f32(const PpfAllenCahnParams* p, const PpfGrid* g,
+                                const PpfBoundary* bc, const float* in,
+                                float* out, const PpfTiling* tiling,
+                               void* stream);
+int32_t ppf_allen_cahn_step_f64(const PpfAllenCahnParams* p, const PpfGrid* g,
+                                const PpfBoundary* bc, const double* in,
+                                double* out, const PpfTiling* tiling,
+                               void* stream);
+
+/* One Cahn-Hilliard step (Engines/CahnHilliard.py:134-146), radius-2
+ * stencil through an on-chip mu tile. mass_accum (nullable) receives
+ * += sum of the new field in double. status (nullable) gets
+ * PPF_STATUS_NONFINITE / PPF_STATUS_RANGE bits or'ed in. */
+int32_t ppf_cahn_hilliard_step_f32(const PpfCahnHilliardParams* p,
+                                   const PpfGrid* g, const PpfBoundary* bc,
+                                   const float* in, float* out,
+                                   double* mass_accum, int32_t* status,
+                                   const PpfTiling* tiling, void* stream);
+int32_t ppf_cahn_hilliard_step_f64(const PpfCahnHilliardParams* p,
+                                   const PpfGrid* g, const PpfBoundary* bc,
+                                   const double* in, double* out,
+                                   double* mass_accum, int32_t* status,
+                                   const PpfTiling* tiling, void* stream);
+
+/* One Warren1995 step of (phi, c) (Engines/Warren1995.py:50-92), 2-D only.
+ * The noise of a step is keyed by step + (*step_base if step_base is not
+ * NULL): a captured graph of several steps passes fixed offsets and a device
+ * counter advanced by ppf_counter_add_u64 after each replay. */
+int32_t ppf_warren1995_step_f32(const PpfWarren1995Params* p, const PpfGrid* g,
+                                const PpfBoundary* bc, const float* phi_in,
+                                const float* c_in, float* phi_out, float* c_out,
+                                uint64_t seed, uint64_t step,
+                                const uint64_t* step_base,
+                                const PpfTiling* tiling, void* stream);
+int32_t ppf_warren1995_step_f64(const PpfWarren1995Params* p, const PpfGrid* g,
+                                const PpfBoundary* bc, const double* phi_in,
+                                const double* c_in, double* phi_out,
+                                double* c_out, uint64_t seed, uint64_t step,
+                                const uint64_t* step_base,
+                                const PpfTiling* tiling, void* stream);
+
+/* ---- diagnostics (FP64 reductions) ------------------------------------ */
+
+/* Bytes of caller-provided device scratch the reductions below need. */
+int32_t ppf_reduce_scratch_bytes(const PpfGrid* g, size_t* bytes);
+/* out[0] = sum of the interior cells in double (deterministic order):
+ * the "mass" diagnostic. No counterpart in the reference (it has none). */
+int32_t ppf_reduce_sum_f32(const float* x, const PpfGrid* g, double* out,
+                           void* scratch, size_t scratch_bytes, void* stream);
+int32_t ppf_reduce_sum_f64(const double* x, const PpfGrid* g, double* out,
+                           void* scratch, size_t scratch_bytes, void* stream);
+/* out[0] = dx^d * sum over cells of [w f(x) + kappa/2 |grad x|^2],
+ * f(x) = x^2 (1-x)^2, forward differences with the boundary rule applied:
+ * the free energy whose variation gives the Allen-Cahn (w = 16 W,
+ * kappa = eps^2) and Cahn-Hilliard (w = 1, kappa = eps^2) updates. */
+int32_t ppf_free_energy_f32(const float* x, const PpfGrid* g,
+                            const PpfBoundary* bc, double dx, double w,
+                            double kappa, double* out, void* scratch,
+                            size_t scratch_bytes, void* stream);
+int32_t ppf_free_energy_f64(const double* x, const PpfGrid* g,
+                            const PpfBoundary* bc, double dx, double w,
+                            double kappa, double* out, void* scratch,
+                            size_t scratch_bytes, void* stream);
+/* Writes PPF_STATUS_NONFINITE into *status if any interior cell is not
+ * finite (the host checks it every window). */
+int32_t ppf_check_finite_f32(const float* x, const PpfGrid* g, int32_t* status,
+                             void* stream);
+
+/* *counter += inc on the device (stream-ordered; one thread). */
+int32_t ppf_counter_add_u64(uint64_t* counter, uint64_t inc, void* stream);
+
+/* ---- CUDA graphs ------------------------------------------------------ */
+
+/* Capture every launch issued on `stream` between begin and end into a
+ * graph (the per-step Python loop of Simulation.simulate, simulation.py:
+ * 262-271, replayed as one launch). */
+int32_t ppf_graph_begin(void* stream);
+int32_t ppf_graph_end(void* stream, void** graph_exec);
+int32_t ppf_graph_launch(void* graph_exec, void* stream);
+int32_t ppf_graph_destroy(void* graph_exec);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PPF_GB300_H */

@@ -1,0 +1,202 @@
+"""Runs pyphasefield's OWN numpy engine functions (TEST INFRASTRUCTURE ONLY).
+
+The reference package imports matplotlib, meshio and tinydb at module level
+(field.py:2, ppf_utils.py:1-6, simulation.py:3-9); none is needed by the
+explicit engines, so this module installs inert stand-ins in sys.modules,
+imports the reference from its checkout, and drives the module-level engine
+functions with a duck-typed simulation object:
+
+  * engine_ExplicitDiffusion (Engines/Diffusion.py:198-208) reads an
+    undefined global ``self`` (:206): it is injected as the duck sim.
+  * engine_CahnAllenExplicit / engine_CahnHilliardExplicit read an undefined
+    global ``user_data`` (CahnAllen.py:131-133, CahnHilliard.py:138-140):
+    injected.
+  * engine_Warren1995 reads sim.W_A etc. as attributes (Warren1995.py:59-84):
+    the duck sim carries them. Its np.random.random draw (:85) is replaced by
+    a caller-supplied array through a numpy proxy in the module's globals.
+  * The ghost fill between steps is oracle.restate.fill_ghosts (the
+    reference's apply_boundary_conditions with every axis filled).
+
+Available only where the reference checkout exists (PPF_REFERENCE_ROOT or the
+default below); callers skip otherwise. Nothing here is used at run time.
+"""
+from __future__ import annotations
+
+import os
+import sys
+import types
+from pathlib import Path
+
+import numpy as np
+
+from . import restate
+
+DEFAULT_ROOT = "/root/reference/pyphasefield"
+
+
+def reference_root() -> Path | None:
+    root = Path(os.environ.get("PPF_REFERENCE_ROOT", DEFAULT_ROOT))
+    return root if (root / "pyphasefield" / "Engines" / "Warren1995.py").exists() else None
+
+
+def available() -> bool:
+    return reference_root() is not None
+
+
+def _install_stubs() -> None:
+    def mod(name):
+        m = sys.modules.get(name)
+        if m is None:
+            m = types.ModuleType(name)
+            sys.modules[name] = m
+        return m
+
+    mpl = mod("matplotlib")
+    colors = mod("matplotlib.colors")
+    cm = mod("matplotlib.cm")
+    plt = mod("matplotlib.pyplot")
+
+    class _Cmap:
+        @staticmethod
+        def from_list(*a, **k):
+            return None
+
+    colors.LinearSegmentedColormap = _Cmap
+    colors.PowerNorm = lambda *a, **k: None
+    mpl.colors, mpl.cm, mpl.pyplot = colors, cm, plt
+    mod("meshio")
+    mod("tinydb").where = lambda *a, **k: None
+
+
+_MODS = None
+
+
+def modules() -> dict:
+    """Import the reference (with stand-ins) and return its engine modules."""
+    global _MODS
+    if _MODS is None:
+        root = reference_root()
+        if root is None:
+            raise RuntimeError("reference checkout not found")
+        _install_stubs()
+        if str(root) not in sys.path:
+            sys.path.insert(0, str(root))
+        import io
+        import contextlib
+        with contextlib.redirect_stdout(io.StringIO()):  # numba-less engines print and skip
+            import pyphasefield  # noqa: F401
+            import pyphasefield.Engines  # noqa: F401
+        _MODS = {k: sys.modules[f"pyphasefield.Engines.{k}"]
+                 for k in ("Diffusion", "CahnAllen", "CahnHilliard", "Warren1995")}
+        _MODS["field"] = sys.modules["pyphasefield.field"]
+    return _MODS
+
+
+class DuckSim:
+    """The attributes the reference engine functions read from a Simulation."""
+
+    def __init__(self, arrays, dx, dt, user_data=None, **attrs):
+        Field = modules()["field"].Field
+        self.dx = dx
+        self.dt = dt
+        self.user_data = dict(user_data or {})
+        self.fields = []
+        for a in arrays:
+            f = Field(data=np.asarray(a, dtype=np.float64), simulation=self, name="f")
+            self.fields.append(f)
+        for k, v in attrs.items():
+            setattr(self, k, v)
+
+    def get_time_step_length(self):
+        return self.dt
+
+    def get_cell_spacing(self):
+        return self.dx
+
+    def get_dimensions(self):
+        return list(self.fields[0].get_cells().shape)
+
+
+class _NumpyWithNoise:
+    """numpy stand-in whose random.random(shape) returns a fixed array."""
+
+    def __init__(self, noise):
+        self.random = types.SimpleNamespace(random=lambda shape: noise)
+
+    def __getattr__(self, name):
+        return getattr(np, name)
+
+
+def run_single(model: str, c0, steps: int, boundary_conditions, dx: float,
+               dt: float, values=None, **params) -> np.ndarray:
+    """Drive the reference's one-field engine function for `steps` steps.
+    For Cahn-Hilliard the reference has no dt: M*dt is passed as its M."""
+    m = modules()
+    sim = DuckSim([c0], dx, dt)
+    bcs = restate.bc_list(boundary_conditions, np.ndim(c0))
+    restate.fill_ghosts([f.data for f in sim.fields], bcs, dx, values)
+    for _ in range(steps):
+        if model == "diffusion":
+            mod = m["Diffusion"]
+            sim.user_data = {"D": params["D"]}
+            mod.self = sim
+            mod.engine_ExplicitDiffusion(sim)
+        elif model == "allen_cahn":
+            mod = m["CahnAllen"]
+            mod.user_data = {k: params[k] for k in ("M", "W", "epsilon")}
+            mod.engine_CahnAllenExplicit(sim)
+        elif model == "cahn_hilliard":
+            mod = m["CahnHilliard"]
+            mod.user_data = {"M": params["M"] * dt, "W": params.get("W", 1.0),
+                             "epsilon": params["epsilon"]}
+            mod.engine_CahnHilliardExplicit(sim)
+        else:
+            raise ValueError(model)
+        restate.fill_ghosts([f.data for f in sim.fields], bcs, dx, values)
+    return sim.fields[0].get_cells().copy()
+
+
+def run_cahn_hilliard_extended(c0, steps: int, boundary_conditions, dx: float,
+                               dt: float, M: float, epsilon: float) -> np.ndarray:
+    """Cahn-Hilliard through the reference's function with its mu-ghost
+    defect kept away from the answer: the field is extended by 2*steps cells
+    per side (periodic wrap or no-flux mirror, the exact continuation of
+    those boundary rules), the reference advances the extended field, and the
+    centre is cropped. The result is the reference's arithmetic on every
+    cell that matters."""
+    c0 = np.asarray(c0, dtype=np.float64)
+    h = 2 * steps + 2
+    bcs = restate.bc_list(boundary_conditions, c0.ndim)
+    ext = c0
+    for ax, b in enumerate(bcs):
+        mode = "wrap" if b == restate.PERIODIC else "symmetric"
+        widths = [(0, 0)] * c0.ndim
+        widths[ax] = (h, h)
+        ext = np.pad(ext, widths, mode=mode)
+    out = run_single("cahn_hilliard", ext, steps, bcs, dx, dt, M=M, epsilon=epsilon)
+    return out[(slice(h, -h),) * c0.ndim].copy()
+
+
+def run_warren(phi0, c0, steps: int, boundary_conditions, dx: float, params: dict,
+               noise=None, values=None):
+    """Drive engine_Warren1995 for `steps` steps. noise: list of interior
+    U[0,1) arrays, one per step (None: no noise term, alpha forced to 0)."""
+    m = modules()
+    mod = m["Warren1995"]
+    p = restate.warren_derived(params, dx)
+    attrs = {k: p[k] for k in ("W_A", "W_B", "L_A", "L_B", "T", "T_mA", "T_mB", "D_S",
+                               "D_L", "v_m", "R", "y_e", "M_A", "M_B", "ebar")}
+    attrs["alpha"] = p["alpha"] if noise is not None else 0.0
+    sim = DuckSim([phi0, c0], dx, p["dt"], **attrs)
+    bcs = restate.bc_list(boundary_conditions, 2)
+    restate.fill_ghosts([f.data for f in sim.fields], bcs, dx, values)
+    saved = mod.np
+    try:
+        for s in range(steps):
+            u = restate.pad(noise[s]) if noise is not None else np.zeros(sim.fields[0].data.shape)
+            mod.np = _NumpyWithNoise(u)
+            mod.engine_Warren1995(sim)
+            restate.fill_ghosts([f.data for f in sim.fields], bcs, dx, values)
+    finally:
+        mod.np = saved
+    return sim.fields[0].get_cells().copy(), sim.fields[1].get_cells().copy()

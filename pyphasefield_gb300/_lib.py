@@ -1,0 +1,146 @@
+"""ctypes binding of libppf_gb300.so (declared in include/ppf_gb300.h).
+
+The library is the only compute path: if it cannot be loaded, every engine
+call raises. Nothing here falls back to a CPU implementation.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import threading
+from pathlib import Path
+
+LIB_PATH = Path(__file__).resolve().parent / "libppf_gb300.so"
+
+PPF_OK = 0
+PPF_ERR_INVALID = -1
+PPF_ERR_CUDA = -2
+PPF_ERR_UNSUPPORTED = -3
+PPF_ERR_TIMEOUT = -4
+PPF_ERR_NONFINITE = -5
+
+PPF_BC_PERIODIC = 0
+PPF_BC_NEUMANN = 1
+PPF_BC_DIRCHLET = 2
+
+PPF_STATUS_NONFINITE = 1
+PPF_STATUS_TIMEOUT = 2
+PPF_STATUS_RANGE = 4
+
+
+class PpfError(RuntimeError):
+    """A libppf_gb300 call returned a negative status."""
+
+    def __init__(self, code: int, func: str, msg: str):
+        super().__init__(f"{func} failed with status {code}: {msg}")
+        self.code = code
+
+
+class PpfGrid(C.Structure):
+    _fields_ = [("ndim", C.c_int32), ("reserved", C.c_int32),
+                ("shape", C.c_int64 * 3), ("pitch", C.c_int64)]
+
+
+class PpfBoundary(C.Structure):
+    _fields_ = [("type", C.c_int32 * 3), ("reserved", C.c_int32),
+                ("value", ((C.c_double * 2) * 3) * 2)]
+
+
+class PpfTiling(C.Structure):
+    _fields_ = [("depth", C.c_int32), ("tile_x", C.c_int32),
+                ("tile_y", C.c_int32), ("pdl", C.c_int32)]
+
+
+class PpfDiffusionParams(C.Structure):
+    _fields_ = [(n, C.c_double) for n in ("dx", "dt", "D")]
+
+
+class PpfAllenCahnParams(C.Structure):
+    _fields_ = [(n, C.c_double) for n in ("dx", "dt", "M", "epsilon", "W")]
+
+
+class PpfCahnHilliardParams(C.Structure):
+    _fields_ = [(n, C.c_double) for n in ("dx", "dt", "M", "epsilon", "quantum")] + [
+        ("centered", C.c_int32), ("reserved", C.c_int32)]
+
+
+WARREN_PARAM_NAMES = ("dx", "dt", "T_mA", "T_mB", "L_A", "L_B", "D_L", "D_S", "v_m",
+                      "R", "y_e", "T", "alpha", "ebar", "W_A", "W_B", "M_A", "M_B")
+
+
+class PpfWarren1995Params(C.Structure):
+    _fields_ = [(n, C.c_double) for n in WARREN_PARAM_NAMES]
+
+
+P = C.c_void_p
+I32 = C.c_int32
+U64 = C.c_uint64
+SZ = C.c_size_t
+PG, PB, PT = C.POINTER(PpfGrid), C.POINTER(PpfBoundary), C.POINTER(PpfTiling)
+
+# name -> argtypes; every function returns int32 status.
+SIGNATURES: dict[str, list] = {
+    "ppf_version": [C.POINTER(I32), C.c_char_p, SZ],
+    "ppf_last_error": [C.c_char_p, SZ],
+    "ppf_device_info": [I32, C.POINTER(I32), C.POINTER(I32), C.POINTER(I32), C.POINTER(I32)],
+    "ppf_diffusion_step_f32": [C.POINTER(PpfDiffusionParams), PG, PB, P, P, PT, P],
+    "ppf_diffusion_step_f64": [C.POINTER(PpfDiffusionParams), PG, PB, P, P, PT, P],
+    "ppf_allen_cahn_step_f32": [C.POINTER(PpfAllenCahnParams), PG, PB, P, P, PT, P],
+    "ppf_allen_cahn_step_f64": [C.POINTER(PpfAllenCahnParams), PG, PB, P, P, PT, P],
+    "ppf_cahn_hilliard_step_f32": [C.POINTER(PpfCahnHilliardParams), PG, PB, P, P, P, P, PT, P],
+    "ppf_cahn_hilliard_step_f64": [C.POINTER(PpfCahnHilliardParams), PG, PB, P, P, P, P, PT, P],
+    "ppf_warren1995_step_f32": [C.POINTER(PpfWarren1995Params), PG, PB, P, P, P, P, U64, U64, P, PT, P],
+    "ppf_warren1995_step_f64": [C.POINTER(PpfWarren1995Params), PG, PB, P, P, P, P, U64, U64, P, PT, P],
+    "ppf_reduce_scratch_bytes": [PG, C.POINTER(SZ)],
+    "ppf_reduce_sum_f32": [P, PG, P, P, SZ, P],
+    "ppf_reduce_sum_f64": [P, PG, P, P, SZ, P],
+    "ppf_free_energy_f32": [P, PG, PB, C.c_double, C.c_double, C.c_double, P, P, SZ, P],
+    "ppf_free_energy_f64": [P, PG, PB, C.c_double, C.c_double, C.c_double, P, P, SZ, P],
+    "ppf_check_finite_f32": [P, PG, P, P],
+    "ppf_counter_add_u64": [P, U64, P],
+    "ppf_graph_begin": [P],
+    "ppf_graph_end": [P, C.POINTER(P)],
+    "ppf_graph_launch": [P, P],
+    "ppf_graph_destroy": [P],
+}
+
+_lib = None
+_lock = threading.Lock()
+
+
+def load(path: str | Path | None = None):
+    """Load the shared library once (raises OSError if it is missing)."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            p = Path(path) if path else LIB_PATH
+            if not p.exists():
+                raise OSError(
+                    f"{p} not found: build it with `python -m pyphasefield_gb300.build` "
+                    "(the CUDA library is the only compute path)")
+            lib = C.CDLL(str(p))
+            for name, argtypes in SIGNATURES.items():
+                fn = getattr(lib, name)
+                fn.argtypes = argtypes
+                fn.restype = C.c_int32
+            _lib = lib
+    return _lib
+
+
+def last_error() -> str:
+    buf = C.create_string_buffer(512)
+    load().ppf_last_error(buf, len(buf))
+    return buf.value.decode(errors="replace")
+
+
+def call(name: str, *args) -> None:
+    """Call a library function and raise PpfError on a negative status."""
+    rc = getattr(load(), name)(*args)
+    if rc != PPF_OK:
+        raise PpfError(rc, name, last_error())
+
+
+def version() -> tuple[int, str]:
+    abi = I32()
+    buf = C.create_string_buffer(128)
+    call("ppf_version", C.byref(abi), buf, len(buf))
+    return abi.value, buf.value.decode()

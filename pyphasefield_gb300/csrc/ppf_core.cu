@@ -1,0 +1,181 @@
+// Library plumbing: error strings, argument validation shared by all
+// kernels, device queries and the CUDA-graph capture helpers.
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <cmath>
+#include <string>
+
+#include "ppf_common.cuh"
+
+namespace ppf {
+
+static thread_local std::string g_last_error;
+
+int32_t fail(int32_t code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+  return code;
+}
+
+void clear_error() { g_last_error.clear(); }
+
+int32_t make_geo(const PpfGrid* g, int want_ndim_min, int want_ndim_max,
+                 Geo* out) {
+  if (!g) return fail(PPF_ERR_INVALID, "grid is NULL");
+  if (g->reserved != 0) return fail(PPF_ERR_INVALID, "grid.reserved must be 0");
+  if (g->ndim < want_ndim_min || g->ndim > want_ndim_max)
+    return fail(PPF_ERR_INVALID, "grid.ndim=%d not in [%d, %d]", g->ndim,
+                want_ndim_min, want_ndim_max);
+  Geo r{};
+  r.ndim = g->ndim;
+  for (int a = 0; a < g->ndim; ++a) {
+    if (g->shape[a] < 1 || g->shape[a] > (int64_t)(1 << 30))
+      return fail(PPF_ERR_INVALID, "grid.shape[%d]=%lld out of range", a,
+                  (long long)g->shape[a]);
+    r.n[a] = (int)g->shape[a];
+  }
+  for (int a = g->ndim; a < 3; ++a) r.n[a] = 1;
+  const int64_t nx = g->shape[g->ndim - 1];
+  if (g->pitch < nx || (g->pitch % 4) != 0)
+    return fail(PPF_ERR_INVALID,
+                "grid.pitch=%lld must be >= %lld and a multiple of 4",
+                (long long)g->pitch, (long long)nx);
+  r.pitch = g->pitch;
+  r.plane = g->ndim == 3 ? g->pitch * g->shape[1] : 0;
+  *out = r;
+  return PPF_OK;
+}
+
+template <typename T>
+int32_t make_bc(const PpfBoundary* b, const Geo& geo, double dx, int nfields,
+                int max_depth, Bc<T>* out) {
+  if (!b) return fail(PPF_ERR_INVALID, "boundary is NULL");
+  Bc<T> r{};
+  for (int a = 0; a < 3; ++a) {
+    const int t = a < geo.ndim ? b->type[a] : PPF_BC_PERIODIC;
+    if (t != PPF_BC_PERIODIC && t != PPF_BC_NEUMANN && t != PPF_BC_DIRCHLET)
+      return fail(PPF_ERR_INVALID, "boundary.type[%d]=%d unknown", a, t);
+    r.type[a] = t;
+    for (int f = 0; f < 2; ++f)
+      for (int s = 0; s < 2; ++s) {
+        const double v = b->value[f][a][s];
+        if (!std::isfinite(v))
+          return fail(PPF_ERR_INVALID, "boundary value not finite");
+        double sh = 0.0;
+        if (t == PPF_BC_NEUMANN) {
+          sh = (s == 0 ? -dx : dx) * v;
+          if (v != 0.0 && f < nfields && max_depth > 1)
+            return fail(PPF_ERR_UNSUPPORTED,
+                        "non-zero NEUMANN gradient needs halo depth 1 "
+                        "(requested %d)",
+                        max_depth);
+        } else if (t == PPF_BC_DIRCHLET) {
+          sh = v;
+        }
+        r.shift[f][a][s] = (T)sh;
+      }
+  }
+  *out = r;
+  return PPF_OK;
+}
+
+template int32_t make_bc<float>(const PpfBoundary*, const Geo&, double, int,
+                                int, Bc<float>*);
+template int32_t make_bc<double>(const PpfBoundary*, const Geo&, double, int,
+                                 int, Bc<double>*);
+
+__global__ void counter_add_kernel(uint64_t* c, uint64_t inc) {
+  pdl_wait();
+  *c += inc;
+}
+
+}  // namespace ppf
+
+using namespace ppf;
+
+extern "C" {
+
+int32_t ppf_version(int32_t* abi_version, char* buf, size_t len) {
+  clear_error();
+  if (abi_version) *abi_version = PPF_ABI_VERSION;
+  if (buf && len) {
+    snprintf(buf, len, "ppf_gb300 abi=%d cuda=%d sm_103a", PPF_ABI_VERSION,
+             CUDART_VERSION);
+  }
+  return PPF_OK;
+}
+
+int32_t ppf_last_error(char* buf, size_t len) {
+  if (buf && len) {
+    strncpy(buf, g_last_error.c_str(), len - 1);
+    buf[len - 1] = 0;
+  }
+  return PPF_OK;
+}
+
+int32_t ppf_device_info(int32_t device, int32_t* sm_count, int32_t* smem_optin,
+                        int32_t* cc_major, int32_t* cc_minor) {
+  clear_error();
+  int v = 0;
+  PPF_TRY_CUDA(cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, device));
+  if (sm_count) *sm_count = v;
+  PPF_TRY_CUDA(cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, device));
+  if (smem_optin) *smem_optin = v;
+  PPF_TRY_CUDA(cudaDeviceGetAttribute(&v, cudaDevAttrComputeCapabilityMajor, device));
+  if (cc_major) *cc_major = v;
+  PPF_TRY_CUDA(cudaDeviceGetAttribute(&v, cudaDevAttrComputeCapabilityMinor, device));
+  if (cc_minor) *cc_minor = v;
+  return PPF_OK;
+}
+
+int32_t ppf_counter_add_u64(uint64_t* counter, uint64_t inc, void* stream) {
+  clear_error();
+  if (!counter) return fail(PPF_ERR_INVALID, "counter is NULL");
+  counter_add_kernel<<<1, 1, 0, (cudaStream_t)stream>>>(counter, inc);
+  PPF_TRY_CUDA(cudaGetLastError());
+  return PPF_OK;
+}
+
+int32_t ppf_graph_begin(void* stream) {
+  clear_error();
+  if (!stream)
+    return fail(PPF_ERR_INVALID, "graph capture needs a non-default stream");
+  PPF_TRY_CUDA(cudaStreamBeginCapture((cudaStream_t)stream,
+                                      cudaStreamCaptureModeThreadLocal));
+  return PPF_OK;
+}
+
+int32_t ppf_graph_end(void* stream, void** graph_exec) {
+  clear_error();
+  if (!graph_exec) return fail(PPF_ERR_INVALID, "graph_exec is NULL");
+  cudaGraph_t graph = nullptr;
+  PPF_TRY_CUDA(cudaStreamEndCapture((cudaStream_t)stream, &graph));
+  cudaGraphExec_t exec = nullptr;
+  cudaError_t e = cudaGraphInstantiate(&exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess)
+    return fail(PPF_ERR_CUDA, "cudaGraphInstantiate: %s", cudaGetErrorString(e));
+  *graph_exec = (void*)exec;
+  return PPF_OK;
+}
+
+int32_t ppf_graph_launch(void* graph_exec, void* stream) {
+  clear_error();
+  if (!graph_exec) return fail(PPF_ERR_INVALID, "graph_exec is NULL");
+  PPF_TRY_CUDA(cudaGraphLaunch((cudaGraphExec_t)graph_exec, (cudaStream_t)stream));
+  return PPF_OK;
+}
+
+int32_t ppf_graph_destroy(void* graph_exec) {
+  clear_error();
+  if (graph_exec) PPF_TRY_CUDA(cudaGraphExecDestroy((cudaGraphExec_t)graph_exec));
+  return PPF_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,7 @@
+"""GB300 engines, exported like the reference's Engines package
+(Engines/__init__.py:8-23 exports every class of every engine module)."""
+from .models import (AllenCahnGB300, CahnAllenGB300, CahnHilliardGB300, DiffusionGB300,
+                     Warren1995GB300, make_engines)
+
+__all__ = ["DiffusionGB300", "CahnAllenGB300", "AllenCahnGB300", "CahnHilliardGB300",
+           "Warren1995GB300", "make_engines"]

@@ -1,0 +1,260 @@
+"""GB300Engine: the device half of every engine in this package.
+
+Mixed into a Simulation subclass (this package's, or the reference's own
+pyphasefield.simulation.Simulation through make_engines), it replaces the
+reference's per-step loop (Simulation.simulate, simulation.py:245-271) and
+its numba device utilities (ppf_gpu_utils.send_fields_to_GPU /
+retrieve_fields_from_GPU / apply_boundary_conditions, ppf_gpu_utils.py:
+396-514):
+
+* fields live on the device as float32 (default) or float64, interior only,
+  in two ping-pong buffer sets; the boundary rule is fused into every
+  kernel's tile load, so apply_boundary_conditions is a no-op on device;
+* simulate(n) advances n steps in captured CUDA graphs of `graph_chunk`
+  launches (each launch with programmatic dependent launch), split at
+  autosave boundaries so autosave cadence and time_step_counter behave as in
+  the reference;
+* send_fields_to_GPU / retrieve_fields_from_GPU move the interiors between
+  Field.data (float64, ghosts refilled on the host) and the device.
+
+User-data keys added to the reference's: precision ("fp32" | "fp64"),
+temporal_depth (steps per HBM pass, 2-D Diffusion/Allen-Cahn), tile
+((tile_x, tile_y) or None), pdl (bool), use_graph (bool), graph_chunk (int).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+import torch
+
+from .. import _lib as L
+from ..device import DeviceGrid, boundary_struct, ptr, require_cuda, tiling_struct
+from ..simulation import fill_ghosts_host
+
+COMMON_DEFAULTS = dict(precision="fp32", temporal_depth=1, tile=None, pdl=True,
+                       use_graph=True, graph_chunk=64)
+
+
+class GB300Engine:
+    #: number of fields the engine advances together
+    NFIELDS = 1
+
+    # ------------------------------------------------------------ subclass API
+    def _ppf_params(self):
+        """Return the ctypes params struct for the library call."""
+        raise NotImplementedError
+
+    def _ppf_step(self, src, dst, depth: int, step: int, step_base, stream_ptr):
+        """Launch one pass advancing `depth` steps from buffers src to dst."""
+        raise NotImplementedError
+
+    def _ppf_max_depth(self) -> int:
+        return 1
+
+    def _ppf_encode(self, j: int, x: np.ndarray) -> np.ndarray:
+        """Host value -> stored value of field j (identity by default)."""
+        return x
+
+    def _ppf_decode(self, j: int, x: np.ndarray) -> np.ndarray:
+        return x
+
+    def _ppf_prepare(self):
+        """Engine-specific set-up before the device copy (derived params)."""
+
+    def _ppf_segment_begin(self, nsteps: int, stream):
+        """Launches issued before a run of steps (captured in graphs)."""
+
+    def _ppf_segment_end(self, nsteps: int, stream):
+        """Host bookkeeping after a run of steps (not captured)."""
+
+    # ------------------------------------------------------------ helpers
+    def _ppf_defaults(self):
+        for k, v in COMMON_DEFAULTS.items():
+            self.user_data.setdefault(k, v)
+
+    @property
+    def _ppf_dtype(self):
+        p = self.user_data.get("precision", "fp32")
+        if p not in ("fp32", "fp64"):
+            raise ValueError(f"precision must be 'fp32' or 'fp64', got {p!r}")
+        return torch.float32 if p == "fp32" else torch.float64
+
+    def _ppf_ready(self) -> bool:
+        return getattr(self, "_ppf_bufs", None) is not None
+
+    def _ppf_setup(self):
+        dev = require_cuda()
+        if not self.fields or len(self.fields) != self.NFIELDS:
+            raise RuntimeError(f"{type(self).__name__} needs {self.NFIELDS} field(s); "
+                               "call initialize_fields_and_imported_data() first")
+        shape = self.fields[0].get_cells().shape
+        self._ppf_release_graphs()
+        self._ppf_grid = DeviceGrid(shape, self._ppf_dtype, dev)
+        self._ppf_bufs = [[self._ppf_grid.empty() for _ in range(self.NFIELDS)] for _ in range(2)]
+        self._ppf_cur = 0
+        self._ppf_stream = torch.cuda.Stream(dev)
+        self._ppf_bc = boundary_struct(self, self._ppf_grid, self.NFIELDS)
+        self._ppf_stepctr = torch.zeros(1, dtype=torch.int64, device=dev)
+        self._ppf_graphs = {}
+        self._ppf_staging = []
+        self._uses_gpu = True
+
+    def _ppf_release_graphs(self):
+        for g in getattr(self, "_ppf_graphs", {}).values():
+            L.call("ppf_graph_destroy", g)
+        self._ppf_graphs = {}
+
+    def __del__(self):
+        try:
+            self._ppf_release_graphs()
+        except Exception:
+            pass
+
+    def _ppf_tiling(self, depth: int):
+        ud = self.user_data
+        return tiling_struct(depth, ud.get("tile"), ud.get("pdl", True))
+
+    # ------------------------------------------------------------ lifecycle
+    def just_before_simulating(self):
+        t = self._temperature_type
+        if t not in (None, "ISOTHERMAL"):
+            raise NotImplementedError(f"temperature type {t!r} is not supported on the device "
+                                      "(isothermal engines only)")
+        self._ppf_prepare()
+        self._ppf_setup()
+        fill_ghosts_host(self)
+        self.send_fields_to_GPU()
+
+    def send_fields_to_GPU(self):
+        if not self._ppf_ready():
+            self._ppf_setup()
+        s = self._ppf_stream
+        self._ppf_staging = [
+            self._ppf_grid.upload(self._ppf_bufs[self._ppf_cur][j],
+                                  self._ppf_encode(j, f.get_cells()), s)
+            for j, f in enumerate(self.fields)]
+
+    def retrieve_fields_from_GPU(self):
+        if not self._ppf_ready():
+            return
+        s = self._ppf_stream
+        for j, f in enumerate(self.fields):
+            f.data[f._slice] = self._ppf_decode(
+                j, self._ppf_grid.download(self._ppf_bufs[self._ppf_cur][j], s))
+        self._ppf_staging = []
+        fill_ghosts_host(self)
+
+    def apply_boundary_conditions(self):
+        if self._ppf_ready():
+            return  # fused into every kernel's tile load
+        fill_ghosts_host(self)
+
+    def update_temperature_field(self, force_cpu=False):
+        if self._temperature_type not in (None, "ISOTHERMAL"):
+            raise NotImplementedError("non-isothermal temperature on the device")
+
+    def simulation_loop(self):
+        """Advance one step on the device (the reference's engine call)."""
+        if not self._ppf_ready():
+            self.just_before_simulating()
+        self._ppf_advance(1, self.time_step_counter)
+
+    def simulate(self, number_of_timesteps):
+        if not self._begun_simulation or not self._ppf_ready():
+            self._begun_simulation = True
+            self.just_before_simulating()
+        n = int(number_of_timesteps)
+        rate = self._autosave_rate if self._autosave_flag else None
+        while n > 0:
+            chunk = n
+            if rate:
+                chunk = min(chunk, rate - self.time_step_counter % rate)
+            # the reference increments the counter before each engine call;
+            # the step index keyed into the noise is the counter before it
+            self._ppf_advance(chunk, self.time_step_counter)
+            self.time_step_counter += chunk
+            n -= chunk
+            if rate and self.time_step_counter % rate == 0:
+                self.retrieve_fields_from_GPU()
+                self.save_simulation()
+
+    # ------------------------------------------------------------ stepping
+    def _ppf_passes(self, nsteps: int) -> list[int]:
+        k = max(1, min(int(self.user_data.get("temporal_depth", 1)), self._ppf_max_depth()))
+        passes = [k] * (nsteps // k)
+        if nsteps % k:
+            passes.append(nsteps % k)
+        return passes
+
+    def _ppf_launch_pass(self, depth, step, step_base):
+        src = self._ppf_bufs[self._ppf_cur]
+        dst = self._ppf_bufs[1 - self._ppf_cur]
+        self._ppf_step(src, dst, depth, step, step_base, C.c_void_p(self._ppf_stream.cuda_stream))
+        self._ppf_cur ^= 1
+
+    def _ppf_graph(self, depths: tuple[int, ...]):
+        key = (self._ppf_cur, depths)
+        g = self._ppf_graphs.get(key)
+        if g is not None:
+            return g
+        s = self._ppf_stream
+        sp = C.c_void_p(s.cuda_stream)
+        cur0 = self._ppf_cur
+        total = sum(depths)
+        L.call("ppf_graph_begin", sp)
+        exec_ = C.c_void_p()
+        try:
+            with torch.cuda.stream(s):
+                self._ppf_segment_begin(total, s)
+                off = 0
+                for d in depths:
+                    self._ppf_launch_pass(d, off, self._ppf_stepctr)
+                    off += d
+                L.call("ppf_counter_add_u64", ptr(self._ppf_stepctr), C.c_uint64(total), sp)
+        finally:
+            L.call("ppf_graph_end", sp, C.byref(exec_))
+            self._ppf_cur = cur0
+        self._ppf_graphs[key] = exec_
+        return exec_
+
+    def _ppf_advance(self, nsteps: int, step0: int):
+        """Advance nsteps from absolute step index step0 (noise key)."""
+        if nsteps <= 0:
+            return
+        passes = self._ppf_passes(nsteps)
+        ud = self.user_data
+        chunk = max(2, int(ud.get("graph_chunk", 64)) // 2 * 2)
+        s = self._ppf_stream
+        sp = C.c_void_p(s.cuda_stream)
+        i = 0
+        step = step0
+        if ud.get("use_graph", True) and len(passes) >= chunk:
+            depths = tuple(passes[:chunk])
+            if all(d == depths[0] for d in depths):
+                g = self._ppf_graph(depths)
+                span = sum(depths)
+                with torch.cuda.stream(s):
+                    self._ppf_stepctr.fill_(step)
+                while len(passes) - i >= chunk:
+                    L.call("ppf_graph_launch", g, sp)
+                    self._ppf_segment_end(span, s)
+                    i += chunk
+                    step += span
+        if i < len(passes):
+            rest = passes[i:]
+            with torch.cuda.stream(s):
+                self._ppf_segment_begin(sum(rest), s)
+                for d in rest:
+                    self._ppf_launch_pass(d, step, None)
+                    step += d
+            self._ppf_segment_end(sum(rest), s)
+
+    # ------------------------------------------------------------ access
+    def device_fields(self) -> list[torch.Tensor]:
+        """Views of the current device fields (interior only, stored values)."""
+        return [self._ppf_grid.view(t) for t in self._ppf_bufs[self._ppf_cur]]
+
+    def synchronize(self):
+        if self._ppf_ready():
+            self._ppf_stream.synchronize()

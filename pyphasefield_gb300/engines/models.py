@@ -1,0 +1,292 @@
+"""The four explicit engines, as drop-in Simulation subclasses.
+
+Each keeps the reference engine's user_data keys and defaults, its field
+names and its initial condition, and advances the fields with the CUDA
+library instead of numpy:
+
+  DiffusionGB300      <- Engines/Diffusion.py:635-733 (explicit solver)
+  CahnAllenGB300      <- Engines/CahnAllen.py:289-361 (explicit solver)
+  CahnHilliardGB300   <- Engines/CahnHilliard.py:347-421 (explicit solver)
+  Warren1995GB300     <- Engines/Warren1995.py:133-207
+
+``make_engines(Base)`` builds the same four classes on any Simulation base
+class, e.g. the reference's own pyphasefield.simulation.Simulation.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+import torch
+
+from .. import _lib as L
+from ..device import ptr
+from ..simulation import Simulation
+from .base import GB300Engine
+
+_F = {torch.float32: "f32", torch.float64: "f64"}
+
+
+def _explicit_only(ud, name):
+    solver = ud.get("solver", "explicit")
+    if solver != "explicit":
+        raise NotImplementedError(f"{name}: only the explicit solver runs on the GB300 "
+                                  f"path (got solver={solver!r})")
+
+
+class _DiffusionMixin(GB300Engine):
+    """c += dt*D*lap(c) (engine_ExplicitDiffusion, Engines/Diffusion.py:198-208)."""
+
+    NFIELDS = 1
+
+    def __init__(self, **kwargs):
+        super().__init__(**kwargs)
+        self.user_data.setdefault("D", 0.1)
+        self.user_data.setdefault("solver", "explicit")
+        self.user_data.setdefault("gmres", False)
+        self.user_data.setdefault("adi", False)
+        self._ppf_defaults()
+
+    def init_fields(self):
+        # unit box over the middle half of every axis (Diffusion.py:641-659)
+        dim = self.dimensions
+        c = np.zeros(dim)
+        c[tuple(slice(n // 4, 3 * n // 4) for n in dim)] = 1
+        self.add_field(c, "c")
+
+    def _ppf_prepare(self):
+        _explicit_only(self.user_data, "Diffusion")
+        if self.dt is None or self.dx is None:
+            raise ValueError("Diffusion needs dx and dt")
+
+    def _ppf_max_depth(self):
+        return 8 if len(self._ppf_grid.kshape) == 2 else 1
+
+    def _ppf_params(self):
+        return L.PpfDiffusionParams(float(self.dx), float(self.dt), float(self.user_data["D"]))
+
+    def _ppf_step(self, src, dst, depth, step, step_base, sp):
+        p = self._ppf_params()
+        L.call(f"ppf_diffusion_step_{_F[self._ppf_dtype]}", C.byref(p),
+               C.byref(self._ppf_grid.grid), C.byref(self._ppf_bc), ptr(src[0]), ptr(dst[0]),
+               C.byref(self._ppf_tiling(depth)), sp)
+
+
+class _CahnAllenMixin(GB300Engine):
+    """phi += dt*M*(eps^2 lap(phi) - 16 W g'(phi))
+    (engine_CahnAllenExplicit, Engines/CahnAllen.py:128-135)."""
+
+    NFIELDS = 1
+
+    def __init__(self, **kwargs):
+        super().__init__(**kwargs)
+        for k, v in dict(M=0.1, epsilon=1.0, W=1.0, solver="explicit", gmres=False,
+                         adi=False).items():
+            self.user_data.setdefault(k, v)
+        self._ppf_defaults()
+
+    def init_fields(self):
+        # 0.4995 + 0.001 U[0,1) (CahnAllen.py:311); seeded when user_data has "seed"
+        rng = np.random.default_rng(self.user_data["seed"]) if "seed" in self.user_data \
+            else np.random
+        self.add_field(0.001 * rng.random(self.dimensions) + 0.4995, "phi")
+
+    def _ppf_prepare(self):
+        _explicit_only(self.user_data, "CahnAllen")
+        if self.dt is None or self.dx is None:
+            raise ValueError("CahnAllen needs dx and dt")
+
+    def _ppf_max_depth(self):
+        return 8 if len(self._ppf_grid.kshape) == 2 else 1
+
+    def _ppf_params(self):
+        ud = self.user_data
+        return L.PpfAllenCahnParams(float(self.dx), float(self.dt), float(ud["M"]),
+                                    float(ud["epsilon"]), float(ud["W"]))
+
+    def _ppf_step(self, src, dst, depth, step, step_base, sp):
+        p = self._ppf_params()
+        L.call(f"ppf_allen_cahn_step_{_F[self._ppf_dtype]}", C.byref(p),
+               C.byref(self._ppf_grid.grid), C.byref(self._ppf_bc), ptr(src[0]), ptr(dst[0]),
+               C.byref(self._ppf_tiling(depth)), sp)
+
+
+CH_QUANTUM_F32 = 2.0 ** -24
+
+
+class _CahnHilliardMixin(GB300Engine):
+    """mu = -eps^2 lap(c) + 4c^3 - 6c^2 + 2c; c += dt*M*lap(mu)
+    (engine_CahnHilliardExplicit, Engines/CahnHilliard.py:134-146, with dt;
+    dt=None keeps the reference's dt-free update, i.e. dt = 1).
+
+    The device field is u = c - 1/2. In fp32 with conserve_mass (default)
+    every face flux is rounded to a multiple of 2^-24 and the initial field
+    is rounded to that grid on upload, so the float field's sum is conserved
+    exactly. With track_mass (default) the FP64 total mass sum(c) of every
+    step is kept in ``mass_history`` (fused into the step kernel)."""
+
+    NFIELDS = 1
+
+    def __init__(self, **kwargs):
+        super().__init__(**kwargs)
+        for k, v in dict(M=0.1, epsilon=1.0, W=1.0, solver="explicit", gmres=False,
+                         adi=False, conserve_mass=True, track_mass=True).items():
+            self.user_data.setdefault(k, v)
+        self._ppf_defaults()
+        self.mass_history: list[float] = []
+
+    def init_fields(self):
+        rng = np.random.default_rng(self.user_data["seed"]) if "seed" in self.user_data \
+            else np.random
+        self.add_field(0.001 * rng.random(self.dimensions) + 0.4995, "phi")
+
+    def _ppf_quantum(self):
+        if self._ppf_dtype == torch.float32 and self.user_data.get("conserve_mass", True):
+            return CH_QUANTUM_F32
+        return 0.0
+
+    def _ppf_prepare(self):
+        _explicit_only(self.user_data, "CahnHilliard")
+        if self.dx is None:
+            raise ValueError("CahnHilliard needs dx")
+        self._ch_k = 0
+        self._ch_mass_parts = []
+
+    def _ppf_setup(self):
+        super()._ppf_setup()
+        chunk = max(2, int(self.user_data.get("graph_chunk", 64)))
+        self._ch_mass = torch.zeros(max(chunk, 1024), dtype=torch.float64,
+                                    device=self._ppf_grid.device)
+        self._ch_status = torch.zeros(1, dtype=torch.int32, device=self._ppf_grid.device)
+
+    def _ppf_encode(self, j, x):
+        u = np.asarray(x, dtype=np.float64) - 0.5
+        q = self._ppf_quantum()
+        return np.rint(u / q) * q if q else u
+
+    def _ppf_decode(self, j, x):
+        return x + 0.5
+
+    def _ppf_params(self):
+        ud = self.user_data
+        dt = 1.0 if self.dt is None else float(self.dt)
+        p = L.PpfCahnHilliardParams(float(self.dx), dt, float(ud["M"]), float(ud["epsilon"]),
+                                    self._ppf_quantum())
+        p.centered = 1
+        p.reserved = 0
+        return p
+
+    def _ppf_segment_begin(self, nsteps, stream):
+        self._ch_k = 0
+        if self.user_data.get("track_mass", True):
+            if nsteps > self._ch_mass.numel():
+                self._ch_mass = torch.zeros(nsteps, dtype=torch.float64,
+                                            device=self._ppf_grid.device)
+            self._ch_mass[:nsteps].zero_()
+
+    def _ppf_segment_end(self, nsteps, stream):
+        if self.user_data.get("track_mass", True):
+            with torch.cuda.stream(stream):
+                self._ch_mass_parts.append(self._ch_mass[:nsteps].clone())
+
+    def _ppf_step(self, src, dst, depth, step, step_base, sp):
+        p = self._ppf_params()
+        mass = None
+        if self.user_data.get("track_mass", True):
+            mass = self._ch_mass[self._ch_k]
+        self._ch_k += 1
+        L.call(f"ppf_cahn_hilliard_step_{_F[self._ppf_dtype]}", C.byref(p),
+               C.byref(self._ppf_grid.grid), C.byref(self._ppf_bc), ptr(src[0]), ptr(dst[0]),
+               ptr(mass), ptr(self._ch_status), C.byref(self._ppf_tiling(depth)), sp)
+
+    def collect_mass_history(self) -> np.ndarray:
+        """FP64 total mass sum(c) after every step run so far (host sync)."""
+        if self._ch_mass_parts:
+            self.synchronize()
+            half = 0.5 * self._ppf_grid.cells
+            new = torch.cat(self._ch_mass_parts).cpu().numpy() + half
+            self.mass_history.extend(new.tolist())
+            self._ch_mass_parts = []
+        return np.asarray(self.mass_history)
+
+    def status_flags(self) -> int:
+        self.synchronize()
+        return int(self._ch_status.item())
+
+
+class _Warren1995Mixin(GB300Engine):
+    """Binary Ni-Cu isothermal solidification (Engines/Warren1995.py:50-207)."""
+
+    NFIELDS = 2
+    DEFAULTS = dict(T_mA=1728.0, T_mB=1358.0, L_A=2350000000.0, L_B=1728000000.0, s_A=0.37,
+                    s_B=0.29, D_L=1e-9, D_S=1e-13, B_A=0.0033, B_B=0.0039, v_m=0.00000742,
+                    R=8.314, y_e=0.04, T=1574.0, alpha=0.3, diamond_size=15)
+
+    def __init__(self, **kwargs):
+        super().__init__(**kwargs)
+        for k, v in self.DEFAULTS.items():
+            self.user_data.setdefault(k, v)
+        self.user_data.setdefault("seed", 0)
+        self._ppf_defaults()
+
+    def init_fields(self):
+        # phi = 1 (liquid) with a diamond of phi = 0 (solid) at the centre,
+        # c = 0.40831 (Warren1995.py:172-185)
+        dim = self.dimensions
+        phi = np.ones(dim)
+        ds = int(self.user_data["diamond_size"])
+        for i in range(ds):
+            phi[int(dim[0] / 2 - i):int(dim[0] / 2 + i),
+                int(dim[1] / 2 - (ds - i)):int(dim[1] / 2 + (ds - i))] = 0
+        self.add_field(phi, "phi")
+        self.add_field(np.full(dim, 0.40831), "c")
+
+    def _ppf_prepare(self):
+        # Warren1995.just_before_simulating (:193-203)
+        ud = self.user_data
+        if self.dx is None:
+            raise ValueError("Warren1995 needs dx (cell spacing in m)")
+        if len(self.dimensions) != 2:
+            raise ValueError("Warren1995 is a 2-D model")
+        dx = float(self.dx)
+        self.set_time_step_length(dx ** 2 / 5.0 / ud["D_L"])
+        ud["d"] = dx / 0.94
+        r2 = np.sqrt(2)
+        ud["ebar"] = np.sqrt(6 * r2 * ud["s_A"] * ud["d"] / ud["T_mA"])
+        ud["W_A"] = 3 * ud["s_A"] / (r2 * ud["T_mA"] * ud["d"])
+        ud["W_B"] = 3 * ud["s_B"] / (r2 * ud["T_mB"] * ud["d"])
+        ud["M_A"] = (ud["T_mA"] ** 2) * ud["B_A"] / (6 * r2 * ud["L_A"] * ud["d"])
+        ud["M_B"] = (ud["T_mB"] ** 2) * ud["B_B"] / (6 * r2 * ud["L_B"] * ud["d"])
+
+    def _ppf_params(self):
+        ud = self.user_data
+        vals = dict(ud, dx=float(self.dx), dt=float(self.dt))
+        return L.PpfWarren1995Params(*[float(vals[n]) for n in L.WARREN_PARAM_NAMES])
+
+    def _ppf_step(self, src, dst, depth, step, step_base, sp):
+        p = self._ppf_params()
+        L.call(f"ppf_warren1995_step_{_F[self._ppf_dtype]}", C.byref(p),
+               C.byref(self._ppf_grid.grid), C.byref(self._ppf_bc), ptr(src[0]), ptr(src[1]),
+               ptr(dst[0]), ptr(dst[1]), C.c_uint64(int(self.user_data["seed"])),
+               C.c_uint64(int(step)), ptr(step_base), C.byref(self._ppf_tiling(depth)), sp)
+
+
+def make_engines(base=Simulation) -> dict:
+    """Build the four engine classes on `base` (any class with the reference
+    Simulation interface). Returns {name: class}."""
+    out = {}
+    for name, mix in (("DiffusionGB300", _DiffusionMixin), ("CahnAllenGB300", _CahnAllenMixin),
+                      ("CahnHilliardGB300", _CahnHilliardMixin),
+                      ("Warren1995GB300", _Warren1995Mixin)):
+        out[name] = type(name, (mix, base), {"__module__": __name__,
+                                            "__doc__": mix.__doc__})
+    out["AllenCahnGB300"] = out["CahnAllenGB300"]
+    return out
+
+
+_engines = make_engines(Simulation)
+DiffusionGB300 = _engines["DiffusionGB300"]
+CahnAllenGB300 = _engines["CahnAllenGB300"]
+AllenCahnGB300 = CahnAllenGB300
+CahnHilliardGB300 = _engines["CahnHilliardGB300"]
+Warren1995GB300 = _engines["Warren1995GB300"]

@@ -1,0 +1,90 @@
+"""Generates tests/golden/*.npz from pyphasefield's OWN engine functions.
+
+Run in a checkout that has the reference (see oracle/refshim.py):
+    python tests/golden/make_golden.py
+Each fixture stores the initial interior field(s), the run parameters, and
+the interior after `steps` steps computed by the reference's numpy engine
+(engine_ExplicitDiffusion, engine_CahnAllenExplicit,
+engine_CahnHilliardExplicit, engine_Warren1995) driven by oracle.refshim.
+The inputs are seeded synthetic fields (numpy default_rng).
+"""
+from __future__ import annotations
+
+import json
+import sys
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+sys.path.insert(0, str(HERE.parents[1]))
+
+from oracle import refshim, restate  # noqa: E402
+from oracle.philox import noise_uniform  # noqa: E402
+
+
+def disk_seed(shape, center, r):
+    yy, xx = np.mgrid[0:shape[0], 0:shape[1]]
+    phi = np.ones(shape)
+    phi[(yy - center[0]) ** 2 + (xx - center[1]) ** 2 < r * r] = 0.0
+    return phi
+
+
+def save(name, meta, **arrays):
+    np.savez_compressed(HERE / f"{name}.npz", meta=json.dumps(meta), **arrays)
+    print(name, {k: v.shape for k, v in arrays.items()})
+
+
+def single(name, model, c0, steps, bc, dx, dt, values=None, **params):
+    if model == "cahn_hilliard":
+        out = refshim.run_cahn_hilliard_extended(c0, steps, bc, dx, dt, params["M"],
+                                                 params["epsilon"])
+    else:
+        out = refshim.run_single(model, c0, steps, bc, dx, dt, values=values, **params)
+    meta = dict(model=model, steps=steps, bc=bc, dx=dx, dt=dt, values=values, params=params)
+    save(name, meta, c0=c0, out=out)
+
+
+def main():
+    if not refshim.available():
+        raise SystemExit("reference checkout not found")
+    rng = np.random.default_rng(20240601)
+    single("diffusion_2d_periodic", "diffusion", 0.5 + 0.01 * rng.standard_normal((24, 20)),
+           10, "PERIODIC", 1.0, 0.2, D=1.0)
+    single("diffusion_1d_neumann", "diffusion", rng.random(40), 10, "NEUMANN", 1.0, 0.5, D=0.1)
+    single("diffusion_3d_mixed", "diffusion", rng.random((10, 9, 8)), 4,
+           ["NEUMANN", "DIRCHLET", "PERIODIC"], 0.5, 0.01,
+           values=[[[0.1, -0.2], [0.3, 0.4], [0.0, 0.0]]], D=1.0)
+    single("diffusion_2d_dirichlet", "diffusion", rng.random((13, 17)), 6,
+           ["DIRCHLET", "NEUMANN"], 1.0, 0.2, values=[[[0.25, 0.75], [0.0, 0.0]]], D=1.0)
+    single("allen_cahn_2d_neumann", "allen_cahn", rng.random((16, 18)), 8, "NEUMANN", 1.0, 0.1,
+           M=0.1, epsilon=1.0, W=1.0)
+    single("allen_cahn_3d_periodic", "allen_cahn", rng.random((8, 10, 12)), 4, "PERIODIC", 1.0,
+           0.05, M=0.1, epsilon=1.0, W=1.0)
+    single("cahn_hilliard_3d_periodic", "cahn_hilliard",
+           0.5 + rng.uniform(-0.05, 0.05, (10, 11, 12)), 3, "PERIODIC", 1.0, 0.01, M=1.0,
+           epsilon=1.0)
+    single("cahn_hilliard_2d_neumann", "cahn_hilliard",
+           0.5 + rng.uniform(-0.2, 0.2, (14, 16)), 3, "NEUMANN", 1.0, 0.01, M=1.0, epsilon=1.0)
+    single("cahn_hilliard_3d_mixed", "cahn_hilliard",
+           0.5 + rng.uniform(-0.2, 0.2, (9, 12, 10)), 2, ["PERIODIC", "NEUMANN", "PERIODIC"],
+           1.0, 0.01, M=1.0, epsilon=1.0)
+
+    dx = 4.6e-8
+    prm = dict(restate.WARREN_DEFAULTS)
+    for name, shape, center, r, bc, steps, alpha, seed in [
+        ("warren_2d_neumann", (32, 32), (16, 16), 5, "NEUMANN", 10, 0.0, 0),
+        ("warren_2d_periodic_noise", (24, 28), (12, 14), 4, "PERIODIC", 4, 0.3, 7),
+        ("warren_2d_mixed_edge", (20, 16), (2, 8), 5, ["NEUMANN", "PERIODIC"], 5, 0.0, 0),
+    ]:
+        phi0 = disk_seed(shape, center, r)
+        c0 = 0.40783 + rng.uniform(-1e-3, 1e-3, shape)
+        p = dict(prm, alpha=alpha)
+        noise = [noise_uniform(seed, s, shape) for s in range(steps)] if alpha else None
+        phi, c = refshim.run_warren(phi0, c0, steps, bc, dx, p, noise=noise)
+        meta = dict(model="warren1995", steps=steps, bc=bc, dx=dx, seed=seed, params=p)
+        save(name, meta, phi0=phi0, c0=c0, phi=phi, c=c)
+
+
+if __name__ == "__main__":
+    main()
