@@ -104,8 +104,9 @@ typedef struct PpfCahnHilliardParams {
  * (engine_Warren1995, Engines/Warren1995.py:50-92). Material constants are
  * the Warren1995 engine's user_data keys (Warren1995.py:138-169); ebar, W_A,
  * W_B, M_A, M_B are the derived values of just_before_simulating
- * (Warren1995.py:193-203). Noise uniform numbers come from Philox4x32-10
- * keyed by (seed, step) with the cell index as counter. */
+ * (Warren1995.py:193-203). The noise draw U[0,1) of cell (row, col) at a
+ * step is word col % 4 of Philox4x32-10 with counter (col / 4, row, step)
+ * and key seed, top 24 bits times 2^-24 (replacing np.random.random, :85). */
 typedef struct PpfWarren1995Params {
   double dx, dt;
   double T_mA, T_mB, L_A, L_B, D_L, D_S, v_m, R, y_e, T, alpha;
@@ -217,6 +218,15 @@ int32_t ppf_free_energy_f64(const double* x, const PpfGrid* g,
  * finite (the host checks it every window). */
 int32_t ppf_check_finite_f32(const float* x, const PpfGrid* g, int32_t* status,
                              void* stream);
+
+/* Reads and clears the library's device status word (PPF_STATUS_* bits
+ * or'ed in by kernels: a bounded wait that gave up, a non-finite value).
+ * Synchronous. */
+int32_t ppf_status_take(int32_t* status);
+/* Launches a kernel whose barrier wait can never complete, with a poll
+ * limit, so that it gives up and reports PPF_STATUS_TIMEOUT (test of the
+ * bounded-wait path; nothing is left in flight). */
+int32_t ppf_selftest_wait_timeout(int32_t poll_limit, void* stream);
 
 /* *counter += inc on the device (stream-ordered; one thread). */
 int32_t ppf_counter_add_u64(uint64_t* counter, uint64_t inc, void* stream);

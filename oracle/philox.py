@@ -36,15 +36,20 @@ def philox4x32_10(ctr, key):
 
 
 def noise_uniform(seed: int, step: int, shape) -> np.ndarray:
-    """U[0,1) per interior cell for time step `step`: first output word of
-    Philox4x32-10 with counter (cell_lo, cell_hi, step_lo, step_hi) and key
-    (seed_lo, seed_hi), top 24 bits times 2^-24 (cell = C-order linear index
-    of the interior cell). Matches ppf::noise_bits in the CUDA library."""
-    n = int(np.prod(shape))
-    cell = np.arange(n, dtype=np.uint64)
+    """U[0,1) per interior cell for time step `step`. Cells are grouped by
+    four along the last axis: cell (row, col) of a 2-D grid (a 1-D grid is
+    one row) takes output word col % 4 of Philox4x32-10 with counter
+    (col // 4, row, step_lo, step_hi) and key (seed_lo, seed_hi); the word's
+    top 24 bits times 2^-24 are the uniform number. Matches ppf::noise_group
+    in the CUDA library."""
+    shape = tuple(shape)
+    rows, cols = (1, shape[0]) if len(shape) == 1 else (int(np.prod(shape[:-1])), shape[-1])
+    nq = (cols + 3) // 4
+    q = np.tile(np.arange(nq, dtype=np.uint64), rows)
+    r = np.repeat(np.arange(rows, dtype=np.uint64), nq)
     step = int(step)
     seed = int(seed)
-    x, _, _, _ = philox4x32_10(
-        (cell & _MASK, cell >> _S32, step & 0xFFFFFFFF, step >> 32),
-        (seed & 0xFFFFFFFF, seed >> 32))
-    return ((x >> np.uint64(8)).astype(np.float64) * 2.0 ** -24).reshape(shape)
+    words = philox4x32_10((q, r, step & 0xFFFFFFFF, step >> 32),
+                          (seed & 0xFFFFFFFF, seed >> 32))
+    w = np.stack(words, axis=-1).reshape(rows, nq * 4)[:, :cols]
+    return ((w >> np.uint64(8)).astype(np.float64) * 2.0 ** -24).reshape(shape)

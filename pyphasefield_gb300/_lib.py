@@ -96,6 +96,8 @@ SIGNATURES: dict[str, list] = {
     "ppf_free_energy_f32": [P, PG, PB, C.c_double, C.c_double, C.c_double, P, P, SZ, P],
     "ppf_free_energy_f64": [P, PG, PB, C.c_double, C.c_double, C.c_double, P, P, SZ, P],
     "ppf_check_finite_f32": [P, PG, P, P],
+    "ppf_status_take": [C.POINTER(I32)],
+    "ppf_selftest_wait_timeout": [I32, P],
     "ppf_counter_add_u64": [P, U64, P],
     "ppf_graph_begin": [P],
     "ppf_graph_end": [P, C.POINTER(P)],

@@ -43,6 +43,11 @@ struct Bc {
   T shift[2][3][2];
 };
 
+// Device address of the library's status word (PPF_STATUS_* bits) on the
+// current device; kernels that wait on barriers or check values OR
+// their findings into it.
+int* status_ptr();
+
 // Validates a PpfGrid and fills a Geo. Returns PPF_OK or an error code.
 int32_t make_geo(const PpfGrid* g, int want_ndim_min, int want_ndim_max,
                  Geo* out);
@@ -177,17 +182,15 @@ __host__ __device__ __forceinline__ U4 philox4x32_10(U4 ctr, uint32_t k0,
   return ctr;
 }
 
-// Uniform number in [0, 1) for cell `cell` at time step `step`: the first
-// 32-bit output word of Philox4x32-10 with counter (cell_lo, cell_hi,
-// step_lo, step_hi) and key (seed_lo, seed_hi), top 24 bits scaled by 2^-24.
-// Exactly representable in float and double, so both precisions and the
-// host oracle see the same number.
-__host__ __device__ __forceinline__ uint32_t noise_bits(uint64_t seed,
-                                                        uint64_t step,
-                                                        uint64_t cell) {
-  U4 c{(uint32_t)cell, (uint32_t)(cell >> 32), (uint32_t)step,
-       (uint32_t)(step >> 32)};
-  return philox4x32_10(c, (uint32_t)seed, (uint32_t)(seed >> 32)).x >> 8;
+// Noise words for the group of 4 cells (row gy, columns 4*gq .. 4*gq+3) at
+// time step `step`: Philox4x32-10 with counter (gq, gy, step_lo, step_hi) and
+// key (seed_lo, seed_hi). Cell (gy, gx) takes word gx & 3; its uniform number
+// in [0, 1) is (word >> 8) * 2^-24, exact in float and double, so both
+// precisions and the host oracle see the same number.
+__host__ __device__ __forceinline__ U4 noise_group(uint64_t seed, uint64_t step,
+                                                  uint32_t gy, uint32_t gq) {
+  return philox4x32_10(U4{gq, gy, (uint32_t)step, (uint32_t)(step >> 32)},
+                       (uint32_t)seed, (uint32_t)(seed >> 32));
 }
 
 }  // namespace ppf

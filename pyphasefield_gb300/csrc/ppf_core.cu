@@ -4,10 +4,16 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <cudaTypedefs.h>
+
 #include <cmath>
+#include <cstring>
+#include <mutex>
 #include <string>
+#include <unordered_map>
 
 #include "ppf_common.cuh"
+#include "ppf_tma.cuh"
 
 namespace ppf {
 
@@ -95,6 +101,117 @@ __global__ void counter_add_kernel(uint64_t* c, uint64_t inc) {
   *c += inc;
 }
 
+// ------------------------------------------------------------ status word
+__device__ int g_status;
+
+int* status_ptr() {
+  static int* cached[64] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+  if (!cached[dev]) {
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_status) != cudaSuccess) return nullptr;
+    cached[dev] = (int*)p;
+  }
+  return cached[dev];
+}
+
+// Waits on an mbarrier that nothing completes, with a small poll limit, to
+// exercise the timeout path: the wait gives up and reports
+// PPF_STATUS_TIMEOUT; nothing is left in flight.
+__global__ void wait_timeout_kernel(uint32_t limit, int* status) {
+  __shared__ __align__(8) uint64_t bar;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    mbar_init_fence();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    if (!mbar_wait(&bar, 0, limit)) atomicOr(status, PPF_STATUS_TIMEOUT);
+    // complete the phase so the barrier is left quiescent
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(&bar)) : "memory");
+  }
+}
+
+// ------------------------------------------------------------ tensor maps
+namespace {
+
+struct MapKey {
+  const void* base;
+  int elem, rank;
+  uint64_t dims[3], strides[2];
+  uint32_t box[3];
+  int device;
+  bool operator==(const MapKey& o) const { return std::memcmp(this, &o, sizeof(*this)) == 0; }
+};
+struct MapKeyHash {
+  size_t operator()(const MapKey& k) const {
+    const unsigned char* p = reinterpret_cast<const unsigned char*>(&k);
+    size_t h = 1469598103934665603ull;
+    for (size_t i = 0; i < sizeof(k); ++i) h = (h ^ p[i]) * 1099511628211ull;
+    return h;
+  }
+};
+
+std::mutex g_map_mutex;
+std::unordered_map<MapKey, CUtensorMap, MapKeyHash>& map_cache() {
+  static std::unordered_map<MapKey, CUtensorMap, MapKeyHash> m;
+  return m;
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+  }
+  return fn;
+}
+
+}  // namespace
+
+int32_t tensor_map(CUtensorMap* out, const void* base, int elem_bytes, int rank,
+                   const uint64_t* dims, const uint64_t* strides_bytes, const uint32_t* box) {
+  MapKey key;
+  std::memset(&key, 0, sizeof(key));
+  key.base = base;
+  key.elem = elem_bytes;
+  key.rank = rank;
+  for (int i = 0; i < rank; ++i) {
+    key.dims[i] = dims[i];
+    key.box[i] = box[i];
+  }
+  for (int i = 0; i + 1 < rank; ++i) key.strides[i] = strides_bytes[i];
+  cudaGetDevice(&key.device);
+  std::lock_guard<std::mutex> lock(g_map_mutex);
+  auto& cache = map_cache();
+  auto it = cache.find(key);
+  if (it != cache.end()) {
+    *out = it->second;
+    return PPF_OK;
+  }
+  auto fn = encode_fn();
+  if (!fn) return fail(PPF_ERR_CUDA, "cuTensorMapEncodeTiled unavailable from the driver");
+  if (((uintptr_t)base) % 16) return fail(PPF_ERR_INVALID, "field base not 16-byte aligned");
+  cuuint32_t estr[3] = {1, 1, 1};
+  CUtensorMap m;
+  CUresult r = fn(&m, elem_bytes == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32
+                                      : CU_TENSOR_MAP_DATA_TYPE_FLOAT64,
+                  (cuuint32_t)rank, const_cast<void*>(base), (const cuuint64_t*)dims,
+                  (const cuuint64_t*)strides_bytes, (const cuuint32_t*)box, estr,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                  CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return fail(PPF_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+  if (cache.size() > 4096) cache.clear();
+  cache.emplace(key, m);
+  *out = m;
+  return PPF_OK;
+}
+
 }  // namespace ppf
 
 using namespace ppf;
@@ -138,6 +255,29 @@ int32_t ppf_counter_add_u64(uint64_t* counter, uint64_t inc, void* stream) {
   clear_error();
   if (!counter) return fail(PPF_ERR_INVALID, "counter is NULL");
   counter_add_kernel<<<1, 1, 0, (cudaStream_t)stream>>>(counter, inc);
+  PPF_TRY_CUDA(cudaGetLastError());
+  return PPF_OK;
+}
+
+int32_t ppf_status_take(int32_t* status) {
+  clear_error();
+  if (!status) return fail(PPF_ERR_INVALID, "status is NULL");
+  int* p = status_ptr();
+  if (!p) return fail(PPF_ERR_CUDA, "status word unavailable");
+  int v = 0;
+  PPF_TRY_CUDA(cudaMemcpy(&v, p, sizeof(int), cudaMemcpyDeviceToHost));
+  PPF_TRY_CUDA(cudaMemset(p, 0, sizeof(int)));
+  *status = v;
+  return PPF_OK;
+}
+
+int32_t ppf_selftest_wait_timeout(int32_t poll_limit, void* stream) {
+  clear_error();
+  if (poll_limit < 1 || poll_limit > (1 << 20))
+    return fail(PPF_ERR_INVALID, "poll_limit must be in [1, 2^20]");
+  int* p = status_ptr();
+  if (!p) return fail(PPF_ERR_CUDA, "status word unavailable");
+  wait_timeout_kernel<<<1, 32, 0, (cudaStream_t)stream>>>((uint32_t)poll_limit, p);
   PPF_TRY_CUDA(cudaGetLastError());
   return PPF_OK;
 }

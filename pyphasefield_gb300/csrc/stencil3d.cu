@@ -1,10 +1,13 @@
 // 3-D explicit steps that march along z: Diffusion / Allen-Cahn (7-point)
 // and Cahn-Hilliard (radius 2 through an on-chip chemical-potential tile).
 //
-// A CTA owns a TY x TX column of the grid and a chunk of ZC planes. It keeps
-// a ring of z-planes (with an xy halo) in shared memory, loads each plane
-// once, and writes each updated plane once, so HBM sees one read and one
-// write per cell per step; xy halos are re-read from L2.
+// A CTA owns a TY x TX column of the grid and a chunk of ZC planes. Its
+// z-planes (with an xy halo) are staged by TMA tensor loads into a ring of
+// shared-memory slots, several planes ahead of the plane being computed, so
+// HBM reads overlap the stencil; each plane is read once and written once
+// (xy halos are re-read from L2). The TMA box starts 4 columns left of the
+// tile (16-byte aligned); cells outside the grid arrive zero-filled and are
+// rewritten with the boundary rule on edge tiles only.
 //
 // Reference: Field.laplacian (field.py:60-67), engine_ExplicitDiffusion
 // (Engines/Diffusion.py:198-208), engine_CahnAllenExplicit
@@ -13,17 +16,18 @@
 #include <cmath>
 
 #include "ppf_common.cuh"
+#include "ppf_tma.cuh"
 
 namespace ppf {
 namespace {
 
 constexpr int kThreads = 256;
+constexpr int kXOff = 4;  // box starts kXOff columns left of the tile
 
 template <typename T>
 struct Diffusion7 {
   T r;
-  __device__ __forceinline__ T operator()(T c, T w, T e, T n, T s, T d,
-                                          T u) const {
+  __device__ __forceinline__ T operator()(T c, T w, T e, T n, T s, T d, T u) const {
     const T lap = (((w + e) + (n + s)) + (d + u)) - T(6) * c;
     return c + r * lap;
   }
@@ -32,67 +36,165 @@ struct Diffusion7 {
 template <typename T>
 struct AllenCahn7 {
   T a, b;
-  __device__ __forceinline__ T operator()(T c, T w, T e, T n, T s, T d,
-                                          T u) const {
+  __device__ __forceinline__ T operator()(T c, T w, T e, T n, T s, T d, T u) const {
     const T lap = (((w + e) + (n + s)) + (d + u)) - T(6) * c;
     const T fp = c * (T(2) + c * (T(-6) + T(4) * c));
     return c + (a * lap - b * fp);
   }
 };
 
-// Loads plane gz of `in` with an xy halo of `h` cells into `dst`
-// ((TY+2h) x (TX+2h), row stride TX+2h). Interior tiles read directly.
-template <typename T>
-__device__ __forceinline__ void load_plane(T* dst, const T* __restrict__ in,
-                                           const Geo& g, const Bc<T>& bc,
-                                           int gz, int y0, int x0, int TX,
-                                           int TY, int h, bool xy_interior) {
-  const int W = TX + 2 * h, H = TY + 2 * h;
-  const bool inside = xy_interior && (unsigned)gz < (unsigned)g.n[0];
-  for (int ly = threadIdx.y; ly < H; ly += kThreads / 32) {
-    const int gy = y0 - h + ly;
-    if (inside) {
-      const T* row = in + (int64_t)gz * g.plane + (int64_t)gy * g.pitch + (x0 - h);
-      for (int lx = threadIdx.x; lx < W; lx += 32) dst[ly * W + lx] = __ldg(row + lx);
-    } else {
-      for (int lx = threadIdx.x; lx < W; lx += 32)
-        dst[ly * W + lx] = fetch<T, 3>(in, g, bc, 0, gz, gy, x0 - h + lx);
+// Shared-memory plane ring fed by TMA. Plane p (p >= pbase) lives in slot
+// (p - pbase) % NS; its k-th use of the slot completes mbarrier phase k.
+template <typename T, int NS>
+struct PlaneRing {
+  T* slots;
+  uint64_t* bars;
+  int slot_elems;  // elements per slot (BX * BY, padded to 128 bytes)
+  int pbase;
+  __device__ T* plane(int p) const { return slots + ((p - pbase) % NS) * slot_elems; }
+  __device__ uint64_t* bar(int p) const { return bars + (p - pbase) % NS; }
+  __device__ uint32_t parity(int p) const { return (uint32_t)(((p - pbase) / NS) & 1); }
+};
+
+struct MarchGeom {
+  int TX, TY, ZC, H;  // tile, z chunk, halo
+  int BX, BY;         // TMA box (BX = TX + 2 * kXOff, BY = TY + 2H)
+};
+
+// Issue (one thread) the load of plane p. A plane outside the grid along a
+// DIRCHLET z axis is not loaded (its cells are fixed values, written by the
+// fix-up); the barrier phase is completed by a plain arrive instead.
+template <typename T, int NS>
+__device__ __forceinline__ void issue_plane(const PlaneRing<T, NS>& ring, const CUtensorMap* map,
+                                            const Geo& g, const Bc<T>& bc, const MarchGeom& m,
+                                            int x0, int y0, int p) {
+  uint64_t* b = ring.bar(p);
+  const int nz = g.n[0];
+  if ((unsigned)p >= (unsigned)nz && bc.type[0] == PPF_BC_DIRCHLET) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(b)) : "memory");
+    return;
+  }
+  int pz = p;
+  if ((unsigned)p >= (unsigned)nz)
+    pz = bc.type[0] == PPF_BC_PERIODIC ? wrap_index(p, nz) : mirror_index(p, nz);
+  fence_proxy_async();
+  mbar_expect_tx(b, (uint32_t)(m.BX * m.BY * sizeof(T)));
+  tma_load_3d(ring.plane(p), map, x0 - kXOff, y0 - m.H, pz, b);
+}
+
+// Rewrite the cells of plane p that the TMA box could not supply: columns or
+// rows outside the grid (edge tiles), or the whole plane on a DIRCHLET z
+// ghost. Uses the generic boundary rule.
+template <typename T, int NS>
+__device__ __forceinline__ void fixup_plane(const PlaneRing<T, NS>& ring, const T* __restrict__ in,
+                                            const Geo& g, const Bc<T>& bc, const MarchGeom& m,
+                                            int x0, int y0, int p, bool xy_edge) {
+  const bool zfixed = (unsigned)p >= (unsigned)g.n[0] && bc.type[0] == PPF_BC_DIRCHLET;
+  if (!xy_edge && !zfixed) return;
+  T* dst = ring.plane(p);
+  const int W = m.TX + 2 * m.H, Hh = m.TY + 2 * m.H;
+  for (int ly = threadIdx.y; ly < Hh; ly += kThreads / 32) {
+    const int gy = y0 - m.H + ly;
+    const bool yout = (unsigned)gy >= (unsigned)g.n[1];
+    for (int lx = threadIdx.x; lx < W; lx += 32) {
+      const int gx = x0 - m.H + lx;
+      if (zfixed || yout || (unsigned)gx >= (unsigned)g.n[2])
+        dst[ly * m.BX + (gx - x0 + kXOff)] = fetch<T, 3>(in, g, bc, 0, p, gy, gx);
     }
   }
 }
 
+// Bounded wait by every thread; returns false (uniformly) if any timed out.
+__device__ __forceinline__ bool wait_all(uint64_t* bar, uint32_t parity, int* abort_flag) {
+  if (!mbar_wait(bar, parity)) *abort_flag = 1;
+  __syncthreads();
+  return *abort_flag == 0;
+}
+
+template <typename T>
+__device__ __forceinline__ void report_timeout(int* status) {
+  if (threadIdx.x == 0 && threadIdx.y == 0) atomicOr(status, PPF_STATUS_TIMEOUT);
+}
+
+// After a timeout: wait (bounded) for every plane still in flight so that no
+// TMA write lands in shared memory after the CTA has exited.
+template <typename T, int NS>
+__device__ void drain(const PlaneRing<T, NS>& ring, int first, int last) {
+  if (threadIdx.x == 0 && threadIdx.y == 0)
+    for (int p = first; p <= last; ++p) mbar_wait(ring.bar(p), ring.parity(p));
+  __syncthreads();
+}
+
+template <typename T>
+__device__ __forceinline__ T* align128(unsigned char* p) {
+  return reinterpret_cast<T*>((reinterpret_cast<uintptr_t>(p) + 127) & ~uintptr_t(127));
+}
+
 // ------------------------------------------------------------- 7-point
+constexpr int kNS7 = 5;  // planes z-1, z, z+1 in use; z+2, z+3 in flight
+
 template <typename T, typename Op>
 __global__ void __launch_bounds__(kThreads)
-    march7_kernel(Op op, Geo g, Bc<T> bc, const T* __restrict__ in,
-                  T* __restrict__ out, int TX, int TY, int ZC) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int W = TX + 2, H = TY + 2, P = W * H;
-  T* ring = reinterpret_cast<T*>(smem_raw);  // 3 planes
-  const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY, z0 = blockIdx.z * ZC;
+    march7_kernel(const __grid_constant__ CUtensorMap map, Op op, Geo g, Bc<T> bc,
+                  const T* __restrict__ in, T* __restrict__ out, MarchGeom m, int slot_elems,
+                  int* status) {
+  extern __shared__ unsigned char smem_raw[];
+  __shared__ __align__(8) uint64_t bars[kNS7];
+  __shared__ int abort_flag;
+  const int x0 = blockIdx.x * m.TX, y0 = blockIdx.y * m.TY, z0 = blockIdx.z * m.ZC;
   const int nz = g.n[0], ny = g.n[1], nx = g.n[2];
-  const int z1 = min(z0 + ZC, nz);
-  const bool xy_in = x0 >= 1 && y0 >= 1 && x0 + TX + 1 <= nx && y0 + TY + 1 <= ny;
+  const int z1 = min(z0 + m.ZC, nz);
+  const bool xy_edge = x0 - 1 < 0 || y0 - 1 < 0 || x0 + m.TX + 1 > nx || y0 + m.TY + 1 > ny ||
+                       x0 - kXOff < 0 || x0 + m.TX + kXOff > nx;
+  PlaneRing<T, kNS7> ring{align128<T>(smem_raw), bars, slot_elems, z0 - 1};
+  const bool leader = threadIdx.x == 0 && threadIdx.y == 0;
 
+  if (leader) {
+    for (int i = 0; i < kNS7; ++i) mbar_init(&bars[i], 1);
+    mbar_init_fence();
+    abort_flag = 0;
+  }
+  __syncthreads();
   pdl_wait();
   pdl_launch_next();
+  const int last = z1;  // last plane needed
+  if (leader)
+    for (int p = z0 - 1; p <= min(z0 + 2, last); ++p) issue_plane(ring, &map, g, bc, m, x0, y0, p);
+  int issued = min(z0 + 2, last);
 
-  load_plane(ring + ((z0 - 1 + 3) % 3) * P, in, g, bc, z0 - 1, y0, x0, TX, TY, 1, xy_in);
-  load_plane(ring + (z0 % 3) * P, in, g, bc, z0, y0, x0, TX, TY, 1, xy_in);
+  for (int p = z0 - 1; p <= z0; ++p) {
+    if (!wait_all(ring.bar(p), ring.parity(p), &abort_flag)) {
+      report_timeout<T>(status);
+      drain(ring, p, issued);
+      return;
+    }
+    fixup_plane(ring, in, g, bc, m, x0, y0, p, xy_edge);
+  }
+  const int W = m.BX;
   for (int z = z0; z < z1; ++z) {
-    load_plane(ring + ((z + 1) % 3) * P, in, g, bc, z + 1, y0, x0, TX, TY, 1, xy_in);
+    if (leader && z + 3 <= last) {
+      issue_plane(ring, &map, g, bc, m, x0, y0, z + 3);
+      issued = z + 3;
+    }
+    if (!wait_all(ring.bar(z + 1), ring.parity(z + 1), &abort_flag)) {
+      report_timeout<T>(status);
+      if (leader) issued = min(z + 3, last);
+      drain(ring, z + 1, min(z + 3, last));
+      return;
+    }
+    fixup_plane(ring, in, g, bc, m, x0, y0, z + 1, xy_edge);
     __syncthreads();
-    const T* pd = ring + ((z + 2) % 3) * P;  // z-1
-    const T* pc = ring + (z % 3) * P;
-    const T* pu = ring + ((z + 1) % 3) * P;
-    for (int ly = 1 + threadIdx.y; ly <= TY; ly += kThreads / 32) {
+    const T* pd = ring.plane(z - 1);
+    const T* pc = ring.plane(z);
+    const T* pu = ring.plane(z + 1);
+    for (int ly = 1 + threadIdx.y; ly <= m.TY; ly += kThreads / 32) {
       const int gy = y0 + ly - 1;
       if (gy >= ny) break;
       T* orow = out + (int64_t)z * g.plane + (int64_t)gy * g.pitch;
-      for (int lx = 1 + threadIdx.x; lx <= TX; lx += 32) {
-        const int gx = x0 + lx - 1;
+      for (int lx = threadIdx.x; lx < m.TX; lx += 32) {
+        const int gx = x0 + lx;
         if (gx >= nx) break;
-        const int i = ly * W + lx;
+        const int i = ly * W + lx + kXOff;
         orow[gx] = op(pc[i], pc[i - 1], pc[i + 1], pc[i - W], pc[i + W], pd[i], pu[i]);
       }
     }
@@ -101,8 +203,8 @@ __global__ void __launch_bounds__(kThreads)
 }
 
 // ------------------------------------------------------------- Cahn-Hilliard
-// mu~ = -(eps^2/dx^2) lap'(c) + (4c^3 - 6c^2 + 2c), lap' the unscaled 7-point
-// sum; c' = c + sum over the 6 faces of F = a (mu~_nbr - mu~_c), a = dt M/dx^2.
+// mu~ = -(eps^2/dx^2) lap'(c) + f'(c), lap' the unscaled 7-point sum;
+// c' = c + sum over the 6 faces of F = a (mu~_nbr - mu~_c), a = dt M/dx^2.
 // With QUANT each face flux is rounded to a multiple of q (a power of two).
 // F(A->B) = -F(B->A) bit for bit (the same mu~ values enter both cells and
 // rounding to nearest is odd-symmetric), so the float field conserves its
@@ -117,12 +219,10 @@ struct ChCoef {
 };
 
 template <typename T>
-__device__ __forceinline__ T ch_mu(const ChCoef<T>& k, T c, T w, T e, T n,
-                                   T s, T d, T u) {
+__device__ __forceinline__ T ch_mu(const ChCoef<T>& k, T c, T w, T e, T n, T s, T d, T u) {
   const T lap = (((w + e) + (n + s)) + (d + u)) - T(6) * c;
   // 4c^3 - 6c^2 + 2c, or in the centered variable 4u^3 - u
-  const T fp = k.centered ? c * (T(4) * c * c - T(1))
-                          : c * (T(2) + c * (T(-6) + T(4) * c));
+  const T fp = k.centered ? c * (T(4) * c * c - T(1)) : c * (T(2) + c * (T(-6) + T(4) * c));
   return fp - k.kap * lap;
 }
 
@@ -133,63 +233,90 @@ __device__ __forceinline__ T ch_flux(const ChCoef<T>& k, T mn, T mc) {
   return f;
 }
 
+constexpr int kNSC = 6;  // c planes z..z+2 in use; z+3, z+4 in flight
+
 template <typename T, bool QUANT>
 __global__ void __launch_bounds__(kThreads)
-    cahn_hilliard_kernel(ChCoef<T> k, Geo g, Bc<T> bc, const T* __restrict__ in,
-                         T* __restrict__ out, double* __restrict__ mass,
-                         int* __restrict__ status, int TX, int TY, int ZC) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int WC = TX + 4, HC = TY + 4, PC = WC * HC;  // c planes, halo 2
-  const int WM = TX + 2, HM = TY + 2, PM = WM * HM;  // mu planes, halo 1
-  T* cring = reinterpret_cast<T*>(smem_raw);          // 5 planes
-  T* mring = cring + 5 * PC;                          // 3 planes
+    cahn_hilliard_kernel(const __grid_constant__ CUtensorMap map, ChCoef<T> k, Geo g, Bc<T> bc,
+                         const T* __restrict__ in, T* __restrict__ out, double* __restrict__ mass,
+                         int* __restrict__ status, MarchGeom m, int slot_elems,
+                         int* __restrict__ lib_status) {
+  extern __shared__ unsigned char smem_raw[];
+  __shared__ __align__(8) uint64_t bars[kNSC];
+  __shared__ int abort_flag;
   __shared__ double red[kThreads / 32];
-  const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY, z0 = blockIdx.z * ZC;
+  const int x0 = blockIdx.x * m.TX, y0 = blockIdx.y * m.TY, z0 = blockIdx.z * m.ZC;
   const int nz = g.n[0], ny = g.n[1], nx = g.n[2];
-  const int z1 = min(z0 + ZC, nz);
-  const bool xy_in = x0 >= 2 && y0 >= 2 && x0 + TX + 2 <= nx && y0 + TY + 2 <= ny;
+  const int z1 = min(z0 + m.ZC, nz);
+  const bool xy_edge = x0 - 2 < 0 || y0 - 2 < 0 || x0 + m.TX + 2 > nx || y0 + m.TY + 2 > ny ||
+                       x0 - kXOff < 0 || x0 + m.TX + kXOff > nx;
+  PlaneRing<T, kNSC> ring{align128<T>(smem_raw), bars, slot_elems, z0 - 2};
+  const int WM = m.TX + 2, HM = m.TY + 2, PM = WM * HM;  // mu planes, halo 1
+  T* mring = ring.slots + kNSC * slot_elems;
+  auto mslot = [&](int z) { return mring + ((z - z0 + 3) % 3) * PM; };
+  const bool leader = threadIdx.x == 0 && threadIdx.y == 0;
+  const int W = m.BX;
 
+  if (leader) {
+    for (int i = 0; i < kNSC; ++i) mbar_init(&bars[i], 1);
+    mbar_init_fence();
+    abort_flag = 0;
+  }
+  __syncthreads();
   pdl_wait();
   pdl_launch_next();
+  const int last = z1 + 1;
+  if (leader)
+    for (int p = z0 - 2; p <= min(z0 + 3, last); ++p) issue_plane(ring, &map, g, bc, m, x0, y0, p);
 
-  auto cslot = [&](int z) { return cring + ((z % 5 + 5) % 5) * PC; };
-  auto mslot = [&](int z) { return mring + ((z % 3 + 3) % 3) * PM; };
-  // mu~ on the (TY+2) x (TX+2) region of plane z from c planes z-1, z, z+1.
+  // mu~ of plane z on the (TY+2) x (TX+2) region from c planes z-1, z, z+1
   auto compute_mu = [&](int z) {
-    const T* cd = cslot(z - 1);
-    const T* cc = cslot(z);
-    const T* cu = cslot(z + 1);
-    T* m = mslot(z);
+    const T* cd = ring.plane(z - 1);
+    const T* cc = ring.plane(z);
+    const T* cu = ring.plane(z + 1);
+    T* mz = mslot(z);
     for (int ly = threadIdx.y; ly < HM; ly += kThreads / 32)
       for (int lx = threadIdx.x; lx < WM; lx += 32) {
-        const int i = (ly + 1) * WC + (lx + 1);
-        m[ly * WM + lx] = ch_mu(k, cc[i], cc[i - 1], cc[i + 1], cc[i - WC],
-                                cc[i + WC], cd[i], cu[i]);
+        const int i = (ly + 1) * W + lx + (kXOff - 1);
+        mz[ly * WM + lx] = ch_mu(k, cc[i], cc[i - 1], cc[i + 1], cc[i - W], cc[i + W], cd[i], cu[i]);
       }
   };
 
-  for (int z = z0 - 2; z <= z0 + 1; ++z)
-    load_plane(cslot(z), in, g, bc, z, y0, x0, TX, TY, 2, xy_in);
+  for (int p = z0 - 2; p <= z0 + 1; ++p) {
+    if (!wait_all(ring.bar(p), ring.parity(p), &abort_flag)) {
+      report_timeout<T>(lib_status);
+      drain(ring, p, min(z0 + 3, last));
+      return;
+    }
+    fixup_plane(ring, in, g, bc, m, x0, y0, p, xy_edge);
+  }
   __syncthreads();
   compute_mu(z0 - 1);
   compute_mu(z0);
+  __syncthreads();  // c(z0-2) is re-filled by the first loop iteration
 
   double acc = 0.0;
   int flags = 0;
   for (int z = z0; z < z1; ++z) {
-    load_plane(cslot(z + 2), in, g, bc, z + 2, y0, x0, TX, TY, 2, xy_in);
+    if (leader && z + 4 <= last) issue_plane(ring, &map, g, bc, m, x0, y0, z + 4);
+    if (!wait_all(ring.bar(z + 2), ring.parity(z + 2), &abort_flag)) {
+      report_timeout<T>(lib_status);
+      drain(ring, z + 2, min(z + 4, last));
+      return;
+    }
+    fixup_plane(ring, in, g, bc, m, x0, y0, z + 2, xy_edge);
     __syncthreads();
     compute_mu(z + 1);
     __syncthreads();
     const T* md = mslot(z - 1);
     const T* mc = mslot(z);
     const T* mu = mslot(z + 1);
-    const T* cc = cslot(z);
-    for (int ly = 1 + threadIdx.y; ly <= TY; ly += kThreads / 32) {
+    const T* cc = ring.plane(z);
+    for (int ly = 1 + threadIdx.y; ly <= m.TY; ly += kThreads / 32) {
       const int gy = y0 + ly - 1;
       if (gy >= ny) break;
       T* orow = out + (int64_t)z * g.plane + (int64_t)gy * g.pitch;
-      for (int lx = 1 + threadIdx.x; lx <= TX; lx += 32) {
+      for (int lx = 1 + threadIdx.x; lx <= m.TX; lx += 32) {
         const int gx = x0 + lx - 1;
         if (gx >= nx) break;
         const int i = ly * WM + lx;
@@ -200,7 +327,7 @@ __global__ void __launch_bounds__(kThreads)
         const T fs = ch_flux<T, QUANT>(k, mc[i + WM], m0);
         const T fd = ch_flux<T, QUANT>(k, md[i], m0);
         const T fu = ch_flux<T, QUANT>(k, mu[i], m0);
-        const T c0 = cc[(ly + 1) * WC + (lx + 1)];
+        const T c0 = cc[(ly + 1) * W + lx + (kXOff - 1)];
         const T v = c0 + (((fw + fe) + (fn + fs)) + (fd + fu));
         orow[gx] = v;
         acc += (double)v;
@@ -225,38 +352,46 @@ __global__ void __launch_bounds__(kThreads)
   }
 }
 
-struct Tile3d {
-  int tx, ty, zc;
-};
-
+// ------------------------------------------------------------- host side
 template <typename T>
-int32_t plan3d(const PpfTiling* t, const Geo& g, int halo, int nplanes_c,
-               int nplanes_m, Tile3d* r, size_t* smem) {
-  r->tx = t && t->tile_x ? t->tile_x : 64;
-  r->ty = t && t->tile_y ? t->tile_y : 16;
+int32_t plan3d(const PpfTiling* t, const Geo& g, int halo, int nslots, int mu_planes,
+               MarchGeom* m, int* slot_elems, size_t* smem) {
+  m->TX = t && t->tile_x ? t->tile_x : 64;
+  m->TY = t && t->tile_y ? t->tile_y : 16;
+  m->H = halo;
   if (t && t->depth > 1)
-    return fail(PPF_ERR_UNSUPPORTED, "3-D steps advance one step per pass (depth=%d)",
-                t->depth);
-  if (r->tx < 1 || r->tx > 512 || r->ty < 1 || r->ty > 512)
-    return fail(PPF_ERR_INVALID, "tile %dx%d invalid", r->tx, r->ty);
-  // z chunk: enough CTAs for ~4 waves of 152 SMs, at least 8 planes.
-  const long tiles = (long)((g.n[2] + r->tx - 1) / r->tx) * ((g.n[1] + r->ty - 1) / r->ty);
-  int zc = (int)((long)g.n[0] * tiles / (152L * 4 * 2));
-  zc = zc < 8 ? 8 : zc;
-  zc = zc > 64 ? 64 : zc;
-  r->zc = zc > g.n[0] ? g.n[0] : zc;
-  *smem = ((size_t)nplanes_c * (r->tx + 2 * halo) * (r->ty + 2 * halo) +
-           (size_t)nplanes_m * (r->tx + 2) * (r->ty + 2)) *
-          sizeof(T);
+    return fail(PPF_ERR_UNSUPPORTED, "3-D steps advance one step per pass (depth=%d)", t->depth);
+  if (m->TX < 4 || m->TX > 256 - 2 * kXOff || (m->TX % 4) != 0 || m->TY < 1 ||
+      m->TY + 2 * halo > 256)
+    return fail(PPF_ERR_INVALID, "tile %dx%d invalid (tile_x multiple of 4, <= %d)", m->TX,
+                m->TY, 256 - 2 * kXOff);
+  m->BX = m->TX + 2 * kXOff;
+  m->BY = m->TY + 2 * halo;
+  // z chunk: about two waves of CTAs over 152 SMs, at least 8 planes.
+  const long tiles = (long)((g.n[2] + m->TX - 1) / m->TX) * ((g.n[1] + m->TY - 1) / m->TY);
+  int zc = (int)((long)g.n[0] * tiles / (152L * 8));
+  zc = zc < 8 ? 8 : (zc > 64 ? 64 : zc);
+  m->ZC = zc > g.n[0] ? g.n[0] : zc;
+  const size_t slot_bytes = ((size_t)m->BX * m->BY * sizeof(T) + 127) / 128 * 128;
+  *slot_elems = (int)(slot_bytes / sizeof(T));
+  *smem = 128 + (size_t)nslots * slot_bytes +
+          (size_t)mu_planes * (m->TX + 2) * (m->TY + 2) * sizeof(T);
   if (*smem > 200 * 1024)
     return fail(PPF_ERR_INVALID, "tile needs %zu bytes of shared memory", *smem);
   return PPF_OK;
 }
 
+template <typename T>
+int32_t plane_map(CUtensorMap* map, const T* base, const Geo& g, const MarchGeom& m) {
+  const uint64_t dims[3] = {(uint64_t)g.n[2], (uint64_t)g.n[1], (uint64_t)g.n[0]};
+  const uint64_t strides[2] = {(uint64_t)g.pitch * sizeof(T), (uint64_t)g.plane * sizeof(T)};
+  const uint32_t box[3] = {(uint32_t)m.BX, (uint32_t)m.BY, 1u};
+  return tensor_map(map, base, (int)sizeof(T), 3, dims, strides, box);
+}
+
 // A 2-D grid runs as a single-plane 3-D grid with a periodic z axis (the
 // z neighbours are the cell itself and cancel in the Laplacian).
-int32_t as3d(const PpfGrid* in, const PpfBoundary* bin, PpfGrid* g3,
-             PpfBoundary* b3) {
+int32_t as3d(const PpfGrid* in, const PpfBoundary* bin, PpfGrid* g3, PpfBoundary* b3) {
   if (!in) return fail(PPF_ERR_INVALID, "grid is NULL");
   if (!bin) return fail(PPF_ERR_INVALID, "boundary is NULL");
   *g3 = *in;
@@ -280,8 +415,8 @@ int32_t as3d(const PpfGrid* in, const PpfBoundary* bin, PpfGrid* g3,
 }
 
 template <typename T, typename Op>
-int32_t run_march7(Op op, double dx, const PpfGrid* grid, const PpfBoundary* b,
-                   const T* in, T* out, const PpfTiling* tiling, void* stream) {
+int32_t run_march7(Op op, double dx, const PpfGrid* grid, const PpfBoundary* b, const T* in,
+                   T* out, const PpfTiling* tiling, void* stream) {
   Geo g;
   int32_t rc = make_geo(grid, 3, 3, &g);
   if (rc) return rc;
@@ -289,23 +424,26 @@ int32_t run_march7(Op op, double dx, const PpfGrid* grid, const PpfBoundary* b,
   if (in == out) return fail(PPF_ERR_INVALID, "in and out must differ");
   Bc<T> bc;
   if ((rc = make_bc<T>(b, g, dx, 1, 1, &bc))) return rc;
-  Tile3d t;
+  MarchGeom m;
+  int slot_elems;
   size_t smem;
-  if ((rc = plan3d<T>(tiling, g, 1, 3, 0, &t, &smem))) return rc;
+  if ((rc = plan3d<T>(tiling, g, 1, kNS7, 0, &m, &slot_elems, &smem))) return rc;
+  CUtensorMap map;
+  if ((rc = plane_map<T>(&map, in, g, m))) return rc;
+  int* st = status_ptr();
+  if (!st) return fail(PPF_ERR_CUDA, "status word unavailable");
   auto kern = march7_kernel<T, Op>;
   PPF_TRY_CUDA(allow_smem(kern, smem));
-  dim3 gd((g.n[2] + t.tx - 1) / t.tx, (g.n[1] + t.ty - 1) / t.ty,
-          (g.n[0] + t.zc - 1) / t.zc);
+  dim3 gd((g.n[2] + m.TX - 1) / m.TX, (g.n[1] + m.TY - 1) / m.TY, (g.n[0] + m.ZC - 1) / m.ZC);
   PPF_TRY_CUDA(launch(kern, gd, dim3(32, kThreads / 32), smem, (cudaStream_t)stream,
-                      tiling && tiling->pdl, op, g, bc, in, out, t.tx, t.ty, t.zc));
+                      tiling && tiling->pdl, map, op, g, bc, in, out, m, slot_elems, st));
   return PPF_OK;
 }
 
 template <typename T>
 int32_t cahn_hilliard(const PpfCahnHilliardParams* p, const PpfGrid* grid_in,
-                      const PpfBoundary* b_in, const T* in, T* out,
-                      double* mass, int32_t* status, const PpfTiling* tiling,
-                      void* stream) {
+                      const PpfBoundary* b_in, const T* in, T* out, double* mass,
+                      int32_t* status, const PpfTiling* tiling, void* stream) {
   clear_error();
   if (!p) return fail(PPF_ERR_INVALID, "params is NULL");
   if (!(p->dx > 0)) return fail(PPF_ERR_INVALID, "dx must be > 0");
@@ -319,27 +457,25 @@ int32_t cahn_hilliard(const PpfCahnHilliardParams* p, const PpfGrid* grid_in,
   if (in == out) return fail(PPF_ERR_INVALID, "in and out must differ");
   for (int a = 0; a < 3; ++a) {
     if (b.type[a] == PPF_BC_DIRCHLET)
-      return fail(PPF_ERR_UNSUPPORTED,
-                  "Cahn-Hilliard supports PERIODIC and NEUMANN axes only");
+      return fail(PPF_ERR_UNSUPPORTED, "Cahn-Hilliard supports PERIODIC and NEUMANN axes only");
     if (b.type[a] == PPF_BC_NEUMANN && (b.value[0][a][0] != 0.0 || b.value[0][a][1] != 0.0))
-      return fail(PPF_ERR_UNSUPPORTED,
-                  "Cahn-Hilliard NEUMANN axes must be no-flux (gradient 0)");
+      return fail(PPF_ERR_UNSUPPORTED, "Cahn-Hilliard NEUMANN axes must be no-flux (gradient 0)");
   }
   Bc<T> bc;
   if ((rc = make_bc<T>(&b, g, p->dx, 1, 2, &bc))) return rc;
-  Tile3d t;
+  MarchGeom m;
+  int slot_elems;
   size_t smem;
-  if ((rc = plan3d<T>(tiling, g, 2, 5, 3, &t, &smem))) return rc;
+  if ((rc = plan3d<T>(tiling, g, 2, kNSC, 3, &m, &slot_elems, &smem))) return rc;
   ChCoef<T> k;
   k.kap = (T)(p->epsilon * p->epsilon / (p->dx * p->dx));
   k.a = (T)(p->dt * p->M / (p->dx * p->dx));
   const bool quant = p->quantum > 0;
   if (quant) {
     int e;
-    const double m = std::frexp(p->quantum, &e);
-    if (m != 0.5 || sizeof(T) != 4)
-      return fail(PPF_ERR_INVALID,
-                  "quantum must be a power of two and needs the float path");
+    const double mant = std::frexp(p->quantum, &e);
+    if (mant != 0.5 || sizeof(T) != 4)
+      return fail(PPF_ERR_INVALID, "quantum must be a power of two and needs the float path");
   }
   k.q = (T)(quant ? p->quantum : 0.0);
   k.iq = (T)(quant ? 1.0 / p->quantum : 0.0);
@@ -347,53 +483,52 @@ int32_t cahn_hilliard(const PpfCahnHilliardParams* p, const PpfGrid* grid_in,
   if (p->centered != 0 && p->centered != 1)
     return fail(PPF_ERR_INVALID, "centered must be 0 or 1");
   k.centered = p->centered;
-  dim3 gd((g.n[2] + t.tx - 1) / t.tx, (g.n[1] + t.ty - 1) / t.ty,
-          (g.n[0] + t.zc - 1) / t.zc);
+  CUtensorMap map;
+  if ((rc = plane_map<T>(&map, in, g, m))) return rc;
+  int* st = status_ptr();
+  if (!st) return fail(PPF_ERR_CUDA, "status word unavailable");
+  dim3 gd((g.n[2] + m.TX - 1) / m.TX, (g.n[1] + m.TY - 1) / m.TY, (g.n[0] + m.ZC - 1) / m.ZC);
   const bool pdl = tiling && tiling->pdl;
   if (quant) {
     auto kern = cahn_hilliard_kernel<T, true>;
     PPF_TRY_CUDA(allow_smem(kern, smem));
-    PPF_TRY_CUDA(launch(kern, gd, dim3(32, kThreads / 32), smem, (cudaStream_t)stream,
-                        pdl, k, g, bc, in, out, mass, (int*)status, t.tx, t.ty, t.zc));
+    PPF_TRY_CUDA(launch(kern, gd, dim3(32, kThreads / 32), smem, (cudaStream_t)stream, pdl,
+                        map, k, g, bc, in, out, mass, (int*)status, m, slot_elems, st));
   } else {
     auto kern = cahn_hilliard_kernel<T, false>;
     PPF_TRY_CUDA(allow_smem(kern, smem));
-    PPF_TRY_CUDA(launch(kern, gd, dim3(32, kThreads / 32), smem, (cudaStream_t)stream,
-                        pdl, k, g, bc, in, out, mass, (int*)status, t.tx, t.ty, t.zc));
+    PPF_TRY_CUDA(launch(kern, gd, dim3(32, kThreads / 32), smem, (cudaStream_t)stream, pdl,
+                        map, k, g, bc, in, out, mass, (int*)status, m, slot_elems, st));
   }
   return PPF_OK;
 }
 
 }  // namespace
 
-int32_t diffusion3d_f32(const PpfDiffusionParams* p, const PpfGrid* g,
-                        const PpfBoundary* b, const float* in, float* out,
-                        const PpfTiling* t, void* s) {
+int32_t diffusion3d_f32(const PpfDiffusionParams* p, const PpfGrid* g, const PpfBoundary* b,
+                        const float* in, float* out, const PpfTiling* t, void* s) {
   clear_error();
   if (!p || !(p->dx > 0)) return fail(PPF_ERR_INVALID, "bad params");
-  return run_march7<float>(Diffusion7<float>{(float)(p->dt * p->D / (p->dx * p->dx))},
-                           p->dx, g, b, in, out, t, s);
+  return run_march7<float>(Diffusion7<float>{(float)(p->dt * p->D / (p->dx * p->dx))}, p->dx, g,
+                           b, in, out, t, s);
 }
-int32_t diffusion3d_f64(const PpfDiffusionParams* p, const PpfGrid* g,
-                        const PpfBoundary* b, const double* in, double* out,
-                        const PpfTiling* t, void* s) {
+int32_t diffusion3d_f64(const PpfDiffusionParams* p, const PpfGrid* g, const PpfBoundary* b,
+                        const double* in, double* out, const PpfTiling* t, void* s) {
   clear_error();
   if (!p || !(p->dx > 0)) return fail(PPF_ERR_INVALID, "bad params");
-  return run_march7<double>(Diffusion7<double>{p->dt * p->D / (p->dx * p->dx)}, p->dx,
-                            g, b, in, out, t, s);
+  return run_march7<double>(Diffusion7<double>{p->dt * p->D / (p->dx * p->dx)}, p->dx, g, b, in,
+                            out, t, s);
 }
-int32_t allen_cahn3d_f32(const PpfAllenCahnParams* p, const PpfGrid* g,
-                         const PpfBoundary* b, const float* in, float* out,
-                         const PpfTiling* t, void* s) {
+int32_t allen_cahn3d_f32(const PpfAllenCahnParams* p, const PpfGrid* g, const PpfBoundary* b,
+                         const float* in, float* out, const PpfTiling* t, void* s) {
   clear_error();
   if (!p || !(p->dx > 0)) return fail(PPF_ERR_INVALID, "bad params");
   AllenCahn7<float> op{(float)(p->dt * p->M * p->epsilon * p->epsilon / (p->dx * p->dx)),
                        (float)(p->dt * p->M * 16.0 * p->W)};
   return run_march7<float>(op, p->dx, g, b, in, out, t, s);
 }
-int32_t allen_cahn3d_f64(const PpfAllenCahnParams* p, const PpfGrid* g,
-                         const PpfBoundary* b, const double* in, double* out,
-                         const PpfTiling* t, void* s) {
+int32_t allen_cahn3d_f64(const PpfAllenCahnParams* p, const PpfGrid* g, const PpfBoundary* b,
+                         const double* in, double* out, const PpfTiling* t, void* s) {
   clear_error();
   if (!p || !(p->dx > 0)) return fail(PPF_ERR_INVALID, "bad params");
   AllenCahn7<double> op{p->dt * p->M * p->epsilon * p->epsilon / (p->dx * p->dx),
@@ -407,18 +542,16 @@ using namespace ppf;
 
 extern "C" {
 
-int32_t ppf_cahn_hilliard_step_f32(const PpfCahnHilliardParams* p,
-                                   const PpfGrid* g, const PpfBoundary* bc,
-                                   const float* in, float* out,
-                                   double* mass_accum, int32_t* status,
-                                   const PpfTiling* tiling, void* stream) {
+int32_t ppf_cahn_hilliard_step_f32(const PpfCahnHilliardParams* p, const PpfGrid* g,
+                                   const PpfBoundary* bc, const float* in, float* out,
+                                   double* mass_accum, int32_t* status, const PpfTiling* tiling,
+                                   void* stream) {
   return cahn_hilliard<float>(p, g, bc, in, out, mass_accum, status, tiling, stream);
 }
-int32_t ppf_cahn_hilliard_step_f64(const PpfCahnHilliardParams* p,
-                                   const PpfGrid* g, const PpfBoundary* bc,
-                                   const double* in, double* out,
-                                   double* mass_accum, int32_t* status,
-                                   const PpfTiling* tiling, void* stream) {
+int32_t ppf_cahn_hilliard_step_f64(const PpfCahnHilliardParams* p, const PpfGrid* g,
+                                   const PpfBoundary* bc, const double* in, double* out,
+                                   double* mass_accum, int32_t* status, const PpfTiling* tiling,
+                                   void* stream) {
   return cahn_hilliard<double>(p, g, bc, in, out, mass_accum, status, tiling, stream);
 }
 
