@@ -61,35 +61,40 @@ struct MarchGeom {
   int BX, BY;         // TMA box (BX = TX + 2 * kXOff, BY = TY + 2H)
 };
 
-// Issue (one thread) the load of plane p. A plane outside the grid along a
-// DIRCHLET z axis is not loaded (its cells are fixed values, written by the
-// fix-up); the barrier phase is completed by a plain arrive instead.
+// A plane outside the grid along a non-periodic z axis is a ghost plane:
+// its values follow the boundary rule (Neumann offset, Dirichlet value), so
+// the fix-up writes all of it.
+template <typename T>
+__device__ __forceinline__ bool ghost_plane(const Geo& g, const Bc<T>& bc, int p) {
+  return (unsigned)p >= (unsigned)g.n[0] && bc.type[0] != PPF_BC_PERIODIC;
+}
+
+// Issue (one thread) the load of plane p. A ghost plane is not loaded; its
+// barrier phase is completed by a plain arrive instead.
 template <typename T, int NS>
 __device__ __forceinline__ void issue_plane(const PlaneRing<T, NS>& ring, const CUtensorMap* map,
                                             const Geo& g, const Bc<T>& bc, const MarchGeom& m,
                                             int x0, int y0, int p) {
   uint64_t* b = ring.bar(p);
   const int nz = g.n[0];
-  if ((unsigned)p >= (unsigned)nz && bc.type[0] == PPF_BC_DIRCHLET) {
+  if (ghost_plane(g, bc, p)) {
     asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(b)) : "memory");
     return;
   }
-  int pz = p;
-  if ((unsigned)p >= (unsigned)nz)
-    pz = bc.type[0] == PPF_BC_PERIODIC ? wrap_index(p, nz) : mirror_index(p, nz);
+  const int pz = wrap_index(p, nz);
   fence_proxy_async();
   mbar_expect_tx(b, (uint32_t)(m.BX * m.BY * sizeof(T)));
   tma_load_3d(ring.plane(p), map, x0 - kXOff, y0 - m.H, pz, b);
 }
 
 // Rewrite the cells of plane p that the TMA box could not supply: columns or
-// rows outside the grid (edge tiles), or the whole plane on a DIRCHLET z
-// ghost. Uses the generic boundary rule.
+// rows outside the grid (edge tiles), or the whole of a ghost plane. Uses the
+// generic boundary rule.
 template <typename T, int NS>
 __device__ __forceinline__ void fixup_plane(const PlaneRing<T, NS>& ring, const T* __restrict__ in,
                                             const Geo& g, const Bc<T>& bc, const MarchGeom& m,
                                             int x0, int y0, int p, bool xy_edge) {
-  const bool zfixed = (unsigned)p >= (unsigned)g.n[0] && bc.type[0] == PPF_BC_DIRCHLET;
+  const bool zfixed = ghost_plane(g, bc, p);
   if (!xy_edge && !zfixed) return;
   T* dst = ring.plane(p);
   const int W = m.TX + 2 * m.H, Hh = m.TY + 2 * m.H;

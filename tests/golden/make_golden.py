@@ -74,10 +74,11 @@ def main():
     prm = dict(restate.WARREN_DEFAULTS)
     for name, shape, center, r, bc, steps, alpha, seed in [
         ("warren_2d_neumann", (32, 32), (16, 16), 5, "NEUMANN", 10, 0.0, 0),
-        ("warren_2d_periodic_noise", (24, 28), (12, 14), 4, "PERIODIC", 4, 0.3, 7),
-        # half-integer centre: no cell sits exactly on the ridge between the
-        # seed and its periodic image, where grad(phi) = 0 and the angle
-        # arctan2(phi_y, phi_x) is set by rounding residue alone
+        # half-integer centres: no cell sits exactly on the seed's centre of
+        # symmetry or on the ridge between the seed and its periodic image,
+        # where grad(phi) = 0 and the angle arctan2(phi_y, phi_x) is set by
+        # rounding residue alone
+        ("warren_2d_periodic_noise", (24, 28), (11.5, 13.5), 4, "PERIODIC", 4, 0.3, 7),
         ("warren_2d_mixed_edge", (20, 16), (2, 7.5), 5, ["NEUMANN", "PERIODIC"], 5, 0.0, 0),
     ]:
         phi0 = disk_seed(shape, center, r)

@@ -145,8 +145,10 @@ def test_warren_vs_oracle_noise_and_edges(cuda):
     shape = (45, 70)
     phi0 = np.ones(shape)
     yy, xx = np.mgrid[0:shape[0], 0:shape[1]]
-    phi0[(yy - 3) ** 2 + (xx - 60) ** 2 < 49] = 0.0
-    phi0[(yy - 30) ** 2 + (xx - 20) ** 2 < 36] = 0.0
+    # half-integer seed centres: no cell on a centre of symmetry (see the
+    # golden generator for why such cells are excluded from fp32 parity)
+    phi0[(yy - 3.5) ** 2 + (xx - 60.5) ** 2 < 49] = 0.0
+    phi0[(yy - 30.5) ** 2 + (xx - 20.5) ** 2 < 36] = 0.0
     c0 = 0.40783 + rng.uniform(-1e-3, 1e-3, shape)
     p = dict(restate.WARREN_DEFAULTS, alpha=0.3)
     for bc in ("NEUMANN", "PERIODIC", ["PERIODIC", "NEUMANN"]):
