@@ -1,12 +1,13 @@
 // Warren-Boettinger (1995) binary-alloy solidification step, fused.
 //
-// Persistent CTAs walk 32 x 32 tiles. For each tile, TMA stages phi and c
-// with a one-cell halo (ghost rule applied to edge tiles), the CTA computes
-// the pointwise solute
+// Each warp owns a 30-column x 8-row block and marches down it; phi and c
+// come from global memory (L2-resident at the benchmark size) with the ghost
+// rule applied at load time. Per cell it computes the pointwise solute
 // diffusivity D_C(phi) and the solute-trapping flux coefficient temp(phi, c)
-// once per staged cell into shared memory, then evaluates the full phi and c
-// updates (anisotropic phase-field term, noise, non-flux-form solute update)
-// and writes phi' and c'. One HBM read and one write of each field per step.
+// once (neighbours get them by shuffles or from the register window), then
+// evaluates the full phi and c updates (anisotropic phase-field term, noise,
+// non-flux-form solute update) and writes phi' and c'. One HBM read and one
+// write of each field per step.
 //
 // Reference: engine_Warren1995 (Engines/Warren1995.py:50-92), helpers
 // _p, _g, _gprime (:17-28) and gradx/grady/gradxx/gradyy (:30-48). Axis 0 of
@@ -14,7 +15,6 @@
 #include <cmath>
 
 #include "ppf_common.cuh"
-#include "ppf_tma.cuh"
 
 namespace ppf {
 namespace {
@@ -50,21 +50,16 @@ __device__ __forceinline__ void w95_point(const W95Coef<T>& k, T phi, T c,
   Qt = Dt * k.vr * c * (T(1) - c) * dH;
 }
 
-// Tile geometry: 32 x 32 cells. Lane l owns column l; warp w owns the kR = 4
-// consecutive rows 4w .. 4w+3 and sweeps down them keeping the
-// north/centre/south values of its column in registers (12 shared-memory
-// loads per cell instead of 25).
-constexpr int kTX = 32;
-constexpr int kR = 4;
-constexpr int kTY = (kThreads / 32) * kR;
-constexpr int kW = kTX + 2;  // pointwise region (tile + 1-cell halo)
-constexpr int kH = kTY + 2;
-constexpr int kN = kW * kH;
-// TMA box: 16-byte aligned start 4 columns left of the tile, 1-row halo.
-constexpr int kXOff = 4;
-constexpr int kBX = kTX + 2 * kXOff;
-constexpr int kBY = kTY + 2;
-constexpr int kRaw = kXOff - 1;  // raw column of region column 0
+// Work split: a warp owns a strip of kStrip = 30 output columns (lanes 1..30;
+// lanes 0 and 31 carry the west/east halo columns) and a band of kRows rows.
+// It marches down the band keeping the north/centre/south values of its
+// column in registers and gets west/east neighbours by warp shuffles: no
+// shared memory and no block-wide barriers. The next row's phi and c are
+// loaded one row ahead of use.
+constexpr int kStrip = 30;
+constexpr int kRows = 8;
+constexpr int kWarpsPerCta = 4;
+constexpr int kCtaThreads = 32 * kWarpsPerCta;
 
 __device__ __forceinline__ float inv_norm(float r2) { return rsqrtf(r2); }
 __device__ __forceinline__ double inv_norm(double r2) { return rsqrt(r2); }
@@ -78,226 +73,127 @@ template <>
 __device__ __forceinline__ double tiny_r2<double>() { return 0.0; }
 
 template <typename T>
-constexpr int raw_elems() {
-  return ((kBX * kBY * (int)sizeof(T) + 127) / 128 * 128) / (int)sizeof(T);
-}
-template <typename T>
-size_t w95_smem_bytes() {
-  return 128 + (size_t)4 * raw_elems<T>() * sizeof(T) + (size_t)2 * kN * sizeof(T);
-}
-
-template <typename T>
-__device__ __forceinline__ T* align128(unsigned char* p) {
-  return reinterpret_cast<T*>((reinterpret_cast<uintptr_t>(p) + 127) & ~uintptr_t(127));
-}
-
-// Persistent kernel: CTA b processes tiles b, b + G, b + 2G, ... The phi and c
-// tiles of the next tile are fetched by TMA into the other half of a
-// two-stage ring while the current tile computes. Cells outside the grid
-// arrive zero-filled and are rewritten with the boundary rule on edge tiles.
-template <typename T>
-__global__ void __launch_bounds__(kThreads, 4)
-    warren1995_kernel(const __grid_constant__ CUtensorMap map_phi,
-                      const __grid_constant__ CUtensorMap map_c, W95Coef<T> k, Geo g, Bc<T> bc,
-                      const T* __restrict__ phi_in, const T* __restrict__ c_in,
-                      T* __restrict__ phi_out, T* __restrict__ c_out, uint64_t seed,
-                      uint64_t step, const uint64_t* __restrict__ step_base, int tiles_x,
-                      int ntiles, int* __restrict__ status) {
-  extern __shared__ unsigned char smem_raw[];
-  __shared__ __align__(8) uint64_t bars[2];
-  __shared__ int abort_flag;
-  constexpr int RE = raw_elems<T>();
-  T* base = align128<T>(smem_raw);
-  T* const sD = base + 4 * RE;
-  T* const sQ = sD + kN;
-  const int lane = threadIdx.x, warp = threadIdx.y;
-  const int tid = lane + 32 * warp;
-  const int ny = g.n[0], nx = g.n[1];
-  const bool leader = tid == 0;
-
-  if (leader) {
-    mbar_init(&bars[0], 1);
-    mbar_init(&bars[1], 1);
-    mbar_init_fence();
-    abort_flag = 0;
+__device__ __forceinline__ void load_cell(const T* __restrict__ phi, const T* __restrict__ c,
+                                          const Geo& g, const Bc<T>& bc, int row, int x,
+                                          bool x_in, T& p, T& cc) {
+  if (x_in && (unsigned)row < (unsigned)g.n[0]) {
+    const int64_t o = (int64_t)row * g.pitch + x;
+    p = __ldg(phi + o);
+    cc = __ldg(c + o);
+  } else {
+    p = fetch<T, 2>(phi, g, bc, 0, row, x);
+    cc = fetch<T, 2>(c, g, bc, 1, row, x);
   }
-  __syncthreads();
+}
+
+template <typename T>
+__device__ __forceinline__ T shfl_w(T v) { return __shfl_up_sync(0xffffffffu, v, 1); }
+template <typename T>
+__device__ __forceinline__ T shfl_e(T v) { return __shfl_down_sync(0xffffffffu, v, 1); }
+
+template <typename T>
+__global__ void __launch_bounds__(kCtaThreads)
+    warren1995_kernel(W95Coef<T> k, Geo g, Bc<T> bc, const T* __restrict__ phi_in,
+                      const T* __restrict__ c_in, T* __restrict__ phi_out,
+                      T* __restrict__ c_out, uint64_t seed, uint64_t step,
+                      const uint64_t* __restrict__ step_base) {
+  const int lane = threadIdx.x, warp = threadIdx.y;
+  const int ny = g.n[0], nx = g.n[1];
+  const int xs = blockIdx.x * kStrip - 1;  // column of lane 0
+  const int x = xs + lane;
+  const int y0 = (blockIdx.y * kWarpsPerCta + warp) * kRows;
+  if (y0 >= ny) return;  // whole warp: no shuffles are left pending
+  const bool x_in = xs >= 0 && xs + 31 < nx;
+  const bool owner = lane >= 1 && lane <= kStrip && x < nx;
+
   pdl_wait();
   pdl_launch_next();
   if (step_base) step += *step_base;
 
-  auto issue = [&](int t, int st) {
-    const int x0 = (t % tiles_x) * kTX, y0 = (t / tiles_x) * kTY;
-    fence_proxy_async();
-    mbar_expect_tx(&bars[st], (uint32_t)(2 * kBX * kBY * sizeof(T)));
-    tma_load_2d(base + (2 * st) * RE, &map_phi, x0 - kXOff, y0 - 1, &bars[st]);
-    tma_load_2d(base + (2 * st + 1) * RE, &map_c, x0 - kXOff, y0 - 1, &bars[st]);
-  };
+  // rows y0-1 and y0 enter the window
+  T pN, cN, p0, c0, DN, QN, D0, Q0;
+  load_cell(phi_in, c_in, g, bc, y0 - 1, x, x_in, pN, cN);
+  load_cell(phi_in, c_in, g, bc, y0, x, x_in, p0, c0);
+  w95_point(k, pN, cN, DN, QN);
+  w95_point(k, p0, c0, D0, Q0);
+  T pNW = shfl_w(pN), pNE = shfl_e(pN);
+  T pW = shfl_w(p0), pE = shfl_e(p0);
+  T nP, nC;  // row y0+1, loaded ahead
+  load_cell(phi_in, c_in, g, bc, y0 + 1, x, x_in, nP, nC);
+  const bool noisy = k.alpha != T(0);
 
-  int t = blockIdx.x;
-  if (leader && t < ntiles) issue(t, 0);
-  for (int it = 0; t < ntiles; ++it, t += gridDim.x) {
-    const int st = it & 1;
-    const int tn = t + gridDim.x;
-    if (leader && tn < ntiles) issue(tn, st ^ 1);
-    if (!mbar_wait(&bars[st], (uint32_t)((it >> 1) & 1))) abort_flag = 1;
-    __syncthreads();
-    if (abort_flag) {
-      if (leader) {
-        atomicOr(status, PPF_STATUS_TIMEOUT);
-        mbar_wait(&bars[st], (uint32_t)((it >> 1) & 1));
-        if (tn < ntiles) mbar_wait(&bars[st ^ 1], (uint32_t)(((it + 1) >> 1) & 1));
-      }
-      __syncthreads();
-      return;
+#pragma unroll 2
+  for (int r = 0; r < kRows; ++r) {
+    const int row = y0 + r;
+    const T pS = nP, cS = nC;
+    if (r + 1 < kRows) load_cell(phi_in, c_in, g, bc, row + 2, x, x_in, nP, nC);
+    T DS, QS;
+    w95_point(k, pS, cS, DS, QS);
+    const T pSW = shfl_w(pS), pSE = shfl_e(pS);
+    const T cW = shfl_w(c0), cE = shfl_e(c0);
+    const T DW = shfl_w(D0), DE = shfl_e(D0);
+    const T QW = shfl_w(Q0), QE = shfl_e(Q0);
+
+    // phi derivatives, unscaled: N/S is axis 0 (reference x), W/E axis 1 (y)
+    const T px = pN - pS;                 // 2dx * gradx(phi)
+    const T py = pW - pE;                 // 2dx * grady(phi)
+    const T pxx = (pN + pS) - T(2) * p0;  // dx^2 * gradxx(phi)
+    const T pyy = (pW + pE) - T(2) * p0;  // dx^2 * gradyy(phi)
+    const T lp = pxx + pyy;
+    const T pxy = T(0.25) * ((pNW - pSW) - (pNE - pSE));  // dx^2 * grady(gradx(phi))
+
+    // dc * dt  (Warren1995.py:69-71)
+    const T lc = ((cN + cS) - T(2) * c0) + ((cW + cE) - T(2) * c0);
+    const T dc = D0 * lc + T(0.25) * ((DN - DS) * (cN - cS) + (DW - DE) * (cW - cE)) +
+                 Q0 * lp + T(0.25) * ((QN - QS) * px + (QW - QE) * py);
+
+    // anisotropy (Warren1995.py:76-81) without trig: theta = atan2(py, px)
+    const T r2 = px * px + py * py;
+    T c2 = T(1), s2 = T(0);
+    if (r2 > tiny_r2<T>()) {
+      const T n = inv_norm(r2);
+      const T ux = px * n, uy = py * n;
+      c2 = ux * ux - uy * uy;
+      s2 = T(2) * ux * uy;
     }
-    const T* sP = base + (2 * st) * RE;
-    const T* sC = base + (2 * st + 1) * RE;
-    const int x0 = (t % tiles_x) * kTX, y0 = (t / tiles_x) * kTY;
+    const T c4 = c2 * c2 - s2 * s2;
+    const T s4 = T(2) * s2 * c2;
+    const T eta = T(1) + k.ye * c4;
+    const T etap = T(-4) * k.ye * s4;
+    const T etapp = T(-16) * k.ye * c4;
 
-    // ---- edge tiles: ghost cells by the boundary rule
-    if (x0 < 1 || y0 < 1 || x0 + kTX + 1 > nx || y0 + kTY + 1 > ny) {
-      T* wP = base + (2 * st) * RE;
-      T* wC = base + (2 * st + 1) * RE;
-      for (int i = tid; i < kN; i += kThreads) {
-        const int ly = i / kW, lx = i - ly * kW;
-        const int gy = y0 - 1 + ly, gx = x0 - 1 + lx;
-        if ((unsigned)gy >= (unsigned)ny || (unsigned)gx >= (unsigned)nx) {
-          wP[ly * kBX + lx + kRaw] = fetch<T, 2>(phi_in, g, bc, 0, gy, gx);
-          wC[ly * kBX + lx + kRaw] = fetch<T, 2>(c_in, g, bc, 1, gy, gx);
-        }
+    // dphi * dt  (Warren1995.py:82-86)
+    const T om = T(1) - p0;
+    const T g0 = p0 * p0 * om * om;
+    const T gp = p0 * (T(2) + p0 * (T(-6) + T(4) * p0));
+    const T HA = k.WA * gp + k.hA * g0;
+    const T HB = k.WB * gp + k.hB * g0;
+    const T Hs = (T(1) - c0) * HA + c0 * HB;
+    const T dtM = (T(1) - c0) * k.dtMA + c0 * k.dtMB;
+    const T dyx = pyy - pxx;
+    const T aniso = eta * eta * lp + eta * etap * (s2 * dyx + T(2) * c2 * pxy) +
+                    T(0.5) * (etap * etap + eta * etapp) * (T(-2) * s2 * pxy + lp + c2 * dyx);
+    T dphi = dtM * (k.e2 * aniso - Hs);
+    // noise (:85-86): cells with g(phi) = 0 get none (the term is
+    // proportional to g); the warp draws only if one of its cells needs it
+    const bool need = noisy && owner && g0 != T(0);
+    if (__any_sync(0xffffffffu, need)) {
+      const U4 w4 = noise_group(seed, step, (uint32_t)row, (uint32_t)(x >> 2));
+      const int j = x & 3;
+      const uint32_t w = j == 0 ? w4.x : (j == 1 ? w4.y : (j == 2 ? w4.z : w4.w));
+      if (need) {
+        const T u = T(w >> 8) * T(5.9604644775390625e-08);
+        dphi += dtM * k.alpha * (T(2) * u - T(1)) * (T(16) * g0) * Hs;
       }
-      __syncthreads();
     }
-
-    // ---- pointwise D~, Q~ on the (kTY+2) x (kTX+2) region
-    for (int i = tid; i < kN; i += kThreads) {
-      const int ly = i / kW, lx = i - ly * kW;
-      const int r = ly * kBX + lx + kRaw;
-      T Dt, Qt;
-      w95_point(k, sP[r], sC[r], Dt, Qt);
-      sD[i] = Dt;
-      sQ[i] = Qt;
+    if (owner && row < ny) {
+      const int64_t o = (int64_t)row * g.pitch + x;
+      phi_out[o] = p0 + dphi;
+      c_out[o] = c0 + dc;
     }
-    __syncthreads();
-
-    // ---- noise: the warp's 4 rows x 32 columns are 32 groups of 4 cells;
-    // lane l draws Philox for group (row l/8, columns 4*(l%8) ..) and the
-    // words are handed out with shuffles. Groups whose 4 cells all have
-    // g(phi) = 0 skip the draw: the noise term is proportional to g(phi).
-    const bool noisy = k.alpha != T(0);
-    U4 nz{0u, 0u, 0u, 0u};
-    const int ly0 = 1 + warp * kR;
-    if (noisy) {
-      const int gr = lane >> 3, gc = lane & 7;
-      const T* row = sP + (ly0 + gr) * kBX + 1 + 4 * gc + kRaw;
-      bool need = false;
-#pragma unroll
-      for (int j = 0; j < 4; ++j) need |= (row[j] != T(0)) && (row[j] != T(1));
-      if (need)
-        nz = noise_group(seed, step, (uint32_t)(y0 + warp * kR + gr),
-                         (uint32_t)((x0 >> 2) + gc));
-    }
-
-    // ---- register-blocked sweep down this warp's rows
-    const int lx = lane + 1;
-    const int gx = x0 + lane;
-    int ir = (ly0 - 1) * kBX + lx + kRaw;  // raw index (phi, c)
-    int id = (ly0 - 1) * kW + lx;          // region index (D~, Q~)
-    T pNW = sP[ir - 1], pN = sP[ir], pNE = sP[ir + 1];
-    T cN = sC[ir], DN = sD[id], QN = sQ[id];
-    ir += kBX;
-    id += kW;
-    T pW = sP[ir - 1], p0 = sP[ir], pE = sP[ir + 1];
-    T c0 = sC[ir], D0 = sD[id], Q0 = sQ[id];
-#pragma unroll
-    for (int r = 0; r < kR; ++r, ir += kBX, id += kW) {
-      const T cW = sC[ir - 1], cE = sC[ir + 1];
-      const T DW = sD[id - 1], DE = sD[id + 1];
-      const T QW = sQ[id - 1], QE = sQ[id + 1];
-      const T pSW = sP[ir + kBX - 1], pS = sP[ir + kBX], pSE = sP[ir + kBX + 1];
-      const T cS = sC[ir + kBX], DS = sD[id + kW], QS = sQ[id + kW];
-
-      // phi derivatives, unscaled: N/S is axis 0 (reference x), W/E axis 1 (y)
-      const T px = pN - pS;                 // 2dx * gradx(phi)
-      const T py = pW - pE;                 // 2dx * grady(phi)
-      const T pxx = (pN + pS) - T(2) * p0;  // dx^2 * gradxx(phi)
-      const T pyy = (pW + pE) - T(2) * p0;  // dx^2 * gradyy(phi)
-      const T lp = pxx + pyy;
-      const T pxy = T(0.25) * ((pNW - pSW) - (pNE - pSE));  // dx^2 * grady(gradx(phi))
-
-      // dc * dt  (Warren1995.py:69-71)
-      const T lc = ((cN + cS) - T(2) * c0) + ((cW + cE) - T(2) * c0);
-      const T dc = D0 * lc + T(0.25) * ((DN - DS) * (cN - cS) + (DW - DE) * (cW - cE)) +
-                   Q0 * lp + T(0.25) * ((QN - QS) * px + (QW - QE) * py);
-
-      // anisotropy (Warren1995.py:76-81) without trig: theta = atan2(py, px)
-      const T r2 = px * px + py * py;
-      T c2 = T(1), s2 = T(0);
-      if (r2 > tiny_r2<T>()) {
-        const T n = inv_norm(r2);
-        const T ux = px * n, uy = py * n;
-        c2 = ux * ux - uy * uy;
-        s2 = T(2) * ux * uy;
-      }
-      const T c4 = c2 * c2 - s2 * s2;
-      const T s4 = T(2) * s2 * c2;
-      const T eta = T(1) + k.ye * c4;
-      const T etap = T(-4) * k.ye * s4;
-      const T etapp = T(-16) * k.ye * c4;
-
-      // dphi * dt  (Warren1995.py:82-86)
-      const T om = T(1) - p0;
-      const T g0 = p0 * p0 * om * om;
-      const T gp = p0 * (T(2) + p0 * (T(-6) + T(4) * p0));
-      const T HA = k.WA * gp + k.hA * g0;
-      const T HB = k.WB * gp + k.hB * g0;
-      const T Hs = (T(1) - c0) * HA + c0 * HB;
-      const T dtM = (T(1) - c0) * k.dtMA + c0 * k.dtMB;
-      const T dyx = pyy - pxx;
-      const T aniso = eta * eta * lp + eta * etap * (s2 * dyx + T(2) * c2 * pxy) +
-                      T(0.5) * (etap * etap + eta * etapp) * (T(-2) * s2 * pxy + lp + c2 * dyx);
-      T dphi = dtM * (k.e2 * aniso - Hs);
-      if (noisy) {
-        const int src = r * 8 + (lane >> 2);
-        const uint32_t wx = __shfl_sync(0xffffffffu, nz.x, src);
-        const uint32_t wy = __shfl_sync(0xffffffffu, nz.y, src);
-        const uint32_t wz = __shfl_sync(0xffffffffu, nz.z, src);
-        const uint32_t ww = __shfl_sync(0xffffffffu, nz.w, src);
-        const int j = lane & 3;
-        const uint32_t w = j == 0 ? wx : (j == 1 ? wy : (j == 2 ? wz : ww));
-        if (g0 != T(0)) {
-          const T u = T(w >> 8) * T(5.9604644775390625e-08);
-          dphi += dtM * k.alpha * (T(2) * u - T(1)) * (T(16) * g0) * Hs;
-        }
-      }
-      const int gy = y0 + ly0 - 1 + r;
-      if (gy < ny && gx < nx) {
-        const int64_t o = (int64_t)gy * g.pitch + gx;
-        phi_out[o] = p0 + dphi;
-        c_out[o] = c0 + dc;
-      }
-      pNW = pW; pN = p0; pNE = pE; cN = c0; DN = D0; QN = Q0;
-      pW = pSW; p0 = pS; pE = pSE; c0 = cS; D0 = DS; Q0 = QS;
-    }
-    __syncthreads();  // stage st and D~/Q~ are rewritten next
+    pNW = pW; pN = p0; pNE = pE; cN = c0; DN = D0; QN = Q0;
+    pW = pSW; p0 = pS; pE = pSE; c0 = cS; D0 = DS; Q0 = QS;
   }
-}
-
-// CTAs of `kern` resident per SM, and the SM count (cached per process).
-template <typename K>
-int resident_ctas(K kern, size_t smem, int* sms) {
-  static int cached_sms = 0;
-  if (!cached_sms) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&cached_sms, cudaDevAttrMultiProcessorCount, dev);
-  }
-  *sms = cached_sms;
-  int n = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kern, kThreads, smem) != cudaSuccess)
-    n = 1;
-  return n > 0 ? n : 1;
 }
 
 template <typename T>
@@ -322,9 +218,9 @@ int32_t warren1995(const PpfWarren1995Params* p, const PpfGrid* grid,
     return fail(PPF_ERR_UNSUPPORTED, "Warren1995 advances one step per pass");
   Bc<T> bc;
   if ((rc = make_bc<T>(b, g, p->dx, 2, 1, &bc))) return rc;
-  if (tiling && ((tiling->tile_x && tiling->tile_x != kTX) ||
-                 (tiling->tile_y && tiling->tile_y != kTY)))
-    return fail(PPF_ERR_UNSUPPORTED, "Warren1995 tiles are %dx%d", kTX, kTY);
+  if (tiling && (tiling->tile_x || tiling->tile_y))
+    return fail(PPF_ERR_UNSUPPORTED, "Warren1995 uses a fixed %d-column x %d-row warp tiling",
+                kStrip, kRows);
 
   const double dx2 = p->dx * p->dx;
   W95Coef<T> k;
@@ -341,28 +237,13 @@ int32_t warren1995(const PpfWarren1995Params* p, const PpfGrid* grid,
   k.ye = (T)p->y_e;
   k.alpha = (T)p->alpha;
 
-  const uint64_t dims[2] = {(uint64_t)g.n[1], (uint64_t)g.n[0]};
-  const uint64_t strides[1] = {(uint64_t)g.pitch * sizeof(T)};
-  const uint32_t box[2] = {(uint32_t)kBX, (uint32_t)kBY};
-  CUtensorMap mp, mc;
-  if ((rc = tensor_map(&mp, phi_in, (int)sizeof(T), 2, dims, strides, box))) return rc;
-  if ((rc = tensor_map(&mc, c_in, (int)sizeof(T), 2, dims, strides, box))) return rc;
-  int* st = status_ptr();
-  if (!st) return fail(PPF_ERR_CUDA, "status word unavailable");
-
-  auto kern = warren1995_kernel<T>;
-  const size_t smem = w95_smem_bytes<T>();
-  PPF_TRY_CUDA(allow_smem(kern, smem));
-  const int tiles_x = (g.n[1] + kTX - 1) / kTX;
-  const long ntiles = (long)tiles_x * ((g.n[0] + kTY - 1) / kTY);
-  if (ntiles > (1L << 30)) return fail(PPF_ERR_INVALID, "grid too large");
-  int sms = 0;
-  const int per_sm = resident_ctas(kern, smem, &sms);
-  const long slots = (long)per_sm * sms;
-  const int grid_x = (int)(ntiles < slots ? ntiles : slots);
-  PPF_TRY_CUDA(launch(kern, dim3(grid_x), dim3(32, kThreads / 32), smem, (cudaStream_t)stream,
-                      tiling && tiling->pdl, mp, mc, k, g, bc, phi_in, c_in, phi_out, c_out, seed,
-                      step, step_base, tiles_x, (int)ntiles, st));
+  const long strips = (g.n[1] + kStrip - 1) / kStrip;
+  const long bands = (g.n[0] + kRows - 1) / kRows;
+  const long gy = (bands + kWarpsPerCta - 1) / kWarpsPerCta;
+  if (strips > (1L << 30) || gy > 65535) return fail(PPF_ERR_INVALID, "grid too large");
+  PPF_TRY_CUDA(launch(warren1995_kernel<T>, dim3((unsigned)strips, (unsigned)gy),
+                      dim3(32, kWarpsPerCta), 0, (cudaStream_t)stream, tiling && tiling->pdl, k,
+                      g, bc, phi_in, c_in, phi_out, c_out, seed, step, step_base));
   return PPF_OK;
 }
 
