@@ -167,8 +167,7 @@ def test_warren_pdl_bit_exact(cuda, shape):
     c0 = 0.40783 + rng.uniform(-1e-3, 1e-3, shape)
     p = dict(restate.WARREN_DEFAULTS, alpha=0.3)
     a = run_warren_gpu(phi0, c0, 6, "NEUMANN", 4.6e-8, p, seed=1, precision="fp32")
-    b = run_warren_gpu(phi0, c0, 6, "NEUMANN", 4.6e-8, p, seed=1, precision="fp32",
-                       tile=(32, 32), pdl=True)
+    b = run_warren_gpu(phi0, c0, 6, "NEUMANN", 4.6e-8, p, seed=1, precision="fp32", pdl=True)
     np.testing.assert_array_equal(a[0], b[0])
     np.testing.assert_array_equal(a[1], b[1])
 
