@@ -116,14 +116,24 @@ typedef struct PpfWarren1995Params {
 /* Launch shape of one explicit-step call. NULL selects the defaults
  * (depth 1, library-chosen tile). depth = time steps advanced per HBM pass
  * (temporal blocking, 1..8, 2-D Diffusion/Allen-Cahn only); tile_x/tile_y =
- * output tile per CTA (0 = default); pdl = 1 launches with programmatic
- * dependent launch so back-to-back steps overlap their launch latency. */
+ * output tile per CTA (0 = default; for Warren1995 tile_y is the number of
+ * rows each warp walks: 2, 4, 8 or 16); pdl = 1 launches with programmatic
+ * dependent launch so back-to-back steps overlap their launch latency;
+ * flags = PPF_TILING_* bits. */
 typedef struct PpfTiling {
   int32_t depth;
   int32_t tile_x;
   int32_t tile_y;
   int32_t pdl;
+  int32_t flags;
+  int32_t reserved;
 } PpfTiling;
+
+/* Warren1995: evaluate the full update on every cell. Without this flag a
+ * row of cells whose 3x3 neighbourhoods are all exactly phi = 1 (or all
+ * exactly 0) takes the exact reduced form phi' = phi, c' = c + D~ lap(c),
+ * bit-identical to the full form there (every phi term is exactly zero). */
+#define PPF_TILING_FULL_EVAL 1
 
 /* ---- library ---------------------------------------------------------- */
 

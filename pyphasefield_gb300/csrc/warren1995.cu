@@ -1,13 +1,13 @@
 // Warren-Boettinger (1995) binary-alloy solidification step, fused.
 //
-// Each warp owns a 30-column x 8-row block and marches down it; phi and c
+// Each warp owns a 30-column x ROWS-row block and marches down it; phi and c
 // come from global memory (L2-resident at the benchmark size) with the ghost
 // rule applied at load time. Per cell it computes the pointwise solute
 // diffusivity D_C(phi) and the solute-trapping flux coefficient temp(phi, c)
 // once (neighbours get them by shuffles or from the register window), then
 // evaluates the full phi and c updates (anisotropic phase-field term, noise,
-// non-flux-form solute update) and writes phi' and c'. One HBM read and one
-// write of each field per step.
+// non-flux-form solute update) and writes phi' and c'. One read and one write
+// of each field per step.
 //
 // Reference: engine_Warren1995 (Engines/Warren1995.py:50-92), helpers
 // _p, _g, _gprime (:17-28) and gradx/grady/gradxx/gradyy (:30-48). Axis 0 of
@@ -18,8 +18,6 @@
 
 namespace ppf {
 namespace {
-
-constexpr int kThreads = 256;
 
 // Host-folded constants (all differences below are unscaled: the 1/(2dx),
 // 1/dx^2 and dt factors are folded in here).
@@ -33,14 +31,14 @@ struct W95Coef {
   T vr;          // v_m / R
   T ye;          // anisotropy strength y_e
   T alpha;       // noise amplitude
+  int bulk;      // take the exact reduced form on bulk rows
 };
 
-// Pointwise part evaluated on every staged cell:
+// Pointwise part evaluated on every cell entering the window:
 //   Dt = dt/dx^2 * D_C,   D_C = D_S + p(phi) (D_L - D_S)          (:69)
 //   Qt = dt/dx^2 * temp,  temp = D_C v_m c (1-c) (H_B - H_A) / R   (:70)
 template <typename T>
-__device__ __forceinline__ void w95_point(const W95Coef<T>& k, T phi, T c,
-                                          T& Dt, T& Qt) {
+__device__ __forceinline__ void w95_point(const W95Coef<T>& k, T phi, T c, T& Dt, T& Qt) {
   const T p = phi * phi * phi * (T(10) + phi * (T(-15) + T(6) * phi));
   const T om = T(1) - phi;
   const T g = phi * phi * om * om;
@@ -51,13 +49,12 @@ __device__ __forceinline__ void w95_point(const W95Coef<T>& k, T phi, T c,
 }
 
 // Work split: a warp owns a strip of kStrip = 30 output columns (lanes 1..30;
-// lanes 0 and 31 carry the west/east halo columns) and a band of kRows rows.
+// lanes 0 and 31 carry the west/east halo columns) and a band of ROWS rows.
 // It marches down the band keeping the north/centre/south values of its
 // column in registers and gets west/east neighbours by warp shuffles: no
 // shared memory and no block-wide barriers. The next row's phi and c are
 // loaded one row ahead of use.
 constexpr int kStrip = 30;
-constexpr int kRows = 8;
 constexpr int kWarpsPerCta = 4;
 constexpr int kCtaThreads = 32 * kWarpsPerCta;
 
@@ -91,7 +88,7 @@ __device__ __forceinline__ T shfl_w(T v) { return __shfl_up_sync(0xffffffffu, v,
 template <typename T>
 __device__ __forceinline__ T shfl_e(T v) { return __shfl_down_sync(0xffffffffu, v, 1); }
 
-template <typename T>
+template <typename T, int ROWS>
 __global__ void __launch_bounds__(kCtaThreads)
     warren1995_kernel(W95Coef<T> k, Geo g, Bc<T> bc, const T* __restrict__ phi_in,
                       const T* __restrict__ c_in, T* __restrict__ phi_out,
@@ -101,7 +98,7 @@ __global__ void __launch_bounds__(kCtaThreads)
   const int ny = g.n[0], nx = g.n[1];
   const int xs = blockIdx.x * kStrip - 1;  // column of lane 0
   const int x = xs + lane;
-  const int y0 = (blockIdx.y * kWarpsPerCta + warp) * kRows;
+  const int y0 = (blockIdx.y * kWarpsPerCta + warp) * ROWS;
   if (y0 >= ny) return;  // whole warp: no shuffles are left pending
   const bool x_in = xs >= 0 && xs + 31 < nx;
   const bool owner = lane >= 1 && lane <= kStrip && x < nx;
@@ -123,84 +120,115 @@ __global__ void __launch_bounds__(kCtaThreads)
   const bool noisy = k.alpha != T(0);
 
 #pragma unroll 2
-  for (int r = 0; r < kRows; ++r) {
+  for (int r = 0; r < ROWS; ++r) {
     const int row = y0 + r;
     const T pS = nP, cS = nC;
-    if (r + 1 < kRows) load_cell(phi_in, c_in, g, bc, row + 2, x, x_in, nP, nC);
+    if (r + 1 < ROWS) load_cell(phi_in, c_in, g, bc, row + 2, x, x_in, nP, nC);
     T DS, QS;
     w95_point(k, pS, cS, DS, QS);
     const T pSW = shfl_w(pS), pSE = shfl_e(pS);
     const T cW = shfl_w(c0), cE = shfl_e(c0);
-    const T DW = shfl_w(D0), DE = shfl_e(D0);
-    const T QW = shfl_w(Q0), QE = shfl_e(Q0);
-
-    // phi derivatives, unscaled: N/S is axis 0 (reference x), W/E axis 1 (y)
-    const T px = pN - pS;                 // 2dx * gradx(phi)
-    const T py = pW - pE;                 // 2dx * grady(phi)
-    const T pxx = (pN + pS) - T(2) * p0;  // dx^2 * gradxx(phi)
-    const T pyy = (pW + pE) - T(2) * p0;  // dx^2 * gradyy(phi)
-    const T lp = pxx + pyy;
-    const T pxy = T(0.25) * ((pNW - pSW) - (pNE - pSE));  // dx^2 * grady(gradx(phi))
-
-    // dc * dt  (Warren1995.py:69-71)
     const T lc = ((cN + cS) - T(2) * c0) + ((cW + cE) - T(2) * c0);
-    const T dc = D0 * lc + T(0.25) * ((DN - DS) * (cN - cS) + (DW - DE) * (cW - cE)) +
-                 Q0 * lp + T(0.25) * ((QN - QS) * px + (QW - QE) * py);
+    T p1, c1;
 
-    // anisotropy (Warren1995.py:76-81) without trig: theta = atan2(py, px)
-    const T r2 = px * px + py * py;
-    T c2 = T(1), s2 = T(0);
-    if (r2 > tiny_r2<T>()) {
-      const T n = inv_norm(r2);
-      const T ux = px * n, uy = py * n;
-      c2 = ux * ux - uy * uy;
-      s2 = T(2) * ux * uy;
+    // Bulk row: every owned cell's 3x3 phi neighbourhood is exactly 1 (or
+    // exactly 0). There every phi difference, g(phi) and g'(phi) is exactly
+    // zero, so dphi = 0, D~ is uniform and Q~ = 0: the full expressions below
+    // reduce exactly to phi' = phi, c' = c + D~ lap(c).
+    bool bulk = true;
+    if (k.bulk && owner) {
+      const T v = p0;
+      bulk = (v == T(1) || v == T(0)) && pN == v && pS == v && pW == v && pE == v &&
+             pNW == v && pNE == v && pSW == v && pSE == v;
     }
-    const T c4 = c2 * c2 - s2 * s2;
-    const T s4 = T(2) * s2 * c2;
-    const T eta = T(1) + k.ye * c4;
-    const T etap = T(-4) * k.ye * s4;
-    const T etapp = T(-16) * k.ye * c4;
+    if (k.bulk && __all_sync(0xffffffffu, bulk)) {
+      p1 = p0;
+      c1 = c0 + D0 * lc;
+    } else {
+      const T DW = shfl_w(D0), DE = shfl_e(D0);
+      const T QW = shfl_w(Q0), QE = shfl_e(Q0);
 
-    // dphi * dt  (Warren1995.py:82-86)
-    const T om = T(1) - p0;
-    const T g0 = p0 * p0 * om * om;
-    const T gp = p0 * (T(2) + p0 * (T(-6) + T(4) * p0));
-    const T HA = k.WA * gp + k.hA * g0;
-    const T HB = k.WB * gp + k.hB * g0;
-    const T Hs = (T(1) - c0) * HA + c0 * HB;
-    const T dtM = (T(1) - c0) * k.dtMA + c0 * k.dtMB;
-    const T dyx = pyy - pxx;
-    const T aniso = eta * eta * lp + eta * etap * (s2 * dyx + T(2) * c2 * pxy) +
-                    T(0.5) * (etap * etap + eta * etapp) * (T(-2) * s2 * pxy + lp + c2 * dyx);
-    T dphi = dtM * (k.e2 * aniso - Hs);
-    // noise (:85-86): cells with g(phi) = 0 get none (the term is
-    // proportional to g); the warp draws only if one of its cells needs it
-    const bool need = noisy && owner && g0 != T(0);
-    if (__any_sync(0xffffffffu, need)) {
-      const U4 w4 = noise_group(seed, step, (uint32_t)row, (uint32_t)(x >> 2));
-      const int j = x & 3;
-      const uint32_t w = j == 0 ? w4.x : (j == 1 ? w4.y : (j == 2 ? w4.z : w4.w));
-      if (need) {
-        const T u = T(w >> 8) * T(5.9604644775390625e-08);
-        dphi += dtM * k.alpha * (T(2) * u - T(1)) * (T(16) * g0) * Hs;
+      // phi derivatives, unscaled: N/S is axis 0 (reference x), W/E axis 1 (y)
+      const T px = pN - pS;                 // 2dx * gradx(phi)
+      const T py = pW - pE;                 // 2dx * grady(phi)
+      const T pxx = (pN + pS) - T(2) * p0;  // dx^2 * gradxx(phi)
+      const T pyy = (pW + pE) - T(2) * p0;  // dx^2 * gradyy(phi)
+      const T lp = pxx + pyy;
+      const T pxy = T(0.25) * ((pNW - pSW) - (pNE - pSE));  // dx^2 * grady(gradx(phi))
+
+      // dc * dt  (Warren1995.py:69-71)
+      const T dc = D0 * lc + T(0.25) * ((DN - DS) * (cN - cS) + (DW - DE) * (cW - cE)) +
+                   Q0 * lp + T(0.25) * ((QN - QS) * px + (QW - QE) * py);
+
+      // anisotropy (Warren1995.py:76-81) without trig: theta = atan2(py, px)
+      const T r2 = px * px + py * py;
+      T c2 = T(1), s2 = T(0);
+      if (r2 > tiny_r2<T>()) {
+        const T n = inv_norm(r2);
+        const T ux = px * n, uy = py * n;
+        c2 = ux * ux - uy * uy;
+        s2 = T(2) * ux * uy;
       }
+      const T c4 = c2 * c2 - s2 * s2;
+      const T s4 = T(2) * s2 * c2;
+      const T eta = T(1) + k.ye * c4;
+      const T etap = T(-4) * k.ye * s4;
+      const T etapp = T(-16) * k.ye * c4;
+
+      // dphi * dt  (Warren1995.py:82-86)
+      const T om = T(1) - p0;
+      const T g0 = p0 * p0 * om * om;
+      const T gp = p0 * (T(2) + p0 * (T(-6) + T(4) * p0));
+      const T HA = k.WA * gp + k.hA * g0;
+      const T HB = k.WB * gp + k.hB * g0;
+      const T Hs = (T(1) - c0) * HA + c0 * HB;
+      const T dtM = (T(1) - c0) * k.dtMA + c0 * k.dtMB;
+      const T dyx = pyy - pxx;
+      const T aniso = eta * eta * lp + eta * etap * (s2 * dyx + T(2) * c2 * pxy) +
+                      T(0.5) * (etap * etap + eta * etapp) * (T(-2) * s2 * pxy + lp + c2 * dyx);
+      T dphi = dtM * (k.e2 * aniso - Hs);
+      // noise (:85-86): cells with g(phi) = 0 get none (the term is
+      // proportional to g); the warp draws only if one of its cells needs it
+      const bool need = noisy && owner && g0 != T(0);
+      if (__any_sync(0xffffffffu, need)) {
+        const U4 w4 = noise_group(seed, step, (uint32_t)row, (uint32_t)(x >> 2));
+        const int j = x & 3;
+        const uint32_t w = j == 0 ? w4.x : (j == 1 ? w4.y : (j == 2 ? w4.z : w4.w));
+        if (need) {
+          const T u = T(w >> 8) * T(5.9604644775390625e-08);
+          dphi += dtM * k.alpha * (T(2) * u - T(1)) * (T(16) * g0) * Hs;
+        }
+      }
+      p1 = p0 + dphi;
+      c1 = c0 + dc;
     }
     if (owner && row < ny) {
       const int64_t o = (int64_t)row * g.pitch + x;
-      phi_out[o] = p0 + dphi;
-      c_out[o] = c0 + dc;
+      phi_out[o] = p1;
+      c_out[o] = c1;
     }
     pNW = pW; pN = p0; pNE = pE; cN = c0; DN = D0; QN = Q0;
     pW = pSW; p0 = pS; pE = pSE; c0 = cS; D0 = DS; Q0 = QS;
   }
 }
 
+template <typename T, int ROWS>
+cudaError_t launch_rows(const W95Coef<T>& k, const Geo& g, const Bc<T>& bc, const T* phi_in,
+                        const T* c_in, T* phi_out, T* c_out, uint64_t seed, uint64_t step,
+                        const uint64_t* step_base, bool pdl, cudaStream_t s) {
+  const long strips = (g.n[1] + kStrip - 1) / kStrip;
+  const long bands = (g.n[0] + ROWS - 1) / ROWS;
+  const long gy = (bands + kWarpsPerCta - 1) / kWarpsPerCta;
+  if (strips > (1L << 30) || gy > 65535) return cudaErrorInvalidConfiguration;
+  return launch(warren1995_kernel<T, ROWS>, dim3((unsigned)strips, (unsigned)gy),
+                dim3(32, kWarpsPerCta), 0, s, pdl, k, g, bc, phi_in, c_in, phi_out, c_out, seed,
+                step, step_base);
+}
+
 template <typename T>
-int32_t warren1995(const PpfWarren1995Params* p, const PpfGrid* grid,
-                   const PpfBoundary* b, const T* phi_in, const T* c_in,
-                   T* phi_out, T* c_out, uint64_t seed, uint64_t step,
-                   const uint64_t* step_base, const PpfTiling* tiling,
+int32_t warren1995(const PpfWarren1995Params* p, const PpfGrid* grid, const PpfBoundary* b,
+                   const T* phi_in, const T* c_in, T* phi_out, T* c_out, uint64_t seed,
+                   uint64_t step, const uint64_t* step_base, const PpfTiling* tiling,
                    void* stream) {
   clear_error();
   if (!p) return fail(PPF_ERR_INVALID, "params is NULL");
@@ -209,8 +237,7 @@ int32_t warren1995(const PpfWarren1995Params* p, const PpfGrid* grid,
   Geo g;
   int32_t rc = make_geo(grid, 2, 2, &g);
   if (rc) return rc;
-  if (!phi_in || !c_in || !phi_out || !c_out)
-    return fail(PPF_ERR_INVALID, "NULL field pointer");
+  if (!phi_in || !c_in || !phi_out || !c_out) return fail(PPF_ERR_INVALID, "NULL field pointer");
   if (phi_in == phi_out || c_in == c_out || phi_in == c_out || c_in == phi_out ||
       phi_out == c_out)
     return fail(PPF_ERR_INVALID, "input and output fields must be distinct");
@@ -218,9 +245,9 @@ int32_t warren1995(const PpfWarren1995Params* p, const PpfGrid* grid,
     return fail(PPF_ERR_UNSUPPORTED, "Warren1995 advances one step per pass");
   Bc<T> bc;
   if ((rc = make_bc<T>(b, g, p->dx, 2, 1, &bc))) return rc;
-  if (tiling && (tiling->tile_x || tiling->tile_y))
-    return fail(PPF_ERR_UNSUPPORTED, "Warren1995 uses a fixed %d-column x %d-row warp tiling",
-                kStrip, kRows);
+  if (tiling && tiling->tile_x && tiling->tile_x != kStrip)
+    return fail(PPF_ERR_UNSUPPORTED, "Warren1995 warps own %d columns", kStrip);
+  const int rows = tiling && tiling->tile_y ? tiling->tile_y : 4;
 
   const double dx2 = p->dx * p->dx;
   W95Coef<T> k;
@@ -236,14 +263,19 @@ int32_t warren1995(const PpfWarren1995Params* p, const PpfGrid* grid,
   k.vr = (T)(p->v_m / p->R);
   k.ye = (T)p->y_e;
   k.alpha = (T)p->alpha;
+  k.bulk = !(tiling && (tiling->flags & PPF_TILING_FULL_EVAL));
 
-  const long strips = (g.n[1] + kStrip - 1) / kStrip;
-  const long bands = (g.n[0] + kRows - 1) / kRows;
-  const long gy = (bands + kWarpsPerCta - 1) / kWarpsPerCta;
-  if (strips > (1L << 30) || gy > 65535) return fail(PPF_ERR_INVALID, "grid too large");
-  PPF_TRY_CUDA(launch(warren1995_kernel<T>, dim3((unsigned)strips, (unsigned)gy),
-                      dim3(32, kWarpsPerCta), 0, (cudaStream_t)stream, tiling && tiling->pdl, k,
-                      g, bc, phi_in, c_in, phi_out, c_out, seed, step, step_base));
+  const bool pdl = tiling && tiling->pdl;
+  const cudaStream_t s = (cudaStream_t)stream;
+  cudaError_t e;
+  switch (rows) {
+    case 2: e = launch_rows<T, 2>(k, g, bc, phi_in, c_in, phi_out, c_out, seed, step, step_base, pdl, s); break;
+    case 4: e = launch_rows<T, 4>(k, g, bc, phi_in, c_in, phi_out, c_out, seed, step, step_base, pdl, s); break;
+    case 8: e = launch_rows<T, 8>(k, g, bc, phi_in, c_in, phi_out, c_out, seed, step, step_base, pdl, s); break;
+    case 16: e = launch_rows<T, 16>(k, g, bc, phi_in, c_in, phi_out, c_out, seed, step, step_base, pdl, s); break;
+    default: return fail(PPF_ERR_INVALID, "Warren1995 rows per warp must be 2, 4, 8 or 16");
+  }
+  if (e != cudaSuccess) return fail(PPF_ERR_CUDA, "warren1995 launch: %s", cudaGetErrorString(e));
   return PPF_OK;
 }
 
@@ -255,22 +287,20 @@ using namespace ppf;
 extern "C" {
 
 int32_t ppf_warren1995_step_f32(const PpfWarren1995Params* p, const PpfGrid* g,
-                                const PpfBoundary* bc, const float* phi_in,
-                                const float* c_in, float* phi_out, float* c_out,
-                                uint64_t seed, uint64_t step,
-                                const uint64_t* step_base,
-                                const PpfTiling* tiling, void* stream) {
-  return warren1995<float>(p, g, bc, phi_in, c_in, phi_out, c_out, seed, step,
-                           step_base, tiling, stream);
+                                const PpfBoundary* bc, const float* phi_in, const float* c_in,
+                                float* phi_out, float* c_out, uint64_t seed, uint64_t step,
+                                const uint64_t* step_base, const PpfTiling* tiling,
+                                void* stream) {
+  return warren1995<float>(p, g, bc, phi_in, c_in, phi_out, c_out, seed, step, step_base,
+                           tiling, stream);
 }
 int32_t ppf_warren1995_step_f64(const PpfWarren1995Params* p, const PpfGrid* g,
-                                const PpfBoundary* bc, const double* phi_in,
-                                const double* c_in, double* phi_out,
-                                double* c_out, uint64_t seed, uint64_t step,
-                                const uint64_t* step_base,
-                                const PpfTiling* tiling, void* stream) {
-  return warren1995<double>(p, g, bc, phi_in, c_in, phi_out, c_out, seed, step,
-                            step_base, tiling, stream);
+                                const PpfBoundary* bc, const double* phi_in, const double* c_in,
+                                double* phi_out, double* c_out, uint64_t seed, uint64_t step,
+                                const uint64_t* step_base, const PpfTiling* tiling,
+                                void* stream) {
+  return warren1995<double>(p, g, bc, phi_in, c_in, phi_out, c_out, seed, step, step_base,
+                            tiling, stream);
 }
 
 }  // extern "C"

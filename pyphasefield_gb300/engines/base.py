@@ -113,7 +113,8 @@ class GB300Engine:
 
     def _ppf_tiling(self, depth: int):
         ud = self.user_data
-        return tiling_struct(depth, ud.get("tile"), ud.get("pdl", True))
+        flags = 0 if ud.get("bulk_shortcut", True) else L.PPF_TILING_FULL_EVAL
+        return tiling_struct(depth, ud.get("tile"), ud.get("pdl", True), flags)
 
     # ------------------------------------------------------------ lifecycle
     def just_before_simulating(self):

@@ -120,7 +120,7 @@ def warren_params_struct(params, dx):
 
 
 def run_warren_gpu(phi0, c0, steps, bc, dx, params, seed=0, precision="fp64", tile=None,
-                   pdl=False, device="cuda", values=None, step0=0):
+                   pdl=False, device="cuda", values=None, step0=0, full_eval=False):
     import torch
     from pyphasefield_gb300 import _lib as L
     dtype = torch.float64 if precision == "fp64" else torch.float32
@@ -133,6 +133,7 @@ def run_warren_gpu(phi0, c0, steps, bc, dx, params, seed=0, precision="fp64", ti
     t.depth = 1
     t.tile_x, t.tile_y = (tile if tile else (0, 0))
     t.pdl = 1 if pdl else 0
+    t.flags = L.PPF_TILING_FULL_EVAL if full_eval else 0
     s = C.c_void_p(torch.cuda.current_stream().cuda_stream)
     for k in range(steps):
         L.call(f"ppf_warren1995_step_{sfx}", C.byref(prm), C.byref(g), C.byref(b),

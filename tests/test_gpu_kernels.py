@@ -203,3 +203,24 @@ def test_no_timeouts_recorded(cuda):
                    1.0, 0.01, M=1.0, epsilon=1.0)
     L.call("ppf_status_take", C.byref(st))
     assert st.value == 0
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+def test_warren_bulk_shortcut_and_rows_bit_exact(cuda, precision):
+    """The exact reduced form on bulk rows (phi exactly 1 or 0 around every
+    cell) and the rows-per-warp choice change nothing, bit for bit."""
+    rng = np.random.default_rng(23)
+    shape = (150, 200)
+    phi0 = np.ones(shape)
+    yy, xx = np.mgrid[0:shape[0], 0:shape[1]]
+    phi0[(yy - 60.5) ** 2 + (xx - 100.5) ** 2 < 100] = 0.0   # solid seed (phi = 0 bulk inside)
+    phi0[(yy - 20.5) ** 2 + (xx - 170.5) ** 2 < 16] = 0.3
+    c0 = 0.40783 + rng.uniform(-1e-3, 1e-3, shape)
+    p = dict(restate.WARREN_DEFAULTS, alpha=0.3)
+    full = run_warren_gpu(phi0, c0, 20, "NEUMANN", 4.6e-8, p, seed=5, precision=precision,
+                          full_eval=True)
+    for rows in (2, 4, 8, 16):
+        got = run_warren_gpu(phi0, c0, 20, "NEUMANN", 4.6e-8, p, seed=5, precision=precision,
+                             tile=(0, rows))
+        np.testing.assert_array_equal(got[0], full[0])
+        np.testing.assert_array_equal(got[1], full[1])
