@@ -24,6 +24,7 @@ temporal_depth (steps per HBM pass, 2-D Diffusion/Allen-Cahn), tile
 from __future__ import annotations
 
 import ctypes as C
+import gc
 
 import numpy as np
 import torch
@@ -203,6 +204,11 @@ class GB300Engine:
         sp = C.c_void_p(s.cuda_stream)
         cur0 = self._ppf_cur
         total = sum(depths)
+        # No Python garbage collection while capturing: collecting another
+        # engine would free its pinned staging buffers and graphs, and those
+        # CUDA calls would invalidate the capture.
+        gc_was_enabled = gc.isenabled()
+        gc.disable()
         L.call("ppf_graph_begin", sp)
         exec_ = C.c_void_p()
         try:
@@ -214,8 +220,12 @@ class GB300Engine:
                     off += d
                 L.call("ppf_counter_add_u64", ptr(self._ppf_stepctr), C.c_uint64(total), sp)
         finally:
-            L.call("ppf_graph_end", sp, C.byref(exec_))
-            self._ppf_cur = cur0
+            try:
+                L.call("ppf_graph_end", sp, C.byref(exec_))
+            finally:
+                self._ppf_cur = cur0
+                if gc_was_enabled:
+                    gc.enable()
         self._ppf_graphs[key] = exec_
         return exec_
 
