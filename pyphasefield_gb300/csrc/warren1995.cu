@@ -107,23 +107,23 @@ __global__ void __launch_bounds__(kCtaThreads)
   pdl_launch_next();
   if (step_base) step += *step_base;
 
-  // rows y0-1 and y0 enter the window
-  T pN, cN, p0, c0, DN, QN, D0, Q0;
-  load_cell(phi_in, c_in, g, bc, y0 - 1, x, x_in, pN, cN);
-  load_cell(phi_in, c_in, g, bc, y0, x, x_in, p0, c0);
+  // All ROWS + 2 rows of the band (with the halo rows) are requested before
+  // any is used, so each warp keeps 2 (ROWS + 2) loads in flight.
+  T bp[ROWS + 2], bcv[ROWS + 2];
+#pragma unroll
+  for (int j = 0; j < ROWS + 2; ++j) load_cell(phi_in, c_in, g, bc, y0 - 1 + j, x, x_in, bp[j], bcv[j]);
+
+  T pN = bp[0], cN = bcv[0], p0 = bp[1], c0 = bcv[1], DN, QN, D0, Q0;
   w95_point(k, pN, cN, DN, QN);
   w95_point(k, p0, c0, D0, Q0);
   T pNW = shfl_w(pN), pNE = shfl_e(pN);
   T pW = shfl_w(p0), pE = shfl_e(p0);
-  T nP, nC;  // row y0+1, loaded ahead
-  load_cell(phi_in, c_in, g, bc, y0 + 1, x, x_in, nP, nC);
   const bool noisy = k.alpha != T(0);
 
-#pragma unroll 2
+#pragma unroll
   for (int r = 0; r < ROWS; ++r) {
     const int row = y0 + r;
-    const T pS = nP, cS = nC;
-    if (r + 1 < ROWS) load_cell(phi_in, c_in, g, bc, row + 2, x, x_in, nP, nC);
+    const T pS = bp[r + 2], cS = bcv[r + 2];
     T DS, QS;
     w95_point(k, pS, cS, DS, QS);
     const T pSW = shfl_w(pS), pSE = shfl_e(pS);
