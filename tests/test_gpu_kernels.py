@@ -206,9 +206,11 @@ def test_no_timeouts_recorded(cuda):
 
 
 @pytest.mark.parametrize("precision", ["fp32", "fp64"])
-def test_warren_bulk_shortcut_and_rows_bit_exact(cuda, precision):
+def test_warren_bulk_shortcut_bit_exact_and_rows(cuda, precision):
     """The exact reduced form on bulk rows (phi exactly 1 or 0 around every
-    cell) and the rows-per-warp choice change nothing, bit for bit."""
+    cell) changes nothing, bit for bit, for every rows-per-warp choice; the
+    rows-per-warp choices agree to rounding (each is its own compiled kernel,
+    so multiply-add contraction may differ)."""
     rng = np.random.default_rng(23)
     shape = (150, 200)
     phi0 = np.ones(shape)
@@ -217,10 +219,15 @@ def test_warren_bulk_shortcut_and_rows_bit_exact(cuda, precision):
     phi0[(yy - 20.5) ** 2 + (xx - 170.5) ** 2 < 16] = 0.3
     c0 = 0.40783 + rng.uniform(-1e-3, 1e-3, shape)
     p = dict(restate.WARREN_DEFAULTS, alpha=0.3)
-    full = run_warren_gpu(phi0, c0, 20, "NEUMANN", 4.6e-8, p, seed=5, precision=precision,
-                          full_eval=True)
+    ref = None
     for rows in (2, 4, 8, 16):
+        full = run_warren_gpu(phi0, c0, 20, "NEUMANN", 4.6e-8, p, seed=5, precision=precision,
+                              tile=(0, rows), full_eval=True)
         got = run_warren_gpu(phi0, c0, 20, "NEUMANN", 4.6e-8, p, seed=5, precision=precision,
                              tile=(0, rows))
         np.testing.assert_array_equal(got[0], full[0])
         np.testing.assert_array_equal(got[1], full[1])
+        if ref is None:
+            ref = full
+        tol = 1e-13 if precision == "fp64" else 1e-6
+        assert rel_l2(full[0], ref[0]) < tol and rel_l2(full[1], ref[1]) < tol
