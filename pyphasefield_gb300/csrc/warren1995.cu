@@ -88,14 +88,31 @@ __device__ __forceinline__ T shfl_w(T v) { return __shfl_up_sync(0xffffffffu, v,
 template <typename T>
 __device__ __forceinline__ T shfl_e(T v) { return __shfl_down_sync(0xffffffffu, v, 1); }
 
-// Updates the ROWS rows y0 .. y0+ROWS-1 of one 32-lane strip from the phi and
-// c values of rows y0-1 .. y0+ROWS (bp, bcv) and writes phi' and c'.
 template <typename T, int ROWS>
-__device__ __forceinline__ void w95_band(const W95Coef<T>& k, const Geo& g, const T (&bp)[ROWS + 2],
-                                         const T (&bcv)[ROWS + 2], int x, int y0, bool owner,
-                                         uint64_t seed, uint64_t step, T* __restrict__ phi_out,
-                                         T* __restrict__ c_out) {
-  const int ny = g.n[0];
+__global__ void __launch_bounds__(kCtaThreads)
+    warren1995_kernel(W95Coef<T> k, Geo g, Bc<T> bc, const T* __restrict__ phi_in,
+                      const T* __restrict__ c_in, T* __restrict__ phi_out,
+                      T* __restrict__ c_out, uint64_t seed, uint64_t step,
+                      const uint64_t* __restrict__ step_base) {
+  const int lane = threadIdx.x, warp = threadIdx.y;
+  const int ny = g.n[0], nx = g.n[1];
+  const int xs = blockIdx.x * kStrip - 1;  // column of lane 0
+  const int x = xs + lane;
+  const int y0 = (blockIdx.y * kWarpsPerCta + warp) * ROWS;
+  if (y0 >= ny) return;  // whole warp: no shuffles are left pending
+  const bool x_in = xs >= 0 && xs + 31 < nx;
+  const bool owner = lane >= 1 && lane <= kStrip && x < nx;
+
+  pdl_wait();
+  pdl_launch_next();
+  if (step_base) step += *step_base;
+
+  // All ROWS + 2 rows of the band (with the halo rows) are requested before
+  // any is used, so each warp keeps 2 (ROWS + 2) loads in flight.
+  T bp[ROWS + 2], bcv[ROWS + 2];
+#pragma unroll
+  for (int j = 0; j < ROWS + 2; ++j) load_cell(phi_in, c_in, g, bc, y0 - 1 + j, x, x_in, bp[j], bcv[j]);
+
   T pN = bp[0], cN = bcv[0], p0 = bp[1], c0 = bcv[1], DN, QN, D0, Q0;
   w95_point(k, pN, cN, DN, QN);
   w95_point(k, p0, c0, D0, Q0);
@@ -195,79 +212,17 @@ __device__ __forceinline__ void w95_band(const W95Coef<T>& k, const Geo& g, cons
   }
 }
 
-// Balanced persistent warps: the (strip, band) items are dealt round-robin
-// to nwarps warps (every warp gets the same count, +-1); each warp requests
-// the rows of its next item before computing the current one, so the
-// L2/HBM latency is paid once per launch rather than once per item.
-template <typename T, int ROWS>
-__global__ void __launch_bounds__(kCtaThreads)
-    warren1995_kernel(W95Coef<T> k, Geo g, Bc<T> bc, const T* __restrict__ phi_in,
-                      const T* __restrict__ c_in, T* __restrict__ phi_out,
-                      T* __restrict__ c_out, uint64_t seed, uint64_t step,
-                      const uint64_t* __restrict__ step_base, int strips, int nitems) {
-  const int lane = threadIdx.x;
-  const int nx = g.n[1];
-  const int nwarps = gridDim.x * kWarpsPerCta;
-  int it = blockIdx.x * kWarpsPerCta + threadIdx.y;
-  if (it >= nitems) return;  // whole warp: no shuffles are left pending
-
-  pdl_wait();
-  pdl_launch_next();
-  if (step_base) step += *step_base;
-
-  T bp[ROWS + 2], bcv[ROWS + 2], np_[ROWS + 2], nc_[ROWS + 2];
-  auto load_item = [&](int item, T (&p)[ROWS + 2], T (&c)[ROWS + 2]) {
-    const int xs = (item % strips) * kStrip - 1;
-    const int y0 = (item / strips) * ROWS;
-    const bool x_in = xs >= 0 && xs + 31 < nx;
-#pragma unroll
-    for (int j = 0; j < ROWS + 2; ++j)
-      load_cell(phi_in, c_in, g, bc, y0 - 1 + j, xs + lane, x_in, p[j], c[j]);
-  };
-  load_item(it, bp, bcv);
-  for (;;) {
-    const int nxt = it + nwarps;
-    if (nxt < nitems) load_item(nxt, np_, nc_);
-    const int xs = (it % strips) * kStrip - 1;
-    const int x = xs + lane;
-    const bool owner = lane >= 1 && lane <= kStrip && x < nx;
-    w95_band<T, ROWS>(k, g, bp, bcv, x, (it / strips) * ROWS, owner, seed, step, phi_out, c_out);
-    if (nxt >= nitems) break;
-    it = nxt;
-#pragma unroll
-    for (int j = 0; j < ROWS + 2; ++j) {
-      bp[j] = np_[j];
-      bcv[j] = nc_[j];
-    }
-  }
-}
-
 template <typename T, int ROWS>
 cudaError_t launch_rows(const W95Coef<T>& k, const Geo& g, const Bc<T>& bc, const T* phi_in,
                         const T* c_in, T* phi_out, T* c_out, uint64_t seed, uint64_t step,
                         const uint64_t* step_base, bool pdl, cudaStream_t s) {
   const long strips = (g.n[1] + kStrip - 1) / kStrip;
   const long bands = (g.n[0] + ROWS - 1) / ROWS;
-  const long nitems = strips * bands;
-  if (nitems > (1L << 30)) return cudaErrorInvalidConfiguration;
-  auto kern = warren1995_kernel<T, ROWS>;
-  // warps resident on the device, then the fewest warps that still give
-  // every warp the same item count (+-1)
-  static int sms = 0, per_sm = 0;
-  if (!sms) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kCtaThreads, 0) !=
-            cudaSuccess || per_sm < 1)
-      per_sm = 1;
-  }
-  const long resident = (long)sms * per_sm * kWarpsPerCta;
-  const long rounds = (nitems + resident - 1) / resident;
-  const long warps = (nitems + rounds - 1) / rounds;
-  const long ctas = (warps + kWarpsPerCta - 1) / kWarpsPerCta;
-  return launch(kern, dim3((unsigned)ctas), dim3(32, kWarpsPerCta), 0, s, pdl, k, g, bc, phi_in,
-                c_in, phi_out, c_out, seed, step, step_base, (int)strips, (int)nitems);
+  const long gy = (bands + kWarpsPerCta - 1) / kWarpsPerCta;
+  if (strips > (1L << 30) || gy > 65535) return cudaErrorInvalidConfiguration;
+  return launch(warren1995_kernel<T, ROWS>, dim3((unsigned)strips, (unsigned)gy),
+                dim3(32, kWarpsPerCta), 0, s, pdl, k, g, bc, phi_in, c_in, phi_out, c_out, seed,
+                step, step_base);
 }
 
 template <typename T>
@@ -292,7 +247,7 @@ int32_t warren1995(const PpfWarren1995Params* p, const PpfGrid* grid, const PpfB
   if ((rc = make_bc<T>(b, g, p->dx, 2, 1, &bc))) return rc;
   if (tiling && tiling->tile_x && tiling->tile_x != kStrip)
     return fail(PPF_ERR_UNSUPPORTED, "Warren1995 warps own %d columns", kStrip);
-  const int rows = tiling && tiling->tile_y ? tiling->tile_y : 4;
+  const int rows = tiling && tiling->tile_y ? tiling->tile_y : 2;
 
   const double dx2 = p->dx * p->dx;
   W95Coef<T> k;
