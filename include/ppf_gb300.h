@@ -212,6 +212,21 @@ int32_t ppf_reduce_sum_f32(const float* x, const PpfGrid* g, double* out,
                            void* scratch, size_t scratch_bytes, void* stream);
 int32_t ppf_reduce_sum_f64(const double* x, const PpfGrid* g, double* out,
                            void* scratch, size_t scratch_bytes, void* stream);
+/* Same result as ppf_reduce_sum_f32, for callers that cannot allocate
+ * device memory: a host application whose memory manager owns the whole
+ * GPU, or code that is not allowed to call cudaMalloc (or any allocating
+ * library routine) at the point where it needs the mass. It takes no
+ * scratch argument and allocates nothing: its partial sums live in a fixed
+ * 8 KiB device array inside the library (1024 doubles, one per first-pass
+ * CTA; grids needing more are rejected with PPF_ERR_INVALID, which the
+ * current split never does). The first call on each device looks up that
+ * array's device address (cudaGetSymbolAddress) with the device current;
+ * make that first call before any stream capture. Every call shares the
+ * array, so calls that overlap on the GPU (different streams, or different
+ * host threads, with no ordering between them) race and give wrong sums.
+ * No counterpart in the reference. */
+int32_t ppf_reduce_sum_f32_noalloc(const float* x, const PpfGrid* g, double* out,
+                                   void* stream);
 /* out[0] = dx^d * sum over cells of [w f(x) + kappa/2 |grad x|^2],
  * f(x) = x^2 (1-x)^2, forward differences with the boundary rule applied:
  * the free energy whose variation gives the Allen-Cahn (w = 16 W,

@@ -96,6 +96,7 @@ SIGNATURES: dict[str, list] = {
     "ppf_reduce_scratch_bytes": [PG, C.POINTER(SZ)],
     "ppf_reduce_sum_f32": [P, PG, P, P, SZ, P],
     "ppf_reduce_sum_f64": [P, PG, P, P, SZ, P],
+    "ppf_reduce_sum_f32_noalloc": [P, PG, P, P],
     "ppf_free_energy_f32": [P, PG, PB, C.c_double, C.c_double, C.c_double, P, P, SZ, P],
     "ppf_free_energy_f64": [P, PG, PB, C.c_double, C.c_double, C.c_double, P, P, SZ, P],
     "ppf_check_finite_f32": [P, PG, P, P],

@@ -162,11 +162,64 @@ int32_t reduce_impl(Op op, const T* x, const PpfGrid* grid, const PpfBoundary* b
   return PPF_OK;
 }
 
+// ------------------------------------------------------------ allocation-free sum
+// Scratch of ppf_reduce_sum_f32_noalloc: the per-CTA partial sums of pass 1
+// live in this fixed device array instead of caller-provided memory. Every
+// GPU that loads the library holds it (8 KiB) until the process exits.
+constexpr int kNoAllocPartials = 1024;
+static __device__ __align__(256) double g_noalloc_partials[kNoAllocPartials];
+
+// Device address of g_noalloc_partials on the current device. Host code must
+// not pass the symbol itself to a kernel (on the host it names a stand-in,
+// not device memory), so the address is looked up once per device, with that
+// device current, and cached.
+static int32_t noalloc_partials(double** out) {
+  static double* cached[64] = {};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return fail(PPF_ERR_CUDA, "cudaGetDevice: %s", cudaGetErrorString(e));
+  if (dev < 0 || dev >= 64) return fail(PPF_ERR_UNSUPPORTED, "device %d out of range", dev);
+  if (!cached[dev]) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_noalloc_partials);
+    if (e != cudaSuccess)
+      return fail(PPF_ERR_CUDA, "cudaGetSymbolAddress: %s", cudaGetErrorString(e));
+    cached[dev] = static_cast<double*>(p);
+  }
+  *out = cached[dev];
+  return PPF_OK;
+}
+
 }  // namespace ppf
 
 using namespace ppf;
 
 extern "C" {
+
+int32_t ppf_reduce_sum_f32_noalloc(const float* x, const PpfGrid* grid, double* out,
+                                   void* stream) {
+  clear_error();
+  Geo g;
+  int32_t rc = make_geo(grid, 2, 3, &g);
+  if (rc) return rc;
+  if (!x || !out) return fail(PPF_ERR_INVALID, "NULL pointer");
+  const int64_t rows = g.ndim == 2 ? (int64_t)g.n[0] : (int64_t)g.n[0] * g.n[1];
+  const int nb = reduce_blocks(rows);
+  if (nb > kNoAllocPartials)
+    return fail(PPF_ERR_INVALID,
+                "grid needs %d partial sums; the allocation-free sum holds at most %d", nb,
+                kNoAllocPartials);
+  double* partials = nullptr;
+  if ((rc = noalloc_partials(&partials))) return rc;
+  Bc<float> bc{};
+  EnergyCoef<float> k{0.0, 0.0};
+  cudaStream_t s = (cudaStream_t)stream;
+  reduce_pass1<float, SumOp><<<nb, kRedThreads, 0, s>>>(SumOp{}, x, g, bc, k, partials);
+  PPF_TRY_CUDA(cudaGetLastError());
+  reduce_pass2<<<1, kRedThreads, 0, s>>>(partials, nb, 1.0, out);
+  PPF_TRY_CUDA(cudaGetLastError());
+  return PPF_OK;
+}
 
 int32_t ppf_reduce_scratch_bytes(const PpfGrid* grid, size_t* bytes) {
   clear_error();
