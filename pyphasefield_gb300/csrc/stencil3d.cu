@@ -238,7 +238,35 @@ __device__ __forceinline__ T ch_flux(const ChCoef<T>& k, T mn, T mc) {
   return f;
 }
 
-constexpr int kNSC = 6;  // c planes z..z+2 in use; z+3, z+4 in flight
+constexpr int kNSC = 6;  // c planes z..z+2 read, z+3 and z+4 in flight
+// Cahn-Hilliard tile: 32 x 16 cells, 256 threads; thread (tx, ty) owns the
+// xy-columns (ty, tx) and (ty + 8, tx) and keeps, per column, c(z..z+2) and
+// mu(z-1..z+1) in registers while marching along z. mu of the tile plus a
+// one-cell ring is kept in a two-plane shared ring for the xy fluxes; the
+// kRingN ring positions are computed by threads 0..kRingN-1.
+constexpr int kCTX = 32;
+constexpr int kCTY = 16;
+constexpr int kMW = kCTX + 2;
+constexpr int kMH = kCTY + 2;
+constexpr int kMN = kMW * kMH;
+constexpr int kRingN = kMN - kCTX * kCTY;  // 100
+
+// Ring position i -> mu-region coordinates (ly, lx) on the border.
+__device__ __forceinline__ void ring_pos(int i, int& ly, int& lx) {
+  if (i < kMW) {
+    ly = 0;
+    lx = i;
+  } else if (i < 2 * kMW) {
+    ly = kMH - 1;
+    lx = i - kMW;
+  } else if (i < 2 * kMW + kCTY) {
+    ly = 1 + (i - 2 * kMW);
+    lx = 0;
+  } else {
+    ly = 1 + (i - 2 * kMW - kCTY);
+    lx = kMW - 1;
+  }
+}
 
 template <typename T, bool QUANT>
 __global__ void __launch_bounds__(kThreads)
@@ -250,17 +278,33 @@ __global__ void __launch_bounds__(kThreads)
   __shared__ __align__(8) uint64_t bars[kNSC];
   __shared__ int abort_flag;
   __shared__ double red[kThreads / 32];
-  const int x0 = blockIdx.x * m.TX, y0 = blockIdx.y * m.TY, z0 = blockIdx.z * m.ZC;
+  const int tx = threadIdx.x, ty = threadIdx.y, tid = tx + 32 * ty;
+  const int x0 = blockIdx.x * kCTX, y0 = blockIdx.y * kCTY, z0 = blockIdx.z * m.ZC;
   const int nz = g.n[0], ny = g.n[1], nx = g.n[2];
   const int z1 = min(z0 + m.ZC, nz);
-  const bool xy_edge = x0 - 2 < 0 || y0 - 2 < 0 || x0 + m.TX + 2 > nx || y0 + m.TY + 2 > ny ||
-                       x0 - kXOff < 0 || x0 + m.TX + kXOff > nx;
+  const bool xy_edge = x0 - kXOff < 0 || y0 - 2 < 0 || x0 + kCTX + kXOff > nx ||
+                       y0 + kCTY + 2 > ny;
   PlaneRing<T, kNSC> ring{align128<T>(smem_raw), bars, slot_elems, z0 - 2};
-  const int WM = m.TX + 2, HM = m.TY + 2, PM = WM * HM;  // mu planes, halo 1
-  T* mring = ring.slots + kNSC * slot_elems;
-  auto mslot = [&](int z) { return mring + ((z - z0 + 3) % 3) * PM; };
-  const bool leader = threadIdx.x == 0 && threadIdx.y == 0;
+  T* const mring = ring.slots + kNSC * slot_elems;  // 2 mu planes
+  auto mslot = [&](int z) { return mring + ((z - z0 + 2) & 1) * kMN; };
+  const bool leader = tid == 0;
   const int W = m.BX;
+
+  // own columns: c-plane index ci, mu-plane index mi
+  int ci[2], mi[2];
+#pragma unroll
+  for (int j = 0; j < 2; ++j) {
+    ci[j] = (ty + 8 * j + 2) * W + tx + kXOff;
+    mi[j] = (ty + 8 * j + 1) * kMW + tx + 1;
+  }
+  const bool has_ring = tid < kRingN;
+  int rci = 0, rmi = 0;
+  if (has_ring) {
+    int ly, lx;
+    ring_pos(tid, ly, lx);
+    rci = (ly + 1) * W + lx + (kXOff - 1);
+    rmi = ly * kMW + lx;
+  }
 
   if (leader) {
     for (int i = 0; i < kNSC; ++i) mbar_init(&bars[i], 1);
@@ -273,20 +317,6 @@ __global__ void __launch_bounds__(kThreads)
   const int last = z1 + 1;
   if (leader)
     for (int p = z0 - 2; p <= min(z0 + 3, last); ++p) issue_plane(ring, &map, g, bc, m, x0, y0, p);
-
-  // mu~ of plane z on the (TY+2) x (TX+2) region from c planes z-1, z, z+1
-  auto compute_mu = [&](int z) {
-    const T* cd = ring.plane(z - 1);
-    const T* cc = ring.plane(z);
-    const T* cu = ring.plane(z + 1);
-    T* mz = mslot(z);
-    for (int ly = threadIdx.y; ly < HM; ly += kThreads / 32)
-      for (int lx = threadIdx.x; lx < WM; lx += 32) {
-        const int i = (ly + 1) * W + lx + (kXOff - 1);
-        mz[ly * WM + lx] = ch_mu(k, cc[i], cc[i - 1], cc[i + 1], cc[i - W], cc[i + W], cd[i], cu[i]);
-      }
-  };
-
   for (int p = z0 - 2; p <= z0 + 1; ++p) {
     if (!wait_all(ring.bar(p), ring.parity(p), &abort_flag)) {
       report_timeout<T>(lib_status);
@@ -296,10 +326,29 @@ __global__ void __launch_bounds__(kThreads)
     fixup_plane(ring, in, g, bc, m, x0, y0, p, xy_edge);
   }
   __syncthreads();
-  compute_mu(z0 - 1);
-  compute_mu(z0);
-  __syncthreads();  // c(z0-2) is re-filled by the first loop iteration
 
+  auto mu_at = [&](const T* cd, const T* cc, const T* cu, int i) {
+    return ch_mu(k, cc[i], cc[i - 1], cc[i + 1], cc[i - W], cc[i + W], cd[i], cu[i]);
+  };
+  T c0[2], c1[2], mu_m[2], mu_0[2];
+  {
+    const T* Pm2 = ring.plane(z0 - 2);
+    const T* Pm1 = ring.plane(z0 - 1);
+    const T* P0 = ring.plane(z0);
+    const T* P1 = ring.plane(z0 + 1);
+    T* M0 = mslot(z0);
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+      mu_m[j] = mu_at(Pm2, Pm1, P0, ci[j]);
+      mu_0[j] = mu_at(Pm1, P0, P1, ci[j]);
+      M0[mi[j]] = mu_0[j];
+      c0[j] = P0[ci[j]];
+      c1[j] = P1[ci[j]];
+    }
+    if (has_ring) M0[rmi] = mu_at(Pm1, P0, P1, rci);
+  }
+
+  long long acc_q = 0;
   double acc = 0.0;
   int flags = 0;
   for (int z = z0; z < z1; ++z) {
@@ -311,48 +360,63 @@ __global__ void __launch_bounds__(kThreads)
     }
     fixup_plane(ring, in, g, bc, m, x0, y0, z + 2, xy_edge);
     __syncthreads();
-    compute_mu(z + 1);
+    const T* P0 = ring.plane(z);
+    const T* P1 = ring.plane(z + 1);
+    const T* P2 = ring.plane(z + 2);
+    T* M1 = mslot(z + 1);
+    T c2[2], mu_p[2];
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+      const int i = ci[j];
+      c2[j] = P2[i];
+      mu_p[j] = ch_mu(k, c1[j], P1[i - 1], P1[i + 1], P1[i - W], P1[i + W], c0[j], c2[j]);
+      M1[mi[j]] = mu_p[j];
+    }
+    if (has_ring) M1[rmi] = mu_at(P0, P1, P2, rci);
     __syncthreads();
-    const T* md = mslot(z - 1);
-    const T* mc = mslot(z);
-    const T* mu = mslot(z + 1);
-    const T* cc = ring.plane(z);
-    for (int ly = 1 + threadIdx.y; ly <= m.TY; ly += kThreads / 32) {
-      const int gy = y0 + ly - 1;
-      if (gy >= ny) break;
-      T* orow = out + (int64_t)z * g.plane + (int64_t)gy * g.pitch;
-      for (int lx = 1 + threadIdx.x; lx <= m.TX; lx += 32) {
-        const int gx = x0 + lx - 1;
-        if (gx >= nx) break;
-        const int i = ly * WM + lx;
-        const T m0 = mc[i];
-        const T fw = ch_flux<T, QUANT>(k, mc[i - 1], m0);
-        const T fe = ch_flux<T, QUANT>(k, mc[i + 1], m0);
-        const T fn = ch_flux<T, QUANT>(k, mc[i - WM], m0);
-        const T fs = ch_flux<T, QUANT>(k, mc[i + WM], m0);
-        const T fd = ch_flux<T, QUANT>(k, md[i], m0);
-        const T fu = ch_flux<T, QUANT>(k, mu[i], m0);
-        const T c0 = cc[(ly + 1) * W + lx + (kXOff - 1)];
-        const T v = c0 + (((fw + fe) + (fn + fs)) + (fd + fu));
-        orow[gx] = v;
-        acc += (double)v;
+    const T* M0 = mslot(z);
+#pragma unroll
+    for (int j = 0; j < 2; ++j) {
+      const int i = mi[j];
+      const T m0 = mu_0[j];
+      const T fw = ch_flux<T, QUANT>(k, M0[i - 1], m0);
+      const T fe = ch_flux<T, QUANT>(k, M0[i + 1], m0);
+      const T fn = ch_flux<T, QUANT>(k, M0[i - kMW], m0);
+      const T fs = ch_flux<T, QUANT>(k, M0[i + kMW], m0);
+      const T fd = ch_flux<T, QUANT>(k, mu_m[j], m0);
+      const T fu = ch_flux<T, QUANT>(k, mu_p[j], m0);
+      const T v = c0[j] + (((fw + fe) + (fn + fs)) + (fd + fu));
+      const int gy = y0 + ty + 8 * j, gx = x0 + tx;
+      if (gy < ny && gx < nx) {
+        out[(int64_t)z * g.plane + (int64_t)gy * g.pitch + gx] = v;
+        if (QUANT) {
+          acc_q += (long long)__float2int_rn((float)(v * k.iq));
+          if (!(fabs(v) < k.range)) flags |= PPF_STATUS_RANGE;
+        } else {
+          acc += (double)v;
+        }
         if (!isfinite(v)) flags |= PPF_STATUS_NONFINITE;
-        if (QUANT && fabs(v) >= k.range) flags |= PPF_STATUS_RANGE;
       }
+      c0[j] = c1[j];
+      c1[j] = c2[j];
+      mu_m[j] = m0;
+      mu_0[j] = mu_p[j];
     }
   }
   if (status && flags) atomicOr(status, flags);
   if (mass) {
+    // QUANT: exact integer count of quanta (|sum| < 2^53), scaled by q at
+    // the end: the total is the same whatever order the CTAs add in.
+    double v = QUANT ? (double)acc_q : acc;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-    const int warp = threadIdx.y;
-    if (threadIdx.x == 0) red[warp] = acc;
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (tx == 0) red[ty] = v;
     __syncthreads();
-    if (warp == 0) {
-      double v = threadIdx.x < kThreads / 32 ? red[threadIdx.x] : 0.0;
+    if (ty == 0) {
+      double s = tx < kThreads / 32 ? red[tx] : 0.0;
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-      if (threadIdx.x == 0) atomicAdd(mass, v);
+      for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+      if (tx == 0) atomicAdd(mass, QUANT ? s * (double)k.q : s);
     }
   }
 }
@@ -471,7 +535,14 @@ int32_t cahn_hilliard(const PpfCahnHilliardParams* p, const PpfGrid* grid_in,
   MarchGeom m;
   int slot_elems;
   size_t smem;
-  if ((rc = plan3d<T>(tiling, g, 2, kNSC, 3, &m, &slot_elems, &smem))) return rc;
+  if (tiling && ((tiling->tile_x && tiling->tile_x != kCTX) ||
+                 (tiling->tile_y && tiling->tile_y != kCTY)))
+    return fail(PPF_ERR_UNSUPPORTED, "Cahn-Hilliard tiles are %dx%d", kCTX, kCTY);
+  PpfTiling ct{};
+  ct.depth = tiling ? tiling->depth : 0;
+  ct.tile_x = kCTX;
+  ct.tile_y = kCTY;
+  if ((rc = plan3d<T>(&ct, g, 2, kNSC, 2, &m, &slot_elems, &smem))) return rc;
   ChCoef<T> k;
   k.kap = (T)(p->epsilon * p->epsilon / (p->dx * p->dx));
   k.a = (T)(p->dt * p->M / (p->dx * p->dx));

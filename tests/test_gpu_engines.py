@@ -1,0 +1,163 @@
+"""The engines through the reference-facing API (Simulation subclasses):
+lifecycle hooks, CUDA-graph stepping, autosave/load, precision, diagnostics.
+Tolerances as in test_gpu_kernels: fp32 within 1e-5 relative L2 of the FP64
+oracle, fp64 within 1e-12; graph vs eager stepping bit for bit."""
+import numpy as np
+import pytest
+
+from oracle import restate
+from tests.helpers import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+
+def _warren(shape, phi0, c0, bc="NEUMANN", **ud):
+    from pyphasefield_gb300 import Warren1995GB300
+    sim = Warren1995GB300(dimensions=list(shape), dx=4.6e-8, boundary_conditions=bc,
+                          user_data=dict(ud))
+    sim.initialize_fields_and_imported_data()
+    sim.fields[0].data[1:-1, 1:-1] = phi0
+    sim.fields[1].data[1:-1, 1:-1] = c0
+    return sim
+
+
+def _seeded(shape, seed=0):
+    rng = np.random.default_rng(seed)
+    phi0 = np.ones(shape)
+    yy, xx = np.mgrid[0:shape[0], 0:shape[1]]
+    phi0[(yy - shape[0] / 2 + 0.5) ** 2 + (xx - shape[1] / 2 + 0.5) ** 2 < 36] = 0.0
+    c0 = 0.40783 + rng.uniform(-1e-3, 1e-3, shape)
+    return phi0, c0
+
+
+def test_warren_engine_matches_oracle_graph_and_eager(cuda):
+    shape = (64, 72)
+    phi0, c0 = _seeded(shape)
+    params = dict(restate.WARREN_DEFAULTS, alpha=0.3)
+    ref = restate.run_warren(phi0, c0, 50, "NEUMANN", 4.6e-8, params, seed=7)
+    a = _warren(shape, phi0, c0, seed=7, graph_chunk=8)
+    a.simulate(50)
+    a.retrieve_fields_from_GPU()
+    b = _warren(shape, phi0, c0, seed=7, use_graph=False)
+    for _ in range(5):
+        b.simulate(10)
+    b.retrieve_fields_from_GPU()
+    for f in (0, 1):
+        np.testing.assert_array_equal(a.fields[f].get_cells(), b.fields[f].get_cells())
+    assert rel_l2(a.fields[0].get_cells(), ref[0]) < 1e-5
+    assert rel_l2(a.fields[1].get_cells(), ref[1]) < 1e-5
+    assert a.time_step_counter == 50 and b.time_step_counter == 50
+    # ghosts refreshed on the host with the no-flux rule
+    d = a.fields[0].data
+    np.testing.assert_array_equal(d[0, 1:-1], d[1, 1:-1])
+    np.testing.assert_array_equal(d[1:-1, -1], d[1:-1, -2])
+
+
+def test_warren_engine_fp64_tight(cuda):
+    shape = (40, 50)
+    phi0, c0 = _seeded(shape, 1)
+    params = dict(restate.WARREN_DEFAULTS, alpha=0.3)
+    ref = restate.run_warren(phi0, c0, 30, ["PERIODIC", "NEUMANN"], 4.6e-8, params, seed=2)
+    sim = _warren(shape, phi0, c0, bc=["PERIODIC", "NEUMANN"], seed=2, precision="fp64",
+                  graph_chunk=4)
+    sim.simulate(30)
+    sim.retrieve_fields_from_GPU()
+    assert rel_l2(sim.fields[0].get_cells(), ref[0]) < 1e-12
+    assert rel_l2(sim.fields[1].get_cells(), ref[1]) < 1e-12
+
+
+def test_autosave_and_load_round_trip(cuda, tmp_path):
+    from pyphasefield_gb300 import DiffusionGB300
+    rng = np.random.default_rng(3)
+    c0 = rng.random((30, 40))
+    sim = DiffusionGB300(dimensions=[30, 40], dx=1.0, dt=0.1, boundary_conditions="PERIODIC",
+                         save_path=str(tmp_path), autosave=True, autosave_rate=7,
+                         user_data={"D": 1.0, "graph_chunk": 4})
+    sim.initialize_fields_and_imported_data()
+    sim.fields[0].data[1:-1, 1:-1] = c0
+    sim.simulate(20)
+    assert sorted(p.name for p in tmp_path.glob("*.npz")) == ["step_14.npz", "step_7.npz"]
+    ref14 = restate.run_single("diffusion", c0, 14, "PERIODIC", 1.0, 0.1, D=1.0)
+    with np.load(tmp_path / "step_14.npz") as z:
+        assert rel_l2(z["c"], ref14) < 1e-5
+    again = DiffusionGB300(dimensions=[30, 40], dx=1.0, dt=0.1, boundary_conditions="PERIODIC",
+                           user_data={"D": 1.0})
+    again.load_simulation(file_path=str(tmp_path / "step_14.npz"))
+    assert again.time_step_counter == 14
+    again.simulate(6)
+    again.retrieve_fields_from_GPU()
+    sim.retrieve_fields_from_GPU()
+    np.testing.assert_array_equal(again.fields[0].get_cells(), sim.fields[0].get_cells())
+
+
+@pytest.mark.parametrize("depth", [1, 4])
+def test_diffusion_engine_temporal_depth(cuda, depth):
+    from pyphasefield_gb300 import DiffusionGB300
+    rng = np.random.default_rng(0)
+    c0 = 0.5 + 0.01 * rng.standard_normal((256, 256))
+    sim = DiffusionGB300(dimensions=[256, 256], dx=1.0, dt=0.2, boundary_conditions="PERIODIC",
+                         user_data={"D": 1.0, "temporal_depth": depth, "graph_chunk": 16})
+    sim.initialize_fields_and_imported_data()
+    sim.fields[0].data[1:-1, 1:-1] = c0
+    sim.simulate(1000)
+    sim.retrieve_fields_from_GPU()
+    ref = restate.run_single("diffusion", c0, 1000, "PERIODIC", 1.0, 0.2, D=1.0)
+    assert rel_l2(sim.fields[0].get_cells(), ref) < 1e-5
+
+
+def test_cahn_hilliard_engine_exact_mass_and_parity(cuda):
+    from pyphasefield_gb300 import CahnHilliardGB300
+    rng = np.random.default_rng(0)
+    shape = (40, 36, 44)
+    c0 = 0.5 + rng.uniform(-0.05, 0.05, shape)
+    sim = CahnHilliardGB300(dimensions=list(shape), dx=1.0, dt=0.01,
+                            boundary_conditions="PERIODIC",
+                            user_data={"M": 1.0, "epsilon": 1.0, "graph_chunk": 16})
+    sim.initialize_fields_and_imported_data()
+    sim.fields[0].data[1:-1, 1:-1, 1:-1] = c0
+    sim.simulate(300)
+    mass = sim.collect_mass_history()
+    assert len(mass) == 300
+    q = 2.0 ** -24
+    m0 = (np.rint((c0 - 0.5) / q) * q + 0.5).sum()
+    assert np.all(mass == mass[0]) and abs(mass[0] - m0) <= 1e-9 * m0
+    sim.retrieve_fields_from_GPU()
+    c0q = np.rint((c0 - 0.5) / q) * q + 0.5
+    ref = restate.run_single("cahn_hilliard", c0q, 300, "PERIODIC", 1.0, 0.01, M=1.0, epsilon=1.0)
+    assert rel_l2(sim.fields[0].get_cells(), ref) < 1e-5
+    assert sim.status_flags() == 0
+
+
+def test_allen_cahn_engine_3d_and_fp64(cuda):
+    from pyphasefield_gb300 import AllenCahnGB300
+    rng = np.random.default_rng(4)
+    c0 = rng.random((20, 24, 28))
+    for prec, tol in (("fp32", 1e-5), ("fp64", 1e-12)):
+        sim = AllenCahnGB300(dimensions=[20, 24, 28], dx=1.0, dt=0.05,
+                             boundary_conditions=["NEUMANN", "PERIODIC", "DIRCHLET"],
+                             user_data={"precision": prec, "graph_chunk": 4})
+        sim.initialize_fields_and_imported_data()
+        sim.fields[0].data[1:-1, 1:-1, 1:-1] = c0
+        sim.simulate(25)
+        sim.retrieve_fields_from_GPU()
+        ref = restate.run_single("allen_cahn", c0, 25, ["NEUMANN", "PERIODIC", "DIRCHLET"], 1.0,
+                                 0.05, M=0.1, epsilon=1.0, W=1.0)
+        assert rel_l2(sim.fields[0].get_cells(), ref) < tol
+
+
+def test_engine_rejections(cuda):
+    from pyphasefield_gb300 import CahnHilliardGB300, DiffusionGB300
+    ch = CahnHilliardGB300(dimensions=[16, 16], dx=1.0, dt=0.01, boundary_conditions="DIRCHLET")
+    ch.initialize_fields_and_imported_data()
+    with pytest.raises(RuntimeError, match="PERIODIC and NEUMANN"):
+        ch.simulate(1)
+    d = DiffusionGB300(dimensions=[16, 16], dx=1.0, dt=0.1, boundary_conditions="NEUMANN",
+                       user_data={"solver": "implicit"})
+    d.initialize_fields_and_imported_data()
+    with pytest.raises(NotImplementedError):
+        d.simulate(1)
+    d2 = DiffusionGB300(dimensions=[16, 16], dx=1.0, dt=0.1, boundary_conditions="NEUMANN")
+    d2.initialize_fields_and_imported_data()
+    d2._boundary_conditions_array[0][0, 3] = 0.5  # non-uniform face
+    with pytest.raises(NotImplementedError, match="non-uniform"):
+        d2.simulate(1)
