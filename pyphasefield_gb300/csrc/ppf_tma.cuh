@@ -44,17 +44,21 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
                : "memory");
 }
 
-// Bounded wait for phase `parity` of `bar`. Returns false on timeout.
+// Bounded wait for phase `parity` of `bar`. Each poll lets the hardware
+// suspend the thread for up to kSuspendNs until the phase completes, so
+// waiting threads do not spin on issue slots; after `limit` polls (well
+// under a second in total) it gives up and returns false.
+constexpr uint32_t kSuspendNs = 20000;
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity,
-                                          uint32_t limit = kWaitLimit) {
+                                          uint32_t limit = kWaitLimit / 128) {
   const uint32_t a = smem_addr(bar);
   for (uint32_t i = 0; i < limit; ++i) {
     uint32_t done;
     asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n"
         " selp.u32 %0, 1, 0, p;\n}\n"
         : "=r"(done)
-        : "r"(a), "r"(parity)
+        : "r"(a), "r"(parity), "n"(kSuspendNs)
         : "memory");
     if (done) return true;
   }
