@@ -308,9 +308,45 @@ def run_gb300(args):
         dist.destroy_process_group()
 
 
+def profile_case(name: str):
+    """Small eager workloads (no timing, no graphs) for ncu captures:
+    warren1024  the benchmark grid, 2005 steps (capture launch 2002: a grown crystal)
+    ch256       Cahn-Hilliard 256^3 periodic, dt 0.01, 5 steps
+    diff4096    Diffusion 2-D 4096^2 periodic, 5 steps (temporal depth from PPF_DEPTH, default 1)
+    """
+    import torch
+    from pyphasefield_gb300 import CahnHilliardGB300, DiffusionGB300
+    rng = np.random.default_rng(0)
+    if name == "warren1024":
+        phi0, c0 = initial_fields()
+        sim = make_sim(phi0, c0, 100)
+        sim.user_data["use_graph"] = False
+        sim.simulate(2005)
+    elif name == "ch256":
+        sim = CahnHilliardGB300(dimensions=[256, 256, 256], dx=1.0, dt=0.01,
+                                boundary_conditions="PERIODIC",
+                                user_data={"M": 1.0, "epsilon": 1.0, "use_graph": False})
+        sim.initialize_fields_and_imported_data()
+        sim.fields[0].data[1:-1, 1:-1, 1:-1] = 0.5 + rng.uniform(-0.05, 0.05, (256, 256, 256))
+        sim.simulate(5)
+    elif name == "diff4096":
+        depth = int(os.environ.get("PPF_DEPTH", "1"))
+        sim = DiffusionGB300(dimensions=[4096, 4096], dx=1.0, dt=0.2,
+                             boundary_conditions="PERIODIC",
+                             user_data={"D": 1.0, "use_graph": False, "temporal_depth": depth})
+        sim.initialize_fields_and_imported_data()
+        sim.fields[0].data[1:-1, 1:-1] = 0.5 + 0.01 * rng.standard_normal((4096, 4096))
+        sim.simulate(5 * depth)
+    else:
+        raise SystemExit(f"unknown profile case {name!r}")
+    torch.cuda.synchronize()
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__,
                                  formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--profile-case", default=None,
+                    help="run a small eager workload for ncu instead of the benchmark")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
@@ -321,6 +357,9 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
+    if args.profile_case:
+        profile_case(args.profile_case)
+        return
     if args.warmup < 3:
         print("warning: fewer than 3 warm-up steps", file=sys.stderr)
     if args.impl == "reference":
