@@ -202,6 +202,47 @@ int32_t ppf_warren1995_step_f64(const PpfWarren1995Params* p, const PpfGrid* g,
                                 const uint64_t* step_base,
                                 const PpfTiling* tiling, void* stream);
 
+/* ---- batched ensemble ------------------------------------------------- */
+
+#define PPF_MODEL_WARREN1995 1
+#define PPF_MODEL_ALLEN_CAHN 2
+
+/* One ensemble member: an independent 2-D float grid with its own ping-pong
+ * buffers and parameters (one reference Simulation instance each). Step
+ * parity p reads phi[p] (and c[p]) and writes phi[1-p] (and c[1-p]). */
+typedef struct PpfMember {
+  int32_t model; /* PPF_MODEL_* */
+  int32_t reserved;
+  int64_t ny, nx, pitch;
+  PpfBoundary bc;
+  float* phi[2];
+  float* c[2]; /* Warren1995 only */
+  uint64_t seed;
+  PpfWarren1995Params w95; /* Warren1995 only */
+  PpfAllenCahnParams ac;   /* Allen-Cahn only */
+} PpfMember;
+
+typedef struct PpfEnsemblePlan {
+  const void* device_table; /* caller device memory holding the member table */
+  int64_t n_items;          /* warp bands over all members */
+  int32_t n_members;
+  int32_t rows; /* rows per warp band (tiling->tile_y: 2, 4 or 8) */
+} PpfEnsemblePlan;
+
+/* Device bytes of the member table for these members. */
+int32_t ppf_ensemble_plan_bytes(const PpfMember* members, int32_t n,
+                                const PpfTiling* tiling, size_t* bytes);
+/* Validates the members, folds their parameters and copies the table into
+ * device_table (waits for that copy on `stream`). */
+int32_t ppf_ensemble_build(const PpfMember* members, int32_t n,
+                           const PpfTiling* tiling, void* device_table,
+                           size_t bytes, PpfEnsemblePlan* plan, void* stream);
+/* One time step of every member in one persistent launch; Warren1995 noise
+ * keyed by (member seed, step + *step_base). */
+int32_t ppf_ensemble_step_f32(const PpfEnsemblePlan* plan, int32_t parity,
+                              uint64_t step, const uint64_t* step_base,
+                              const PpfTiling* tiling, void* stream);
+
 /* ---- diagnostics (FP64 reductions) ------------------------------------ */
 
 /* Bytes of caller-provided device scratch the reductions below need. */

@@ -74,6 +74,22 @@ class PpfWarren1995Params(C.Structure):
     _fields_ = [(n, C.c_double) for n in WARREN_PARAM_NAMES]
 
 
+PPF_MODEL_WARREN1995 = 1
+PPF_MODEL_ALLEN_CAHN = 2
+
+
+class PpfMember(C.Structure):
+    _fields_ = [("model", C.c_int32), ("reserved", C.c_int32), ("ny", C.c_int64),
+                ("nx", C.c_int64), ("pitch", C.c_int64), ("bc", PpfBoundary),
+                ("phi", C.c_void_p * 2), ("c", C.c_void_p * 2), ("seed", C.c_uint64),
+                ("w95", PpfWarren1995Params), ("ac", PpfAllenCahnParams)]
+
+
+class PpfEnsemblePlan(C.Structure):
+    _fields_ = [("device_table", C.c_void_p), ("n_items", C.c_int64),
+                ("n_members", C.c_int32), ("rows", C.c_int32)]
+
+
 P = C.c_void_p
 I32 = C.c_int32
 U64 = C.c_uint64
@@ -93,6 +109,9 @@ SIGNATURES: dict[str, list] = {
     "ppf_cahn_hilliard_step_f64": [C.POINTER(PpfCahnHilliardParams), PG, PB, P, P, P, P, PT, P],
     "ppf_warren1995_step_f32": [C.POINTER(PpfWarren1995Params), PG, PB, P, P, P, P, U64, U64, P, PT, P],
     "ppf_warren1995_step_f64": [C.POINTER(PpfWarren1995Params), PG, PB, P, P, P, P, U64, U64, P, PT, P],
+    "ppf_ensemble_plan_bytes": [C.POINTER(PpfMember), I32, PT, C.POINTER(SZ)],
+    "ppf_ensemble_build": [C.POINTER(PpfMember), I32, PT, P, SZ, C.POINTER(PpfEnsemblePlan), P],
+    "ppf_ensemble_step_f32": [C.POINTER(PpfEnsemblePlan), I32, U64, P, PT, P],
     "ppf_reduce_scratch_bytes": [PG, C.POINTER(SZ)],
     "ppf_reduce_sum_f32": [P, PG, P, P, SZ, P],
     "ppf_reduce_sum_f64": [P, PG, P, P, SZ, P],

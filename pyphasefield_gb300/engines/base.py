@@ -112,6 +112,48 @@ class GB300Engine:
         except Exception:
             pass
 
+    def _ppf_tune_candidates(self) -> list:
+        """Launch shapes the autotuner may try (user_data updates)."""
+        return []
+
+    def _ppf_autotune(self):
+        """Pick tile / temporal depth by timing candidates on scratch copies
+        of the current fields (user_data["autotune"] = True); the choice is
+        cached per kernel, shape, dtype and device (autotune.py)."""
+        from .. import autotune
+
+        cands = self._ppf_tune_candidates()
+        if len(cands) < 2:
+            return
+        key = autotune.make_key(type(self).__name__, self._ppf_grid.kshape, self._ppf_dtype,
+                                str(len(self.dimensions)))
+        s = self._ppf_stream
+        sp = C.c_void_p(s.cuda_stream)
+        with torch.cuda.stream(s):
+            scratch = [[t.clone() for t in self._ppf_bufs[self._ppf_cur]] for _ in range(2)]
+        saved = {k: self.user_data.get(k) for c in cands for k in c}
+
+        def measure(cand):
+            self.user_data.update(cand)
+            depth = max(1, min(int(self.user_data.get("temporal_depth", 1)), self._ppf_max_depth()))
+            flip = [0]
+
+            def run():
+                self._ppf_step(scratch[flip[0]], scratch[1 - flip[0]], depth, 0, None, sp)
+                flip[0] ^= 1
+
+            return autotune.time_candidate(run, s) / depth
+
+        try:
+            best = autotune.pick(key, cands, measure)
+        finally:
+            self.user_data.update(saved)
+        self.user_data.update(best)
+        self._ppf_graphs_reset()
+
+    def _ppf_graphs_reset(self):
+        self._ppf_release_graphs()
+
     def _ppf_tiling(self, depth: int):
         ud = self.user_data
         flags = 0 if ud.get("bulk_shortcut", True) else L.PPF_TILING_FULL_EVAL
@@ -127,6 +169,8 @@ class GB300Engine:
         self._ppf_setup()
         fill_ghosts_host(self)
         self.send_fields_to_GPU()
+        if self.user_data.get("autotune", False):
+            self._ppf_autotune()
 
     def send_fields_to_GPU(self):
         if not self._ppf_ready():

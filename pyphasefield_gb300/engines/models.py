@@ -34,6 +34,15 @@ def _explicit_only(ud, name):
                                   f"path (got solver={solver!r})")
 
 
+def _stencil_candidates(sim) -> list:
+    """Diffusion / Allen-Cahn launch shapes: temporal depth x tile (2-D),
+    tile (3-D)."""
+    if len(sim._ppf_grid.kshape) == 2:
+        return [{"temporal_depth": d, "tile": t} for d in (1, 2, 4, 8)
+                for t in ((128, 32), (64, 32), (256, 16), (128, 16))]
+    return [{"tile": t} for t in ((64, 16), (32, 16), (128, 8), (64, 8))]
+
+
 class _DiffusionMixin(GB300Engine):
     """c += dt*D*lap(c) (engine_ExplicitDiffusion, Engines/Diffusion.py:198-208)."""
 
@@ -61,6 +70,9 @@ class _DiffusionMixin(GB300Engine):
 
     def _ppf_max_depth(self):
         return 8 if len(self._ppf_grid.kshape) == 2 else 1
+
+    def _ppf_tune_candidates(self):
+        return _stencil_candidates(self)
 
     def _ppf_params(self):
         return L.PpfDiffusionParams(float(self.dx), float(self.dt), float(self.user_data["D"]))
@@ -98,6 +110,9 @@ class _CahnAllenMixin(GB300Engine):
 
     def _ppf_max_depth(self):
         return 8 if len(self._ppf_grid.kshape) == 2 else 1
+
+    def _ppf_tune_candidates(self):
+        return _stencil_candidates(self)
 
     def _ppf_params(self):
         ud = self.user_data
@@ -257,6 +272,9 @@ class _Warren1995Mixin(GB300Engine):
         ud["W_B"] = 3 * ud["s_B"] / (r2 * ud["T_mB"] * ud["d"])
         ud["M_A"] = (ud["T_mA"] ** 2) * ud["B_A"] / (6 * r2 * ud["L_A"] * ud["d"])
         ud["M_B"] = (ud["T_mB"] ** 2) * ud["B_B"] / (6 * r2 * ud["L_B"] * ud["d"])
+
+    def _ppf_tune_candidates(self):
+        return [{"tile": (0, rows)} for rows in (2, 4, 8)]
 
     def _ppf_params(self):
         ud = self.user_data

@@ -1,0 +1,227 @@
+"""Batched ensembles: many Warren1995 / Allen-Cahn engines advanced together.
+
+The reference runs one Simulation at a time; an ensemble here is a list of
+ordinary engine instances (each with its own fields, parameters and grid
+size) whose device buffers are stepped by ONE persistent launch per time step
+(`ppf_ensemble_step_f32`), captured `graph_chunk` steps per CUDA graph.
+Afterwards each member is an ordinary engine again: retrieve_fields_from_GPU,
+save_simulation etc. work on it.
+
+`make_config_ensemble` builds the benchmark ensemble: n members whose square
+sides are drawn log-uniform in [128, 1024]; even members are Warren1995 at
+T = T_liquidus(c0) - dT with dT ~ U[5, 40] K and a solid nucleus at a random
+position, odd members Allen-Cahn (reference defaults M=0.1, eps=1, W=1) with a
+phi = 1 nucleus at a random position.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import gc
+
+import numpy as np
+import torch
+
+from . import _lib as L
+from .device import ptr, tiling_struct
+from .engines import CahnAllenGB300, Warren1995GB300
+
+
+def warren_liquidus(c0: float, ud: dict) -> float:
+    """Liquidus temperature of composition c0 in the Warren1995 model's own
+    ideal-solution thermodynamics: with k_A = exp(v_m L_A (1/T - 1/T_mA)/R)
+    and k_B = exp(v_m L_B (1/T - 1/T_mB)/R) the equilibrium liquid
+    composition is c_L = (1 - k_A) / (k_B - k_A) (equal diffusion and grand
+    potentials of phi = 0 and phi = 1 in the free energy whose phi-derivatives
+    are the engine's H_A, H_B). Solved for T by bisection between the pure
+    melting points."""
+    vr = ud["v_m"] / ud["R"]
+
+    def c_liquid(T):
+        ka = np.exp(vr * ud["L_A"] * (1 / T - 1 / ud["T_mA"]))
+        kb = np.exp(vr * ud["L_B"] * (1 / T - 1 / ud["T_mB"]))
+        return (1 - ka) / (kb - ka)
+
+    lo, hi = ud["T_mB"] + 1e-6, ud["T_mA"] - 1e-6  # c_L falls from ~1 to ~0
+    for _ in range(200):
+        mid = 0.5 * (lo + hi)
+        if c_liquid(mid) > c0:
+            lo = mid
+        else:
+            hi = mid
+    return 0.5 * (lo + hi)
+
+
+def make_config_ensemble(n: int = 64, seed: int = 0, side_range=(128, 1024), c0=0.40783,
+                         dT_range=(5.0, 40.0), **user_data) -> list:
+    """Initialised (not yet stepped) engine instances of the ensemble
+    benchmark. Extra keyword arguments go into every member's user_data."""
+    rng = np.random.default_rng(seed)
+    sides = np.rint(np.exp(rng.uniform(np.log(side_range[0]), np.log(side_range[1]), n)))
+    sims = []
+    t_ref = warren_liquidus(c0, Warren1995GB300.DEFAULTS)
+    for m, s in enumerate(sides.astype(int)):
+        cy, cx = rng.uniform(0.1 * s, 0.9 * s, 2)
+        yy, xx = np.mgrid[0:s, 0:s]
+        disk = (yy - cy) ** 2 + (xx - cx) ** 2 < 25.0
+        if m % 2 == 0:
+            ud = dict(user_data, T=float(t_ref - rng.uniform(*dT_range)), seed=int(seed * 1000 + m))
+            sim = Warren1995GB300(dimensions=[s, s], dx=4.6e-8, boundary_conditions="NEUMANN",
+                                  user_data=ud)
+            sim.initialize_fields_and_imported_data()
+            phi = np.ones((s, s))
+            phi[disk] = 0.0
+            sim.fields[0].data[1:-1, 1:-1] = phi
+            sim.fields[1].data[1:-1, 1:-1] = c0 + rng.uniform(-1e-3, 1e-3, (s, s))
+        else:
+            sim = CahnAllenGB300(dimensions=[s, s], dx=1.0, dt=0.1, boundary_conditions="NEUMANN",
+                                 user_data=dict(user_data, seed=int(seed * 1000 + m)))
+            sim.initialize_fields_and_imported_data()
+            sim.fields[0].data[1:-1, 1:-1] = disk.astype(float)
+        sims.append(sim)
+    return sims
+
+
+def partition_members(cells, world: int) -> list:
+    """Split members (by index) across `world` ranks balancing total cells:
+    largest first onto the least-loaded rank (members are independent, so a
+    multi-GPU ensemble needs no data-path collective). Returns one sorted
+    index list per rank."""
+    loads = [0] * world
+    parts = [[] for _ in range(world)]
+    for i in sorted(range(len(cells)), key=lambda i: (-cells[i], i)):
+        r = min(range(world), key=lambda r: (loads[r], r))
+        parts[r].append(i)
+        loads[r] += cells[i]
+    return [sorted(p) for p in parts]
+
+
+class Ensemble:
+    """Steps a list of 2-D float32 Warren1995GB300 / CahnAllenGB300 engines
+    together. All members must be at the same time step."""
+
+    def __init__(self, sims, rows: int = 2, graph_chunk: int = 64, pdl: bool = True,
+                 bulk_shortcut: bool = True):
+        if not sims:
+            raise ValueError("empty ensemble")
+        self.sims = list(sims)
+        for s in self.sims:
+            if not isinstance(s, (Warren1995GB300, CahnAllenGB300)):
+                raise TypeError(f"{type(s).__name__} cannot join an ensemble")
+            if len(s.dimensions) != 2:
+                raise ValueError("ensemble members are 2-D")
+            if s.user_data.get("precision", "fp32") != "fp32":
+                raise ValueError("ensemble members are float32")
+            if not s._ppf_ready():
+                s._begun_simulation = True
+                s.just_before_simulating()
+        if len({s.time_step_counter for s in self.sims}) != 1 or \
+                len({s._ppf_cur for s in self.sims}) != 1:
+            raise ValueError("ensemble members must be at the same step")
+        self.step = self.sims[0].time_step_counter
+        self.cur = self.sims[0]._ppf_cur
+        self.graph_chunk = max(2, int(graph_chunk) // 2 * 2)
+        self.tiling = tiling_struct(1, (0, rows), pdl, 0 if bulk_shortcut else L.PPF_TILING_FULL_EVAL)
+        dev = self.sims[0]._ppf_grid.device
+        self.stream = torch.cuda.Stream(dev)
+        self.stepctr = torch.zeros(1, dtype=torch.int64, device=dev)
+        self.graphs = {}
+        self._build()
+
+    @property
+    def cells(self) -> int:
+        return sum(s._ppf_grid.cells for s in self.sims)
+
+    def _member(self, s) -> L.PpfMember:
+        m = L.PpfMember()
+        g = s._ppf_grid
+        m.ny, m.nx = g.kshape
+        m.pitch = g.pitch
+        m.bc = s._ppf_bc
+        m.phi[0] = s._ppf_bufs[0][0].data_ptr()
+        m.phi[1] = s._ppf_bufs[1][0].data_ptr()
+        if isinstance(s, Warren1995GB300):
+            m.model = L.PPF_MODEL_WARREN1995
+            m.c[0] = s._ppf_bufs[0][1].data_ptr()
+            m.c[1] = s._ppf_bufs[1][1].data_ptr()
+            m.seed = int(s.user_data["seed"])
+            m.w95 = s._ppf_params()
+        else:
+            m.model = L.PPF_MODEL_ALLEN_CAHN
+            m.ac = s._ppf_params()
+        return m
+
+    def _build(self):
+        n = len(self.sims)
+        self.members = (L.PpfMember * n)(*[self._member(s) for s in self.sims])
+        nbytes = C.c_size_t()
+        L.call("ppf_ensemble_plan_bytes", self.members, n, C.byref(self.tiling), C.byref(nbytes))
+        self.table = torch.empty(max(16, nbytes.value), dtype=torch.uint8,
+                                 device=self.stepctr.device)
+        self.plan = L.PpfEnsemblePlan()
+        for s in self.sims:  # member uploads must land before the first step
+            self.stream.wait_stream(s._ppf_stream)
+        L.call("ppf_ensemble_build", self.members, n, C.byref(self.tiling), ptr(self.table),
+               C.c_size_t(self.table.numel()), C.byref(self.plan), C.c_void_p(self.stream.cuda_stream))
+
+    def _launch(self, parity, step, base):
+        L.call("ppf_ensemble_step_f32", C.byref(self.plan), int(parity), C.c_uint64(step), ptr(base),
+               C.byref(self.tiling), C.c_void_p(self.stream.cuda_stream))
+
+    def _graph(self):
+        key = self.cur
+        g = self.graphs.get(key)
+        if g is not None:
+            return g
+        sp = C.c_void_p(self.stream.cuda_stream)
+        gc_was = gc.isenabled()
+        gc.disable()
+        exec_ = C.c_void_p()
+        L.call("ppf_graph_begin", sp)
+        try:
+            for k in range(self.graph_chunk):
+                self._launch((self.cur + k) & 1, k, self.stepctr)
+            L.call("ppf_counter_add_u64", ptr(self.stepctr), C.c_uint64(self.graph_chunk), sp)
+        finally:
+            try:
+                L.call("ppf_graph_end", sp, C.byref(exec_))
+            finally:
+                if gc_was:
+                    gc.enable()
+        self.graphs[key] = exec_
+        return exec_
+
+    def simulate(self, n: int, use_graph: bool = True):
+        """Advance every member n steps."""
+        n = int(n)
+        sp = C.c_void_p(self.stream.cuda_stream)
+        if use_graph and n >= self.graph_chunk:
+            g = self._graph()
+            with torch.cuda.stream(self.stream):
+                self.stepctr.fill_(self.step)
+            while n >= self.graph_chunk:
+                L.call("ppf_graph_launch", g, sp)
+                self.step += self.graph_chunk
+                n -= self.graph_chunk
+        for _ in range(n):
+            self._launch(self.cur, self.step, None)
+            self.cur ^= 1
+            self.step += 1
+        for s in self.sims:
+            s._ppf_cur = self.cur
+            s.time_step_counter = self.step
+            s._ppf_stream.wait_stream(self.stream)
+
+    def synchronize(self):
+        self.stream.synchronize()
+
+    def retrieve_fields_from_GPU(self):
+        self.synchronize()
+        for s in self.sims:
+            s.retrieve_fields_from_GPU()
+
+    def __del__(self):
+        try:
+            for g in self.graphs.values():
+                L.call("ppf_graph_destroy", g)
+        except Exception:
+            pass

@@ -1,0 +1,97 @@
+"""The batched ensemble (one persistent launch per step over many engines)
+and the autotuner, on the GPU. Ensemble members must match the same engines
+stepped one by one (fp32: within 1e-6 relative L2; the ensemble's Allen-Cahn
+band is a different kernel from the single-grid one, so rounding may differ)
+and the FP64 oracle (1e-5)."""
+import numpy as np
+import pytest
+
+from oracle import restate
+from tests.helpers import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+
+def _members(seed=1):
+    from pyphasefield_gb300.ensemble import make_config_ensemble
+    return make_config_ensemble(n=5, seed=seed, side_range=(40, 150), graph_chunk=8)
+
+
+def _snapshot(sims):
+    return [[f.get_cells().copy() for f in s.fields] for s in sims]
+
+
+@pytest.mark.parametrize("rows", [2, 4, 8])
+def test_ensemble_matches_members_stepped_alone(cuda, rows):
+    from pyphasefield_gb300.ensemble import Ensemble
+    a = _members()
+    b = _members()
+    for s in b:
+        s.user_data["tile"] = (0, rows)
+    ens = Ensemble(a, rows=rows, graph_chunk=8)
+    ens.simulate(40)
+    ens.retrieve_fields_from_GPU()
+    for s in b:
+        s.simulate(40)
+        s.retrieve_fields_from_GPU()
+    for sa, sb in zip(a, b):
+        assert sa.time_step_counter == sb.time_step_counter == 40
+        for fa, fb in zip(sa.fields, sb.fields):
+            assert rel_l2(fa.get_cells(), fb.get_cells()) < 1e-6
+
+
+def test_ensemble_graph_equals_eager_and_oracle(cuda):
+    from pyphasefield_gb300.ensemble import Ensemble
+    a = _members(2)
+    init = _snapshot(a)
+    b = _members(2)
+    Ensemble(a, graph_chunk=4).simulate(24)
+    eb = Ensemble(b, graph_chunk=4)
+    for _ in range(24):
+        eb.simulate(1, use_graph=False)
+    for sa, sb in zip(a, b):
+        sa.retrieve_fields_from_GPU()
+        sb.retrieve_fields_from_GPU()
+        for fa, fb in zip(sa.fields, sb.fields):
+            np.testing.assert_array_equal(fa.get_cells(), fb.get_cells())
+    # member 0 is Warren1995, member 1 Allen-Cahn: against the FP64 oracle
+    w = a[0]
+    params = {k: w.user_data[k] for k in restate.WARREN_DEFAULTS}
+    ref = restate.run_warren(init[0][0], init[0][1], 24, "NEUMANN", w.dx, params,
+                             seed=w.user_data["seed"])
+    assert rel_l2(w.fields[0].get_cells(), ref[0]) < 1e-5
+    assert rel_l2(w.fields[1].get_cells(), ref[1]) < 1e-5
+    ac = a[1]
+    ref = restate.run_single("allen_cahn", init[1][0], 24, "NEUMANN", 1.0, 0.1, M=0.1,
+                             epsilon=1.0, W=1.0)
+    assert rel_l2(ac.fields[0].get_cells(), ref) < 1e-5
+
+
+def test_config_ensemble_shape():
+    from pyphasefield_gb300.ensemble import make_config_ensemble
+    sims = make_config_ensemble(n=64, seed=0)
+    sides = [s.dimensions[0] for s in sims]
+    assert len(sims) == 64 and min(sides) >= 128 and max(sides) <= 1024
+    cells = sum(s * s for s in sides)
+    assert 0.5e7 < cells < 4e7
+
+
+def test_autotune_picks_and_caches(cuda, tmp_path, monkeypatch):
+    import json
+    from pyphasefield_gb300 import DiffusionGB300
+    monkeypatch.setenv("PPF_AUTOTUNE_CACHE", str(tmp_path / "tune.json"))
+    rng = np.random.default_rng(0)
+    c0 = rng.random((512, 512))
+    sim = DiffusionGB300(dimensions=[512, 512], dx=1.0, dt=0.2, boundary_conditions="PERIODIC",
+                         user_data={"D": 1.0, "autotune": True, "graph_chunk": 8})
+    sim.initialize_fields_and_imported_data()
+    sim.fields[0].data[1:-1, 1:-1] = c0
+    sim.simulate(16)
+    sim.retrieve_fields_from_GPU()
+    cache = json.loads((tmp_path / "tune.json").read_text())
+    assert len(cache) == 1
+    entry = next(iter(cache.values()))
+    assert entry["config"]["temporal_depth"] == sim.user_data["temporal_depth"]
+    assert len(entry["tried"]) == 16
+    ref = restate.run_single("diffusion", c0, 16, "PERIODIC", 1.0, 0.2, D=1.0)
+    assert rel_l2(sim.fields[0].get_cells(), ref) < 1e-5  # tuning did not change the state

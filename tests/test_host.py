@@ -1,0 +1,159 @@
+"""Host-side logic without a GPU: the Simulation interface, ghost fill,
+checkpoints, boundary structs, the ensemble's thermodynamics and
+partitioning, the autotune cache and the C-ABI library's exports."""
+import ctypes as C
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from oracle import restate
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+def test_user_data_is_copied_and_defaults_do_not_leak():
+    from pyphasefield_gb300 import Warren1995GB300, DiffusionGB300
+    shared = {}
+    a = DiffusionGB300(dimensions=[8, 8], dx=1.0, dt=0.1, boundary_conditions="PERIODIC",
+                       user_data=shared)
+    b = Warren1995GB300(dimensions=[8, 8], dx=1.0, boundary_conditions="PERIODIC",
+                        user_data=shared)
+    assert shared == {}
+    assert "T_mA" not in a.user_data and a.user_data["D"] == 0.1
+    assert b.user_data["T_mA"] == 1728.0 and "D" not in b.user_data
+
+
+@pytest.mark.parametrize("bc", ["PERIODIC", "NEUMANN", "DIRCHLET", ["PERIODIC", "NEUMANN"],
+                                ["NEUMANN", "DIRCHLET", "PERIODIC"]])
+def test_host_ghost_fill_matches_oracle(bc):
+    from pyphasefield_gb300 import Simulation
+    rng = np.random.default_rng(1)
+    nd = 2 if isinstance(bc, str) else len(bc)
+    shape = [5, 6, 7][:nd]
+    sim = Simulation(dimensions=shape, dx=0.5, boundary_conditions=bc)
+    sim.add_field(rng.random(shape), "a")
+    sim.add_field(rng.random(shape), "b")
+    sim.init_boundary_conditions()
+    bcs = [bc] * nd if isinstance(bc, str) else bc
+    vals = [[[0.1 * (j + 1), -0.2 * (a + 1)] for a in range(nd)] for j in range(2)]
+    for j in range(2):
+        for a in range(nd):
+            for side, k in ((0, 0), (1, -1)):
+                idx = (slice(None),) * a + (k,)
+                sim._boundary_conditions_array[j][idx] = vals[j][a][side]
+    ref = [f.data.copy() for f in sim.fields]
+    sim.apply_boundary_conditions()
+    restate.fill_ghosts(ref, bcs, 0.5, vals)
+    for f, r in zip(sim.fields, ref):
+        np.testing.assert_array_equal(f.data, r)
+
+
+def test_save_load_round_trip(tmp_path):
+    from pyphasefield_gb300 import Simulation
+    sim = Simulation(dimensions=[4, 5], save_path=str(tmp_path), boundary_conditions="PERIODIC")
+    sim.add_field(np.arange(20.0).reshape(4, 5), "phi")
+    sim.add_field(np.ones((4, 5)), "c")
+    sim.time_step_counter = 12
+    sim.save_simulation()
+    other = Simulation(dimensions=None, save_path=str(tmp_path))
+    other.load_simulation(step=12)
+    assert other.time_step_counter == 12 and other.dimensions == [4, 5]
+    np.testing.assert_array_equal(other.fields[0].get_cells(), sim.fields[0].get_cells())
+    assert [f.name for f in other.fields] == ["phi", "c"]
+
+
+def test_begun_simulation_runs_setup_once():
+    from pyphasefield_gb300 import Simulation
+
+    class Counting(Simulation):
+        calls = 0
+
+        def just_before_simulating(self):
+            Counting.calls += 1
+
+    s = Counting(dimensions=[4], boundary_conditions="PERIODIC")
+    s.simulate(2)
+    s.simulate(3)
+    assert Counting.calls == 1 and s.time_step_counter == 5
+
+
+def test_boundary_struct_from_simulation():
+    from pyphasefield_gb300 import DiffusionGB300
+    from pyphasefield_gb300.device import DeviceGrid, boundary_struct
+    import torch
+    sim = DiffusionGB300(dimensions=[6, 7], dx=1.0, dt=0.1,
+                         boundary_conditions=["DIRCHLET", "NEUMANN"])
+    sim.initialize_fields_and_imported_data()
+    sim._boundary_conditions_array[0][0, 1:-1] = 0.25
+    sim._boundary_conditions_array[0][1:-1, -1] = -1.5
+    b = boundary_struct(sim, DeviceGrid([6, 7], torch.float32, torch.device("cpu")), 1)
+    assert list(b.type) == [2, 1, 0]
+    assert b.value[0][0][0] == 0.25 and b.value[0][1][1] == -1.5
+    one = DiffusionGB300(dimensions=[9], dx=1.0, dt=0.1, boundary_conditions="NEUMANN")
+    one.initialize_fields_and_imported_data()
+    b1 = boundary_struct(one, DeviceGrid([9], torch.float32, torch.device("cpu")), 1)
+    assert list(b1.type)[:2] == [0, 1]
+
+
+def test_warren_liquidus_is_the_equilibrium_liquid():
+    from pyphasefield_gb300.ensemble import warren_liquidus
+    from pyphasefield_gb300 import Warren1995GB300
+    ud = Warren1995GB300.DEFAULTS
+    t = warren_liquidus(0.40783, ud)
+    assert ud["T_mB"] < t < ud["T_mA"]
+    vr = ud["v_m"] / ud["R"]
+    ka = np.exp(vr * ud["L_A"] * (1 / t - 1 / ud["T_mA"]))
+    kb = np.exp(vr * ud["L_B"] * (1 / t - 1 / ud["T_mB"]))
+    assert abs((1 - ka) / (kb - ka) - 0.40783) < 1e-9
+    assert warren_liquidus(0.3, ud) > t > warren_liquidus(0.5, ud)
+
+
+def test_autotune_cache_roundtrip(tmp_path, monkeypatch):
+    from pyphasefield_gb300 import autotune
+    monkeypatch.setenv("PPF_AUTOTUNE_CACHE", str(tmp_path / "t.json"))
+    calls = []
+
+    def measure(c):
+        calls.append(c)
+        return {1: 3.0, 2: 1.0, 4: 2.0}[c["d"]]
+
+    cands = [{"d": 1}, {"d": 2}, {"d": 4}]
+    assert autotune.pick("k", cands, measure) == {"d": 2}
+    assert autotune.pick("k", cands, measure) == {"d": 2}
+    assert len(calls) == 3
+
+
+def _header_functions():
+    text = (ROOT / "include" / "ppf_gb300.h").read_text()
+    return sorted(set(re.findall(r"^int32_t\s+(ppf_\w+)\s*\(", text, re.M)))
+
+
+def test_library_exports_every_header_symbol(built_lib):
+    lib = C.CDLL(str(built_lib))
+    names = _header_functions()
+    assert len(names) >= 20
+    for n in names:
+        assert hasattr(lib, n), n
+    from pyphasefield_gb300 import _lib
+    assert sorted(_lib.SIGNATURES) == names
+
+
+def test_library_rejects_bad_arguments_without_gpu(built_lib):
+    from pyphasefield_gb300 import _lib as L
+    L.load()
+    abi, text = L.version()
+    assert abi == 1 and "sm_103a" in text
+    g = L.PpfGrid()
+    g.ndim = 2
+    g.shape[0], g.shape[1] = 8, 8
+    g.pitch = 6  # < nx
+    b = L.PpfBoundary()
+    p = L.PpfDiffusionParams(1.0, 0.1, 1.0)
+    rc = L.load().ppf_diffusion_step_f32(C.byref(p), C.byref(g), C.byref(b), None, None, None,
+                                         None)
+    assert rc == L.PPF_ERR_INVALID
+    assert "pitch" in L.last_error()
+    with pytest.raises(L.PpfError):
+        L.call("ppf_diffusion_step_f32", None, C.byref(g), C.byref(b), None, None, None, None)
