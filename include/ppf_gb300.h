@@ -243,6 +243,69 @@ int32_t ppf_ensemble_step_f32(const PpfEnsemblePlan* plan, int32_t parity,
                               uint64_t step, const uint64_t* step_base,
                               const PpfTiling* tiling, void* stream);
 
+/* ---- learned surrogate (no counterpart in the reference) --------------- *
+ * A convolutional encoder-decoder that advances a Warren1995 (phi, c) state
+ * by k stencil steps: patchify conv (P x P, stride P) -> L blocks of
+ * [depthwise 3x3 conv, 1x1 conv C->E, GELU, 1x1 conv E->C, residual] ->
+ * unpatchify conv predicting the normalised k-step change. The patch and 1x1
+ * convolutions are implicit GEMMs on BF16 tensor cores (mma.sync m16n8k16,
+ * FP32 accumulation); the patch gather / scatter happens in the GEMM's
+ * operand loader and epilogue. Activations are channels-last [token][ch];
+ * fields are [b][ch][H][pitch] float. Weights W[out][in] (bf16 for the
+ * GEMMs). Gradient entry points accumulate (+=) into fp32 buffers. */
+typedef struct PpfSgShape {
+  int32_t B, H, W, pitch, P, C, E;
+  float s0, s1;                          /* change scale of phi and c */
+  float in_off0, in_sc0, in_off1, in_sc1; /* input (v - off) * sc */
+  float lo0, hi0, lo1, hi1;               /* predictions clamped to [lo, hi] */
+} PpfSgShape;
+
+int32_t ppf_sg_gemm(const void* a, long long sam, long long sak, const void* b,
+                    long long sbk, long long sbn, float* y, long long ldy,
+                    const float* bias, int32_t accumulate, long long M,
+                    long long N, long long K, int32_t splits, void* stream);
+int32_t ppf_sg_patch_fwd(const PpfSgShape* s, const float* fields,
+                         const void* w_in_bf16, const float* b_in, float* y,
+                         void* y_bf16, void* stream);
+int32_t ppf_sg_patch_bwd_weight(const PpfSgShape* s, const float* fields,
+                                const void* dy_bf16, float* dw_in, float* db_in,
+                                void* stream);
+int32_t ppf_sg_block_fwd(const PpfSgShape* s, const float* y, const float* w_dw,
+                         const float* b_dw, float* h, void* h_bf16,
+                         const void* w1_bf16, const float* b1, float* pre,
+                         void* act_bf16, const void* w2_bf16, const float* b2,
+                         float* y_out, void* y_out_bf16, void* stream);
+int32_t ppf_sg_block_bwd(const PpfSgShape* s, const float* y, const void* h_bf16,
+                         const float* pre, const void* act_bf16,
+                         const void* w1_bf16, const void* w2_bf16,
+                         const float* w_dw, const float* dy_out,
+                         const void* dy_out_bf16, void* dpre_bf16, float* dh,
+                         void* dh_bf16, float* dy, float* dw1, float* db1,
+                         float* dw2, float* db2, float* dw_dw, float* db_dw,
+                         void* stream);
+int32_t ppf_sg_head_fwd(const PpfSgShape* s, const void* y_bf16,
+                        const void* w_out_bf16, const float* b_out, float* out,
+                        void* stream);
+int32_t ppf_sg_head_bwd(const PpfSgShape* s, const void* y_bf16,
+                        const void* w_out_bf16, const void* dout_bf16,
+                        float* dw_out, float* db_out, float* dy, void* dy_bf16,
+                        void* stream);
+/* loss += mean((out - (f_new - f_old) * s)^2); grad = d loss / d out (bf16) */
+int32_t ppf_sg_mse(const PpfSgShape* s, const float* out, const float* f_old,
+                   const float* f_new, void* grad_bf16, double* loss,
+                   void* stream);
+/* f_new = clamp(f_old + out / s, lo, hi) (the surrogate's k-step prediction) */
+int32_t ppf_sg_apply(const PpfSgShape* s, const float* out, const float* f_old,
+                     float* f_new, void* stream);
+/* Window check: per sample b, out[3b] = sum_phi (k (stepped - pred) - (pred - u))^2,
+ * out[3b+1] = sum_phi pred^2, out[3b+2] = cells with a non-finite pred or stepped. */
+int32_t ppf_sg_residual(const PpfSgShape* s, const float* u, const float* pred,
+                        const float* stepped, int32_t k, double* out, void* stream);
+int32_t ppf_sg_cast_bf16(const float* x, void* y, long long n, void* stream);
+int32_t ppf_sg_adam(float* w, void* w_bf16, const float* g, float* m1, float* m2,
+                    long long n, float lr, float b1, float b2, float eps,
+                    int32_t step, float weight_decay, void* stream);
+
 /* ---- diagnostics (FP64 reductions) ------------------------------------ */
 
 /* Bytes of caller-provided device scratch the reductions below need. */

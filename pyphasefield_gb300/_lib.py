@@ -90,6 +90,12 @@ class PpfEnsemblePlan(C.Structure):
                 ("n_members", C.c_int32), ("rows", C.c_int32)]
 
 
+class PpfSgShape(C.Structure):
+    _fields_ = [(n, C.c_int32) for n in ("B", "H", "W", "pitch", "P", "C", "E")] + [
+        (n, C.c_float) for n in ("s0", "s1", "in_off0", "in_sc0", "in_off1", "in_sc1",
+                                 "lo0", "hi0", "lo1", "hi1")]
+
+
 P = C.c_void_p
 I32 = C.c_int32
 U64 = C.c_uint64
@@ -112,6 +118,20 @@ SIGNATURES: dict[str, list] = {
     "ppf_ensemble_plan_bytes": [C.POINTER(PpfMember), I32, PT, C.POINTER(SZ)],
     "ppf_ensemble_build": [C.POINTER(PpfMember), I32, PT, P, SZ, C.POINTER(PpfEnsemblePlan), P],
     "ppf_ensemble_step_f32": [C.POINTER(PpfEnsemblePlan), I32, U64, P, PT, P],
+    "ppf_sg_gemm": [P, C.c_longlong, C.c_longlong, P, C.c_longlong, C.c_longlong, P,
+                    C.c_longlong, P, I32, C.c_longlong, C.c_longlong, C.c_longlong, I32, P],
+    "ppf_sg_patch_fwd": [C.POINTER(PpfSgShape), P, P, P, P, P, P],
+    "ppf_sg_patch_bwd_weight": [C.POINTER(PpfSgShape), P, P, P, P, P],
+    "ppf_sg_residual": [C.POINTER(PpfSgShape), P, P, P, C.c_int32, P, P],
+    "ppf_sg_block_fwd": [C.POINTER(PpfSgShape)] + [P] * 14,
+    "ppf_sg_block_bwd": [C.POINTER(PpfSgShape)] + [P] * 20,
+    "ppf_sg_head_fwd": [C.POINTER(PpfSgShape), P, P, P, P, P],
+    "ppf_sg_head_bwd": [C.POINTER(PpfSgShape), P, P, P, P, P, P, P, P],
+    "ppf_sg_mse": [C.POINTER(PpfSgShape), P, P, P, P, P, P],
+    "ppf_sg_apply": [C.POINTER(PpfSgShape), P, P, P, P],
+    "ppf_sg_cast_bf16": [P, P, C.c_longlong, P],
+    "ppf_sg_adam": [P, P, P, P, P, C.c_longlong, C.c_float, C.c_float, C.c_float, C.c_float,
+                    I32, C.c_float, P],
     "ppf_reduce_scratch_bytes": [PG, C.POINTER(SZ)],
     "ppf_reduce_sum_f32": [P, PG, P, P, SZ, P],
     "ppf_reduce_sum_f64": [P, PG, P, P, SZ, P],
