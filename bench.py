@@ -308,6 +308,114 @@ def run_gb300(args):
         dist.destroy_process_group()
 
 
+SWEEP = {
+    # name: (model, grid, temporal depth, steps); grids exceed the 129 MB L2
+    "diffusion_4096": ("diffusion", (4096, 4096), 1, 200),
+    "diffusion_8192": ("diffusion", (8192, 8192), 1, 100),
+    "diffusion_16384": ("diffusion", (16384, 16384), 1, 100),
+    "diffusion_8192_d4": ("diffusion", (8192, 8192), 4, 200),
+    "diffusion_16384_d4": ("diffusion", (16384, 16384), 4, 100),
+    "diffusion_16384_d8": ("diffusion", (16384, 16384), 8, 200),
+    "allen_cahn_4096": ("allen_cahn", (4096, 4096), 1, 200),
+    "allen_cahn_8192": ("allen_cahn", (8192, 8192), 1, 100),
+    "allen_cahn_16384": ("allen_cahn", (16384, 16384), 1, 100),
+    "allen_cahn_16384_d4": ("allen_cahn", (16384, 16384), 4, 100),
+    "warren1995_4096": ("warren1995", (4096, 4096), 1, 100),
+    "warren1995_8192": ("warren1995", (8192, 8192), 1, 100),
+    "cahn_hilliard_256": ("cahn_hilliard", (256, 256, 256), 1, 500),
+    "cahn_hilliard_384": ("cahn_hilliard", (384, 384, 384), 1, 100),
+    "cahn_hilliard_512": ("cahn_hilliard", (512, 512, 512), 1, 100),
+    "ensemble_64": ("ensemble", None, 1, 2000),
+}
+SWEEP_B_ALG = {"diffusion": 8, "allen_cahn": 8, "cahn_hilliard": 8, "warren1995": 16}
+
+
+def sweep_engine(model, grid, depth, steps, rng):
+    """An engine of `model` on `grid` with seeded synthetic fields."""
+    from pyphasefield_gb300 import (CahnAllenGB300, CahnHilliardGB300, DiffusionGB300,
+                                    Warren1995GB300)
+    ud = {"graph_chunk": min(steps, 100), "temporal_depth": depth}
+    if model == "diffusion":
+        sim = DiffusionGB300(dimensions=list(grid), dx=1.0, dt=0.2,
+                             boundary_conditions="PERIODIC", user_data=dict(ud, D=1.0))
+        init = [0.5 + 0.01 * rng.standard_normal(grid)]
+    elif model == "allen_cahn":
+        sim = CahnAllenGB300(dimensions=list(grid), dx=1.0, dt=0.1,
+                             boundary_conditions="NEUMANN", user_data=dict(ud))
+        init = [rng.random(grid)]
+    elif model == "cahn_hilliard":
+        sim = CahnHilliardGB300(dimensions=list(grid), dx=1.0, dt=0.01,
+                                boundary_conditions="PERIODIC",
+                                user_data=dict(ud, M=1.0, epsilon=1.0))
+        init = [0.5 + rng.uniform(-0.05, 0.05, grid)]
+    else:
+        sim = Warren1995GB300(dimensions=list(grid), dx=DX, boundary_conditions="NEUMANN",
+                              user_data=dict(ud, seed=SEED, alpha=0.3))
+        phi, c = initial_fields(grid)
+        init = [phi, c]
+    sim.initialize_fields_and_imported_data()
+    sl = (slice(1, -1),) * len(grid)
+    for f, v in zip(sim.fields, init):
+        f.data[sl] = v
+    return sim
+
+
+def run_sweep(args):
+    """Roofline sweep at sizes beyond L2 (plus the Cahn-Hilliard 256^3 and
+    64-member ensemble workloads): one JSON line per case."""
+    import torch
+    import __graft_entry__
+    if not (ROOT / "pyphasefield_gb300" / "libppf_gb300.so").exists():
+        __graft_entry__.build()
+    peak, peak_kind = peaks()
+    names = list(SWEEP) if args.sweep == "all" else args.sweep.split(",")
+    for name in names:
+        model, grid, depth, steps = SWEEP[name]
+        rng = np.random.default_rng(0)
+        if model == "ensemble":
+            from pyphasefield_gb300.ensemble import Ensemble, make_config_ensemble
+            sims = make_config_ensemble(n=64, seed=0)
+            runner = Ensemble(sims, graph_chunk=100)
+            cells = runner.cells
+            bytes_per_step = sum(s._ppf_grid.cells * (16 if len(s.fields) == 2 else 8)
+                                 for s in sims)
+            stream = runner.stream
+            advance = runner.simulate
+        else:
+            sim = sweep_engine(model, grid, depth, steps, rng)
+            cells = int(np.prod(grid))
+            bytes_per_step = SWEEP_B_ALG[model] * cells
+            advance = sim.simulate
+        advance(min(steps, 100))  # set-up, upload, graph capture, warm-up
+        if model != "ensemble":
+            stream = sim._ppf_stream
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        advance(steps)
+        e1.record(stream)
+        e1.synchronize()
+        sec = e0.elapsed_time(e1) / 1e3
+        line = {"sweep": name, "model": model, "grid": list(grid) if grid else "config ensemble",
+                "temporal_depth": depth, "steps": steps, "cells": cells,
+                "cell_updates_per_s": cells * steps / sec, "ms_per_step": 1e3 * sec / steps,
+                "algorithmic_bytes_per_step": bytes_per_step,
+                "achieved_gbs": bytes_per_step * steps / sec / 1e9, "peak_gbs": peak,
+                "peak_source": peak_kind}
+        line["frac"] = line["achieved_gbs"] / peak
+        if model == "cahn_hilliard":
+            m = sim.collect_mass_history()
+            line["mass_rel_drift"] = float(abs(m[-1] - m[0]) / abs(m[0]))
+        print(json.dumps(line), flush=True)
+        del advance, stream
+        if model == "ensemble":
+            del runner, sims
+        else:
+            del sim
+        torch.cuda.empty_cache()
+
+
 def profile_case(name: str):
     """Small eager workloads (no timing, no graphs) for ncu captures:
     warren1024  the benchmark grid, 2005 steps (capture launch 2002: a grown crystal)
@@ -356,7 +464,13 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--sweep", default=None,
+                    help="roofline sweep instead of the benchmark: 'all' or a comma list of "
+                         + ", ".join(SWEEP))
     args = ap.parse_args()
+    if args.sweep:
+        run_sweep(args)
+        return
     if args.profile_case:
         profile_case(args.profile_case)
         return
