@@ -336,6 +336,9 @@ SWEEP = {
     "allen_cahn_16384_d4": ("allen_cahn", (16384, 16384), 4, 100),
     "warren1995_4096": ("warren1995", (4096, 4096), 1, 100),
     "warren1995_8192": ("warren1995", (8192, 8192), 1, 100),
+    # every cell takes the full update (no exact bulk shortcut): the cost of
+    # a grid that is interface everywhere
+    "warren1995_4096_full": ("warren1995", (4096, 4096), 1, 100, {"bulk_shortcut": False}),
     "cahn_hilliard_256": ("cahn_hilliard", (256, 256, 256), 1, 500),
     "cahn_hilliard_384": ("cahn_hilliard", (384, 384, 384), 1, 100),
     "cahn_hilliard_512": ("cahn_hilliard", (512, 512, 512), 1, 100),
@@ -344,11 +347,11 @@ SWEEP = {
 SWEEP_B_ALG = {"diffusion": 8, "allen_cahn": 8, "cahn_hilliard": 8, "warren1995": 16}
 
 
-def sweep_engine(model, grid, depth, steps, rng):
+def sweep_engine(model, grid, depth, steps, rng, extra=None):
     """An engine of `model` on `grid` with seeded synthetic fields."""
     from pyphasefield_gb300 import (CahnAllenGB300, CahnHilliardGB300, DiffusionGB300,
                                     Warren1995GB300)
-    ud = {"graph_chunk": min(steps, 100), "temporal_depth": depth}
+    ud = dict({"graph_chunk": min(steps, 100), "temporal_depth": depth}, **(extra or {}))
     if model == "diffusion":
         sim = DiffusionGB300(dimensions=list(grid), dx=1.0, dt=0.2,
                              boundary_conditions="PERIODIC", user_data=dict(ud, D=1.0))
@@ -384,7 +387,8 @@ def run_sweep(args):
     peak, peak_kind = peaks()
     names = list(SWEEP) if args.sweep == "all" else args.sweep.split(",")
     for name in names:
-        model, grid, depth, steps = SWEEP[name]
+        model, grid, depth, steps = SWEEP[name][:4]
+        extra = SWEEP[name][4] if len(SWEEP[name]) > 4 else None
         rng = np.random.default_rng(0)
         if model == "ensemble":
             from pyphasefield_gb300.ensemble import Ensemble, make_config_ensemble
@@ -396,7 +400,7 @@ def run_sweep(args):
             stream = runner.stream
             advance = runner.simulate
         else:
-            sim = sweep_engine(model, grid, depth, steps, rng)
+            sim = sweep_engine(model, grid, depth, steps, rng, extra)
             cells = int(np.prod(grid))
             bytes_per_step = SWEEP_B_ALG[model] * cells
             advance = sim.simulate
@@ -412,7 +416,7 @@ def run_sweep(args):
         e1.synchronize()
         sec = e0.elapsed_time(e1) / 1e3
         line = {"sweep": name, "model": model, "grid": list(grid) if grid else "config ensemble",
-                "temporal_depth": depth, "steps": steps, "cells": cells,
+                "temporal_depth": depth, "steps": steps, "cells": cells, "options": extra or {},
                 "cell_updates_per_s": cells * steps / sec, "ms_per_step": 1e3 * sec / steps,
                 "algorithmic_bytes_per_step": bytes_per_step,
                 "achieved_gbs": bytes_per_step * steps / sec / 1e9, "peak_gbs": peak,

@@ -97,6 +97,56 @@ __device__ __forceinline__ void load_cell(const T* __restrict__ phi, const T* __
   }
 }
 
+// Noise words of a band, computed once per Philox block. Cell (row, x)
+// takes word x % 4 of the block with counter (x / 4, row, step): the band's
+// owned columns x0 .. x0 + 29 span at most kGroups blocks per row, so the
+// ROWS * kGroups blocks of a band are spread over the lanes (one block per
+// lane and pass) and each cell fetches its word from the computing lane by
+// shuffles, instead of every lane evaluating the block of its own column.
+constexpr int kGroups = 9;
+
+template <int ROWS>
+struct BandNoise {
+  static constexpr int kJobs = ROWS * kGroups;
+  static constexpr int kPasses = (kJobs + 31) / 32;
+  U4 w[kPasses];
+
+  __device__ __forceinline__ void draw(uint64_t seed, uint64_t step, int y0, uint32_t gbase) {
+    const int lane = threadIdx.x;
+#pragma unroll
+    for (int p = 0; p < kPasses; ++p) {
+      const int job = p * 32 + lane;
+      const int r = job / kGroups, i = job - r * kGroups;
+      w[p] = job < kJobs ? noise_group(seed, step, (uint32_t)(y0 + r), gbase + (uint32_t)i)
+                         : U4{0u, 0u, 0u, 0u};
+    }
+  }
+  // Word of column x (x / 4 - gbase in [0, kGroups)) on band row r; every
+  // lane of the warp must call this together.
+  __device__ __forceinline__ uint32_t word(int r, int x, uint32_t gbase) const {
+    int i = (int)((uint32_t)x / 4u - gbase);
+    i = i < 0 ? 0 : (i >= kGroups ? kGroups - 1 : i);  // halo lanes: any valid source
+    const int job = r * kGroups + i;
+    uint32_t v[4] = {0u, 0u, 0u, 0u};
+#pragma unroll
+    for (int p = 0; p < kPasses; ++p) {
+      const int src = job - p * 32;
+      const uint32_t a = __shfl_sync(0xffffffffu, w[p].x, src & 31);
+      const uint32_t b = __shfl_sync(0xffffffffu, w[p].y, src & 31);
+      const uint32_t c = __shfl_sync(0xffffffffu, w[p].z, src & 31);
+      const uint32_t d = __shfl_sync(0xffffffffu, w[p].w, src & 31);
+      if (src >= 0 && src < 32) {
+        v[0] = a;
+        v[1] = b;
+        v[2] = c;
+        v[3] = d;
+      }
+    }
+    const int j = x & 3;
+    return j == 0 ? v[0] : (j == 1 ? v[1] : (j == 2 ? v[2] : v[3]));
+  }
+};
+
 template <typename T>
 __device__ __forceinline__ T shfl_w(T v) { return __shfl_up_sync(0xffffffffu, v, 1); }
 template <typename T>
@@ -125,6 +175,10 @@ __device__ __forceinline__ void band(const Coef<T>& k, const Geo& g, const Bc<T>
   T pNW = shfl_w(pN), pNE = shfl_e(pN);
   T pW = shfl_w(p0), pE = shfl_e(p0);
   const bool noisy = k.alpha != T(0);
+  // first owned column's Philox block (owners are lanes 1..30, x >= 0)
+  const uint32_t gbase = (uint32_t)(xs + 1) / 4u;
+  BandNoise<ROWS> noise;
+  bool drawn = false;
 
 #pragma unroll
   for (int r = 0; r < ROWS; ++r) {
@@ -141,13 +195,15 @@ __device__ __forceinline__ void band(const Coef<T>& k, const Geo& g, const Bc<T>
     // exactly 0). There every phi difference, g(phi) and g'(phi) is exactly
     // zero, so dphi = 0, D~ is uniform and Q~ = 0: the full expressions below
     // reduce exactly to phi' = phi, c' = c + D~ lap(c).
-    bool bulk = true;
-    if (k.bulk && owner) {
+    // (bitwise, branch-free test: no divergence on the common non-bulk path)
+    bool bulk = false;
+    if (k.bulk) {
       const T v = p0;
-      bulk = (v == T(1) || v == T(0)) && pN == v && pS == v && pW == v && pE == v &&
-             pNW == v && pNE == v && pSW == v && pSE == v;
+      const bool b = ((v == T(1)) | (v == T(0))) & (pN == v) & (pS == v) & (pW == v) &
+                     (pE == v) & (pNW == v) & (pNE == v) & (pSW == v) & (pSE == v);
+      bulk = __all_sync(0xffffffffu, b | !owner);
     }
-    if (k.bulk && __all_sync(0xffffffffu, bulk)) {
+    if (bulk) {
       p1 = p0;
       c1 = c0 + D0 * lc;
     } else {
@@ -197,9 +253,11 @@ __device__ __forceinline__ void band(const Coef<T>& k, const Geo& g, const Bc<T>
       // proportional to g); the warp draws only if one of its cells needs it
       const bool need = noisy && owner && g0 != T(0);
       if (__any_sync(0xffffffffu, need)) {
-        const U4 w4 = noise_group(seed, step, (uint32_t)row, (uint32_t)(x >> 2));
-        const int j = x & 3;
-        const uint32_t w = j == 0 ? w4.x : (j == 1 ? w4.y : (j == 2 ? w4.z : w4.w));
+        if (!drawn) {  // the band's blocks, at the first row that needs any
+          noise.draw(seed, step, y0, gbase);
+          drawn = true;
+        }
+        const uint32_t w = noise.word(r, x, gbase);
         if (need) {
           const T u = T(w >> 8) * T(5.9604644775390625e-08);
           dphi += dtM * k.alpha * (T(2) * u - T(1)) * (T(16) * g0) * Hs;
