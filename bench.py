@@ -437,17 +437,19 @@ def run_sweep(args):
 def profile_case(name: str):
     """Small eager workloads (no timing, no graphs) for ncu captures:
     warren1024  the benchmark grid, 2005 steps (capture launch 2002: a grown crystal)
+    warren1024_late  the benchmark grid, 9605 steps (capture launch 9600: the state the
+                last tenth of a bench step runs on; no cell is exactly bulk any more)
     ch256       Cahn-Hilliard 256^3 periodic, dt 0.01, 5 steps
     diff4096    Diffusion 2-D 4096^2 periodic, 5 steps (temporal depth from PPF_DEPTH, default 1)
     """
     import torch
     from pyphasefield_gb300 import CahnHilliardGB300, DiffusionGB300
     rng = np.random.default_rng(0)
-    if name == "warren1024":
+    if name in ("warren1024", "warren1024_late"):
         phi0, c0 = initial_fields()
         sim = make_sim(phi0, c0, 100)
         sim.user_data["use_graph"] = False
-        sim.simulate(2005)
+        sim.simulate(2005 if name == "warren1024" else 9605)
     elif name == "ch256":
         sim = CahnHilliardGB300(dimensions=[256, 256, 256], dx=1.0, dt=0.01,
                                 boundary_conditions="PERIODIC",

@@ -152,22 +152,45 @@ __device__ __forceinline__ T shfl_w(T v) { return __shfl_up_sync(0xffffffffu, v,
 template <typename T>
 __device__ __forceinline__ T shfl_e(T v) { return __shfl_down_sync(0xffffffffu, v, 1); }
 
+// Loads of one band (rows y0 - 1 .. y0 + ROWS, this lane's column).
+template <typename T, int ROWS>
+__device__ __forceinline__ void band_load(const Geo& g, const Bc<T>& bc,
+                                          const T* __restrict__ phi_in,
+                                          const T* __restrict__ c_in, int xs, int y0,
+                                          T (&bp)[ROWS + 2], T (&bcv)[ROWS + 2]) {
+  const int x = xs + (int)threadIdx.x;
+  const bool x_in = xs >= 0 && xs + 31 < g.n[1];
+#pragma unroll
+  for (int j = 0; j < ROWS + 2; ++j)
+    load_cell(phi_in, c_in, g, bc, y0 - 1 + j, x, x_in, bp[j], bcv[j]);
+}
+
+template <typename T, int ROWS>
+__device__ __forceinline__ void band_compute(const Coef<T>& k, const Geo& g,
+                                             T* __restrict__ phi_out, T* __restrict__ c_out,
+                                             uint64_t seed, uint64_t step, int xs, int y0,
+                                             const T (&bp)[ROWS + 2], const T (&bcv)[ROWS + 2]);
+
 // One band: strip whose lane 0 sits at column xs, rows y0 .. y0+ROWS-1.
 template <typename T, int ROWS>
 __device__ __forceinline__ void band(const Coef<T>& k, const Geo& g, const Bc<T>& bc,
                                      const T* __restrict__ phi_in, const T* __restrict__ c_in,
                                      T* __restrict__ phi_out, T* __restrict__ c_out,
                                      uint64_t seed, uint64_t step, int xs, int y0) {
+  T bp[ROWS + 2], bcv[ROWS + 2];
+  band_load<T, ROWS>(g, bc, phi_in, c_in, xs, y0, bp, bcv);
+  band_compute<T, ROWS>(k, g, phi_out, c_out, seed, step, xs, y0, bp, bcv);
+}
+
+template <typename T, int ROWS>
+__device__ __forceinline__ void band_compute(const Coef<T>& k, const Geo& g,
+                                             T* __restrict__ phi_out, T* __restrict__ c_out,
+                                             uint64_t seed, uint64_t step, int xs, int y0,
+                                             const T (&bp)[ROWS + 2], const T (&bcv)[ROWS + 2]) {
   const int lane = threadIdx.x;
   const int ny = g.n[0], nx = g.n[1];
   const int x = xs + lane;
-  const bool x_in = xs >= 0 && xs + 31 < nx;
   const bool owner = lane >= 1 && lane <= kStrip && x < nx;
-
-  T bp[ROWS + 2], bcv[ROWS + 2];
-#pragma unroll
-  for (int j = 0; j < ROWS + 2; ++j)
-    load_cell(phi_in, c_in, g, bc, y0 - 1 + j, x, x_in, bp[j], bcv[j]);
 
   T pN = bp[0], cN = bcv[0], p0 = bp[1], c0 = bcv[1], DN, QN, D0, Q0;
   point(k, pN, cN, DN, QN);
