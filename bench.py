@@ -339,6 +339,7 @@ SWEEP = {
     # every cell takes the full update (no exact bulk shortcut): the cost of
     # a grid that is interface everywhere
     "warren1995_4096_full": ("warren1995", (4096, 4096), 1, 100, {"bulk_shortcut": False}),
+    "diffusion3d_512": ("diffusion", (512, 512, 512), 1, 100),
     "cahn_hilliard_256": ("cahn_hilliard", (256, 256, 256), 1, 500),
     "cahn_hilliard_384": ("cahn_hilliard", (384, 384, 384), 1, 100),
     "cahn_hilliard_512": ("cahn_hilliard", (512, 512, 512), 1, 100),
@@ -434,6 +435,116 @@ def run_sweep(args):
         torch.cuda.empty_cache()
 
 
+def _errors(a, b):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    return {"rel_l2": float(np.linalg.norm(a - b) / np.linalg.norm(b)),
+            "linf": float(np.abs(a - b).max())}
+
+
+def run_accuracy(args):
+    """FP32 engines against FP64 references per configuration, one JSON
+    line each: Diffusion 256^2 against the numpy oracle (oracle/restate.py,
+    the reference's own engine functions restated), Warren1995 1024^2,
+    Cahn-Hilliard 256^3 and ensemble members against the FP64 engines (the
+    same kernels in double, equal to the oracle within 1e-12 in the tests)."""
+    import __graft_entry__
+    from oracle import restate
+    from pyphasefield_gb300 import DiffusionGB300
+    if not (ROOT / "pyphasefield_gb300" / "libppf_gb300.so").exists():
+        __graft_entry__.build()
+    rng = np.random.default_rng(SEED)
+
+    def cells(sim):
+        sim.retrieve_fields_from_GPU()
+        return [f.get_cells().copy() for f in sim.fields]
+
+    # configuration 1: Diffusion 2-D 256^2, dt = 0.2, periodic, 1000 steps
+    c0 = 0.5 + 0.01 * rng.standard_normal((256, 256))
+    sim = DiffusionGB300(dimensions=[256, 256], dx=1.0, dt=0.2, boundary_conditions="PERIODIC",
+                         user_data={"D": 1.0})
+    sim.initialize_fields_and_imported_data()
+    sim.fields[0].data[1:-1, 1:-1] = c0
+    sim.simulate(1000)
+    ref = restate.run_single("diffusion", c0, 1000, "PERIODIC", 1.0, 0.2, D=1.0)
+    print(json.dumps({"accuracy": "diffusion_256_1000", "reference": "fp64 numpy oracle",
+                      "c": _errors(cells(sim)[0], ref)}), flush=True)
+
+    # configuration 2: Warren1995 1024^2, alpha = 0 (parity run), 1000 and 10,000 steps
+    phi0, cc0 = initial_fields()
+    _warren_accuracy(phi0, cc0, cells, "")
+    # the same with the disk centred between cells (511.5, 511.5): no cell
+    # sits at the seed's centre, where grad phi = 0 exactly and the angle
+    # is set by rounding residue (atan2 of two FP64 residues)
+    yy, xx = np.mgrid[0:SHAPE[0], 0:SHAPE[1]]
+    phi_h = np.ones(SHAPE)
+    phi_h[(yy - 511.5) ** 2 + (xx - 511.5) ** 2 < 25] = 0.0
+    _warren_accuracy(phi_h, cc0, cells, "_offcentre")
+    _rest_of_accuracy(rng, cells)
+
+
+def _warren_accuracy(phi0, cc0, cells, tag):
+    from pyphasefield_gb300 import Warren1995GB300
+    runs = {}
+    for prec in ("fp32", "fp64"):
+        w = Warren1995GB300(dimensions=list(SHAPE), dx=DX, boundary_conditions="NEUMANN",
+                            user_data={"seed": SEED, "alpha": 0.0, "precision": prec})
+        w.initialize_fields_and_imported_data()
+        w.fields[0].data[1:-1, 1:-1] = phi0
+        w.fields[1].data[1:-1, 1:-1] = cc0
+        w.simulate(1000)
+        a = cells(w)
+        w.simulate(9000)
+        runs[prec] = (a, cells(w))
+    for i, n in enumerate((1000, 10000)):
+        print(json.dumps({"accuracy": f"warren1995_1024_{n}{tag}", "reference": "fp64 engine",
+                          "alpha": 0.0,
+                          "phi": _errors(runs["fp32"][i][0], runs["fp64"][i][0]),
+                          "c": _errors(runs["fp32"][i][1], runs["fp64"][i][1])}), flush=True)
+
+
+def _rest_of_accuracy(rng, cells):
+    import torch
+    from pyphasefield_gb300 import CahnHilliardGB300
+    # configuration 3: Cahn-Hilliard 3-D 256^3, dt = 0.01, periodic, 1000 steps
+    u0 = 0.5 + rng.uniform(-0.05, 0.05, (256, 256, 256))
+    out = {}
+    for prec in ("fp32", "fp64"):
+        ch = CahnHilliardGB300(dimensions=[256, 256, 256], dx=1.0, dt=0.01,
+                               boundary_conditions="PERIODIC",
+                               user_data={"M": 1.0, "epsilon": 1.0, "precision": prec})
+        ch.initialize_fields_and_imported_data()
+        ch.fields[0].data[1:-1, 1:-1, 1:-1] = u0
+        ch.simulate(1000)
+        m = ch.collect_mass_history()
+        out[prec] = (cells(ch)[0], float(abs(m[-1] - m[0]) / abs(m[0])))
+        del ch
+        torch.cuda.empty_cache()
+    print(json.dumps({"accuracy": "cahn_hilliard_256_1000", "reference": "fp64 engine",
+                      "c": _errors(out["fp32"][0], out["fp64"][0]),
+                      "mass_rel_drift_fp32": out["fp32"][1],
+                      "mass_rel_drift_fp64": out["fp64"][1]}), flush=True)
+
+    # configuration 4: ensemble members (fp32, one launch per step) against
+    # the same members stepped alone in fp64, 2000 steps (first 8 members)
+    from pyphasefield_gb300.ensemble import Ensemble, make_config_ensemble
+    ens_sims = make_config_ensemble(n=64, seed=0)[:8]
+    solo = make_config_ensemble(n=64, seed=0, precision="fp64")[:8]
+    Ensemble(ens_sims, graph_chunk=100).simulate(2000)
+    members = []
+    for a, b in zip(ens_sims, solo):
+        b.simulate(2000)
+        m = {"model": type(a).__name__, "side": a.dimensions[0]}
+        for name, fa, fb in zip(("phi", "c"), cells(a), cells(b)):
+            e = _errors(fa, fb)
+            if not np.linalg.norm(fb) > 1e-6 * np.sqrt(fb.size):  # field gone to ~0
+                e = {"rms": float(np.sqrt(np.mean((fa - fb) ** 2))), "linf": e["linf"]}
+            m[name] = e
+        members.append(m)
+    print(json.dumps({"accuracy": "ensemble_members_2000", "reference": "fp64 engines, alone",
+                      "alpha": 0.3, "members": members}), flush=True)
+
+
 def profile_case(name: str):
     """Small eager workloads (no timing, no graphs) for ncu captures:
     warren1024  the benchmark grid, 2005 steps (capture launch 2002: a grown crystal)
@@ -487,7 +598,12 @@ def main():
     ap.add_argument("--sweep", default=None,
                     help="roofline sweep instead of the benchmark: 'all' or a comma list of "
                          + ", ".join(SWEEP))
+    ap.add_argument("--accuracy", action="store_true",
+                    help="FP32 vs FP64 errors per configuration instead of the benchmark")
     args = ap.parse_args()
+    if args.accuracy:
+        run_accuracy(args)
+        return
     if args.sweep:
         run_sweep(args)
         return

@@ -51,9 +51,10 @@ struct PlaneRing {
   uint64_t* bars;
   int slot_elems;  // elements per slot (BX * BY, padded to 128 bytes)
   int pbase;
-  __device__ T* plane(int p) const { return slots + ((p - pbase) % NS) * slot_elems; }
-  __device__ uint64_t* bar(int p) const { return bars + (p - pbase) % NS; }
-  __device__ uint32_t parity(int p) const { return (uint32_t)(((p - pbase) / NS) & 1); }
+  // p >= pbase always: unsigned arithmetic (a mask when NS is a power of two)
+  __device__ T* plane(int p) const { return slots + ((unsigned)(p - pbase) % NS) * slot_elems; }
+  __device__ uint64_t* bar(int p) const { return bars + (unsigned)(p - pbase) % NS; }
+  __device__ uint32_t parity(int p) const { return ((unsigned)(p - pbase) / NS) & 1u; }
 };
 
 struct MarchGeom {
@@ -130,9 +131,13 @@ __device__ void drain(const PlaneRing<T, NS>& ring, int first, int last) {
   __syncthreads();
 }
 
+// First 128-byte aligned address at or after p (the dynamic shared memory
+// base). The offset is added to p itself, not to an integer copy of it, so
+// the compiler keeps the shared address space and emits shared loads.
 template <typename T>
 __device__ __forceinline__ T* align128(unsigned char* p) {
-  return reinterpret_cast<T*>((reinterpret_cast<uintptr_t>(p) + 127) & ~uintptr_t(127));
+  const uint32_t a = (uint32_t)__cvta_generic_to_shared(p);
+  return reinterpret_cast<T*>(p + ((128u - (a & 127u)) & 127u));
 }
 
 // ------------------------------------------------------------- 7-point
@@ -238,7 +243,7 @@ __device__ __forceinline__ T ch_flux(const ChCoef<T>& k, T mn, T mc) {
   return f;
 }
 
-constexpr int kNSC = 6;  // c planes z..z+2 read, z+3 and z+4 in flight
+constexpr int kNSC = 8;  // c planes z-2..z+2 in use or kept, z+3 .. z+5 in flight
 // Cahn-Hilliard tile: 32 x 16 cells, 256 threads; thread (tx, ty) owns the
 // xy-columns (ty, tx) and (ty + 8, tx) and keeps, per column, c(z..z+2) and
 // mu(z-1..z+1) in registers while marching along z. mu of the tile plus a
@@ -316,11 +321,12 @@ __global__ void __launch_bounds__(kThreads)
   pdl_launch_next();
   const int last = z1 + 1;
   if (leader)
-    for (int p = z0 - 2; p <= min(z0 + 3, last); ++p) issue_plane(ring, &map, g, bc, m, x0, y0, p);
+    for (int p = z0 - 2; p <= min(z0 + kNSC - 3, last); ++p)
+      issue_plane(ring, &map, g, bc, m, x0, y0, p);
   for (int p = z0 - 2; p <= z0 + 1; ++p) {
     if (!wait_all(ring.bar(p), ring.parity(p), &abort_flag)) {
       report_timeout<T>(lib_status);
-      drain(ring, p, min(z0 + 3, last));
+      drain(ring, p, min(z0 + kNSC - 3, last));
       return;
     }
     fixup_plane(ring, in, g, bc, m, x0, y0, p, xy_edge);
@@ -351,11 +357,22 @@ __global__ void __launch_bounds__(kThreads)
   long long acc_q = 0;
   double acc = 0.0;
   int flags = 0;
+  T* optr[2];
+  bool oin[2];
+#pragma unroll
+  for (int j = 0; j < 2; ++j) {
+    const int gy = y0 + ty + 8 * j, gx = x0 + tx;
+    oin[j] = gy < ny && gx < nx;
+    optr[j] = out + (int64_t)z0 * g.plane + (int64_t)gy * g.pitch + gx;
+  }
   for (int z = z0; z < z1; ++z) {
-    if (leader && z + 4 <= last) issue_plane(ring, &map, g, bc, m, x0, y0, z + 4);
+    // plane z + kNSC - 2 reuses the slot of plane z - 2, last read in
+    // iteration z - 2 (c plane q is read in iterations q - 2 .. q), before
+    // the barriers of iteration z - 1
+    if (leader && z + kNSC - 2 <= last) issue_plane(ring, &map, g, bc, m, x0, y0, z + kNSC - 2);
     if (!wait_all(ring.bar(z + 2), ring.parity(z + 2), &abort_flag)) {
       report_timeout<T>(lib_status);
-      drain(ring, z + 2, min(z + 4, last));
+      drain(ring, z + 2, min(z + kNSC - 2, last));
       return;
     }
     fixup_plane(ring, in, g, bc, m, x0, y0, z + 2, xy_edge);
@@ -386,9 +403,8 @@ __global__ void __launch_bounds__(kThreads)
       const T fd = ch_flux<T, QUANT>(k, mu_m[j], m0);
       const T fu = ch_flux<T, QUANT>(k, mu_p[j], m0);
       const T v = c0[j] + (((fw + fe) + (fn + fs)) + (fd + fu));
-      const int gy = y0 + ty + 8 * j, gx = x0 + tx;
-      if (gy < ny && gx < nx) {
-        out[(int64_t)z * g.plane + (int64_t)gy * g.pitch + gx] = v;
+      if (oin[j]) {
+        *optr[j] = v;
         if (QUANT) {
           acc_q += (long long)__float2int_rn((float)(v * k.iq));
           if (!(fabs(v) < k.range)) flags |= PPF_STATUS_RANGE;
@@ -401,6 +417,7 @@ __global__ void __launch_bounds__(kThreads)
       c1[j] = c2[j];
       mu_m[j] = m0;
       mu_0[j] = mu_p[j];
+      optr[j] += g.plane;
     }
   }
   if (status && flags) atomicOr(status, flags);
