@@ -534,7 +534,7 @@ def _rest_of_accuracy(rng, cells):
     members = []
     for a, b in zip(ens_sims, solo):
         b.simulate(2000)
-        m = {"model": type(a).__name__, "side": a.dimensions[0]}
+        m = {"model": type(a).__name__, "side": int(a.dimensions[0])}
         for name, fa, fb in zip(("phi", "c"), cells(a), cells(b)):
             e = _errors(fa, fb)
             if not np.linalg.norm(fb) > 1e-6 * np.sqrt(fb.size):  # field gone to ~0

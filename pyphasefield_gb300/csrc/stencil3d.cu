@@ -243,18 +243,25 @@ __device__ __forceinline__ T ch_flux(const ChCoef<T>& k, T mn, T mc) {
   return f;
 }
 
-constexpr int kNSC = 8;  // c planes z-2..z+2 in use or kept, z+3 .. z+5 in flight
-// Cahn-Hilliard tile: 32 x 16 cells, 256 threads; thread (tx, ty) owns the
-// xy-columns (ty, tx) and (ty + 8, tx) and keeps, per column, c(z..z+2) and
-// mu(z-1..z+1) in registers while marching along z. mu of the tile plus a
-// one-cell ring is kept in a two-plane shared ring for the xy fluxes; the
-// kRingN ring positions are computed by threads 0..kRingN-1.
+constexpr int kNSC = 8;  // c planes z..z+2 read, z+3 .. z+6 in flight
+// Cahn-Hilliard tile: 32 x 32 cells, 256 threads; thread (tx, ty) owns the
+// kCQ = 4 xy-columns (ty + 8q, tx) and keeps, per column, c(z), c(z+1),
+// mu(z) and the flux through the face below plane z in registers while
+// marching along z (the flux through a face is computed once: the cell
+// above takes it negated, bit for bit). mu of the tile plus a one-cell ring
+// lives in a two-plane shared ring for the xy fluxes; the kRingN ring
+// positions are computed by threads 0..kRingN-1. Every shared index is a
+// compile-time offset from a per-thread base.
 constexpr int kCTX = 32;
-constexpr int kCTY = 16;
+constexpr int kCTY = 32;
+constexpr int kCQ = kCTY / 8;
+constexpr int kCW = kCTX + 2 * kXOff;     // c plane row length (TMA box width)
+constexpr int kCH = kCTY + 4;             // c plane rows (halo 2)
+constexpr int kCSlot = kCW * kCH;         // 1440 elements, a multiple of 128 bytes
 constexpr int kMW = kCTX + 2;
 constexpr int kMH = kCTY + 2;
 constexpr int kMN = kMW * kMH;
-constexpr int kRingN = kMN - kCTX * kCTY;  // 100
+constexpr int kRingN = kMN - kCTX * kCTY;  // 132
 
 // Ring position i -> mu-region coordinates (ly, lx) on the border.
 __device__ __forceinline__ void ring_pos(int i, int& ly, int& lx) {
@@ -289,25 +296,21 @@ __global__ void __launch_bounds__(kThreads)
   const int z1 = min(z0 + m.ZC, nz);
   const bool xy_edge = x0 - kXOff < 0 || y0 - 2 < 0 || x0 + kCTX + kXOff > nx ||
                        y0 + kCTY + 2 > ny;
-  PlaneRing<T, kNSC> ring{align128<T>(smem_raw), bars, slot_elems, z0 - 2};
-  T* const mring = ring.slots + kNSC * slot_elems;  // 2 mu planes
-  auto mslot = [&](int z) { return mring + ((z - z0 + 2) & 1) * kMN; };
+  PlaneRing<T, kNSC> ring{align128<T>(smem_raw), bars, kCSlot, z0 - 2};
+  T* const mring = ring.slots + kNSC * kCSlot;  // 2 mu planes
+  auto mslot = [&](int z) { return mring + ((z - z0) & 1) * kMN; };
   const bool leader = tid == 0;
-  const int W = m.BX;
+  (void)slot_elems;
 
-  // own columns: c-plane index ci, mu-plane index mi
-  int ci[2], mi[2];
-#pragma unroll
-  for (int j = 0; j < 2; ++j) {
-    ci[j] = (ty + 8 * j + 2) * W + tx + kXOff;
-    mi[j] = (ty + 8 * j + 1) * kMW + tx + 1;
-  }
+  // own cells q: c-plane index ci + q * 8 * kCW, mu-plane index mi + q * 8 * kMW
+  const int ci = (ty + 2) * kCW + tx + kXOff;
+  const int mi = (ty + 1) * kMW + tx + 1;
   const bool has_ring = tid < kRingN;
   int rci = 0, rmi = 0;
   if (has_ring) {
     int ly, lx;
     ring_pos(tid, ly, lx);
-    rci = (ly + 1) * W + lx + (kXOff - 1);
+    rci = (ly + 1) * kCW + lx + (kXOff - 1);
     rmi = ly * kMW + lx;
   }
 
@@ -334,9 +337,9 @@ __global__ void __launch_bounds__(kThreads)
   __syncthreads();
 
   auto mu_at = [&](const T* cd, const T* cc, const T* cu, int i) {
-    return ch_mu(k, cc[i], cc[i - 1], cc[i + 1], cc[i - W], cc[i + W], cd[i], cu[i]);
+    return ch_mu(k, cc[i], cc[i - 1], cc[i + 1], cc[i - kCW], cc[i + kCW], cd[i], cu[i]);
   };
-  T c0[2], c1[2], mu_m[2], mu_0[2];
+  T c0[kCQ], c1[kCQ], mu0[kCQ], fup[kCQ];
   {
     const T* Pm2 = ring.plane(z0 - 2);
     const T* Pm1 = ring.plane(z0 - 1);
@@ -344,30 +347,33 @@ __global__ void __launch_bounds__(kThreads)
     const T* P1 = ring.plane(z0 + 1);
     T* M0 = mslot(z0);
 #pragma unroll
-    for (int j = 0; j < 2; ++j) {
-      mu_m[j] = mu_at(Pm2, Pm1, P0, ci[j]);
-      mu_0[j] = mu_at(Pm1, P0, P1, ci[j]);
-      M0[mi[j]] = mu_0[j];
-      c0[j] = P0[ci[j]];
-      c1[j] = P1[ci[j]];
+    for (int q = 0; q < kCQ; ++q) {
+      const int i = ci + q * 8 * kCW;
+      const T mum = mu_at(Pm2, Pm1, P0, i);
+      mu0[q] = mu_at(Pm1, P0, P1, i);
+      M0[mi + q * 8 * kMW] = mu0[q];
+      c0[q] = P0[i];
+      c1[q] = P1[i];
+      // flux through the face below z0, stored negated as "flux into the
+      // cell below from above": the loop takes fd = -fup
+      fup[q] = -ch_flux<T, QUANT>(k, mum, mu0[q]);
     }
     if (has_ring) M0[rmi] = mu_at(Pm1, P0, P1, rci);
   }
 
+  T* optr = out + (int64_t)z0 * g.plane + (int64_t)(y0 + ty) * g.pitch + x0 + tx;
+  const int64_t qstride = (int64_t)8 * g.pitch;
+  const bool xin = x0 + tx < nx;
+  int nq = 0;  // own rows inside the grid: rows ty + 8q < ny - y0
+#pragma unroll
+  for (int q = 0; q < kCQ; ++q) nq += (xin && y0 + ty + 8 * q < ny) ? 1 : 0;
+
   long long acc_q = 0;
   double acc = 0.0;
-  int flags = 0;
-  T* optr[2];
-  bool oin[2];
-#pragma unroll
-  for (int j = 0; j < 2; ++j) {
-    const int gy = y0 + ty + 8 * j, gx = x0 + tx;
-    oin[j] = gy < ny && gx < nx;
-    optr[j] = out + (int64_t)z0 * g.plane + (int64_t)gy * g.pitch + gx;
-  }
+  T vmax = T(0), vsum = T(0);
   for (int z = z0; z < z1; ++z) {
     // plane z + kNSC - 2 reuses the slot of plane z - 2, last read in
-    // iteration z - 2 (c plane q is read in iterations q - 2 .. q), before
+    // iteration z - 2 (c plane p is read in iterations p - 2 .. p), before
     // the barriers of iteration z - 1
     if (leader && z + kNSC - 2 <= last) issue_plane(ring, &map, g, bc, m, x0, y0, z + kNSC - 2);
     if (!wait_all(ring.bar(z + 2), ring.parity(z + 2), &abort_flag)) {
@@ -375,51 +381,55 @@ __global__ void __launch_bounds__(kThreads)
       drain(ring, z + 2, min(z + kNSC - 2, last));
       return;
     }
-    fixup_plane(ring, in, g, bc, m, x0, y0, z + 2, xy_edge);
-    __syncthreads();
+    if (xy_edge || ghost_plane(g, bc, z + 2)) {
+      fixup_plane(ring, in, g, bc, m, x0, y0, z + 2, xy_edge);
+      __syncthreads();
+    }
     const T* P0 = ring.plane(z);
     const T* P1 = ring.plane(z + 1);
     const T* P2 = ring.plane(z + 2);
     T* M1 = mslot(z + 1);
-    T c2[2], mu_p[2];
+    T c2[kCQ], mup[kCQ];
 #pragma unroll
-    for (int j = 0; j < 2; ++j) {
-      const int i = ci[j];
-      c2[j] = P2[i];
-      mu_p[j] = ch_mu(k, c1[j], P1[i - 1], P1[i + 1], P1[i - W], P1[i + W], c0[j], c2[j]);
-      M1[mi[j]] = mu_p[j];
+    for (int q = 0; q < kCQ; ++q) {
+      const int i = ci + q * 8 * kCW;
+      c2[q] = P2[i];
+      mup[q] = ch_mu(k, c1[q], P1[i - 1], P1[i + 1], P1[i - kCW], P1[i + kCW], c0[q], c2[q]);
+      M1[mi + q * 8 * kMW] = mup[q];
     }
     if (has_ring) M1[rmi] = mu_at(P0, P1, P2, rci);
     __syncthreads();
     const T* M0 = mslot(z);
+    int32_t quanta = 0;
 #pragma unroll
-    for (int j = 0; j < 2; ++j) {
-      const int i = mi[j];
-      const T m0 = mu_0[j];
+    for (int q = 0; q < kCQ; ++q) {
+      const int i = mi + q * 8 * kMW;
+      const T m0 = mu0[q];
       const T fw = ch_flux<T, QUANT>(k, M0[i - 1], m0);
       const T fe = ch_flux<T, QUANT>(k, M0[i + 1], m0);
       const T fn = ch_flux<T, QUANT>(k, M0[i - kMW], m0);
       const T fs = ch_flux<T, QUANT>(k, M0[i + kMW], m0);
-      const T fd = ch_flux<T, QUANT>(k, mu_m[j], m0);
-      const T fu = ch_flux<T, QUANT>(k, mu_p[j], m0);
-      const T v = c0[j] + (((fw + fe) + (fn + fs)) + (fd + fu));
-      if (oin[j]) {
-        *optr[j] = v;
-        if (QUANT) {
-          acc_q += (long long)__float2int_rn((float)(v * k.iq));
-          if (!(fabs(v) < k.range)) flags |= PPF_STATUS_RANGE;
-        } else {
-          acc += (double)v;
-        }
-        if (!isfinite(v)) flags |= PPF_STATUS_NONFINITE;
+      const T fu = ch_flux<T, QUANT>(k, mup[q], m0);
+      const T fd = -fup[q];
+      const T v = c0[q] + (((fw + fe) + (fn + fs)) + (fd + fu));
+      if (q < nq) {
+        optr[q * qstride] = v;
+        if (QUANT) quanta += __float2int_rn((float)(v * k.iq));  // exact: |v / q| < 2^24
+        else acc += (double)v;
+        vmax = fmax(vmax, fabs(v));
+        vsum += v;
       }
-      c0[j] = c1[j];
-      c1[j] = c2[j];
-      mu_m[j] = m0;
-      mu_0[j] = mu_p[j];
-      optr[j] += g.plane;
+      c0[q] = c1[q];
+      c1[q] = c2[q];
+      mu0[q] = mup[q];
+      fup[q] = fu;
     }
+    acc_q += quanta;
+    optr += g.plane;
   }
+  int flags = 0;
+  if (QUANT && !(vmax < k.range)) flags |= PPF_STATUS_RANGE;
+  if (!isfinite(vsum) || !isfinite(vmax)) flags |= PPF_STATUS_NONFINITE;
   if (status && flags) atomicOr(status, flags);
   if (mass) {
     // QUANT: exact integer count of quanta (|sum| < 2^53), scaled by q at
@@ -560,6 +570,8 @@ int32_t cahn_hilliard(const PpfCahnHilliardParams* p, const PpfGrid* grid_in,
   ct.tile_x = kCTX;
   ct.tile_y = kCTY;
   if ((rc = plan3d<T>(&ct, g, 2, kNSC, 2, &m, &slot_elems, &smem))) return rc;
+  if (slot_elems != kCSlot || m.BX != kCW || m.BY != kCH)
+    return fail(PPF_ERR_INVALID, "Cahn-Hilliard plane slot mismatch");
   ChCoef<T> k;
   k.kap = (T)(p->epsilon * p->epsilon / (p->dx * p->dx));
   k.a = (T)(p->dt * p->M / (p->dx * p->dx));
