@@ -223,6 +223,7 @@ template <typename T>
 struct ChCoef {
   T kap;         // eps^2/dx^2
   T a;           // dt*M/dx^2
+  T aiq;         // a / q (QUANT only; exact: q is a power of two)
   T q, iq;       // quantum and its inverse (QUANT only)
   T range;       // 2^24 q: |c| beyond this loses exactness (QUANT only)
   int centered;  // field holds u = c - 1/2
@@ -238,9 +239,9 @@ __device__ __forceinline__ T ch_mu(const ChCoef<T>& k, T c, T w, T e, T n, T s, 
 
 template <typename T, bool QUANT>
 __device__ __forceinline__ T ch_flux(const ChCoef<T>& k, T mn, T mc) {
-  const T f = k.a * (mn - mc);
-  if (QUANT) return rint(f * k.iq) * k.q;
-  return f;
+  // (a d) / q == (a / q) d bit for bit: scaling by a power of two is exact
+  if (QUANT) return rint(k.aiq * (mn - mc)) * k.q;
+  return k.a * (mn - mc);
 }
 
 constexpr int kNSC = 8;  // c planes z..z+2 read, z+3 .. z+6 in flight
@@ -367,6 +368,8 @@ __global__ void __launch_bounds__(kThreads)
   int nq = 0;  // own rows inside the grid: rows ty + 8q < ny - y0
 #pragma unroll
   for (int q = 0; q < kCQ; ++q) nq += (xin && y0 + ty + 8 * q < ny) ? 1 : 0;
+  // CTA-uniform: the whole tile lies inside the grid (no per-cell checks)
+  const bool full = x0 + kCTX <= nx && y0 + kCTY <= ny;
 
   long long acc_q = 0;
   double acc = 0.0;
@@ -412,7 +415,7 @@ __global__ void __launch_bounds__(kThreads)
       const T fu = ch_flux<T, QUANT>(k, mup[q], m0);
       const T fd = -fup[q];
       const T v = c0[q] + (((fw + fe) + (fn + fs)) + (fd + fu));
-      if (q < nq) {
+      if (full || q < nq) {
         optr[q * qstride] = v;
         if (QUANT) quanta += __float2int_rn((float)(v * k.iq));  // exact: |v / q| < 2^24
         else acc += (double)v;
@@ -584,6 +587,7 @@ int32_t cahn_hilliard(const PpfCahnHilliardParams* p, const PpfGrid* grid_in,
   }
   k.q = (T)(quant ? p->quantum : 0.0);
   k.iq = (T)(quant ? 1.0 / p->quantum : 0.0);
+  k.aiq = (T)(quant ? (double)k.a * (1.0 / p->quantum) : 0.0);
   k.range = (T)(quant ? std::ldexp(p->quantum, 24) : 0.0);
   if (p->centered != 0 && p->centered != 1)
     return fail(PPF_ERR_INVALID, "centered must be 0 or 1");
