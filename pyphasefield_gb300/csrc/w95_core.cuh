@@ -14,6 +14,8 @@
 // the C-order grid is the reference's "x", axis 1 its "y".
 #pragma once
 
+#include <type_traits>
+
 #include "ppf_common.cuh"
 
 namespace ppf {
@@ -152,6 +154,12 @@ __device__ __forceinline__ T shfl_w(T v) { return __shfl_up_sync(0xffffffffu, v,
 template <typename T>
 __device__ __forceinline__ T shfl_e(T v) { return __shfl_down_sync(0xffffffffu, v, 1); }
 
+}  // namespace w95
+}  // namespace ppf
+#include "w95_pack.cuh"
+namespace ppf {
+namespace w95 {
+
 // Loads of one band (rows y0 - 1 .. y0 + ROWS, this lane's column).
 template <typename T, int ROWS>
 __device__ __forceinline__ void band_load(const Geo& g, const Bc<T>& bc,
@@ -187,6 +195,12 @@ __device__ __forceinline__ void band_compute(const Coef<T>& k, const Geo& g,
                                              T* __restrict__ phi_out, T* __restrict__ c_out,
                                              uint64_t seed, uint64_t step, int xs, int y0,
                                              const T (&bp)[ROWS + 2], const T (&bcv)[ROWS + 2]) {
+#ifndef PPF_W95_SCALAR
+  if constexpr (std::is_same<T, float>::value && ROWS == 2) {
+    band_compute_f2(k, g, phi_out, c_out, seed, step, xs, y0, bp, bcv);
+    return;
+  }
+#endif
   const int lane = threadIdx.x;
   const int ny = g.n[0], nx = g.n[1];
   const int x = xs + lane;
