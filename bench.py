@@ -339,7 +339,9 @@ SWEEP = {
     # every cell takes the full update (no exact bulk shortcut): the cost of
     # a grid that is interface everywhere
     "warren1995_4096_full": ("warren1995", (4096, 4096), 1, 100, {"bulk_shortcut": False}),
+    "diffusion3d_384": ("diffusion", (384, 384, 384), 1, 100),
     "diffusion3d_512": ("diffusion", (512, 512, 512), 1, 100),
+    "allen_cahn3d_512": ("allen_cahn", (512, 512, 512), 1, 100),
     "cahn_hilliard_256": ("cahn_hilliard", (256, 256, 256), 1, 500),
     "cahn_hilliard_384": ("cahn_hilliard", (384, 384, 384), 1, 100),
     "cahn_hilliard_512": ("cahn_hilliard", (512, 512, 512), 1, 100),
@@ -552,6 +554,7 @@ def profile_case(name: str):
                 last tenth of a bench step runs on; no cell is exactly bulk any more)
     ch256       Cahn-Hilliard 256^3 periodic, dt 0.01, 5 steps
     diff4096    Diffusion 2-D 4096^2 periodic, 5 steps (temporal depth from PPF_DEPTH, default 1)
+    diff3d384   Diffusion 3-D 384^3 periodic, 5 steps
     """
     import torch
     from pyphasefield_gb300 import CahnHilliardGB300, DiffusionGB300
@@ -576,6 +579,12 @@ def profile_case(name: str):
         sim.initialize_fields_and_imported_data()
         sim.fields[0].data[1:-1, 1:-1] = 0.5 + 0.01 * rng.standard_normal((4096, 4096))
         sim.simulate(5 * depth)
+    elif name == "diff3d384":
+        sim = DiffusionGB300(dimensions=[384, 384, 384], dx=1.0, dt=0.1,
+                             boundary_conditions="PERIODIC", user_data={"D": 1.0, "use_graph": False})
+        sim.initialize_fields_and_imported_data()
+        sim.fields[0].data[1:-1, 1:-1, 1:-1] = 0.5 + 0.01 * rng.standard_normal((384, 384, 384))
+        sim.simulate(5)
     else:
         raise SystemExit(f"unknown profile case {name!r}")
     torch.cuda.synchronize()

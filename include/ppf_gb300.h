@@ -119,14 +119,15 @@ typedef struct PpfWarren1995Params {
  * output tile per CTA (0 = default; for Warren1995 tile_y is the number of
  * rows each warp walks: 2, 4, 8 or 16); pdl = 1 launches with programmatic
  * dependent launch so back-to-back steps overlap their launch latency;
- * flags = PPF_TILING_* bits. */
+ * flags = PPF_TILING_* bits; zchunk (3-D kernels) = planes per CTA along z,
+ * 0 = chosen by the library. */
 typedef struct PpfTiling {
   int32_t depth;
   int32_t tile_x;
   int32_t tile_y;
   int32_t pdl;
   int32_t flags;
-  int32_t reserved;
+  int32_t zchunk;
 } PpfTiling;
 
 /* Warren1995: evaluate the full update on every cell. Without this flag a

@@ -47,7 +47,7 @@ class PpfBoundary(C.Structure):
 
 class PpfTiling(C.Structure):
     _fields_ = [("depth", C.c_int32), ("tile_x", C.c_int32), ("tile_y", C.c_int32),
-                ("pdl", C.c_int32), ("flags", C.c_int32), ("reserved", C.c_int32)]
+                ("pdl", C.c_int32), ("flags", C.c_int32), ("zchunk", C.c_int32)]
 
 
 PPF_TILING_FULL_EVAL = 1

@@ -212,6 +212,105 @@ __global__ void __launch_bounds__(kThreads)
   }
 }
 
+// Lean 7-point kernel (the default tile): 32 x 32 cells, 256 threads, each
+// thread owns the 4 xy-columns (ty + 8q, tx) and keeps c(z - 1), c(z) of
+// each in registers while marching along z, so a cell reads only its four
+// xy neighbours and the new plane's centre from shared memory; every shared
+// index is a compile-time offset from one per-thread base and there is one
+// block barrier per plane.
+constexpr int kLTX = 32;
+constexpr int kLTY = 32;
+constexpr int kLQ = kLTY / 8;
+constexpr int kLW = kLTX + 2 * kXOff;  // TMA box width
+constexpr int kNSL = 6;                // planes z, z+1 read; z+2 .. z+4 in flight
+
+template <typename T, typename Op>
+__global__ void __launch_bounds__(kThreads)
+    march7_lean_kernel(const __grid_constant__ CUtensorMap map, Op op, Geo g, Bc<T> bc,
+                       const T* __restrict__ in, T* __restrict__ out, MarchGeom m,
+                       int slot_elems, int* status) {
+  extern __shared__ unsigned char smem_raw[];
+  __shared__ __align__(8) uint64_t bars[kNSL];
+  __shared__ int abort_flag;
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int x0 = blockIdx.x * kLTX, y0 = blockIdx.y * kLTY, z0 = blockIdx.z * m.ZC;
+  const int nz = g.n[0], ny = g.n[1], nx = g.n[2];
+  const int z1 = min(z0 + m.ZC, nz);
+  const bool xy_edge = x0 - kXOff < 0 || y0 - 1 < 0 || x0 + kLTX + kXOff > nx ||
+                       y0 + kLTY + 1 > ny;
+  PlaneRing<T, kNSL> ring{align128<T>(smem_raw), bars, slot_elems, z0 - 1};
+  const bool leader = tx == 0 && ty == 0;
+
+  if (leader) {
+    for (int i = 0; i < kNSL; ++i) mbar_init(&bars[i], 1);
+    mbar_init_fence();
+    abort_flag = 0;
+  }
+  __syncthreads();
+  pdl_wait();
+  pdl_launch_next();
+  const int last = z1;  // plane z1 is the upper neighbour of the last plane
+  if (leader)
+    for (int p = z0 - 1; p <= min(z0 + kNSL - 3, last); ++p)
+      issue_plane(ring, &map, g, bc, m, x0, y0, p);
+  for (int p = z0 - 1; p <= z0; ++p) {
+    if (!wait_all(ring.bar(p), ring.parity(p), &abort_flag)) {
+      report_timeout<T>(status);
+      drain(ring, p, min(z0 + kNSL - 3, last));
+      return;
+    }
+    fixup_plane(ring, in, g, bc, m, x0, y0, p, xy_edge);
+  }
+  __syncthreads();
+
+  const int ci = (ty + 1) * kLW + tx + kXOff;
+  T cm[kLQ], c0[kLQ];
+  {
+    const T* Pm = ring.plane(z0 - 1);
+    const T* P0 = ring.plane(z0);
+#pragma unroll
+    for (int q = 0; q < kLQ; ++q) {
+      cm[q] = Pm[ci + q * 8 * kLW];
+      c0[q] = P0[ci + q * 8 * kLW];
+    }
+  }
+  T* optr = out + (int64_t)z0 * g.plane + (int64_t)(y0 + ty) * g.pitch + x0 + tx;
+  const int64_t qstride = (int64_t)8 * g.pitch;
+  const bool xin = x0 + tx < nx;
+  int nq = 0;
+#pragma unroll
+  for (int q = 0; q < kLQ; ++q) nq += (xin && y0 + ty + 8 * q < ny) ? 1 : 0;
+  const bool full = x0 + kLTX <= nx && y0 + kLTY <= ny;
+
+  for (int z = z0; z < z1; ++z) {
+    // plane z + kNSL - 2 takes the slot of plane z - 2, last read in
+    // iteration z - 2 (plane p is read in iterations p - 1 and p), which
+    // every thread finished before the barrier of iteration z - 1
+    if (leader && z + kNSL - 2 <= last) issue_plane(ring, &map, g, bc, m, x0, y0, z + kNSL - 2);
+    if (!wait_all(ring.bar(z + 1), ring.parity(z + 1), &abort_flag)) {
+      report_timeout<T>(status);
+      drain(ring, z + 1, min(z + kNSL - 2, last));
+      return;
+    }
+    if (xy_edge || ghost_plane(g, bc, z + 1)) {
+      fixup_plane(ring, in, g, bc, m, x0, y0, z + 1, xy_edge);
+      __syncthreads();
+    }
+    const T* P0 = ring.plane(z);
+    const T* P1 = ring.plane(z + 1);
+#pragma unroll
+    for (int q = 0; q < kLQ; ++q) {
+      const int i = ci + q * 8 * kLW;
+      const T cp = P1[i];
+      const T v = op(c0[q], P0[i - 1], P0[i + 1], P0[i - kLW], P0[i + kLW], cm[q], cp);
+      if (full || q < nq) optr[q * qstride] = v;
+      cm[q] = c0[q];
+      c0[q] = cp;
+    }
+    optr += g.plane;
+  }
+}
+
 // ------------------------------------------------------------- Cahn-Hilliard
 // mu~ = -(eps^2/dx^2) lap'(c) + f'(c), lap' the unscaled 7-point sum;
 // c' = c + sum over the 6 faces of F = a (mu~_nbr - mu~_c), a = dt M/dx^2.
@@ -466,11 +565,8 @@ int32_t plan3d(const PpfTiling* t, const Geo& g, int halo, int nslots, int mu_pl
                 m->TY, 256 - 2 * kXOff);
   m->BX = m->TX + 2 * kXOff;
   m->BY = m->TY + 2 * halo;
-  // z chunk: about two waves of CTAs over 152 SMs, at least 8 planes.
-  const long tiles = (long)((g.n[2] + m->TX - 1) / m->TX) * ((g.n[1] + m->TY - 1) / m->TY);
-  int zc = (int)((long)g.n[0] * tiles / (152L * 8));
-  zc = zc < 8 ? 8 : (zc > 64 ? 64 : zc);
-  m->ZC = zc > g.n[0] ? g.n[0] : zc;
+  if (t && t->zchunk < 0) return fail(PPF_ERR_INVALID, "zchunk must be >= 0");
+  m->ZC = 0;  // set by the caller (zchunk_of)
   const size_t slot_bytes = ((size_t)m->BX * m->BY * sizeof(T) + 127) / 128 * 128;
   *slot_elems = (int)(slot_bytes / sizeof(T));
   *smem = 128 + (size_t)nslots * slot_bytes +
@@ -478,6 +574,17 @@ int32_t plan3d(const PpfTiling* t, const Geo& g, int halo, int nslots, int mu_pl
   if (*smem > 200 * 1024)
     return fail(PPF_ERR_INVALID, "tile needs %zu bytes of shared memory", *smem);
   return PPF_OK;
+}
+
+// Planes per CTA along z when the caller leaves it open: short chunks (many
+// CTAs in flight over a compact stretch of z) measured fastest on GB300 for
+// both 3-D kernels (384^3 and 512^3: 8-16 planes beat 32-64 by 1.3-1.9x, and
+// sizing the chunks to one wave of CTAs was slower still).
+constexpr int kDefaultZChunk = 12;
+
+int zchunk_of(const PpfTiling* t, const Geo& g) {
+  const int zc = t && t->zchunk > 0 ? t->zchunk : kDefaultZChunk;
+  return zc < g.n[0] ? zc : g.n[0];
 }
 
 template <typename T>
@@ -526,11 +633,30 @@ int32_t run_march7(Op op, double dx, const PpfGrid* grid, const PpfBoundary* b, 
   MarchGeom m;
   int slot_elems;
   size_t smem;
-  if ((rc = plan3d<T>(tiling, g, 1, kNS7, 0, &m, &slot_elems, &smem))) return rc;
-  CUtensorMap map;
-  if ((rc = plane_map<T>(&map, in, g, m))) return rc;
   int* st = status_ptr();
   if (!st) return fail(PPF_ERR_CUDA, "status word unavailable");
+  const bool lean = !tiling || ((tiling->tile_x == 0 || tiling->tile_x == kLTX) &&
+                                (tiling->tile_y == 0 || tiling->tile_y == kLTY));
+  if (lean) {
+    PpfTiling lt{};
+    lt.depth = tiling ? tiling->depth : 0;
+    lt.tile_x = kLTX;
+    lt.tile_y = kLTY;
+    if ((rc = plan3d<T>(&lt, g, 1, kNSL, 0, &m, &slot_elems, &smem))) return rc;
+    CUtensorMap map;
+    if ((rc = plane_map<T>(&map, in, g, m))) return rc;
+    auto kern = march7_lean_kernel<T, Op>;
+    PPF_TRY_CUDA(allow_smem(kern, smem));
+    m.ZC = zchunk_of(tiling, g);
+    dim3 gd((g.n[2] + kLTX - 1) / kLTX, (g.n[1] + kLTY - 1) / kLTY, (g.n[0] + m.ZC - 1) / m.ZC);
+    PPF_TRY_CUDA(launch(kern, gd, dim3(32, kThreads / 32), smem, (cudaStream_t)stream,
+                        tiling && tiling->pdl, map, op, g, bc, in, out, m, slot_elems, st));
+    return PPF_OK;
+  }
+  if ((rc = plan3d<T>(tiling, g, 1, kNS7, 0, &m, &slot_elems, &smem))) return rc;
+  m.ZC = zchunk_of(tiling, g);
+  CUtensorMap map;
+  if ((rc = plane_map<T>(&map, in, g, m))) return rc;
   auto kern = march7_kernel<T, Op>;
   PPF_TRY_CUDA(allow_smem(kern, smem));
   dim3 gd((g.n[2] + m.TX - 1) / m.TX, (g.n[1] + m.TY - 1) / m.TY, (g.n[0] + m.ZC - 1) / m.ZC);
@@ -601,11 +727,15 @@ int32_t cahn_hilliard(const PpfCahnHilliardParams* p, const PpfGrid* grid_in,
   if (quant) {
     auto kern = cahn_hilliard_kernel<T, true>;
     PPF_TRY_CUDA(allow_smem(kern, smem));
+    m.ZC = zchunk_of(tiling, g);
+    gd.z = (unsigned)((g.n[0] + m.ZC - 1) / m.ZC);
     PPF_TRY_CUDA(launch(kern, gd, dim3(32, kThreads / 32), smem, (cudaStream_t)stream, pdl,
                         map, k, g, bc, in, out, mass, (int*)status, m, slot_elems, st));
   } else {
     auto kern = cahn_hilliard_kernel<T, false>;
     PPF_TRY_CUDA(allow_smem(kern, smem));
+    m.ZC = zchunk_of(tiling, g);
+    gd.z = (unsigned)((g.n[0] + m.ZC - 1) / m.ZC);
     PPF_TRY_CUDA(launch(kern, gd, dim3(32, kThreads / 32), smem, (cudaStream_t)stream, pdl,
                         map, k, g, bc, in, out, mass, (int*)status, m, slot_elems, st));
   }

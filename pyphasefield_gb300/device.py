@@ -110,12 +110,13 @@ def boundary_struct(sim, grid: DeviceGrid, nfields: int) -> L.PpfBoundary:
     return b
 
 
-def tiling_struct(depth=1, tile=None, pdl=True, flags=0) -> L.PpfTiling:
+def tiling_struct(depth=1, tile=None, pdl=True, flags=0, zchunk=0) -> L.PpfTiling:
     t = L.PpfTiling()
     t.depth = int(depth)
     t.tile_x, t.tile_y = (int(tile[0]), int(tile[1])) if tile else (0, 0)
     t.pdl = 1 if pdl else 0
     t.flags = int(flags)
+    t.zchunk = int(zchunk or 0)
     return t
 
 

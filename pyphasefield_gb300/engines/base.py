@@ -157,7 +157,7 @@ class GB300Engine:
     def _ppf_tiling(self, depth: int):
         ud = self.user_data
         flags = 0 if ud.get("bulk_shortcut", True) else L.PPF_TILING_FULL_EVAL
-        return tiling_struct(depth, ud.get("tile"), ud.get("pdl", True), flags)
+        return tiling_struct(depth, ud.get("tile"), ud.get("pdl", True), flags, ud.get("zchunk", 0))
 
     # ------------------------------------------------------------ lifecycle
     def just_before_simulating(self):
