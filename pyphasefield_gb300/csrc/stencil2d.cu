@@ -149,6 +149,79 @@ __global__ void __launch_bounds__(kThreads)
   }
 }
 
+// Lean depth-1 kernel: a warp owns WW = 32 V columns (V cells of one
+// 16-byte vector per lane) and kRB rows. It requests the kRB + 2 rows it
+// reads (band plus halo rows) as vector loads up front, takes the west /
+// east neighbours across lanes by shuffles (lanes 0 and 31 load the strip's
+// outer neighbours), and writes each output row as one vector per lane: no
+// shared memory, no barriers. Edge bands use the generic ghost rule.
+constexpr int kRB = 8;
+
+template <typename T, typename Op>
+__global__ void __launch_bounds__(kThreads)
+    stencil2d_lean_kernel(Op op, Geo g, Bc<T> bc, const T* __restrict__ in, T* __restrict__ out,
+                          int vec_ok) {
+  constexpr int V = Vec16<T>::n;
+  using VT = typename Vec16<T>::type;
+  constexpr int WW = 32 * V;
+  const int lane = threadIdx.x;
+  const int x0 = blockIdx.x * WW;
+  const int y0 = (blockIdx.y * (kThreads / 32) + threadIdx.y) * kRB;
+  const int ny = g.n[0], nx = g.n[1];
+  pdl_wait();
+  pdl_launch_next();
+  if (y0 >= ny) return;  // whole warp
+  const bool fast = vec_ok && x0 >= 1 && x0 + WW + 1 <= nx && y0 >= 1 && y0 + kRB + 1 <= ny;
+  if (fast) {
+    const T* base = in + (int64_t)(y0 - 1) * g.pitch + x0;
+    VT r[kRB + 2];
+#pragma unroll
+    for (int j = 0; j < kRB + 2; ++j)
+      r[j] = __ldg(reinterpret_cast<const VT*>(base + (int64_t)j * g.pitch) + lane);
+    T wv[kRB], ev[kRB];
+#pragma unroll
+    for (int j = 0; j < kRB; ++j) {
+      const T* row = base + (int64_t)(j + 1) * g.pitch;
+      wv[j] = lane == 0 ? __ldg(row - 1) : T(0);
+      ev[j] = lane == 31 ? __ldg(row + WW) : T(0);
+    }
+    T* obase = out + (int64_t)y0 * g.pitch + x0 + lane * V;
+#pragma unroll
+    for (int j = 1; j <= kRB; ++j) {
+      const T* c = reinterpret_cast<const T*>(&r[j]);
+      const T* n = reinterpret_cast<const T*>(&r[j - 1]);
+      const T* sv = reinterpret_cast<const T*>(&r[j + 1]);
+      T wl = __shfl_up_sync(0xffffffffu, c[V - 1], 1);
+      T er = __shfl_down_sync(0xffffffffu, c[0], 1);
+      if (lane == 0) wl = wv[j - 1];
+      if (lane == 31) er = ev[j - 1];
+      VT o;
+      T* ov = reinterpret_cast<T*>(&o);
+#pragma unroll
+      for (int e = 0; e < V; ++e) {
+        const T w = e == 0 ? wl : c[e - 1];
+        const T ea = e == V - 1 ? er : c[e + 1];
+        ov[e] = op(c[e], w, ea, n[e], sv[e]);
+      }
+      *reinterpret_cast<VT*>(obase + (int64_t)(j - 1) * g.pitch) = o;
+    }
+  } else {
+    for (int j = 0; j < kRB; ++j) {
+      const int row = y0 + j;
+      if (row >= ny) break;
+#pragma unroll
+      for (int e = 0; e < V; ++e) {
+        const int x = x0 + lane * V + e;
+        if (x < nx)
+          out[(int64_t)row * g.pitch + x] =
+              op(fetch<T, 2>(in, g, bc, 0, row, x), fetch<T, 2>(in, g, bc, 0, row, x - 1),
+                 fetch<T, 2>(in, g, bc, 0, row, x + 1), fetch<T, 2>(in, g, bc, 0, row - 1, x),
+                 fetch<T, 2>(in, g, bc, 0, row + 1, x));
+      }
+    }
+  }
+}
+
 struct Tile2d {
   int tx, ty, k, ka;
   size_t smem;
@@ -188,12 +261,22 @@ int32_t run2d(Op op, double dx, const PpfGrid* grid, const PpfBoundary* b,
   if ((rc = plan_tile2d<T>(tiling, &t))) return rc;
   Bc<T> bc;
   if ((rc = make_bc<T>(b, g, dx, 1, t.k, &bc))) return rc;
-  const int vec_ok = (((uintptr_t)in) % 16 == 0) && ((g.pitch * sizeof(T)) % 16 == 0);
+  const int vec_ok = (((uintptr_t)in) % 16 == 0) && (((uintptr_t)out) % 16 == 0) &&
+                     ((g.pitch * sizeof(T)) % 16 == 0);
+  const bool pdl = tiling && tiling->pdl;
+  if (t.k == 1 && !(tiling && (tiling->tile_x || tiling->tile_y))) {
+    constexpr int WW = 32 * Vec16<T>::n;
+    dim3 grid_dim((g.n[1] + WW - 1) / WW,
+                  (g.n[0] + kRB * (kThreads / 32) - 1) / (kRB * (kThreads / 32)));
+    if (grid_dim.y > 65535) return fail(PPF_ERR_INVALID, "too many row bands");
+    PPF_TRY_CUDA(launch(stencil2d_lean_kernel<T, Op>, grid_dim, dim3(32, kThreads / 32), 0,
+                        (cudaStream_t)stream, pdl, op, g, bc, in, out, vec_ok));
+    return PPF_OK;
+  }
   auto kern = stencil2d_tb_kernel<T, Op>;
   PPF_TRY_CUDA(allow_smem(kern, t.smem));
   dim3 grid_dim((g.n[1] + t.tx - 1) / t.tx, (g.n[0] + t.ty - 1) / t.ty);
   if (grid_dim.y > 65535) return fail(PPF_ERR_INVALID, "too many tile rows");
-  const bool pdl = tiling && tiling->pdl;
   PPF_TRY_CUDA(launch(kern, grid_dim, dim3(32, kThreads / 32), t.smem,
                       (cudaStream_t)stream, pdl, op, g, bc, in, out, t.tx,
                       t.ty, t.k, t.ka, vec_ok));

@@ -38,8 +38,9 @@ def _stencil_candidates(sim) -> list:
     """Diffusion / Allen-Cahn launch shapes: temporal depth x tile (2-D),
     tile and planes per CTA along z (3-D)."""
     if len(sim._ppf_grid.kshape) == 2:
-        return [{"temporal_depth": d, "tile": t} for d in (1, 2, 4, 8)
-                for t in ((128, 32), (64, 32), (256, 16), (128, 16))]
+        return [{"temporal_depth": 1, "tile": None}] + \
+            [{"temporal_depth": d, "tile": t} for d in (1, 2, 4, 8)
+             for t in ((128, 32), (64, 32), (256, 16), (128, 16))]
     return [{"tile": (32, 32), "zchunk": z} for z in (8, 12, 16, 24)] + \
         [{"tile": t} for t in ((64, 16), (32, 16), (128, 8))]
 
