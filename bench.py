@@ -555,6 +555,7 @@ def profile_case(name: str):
     ch256       Cahn-Hilliard 256^3 periodic, dt 0.01, 5 steps
     diff4096    Diffusion 2-D 4096^2 periodic, 5 steps (temporal depth from PPF_DEPTH, default 1)
     diff3d384   Diffusion 3-D 384^3 periodic, 5 steps
+    diff16384   Diffusion 2-D 16384^2 periodic, 5 steps (2 GiB of fields: beyond L2)
     """
     import torch
     from pyphasefield_gb300 import CahnHilliardGB300, DiffusionGB300
@@ -579,6 +580,12 @@ def profile_case(name: str):
         sim.initialize_fields_and_imported_data()
         sim.fields[0].data[1:-1, 1:-1] = 0.5 + 0.01 * rng.standard_normal((4096, 4096))
         sim.simulate(5 * depth)
+    elif name == "diff16384":
+        sim = DiffusionGB300(dimensions=[16384, 16384], dx=1.0, dt=0.2,
+                             boundary_conditions="PERIODIC", user_data={"D": 1.0, "use_graph": False})
+        sim.initialize_fields_and_imported_data()
+        sim.fields[0].data[1:-1, 1:-1] = 0.5 + 0.01 * rng.standard_normal((16384, 16384))
+        sim.simulate(5)
     elif name == "diff3d384":
         sim = DiffusionGB300(dimensions=[384, 384, 384], dx=1.0, dt=0.1,
                              boundary_conditions="PERIODIC", user_data={"D": 1.0, "use_graph": False})
