@@ -71,7 +71,7 @@ __device__ __forceinline__ void ac_band(float a, float b, const Geo& g, const Bc
 }
 
 template <int ROWS>
-__global__ void __launch_bounds__(kCtaThreads)
+__global__ void __launch_bounds__(kCtaThreads, 8)
     ensemble_kernel(const MemberDev* __restrict__ members, int n_members, long long n_items,
                     int parity, uint64_t step, const uint64_t* __restrict__ step_base) {
   const long long nwarps = (long long)gridDim.x * kWarpsPerCta;
@@ -91,11 +91,18 @@ __global__ void __launch_bounds__(kCtaThreads)
     const int local = (int)(it - m.item_begin);
     const int xs = (local % m.strips) * w95::kStrip - 1;
     const int y0 = (local / m.strips) * ROWS;
-    if (m.model == PPF_MODEL_WARREN1995)
-      w95::band<float, ROWS>(m.w, m.g, m.bc, m.phi[parity], m.c[parity], m.phi[1 - parity],
+    // the member's constants are copied to registers once per item: the
+    // band reads them many times, and from global memory each read would be
+    // a dependent load
+    const Geo g = m.g;
+    const Bc<float> bc = m.bc;
+    if (m.model == PPF_MODEL_WARREN1995) {
+      const w95::Coef<float> k = m.w;
+      w95::band<float, ROWS>(k, g, bc, m.phi[parity], m.c[parity], m.phi[1 - parity],
                              m.c[1 - parity], m.seed, step, xs, y0);
-    else
-      ac_band<ROWS>(m.ac_a, m.ac_b, m.g, m.bc, m.phi[parity], m.phi[1 - parity], xs, y0);
+    } else {
+      ac_band<ROWS>(m.ac_a, m.ac_b, g, bc, m.phi[parity], m.phi[1 - parity], xs, y0);
+    }
   }
 }
 
