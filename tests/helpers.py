@@ -69,7 +69,8 @@ def from_dev(t, kshape, shape):
 
 
 def run_single_gpu(model, c0, steps, bc, dx, dt, values=None, precision="fp64", depth=1,
-                   tile=None, pdl=False, device="cuda", quantum=0.0, centered=0, **params):
+                   tile=None, pdl=False, device="cuda", quantum=0.0, centered=0, zchunk=0,
+                   **params):
     """Advance a one-field model `steps` steps through the C-ABI (ping-pong)."""
     import torch
     from pyphasefield_gb300 import _lib as L
@@ -83,6 +84,7 @@ def run_single_gpu(model, c0, steps, bc, dx, dt, values=None, precision="fp64", 
     t = L.PpfTiling()
     t.tile_x, t.tile_y = (tile if tile else (0, 0))
     t.pdl = 1 if pdl else 0
+    t.zchunk = int(zchunk)
     s = C.c_void_p(torch.cuda.current_stream().cuda_stream)
     done = 0
     while done < steps:

@@ -94,8 +94,50 @@ def test_one_dimensional_grid(cuda):
     c0 = rng.random(97)
     for bc in ("PERIODIC", "NEUMANN", "DIRCHLET"):
         ref = restate.run_single("diffusion", c0, 9, bc, 1.0, 0.3, D=1.0)
-        out = run_single_gpu("diffusion", c0, 9, bc, 1.0, 0.3, precision="fp64", depth=2, D=1.0)
-        assert rel_l2(out, ref) < F64_TOL
+        for depth in (1, 2):
+            out = run_single_gpu("diffusion", c0, 9, bc, 1.0, 0.3, precision="fp64", depth=depth,
+                                 D=1.0)
+            assert rel_l2(out, ref) < F64_TOL, (bc, depth)
+
+
+@pytest.mark.parametrize("model", ["diffusion", "allen_cahn"])
+def test_lean_2d_kernel_matches_tiled_and_oracle(cuda, model):
+    """The default depth-1 kernel (warp strips of 16-byte vectors) against
+    the shared-memory tile kernel (bit for bit) and the FP64 oracle, on a grid
+    with interior strips, ragged right and bottom edges and every BC type."""
+    rng = np.random.default_rng(15)
+    c0 = rng.random((203, 517))
+    params = dict(D=1.0) if model == "diffusion" else dict(M=0.1, epsilon=1.0, W=1.0)
+    for bc in ("PERIODIC", "NEUMANN", ["DIRCHLET", "NEUMANN"], ["PERIODIC", "DIRCHLET"]):
+        bcs = [bc] * 2 if isinstance(bc, str) else bc
+        vals = [[[0.25, 0.75] if b == "DIRCHLET" else [0.0, 0.0] for b in bcs]]
+        for prec in ("fp32", "fp64"):
+            lean = run_single_gpu(model, c0, 7, bc, 1.0, 0.1, values=vals, precision=prec,
+                                  **params)
+            tiled = run_single_gpu(model, c0, 7, bc, 1.0, 0.1, values=vals, precision=prec,
+                                   tile=(128, 32), **params)
+            np.testing.assert_array_equal(lean, tiled)
+        ref = restate.run_single(model, c0, 7, bc, 1.0, 0.1, values=vals, **params)
+        assert rel_l2(lean, ref) < F64_TOL, bc
+
+
+@pytest.mark.parametrize("model", ["diffusion", "allen_cahn"])
+def test_lean_3d_kernel_and_z_chunks(cuda, model):
+    """The default 3-D kernel (32x32 tiles, register z-window) against the
+    generic tile kernel and the FP64 oracle on a grid with interior tiles,
+    for several planes-per-CTA settings (results identical bit for bit)."""
+    rng = np.random.default_rng(16)
+    c0 = rng.random((45, 70, 101))
+    params = dict(D=1.0) if model == "diffusion" else dict(M=0.1, epsilon=1.0, W=1.0)
+    for bc in ("PERIODIC", ["NEUMANN", "PERIODIC", "DIRCHLET"]):
+        outs = [run_single_gpu(model, c0, 4, bc, 1.0, 0.05, precision="fp64", zchunk=z, **params)
+                for z in (0, 1, 7, 12, 64)]
+        outs.append(run_single_gpu(model, c0, 4, bc, 1.0, 0.05, precision="fp64",
+                                   tile=(64, 16), **params))
+        for o in outs[1:]:
+            np.testing.assert_array_equal(o, outs[0])
+        ref = restate.run_single(model, c0, 4, bc, 1.0, 0.05, **params)
+        assert rel_l2(outs[0], ref) < F64_TOL, bc
 
 
 @pytest.mark.parametrize("shape", [(5, 6, 7), (17, 3, 40), (1, 9, 70)])
@@ -138,6 +180,13 @@ def test_cahn_hilliard_quantised_conserves_mass_exactly(cuda):
                          quantum=q, centered=1, M=1.0, epsilon=1.0)
     assert rel_l2(out, ref) < F32_TOL
     assert (out - 0.5).sum() == (c0 - 0.5).sum()
+    # planes per CTA along z change only the work split, not one bit
+    for zc in (1, 5, 32):
+        o2 = run_single_gpu("cahn_hilliard", c0, 20, "PERIODIC", 1.0, 0.01, precision="fp32",
+                            quantum=q, centered=1, zchunk=zc, M=1.0, epsilon=1.0)
+        o1 = run_single_gpu("cahn_hilliard", c0, 20, "PERIODIC", 1.0, 0.01, precision="fp32",
+                            quantum=q, centered=1, M=1.0, epsilon=1.0)
+        np.testing.assert_array_equal(o1, o2)
 
 
 def test_warren_vs_oracle_noise_and_edges(cuda):
