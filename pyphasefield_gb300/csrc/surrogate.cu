@@ -27,12 +27,9 @@ constexpr int kPad = 8;  // shared row padding (bf16 elements)
 
 // ---------------------------------------------------------------- loaders
 // A(m, k) and B(k, n) element accessors (return float; converted to bf16).
-struct StridedBf16 {  // x[i * si + j * sj]
+struct StridedBf16 {  // element (i, j) = x[i * si + j * sj]
   const __nv_bfloat16* x;
   long long si, sj;
-  __device__ float operator()(long long i, long long j) const {
-    return __bfloat162float(x[i * si + j * sj]);
-  }
 };
 
 // Patch gather of a 2-channel state field stack: rows are tokens
@@ -138,10 +135,6 @@ struct StoreAtomic {  // y[m * ld + n] += acc (split-k weight gradients)
 };
 
 // ---------------------------------------------------------------- GEMM
-__device__ __forceinline__ uint32_t pack2(__nv_bfloat16 lo, __nv_bfloat16 hi) {
-  return (uint32_t)__bfloat16_as_ushort(lo) | ((uint32_t)__bfloat16_as_ushort(hi) << 16);
-}
-
 __device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4],
                                          const uint32_t (&b)[2]) {
   asm volatile(
@@ -217,6 +210,81 @@ __device__ __forceinline__ void fill_b(__nv_bfloat16 (*S)[BK + kPad], const Stri
                                        long long n0, long long N, long long k0, long long ke,
                                        int tid) {
   fill_strided(S, lb.x + k0 * lb.si + n0 * lb.sj, lb.sj, lb.si, 0, N - n0, 0, ke - k0, tid);
+}
+
+// Patch gather, 4 consecutive patch columns (px .. px + 3 of one patch row,
+// P a multiple of 4) per 16-byte load: (token t, column k) -> fields
+// offset; the columns of a 4-group share channel and patch row.
+__device__ __forceinline__ long long patch_offset(const PatchGather& p, long long t, int k) {
+  const int per = p.gh * p.gw;
+  const int b = (int)(t / per);
+  const int r = (int)(t - (long long)b * per);
+  const int ty = r / p.gw, tx = r - ty * p.gw;
+  const int ch = k / (p.P * p.P);
+  const int q = k - ch * p.P * p.P;
+  const int py = q / p.P, px = q - py * p.P;
+  return (((long long)b * 2 + ch) * p.H + ty * p.P + py) * p.pitch + tx * p.P + px;
+}
+
+__device__ __forceinline__ void fill_a(__nv_bfloat16 (*S)[BK + kPad], const PatchGather& la,
+                                       long long m0, long long M, long long k0, long long ke,
+                                       int tid) {
+  if ((la.P & 3) || (la.pitch & 3) || (reinterpret_cast<uintptr_t>(la.f) & 15)) {
+    fill_tile<PatchGather, false>(S, la, m0, M, k0, ke, tid);
+    return;
+  }
+  for (int i = tid; i < 64 * (BK / 4); i += kGemmThreads) {
+    const int r = i / (BK / 4), c = (i - r * (BK / 4)) * 4;
+    const long long m = m0 + r, k = k0 + c;
+    float v[4] = {0.f, 0.f, 0.f, 0.f};
+    if (m < M && k + 4 <= ke) {
+      const float4 x = *reinterpret_cast<const float4*>(la.f + patch_offset(la, m, (int)k));
+      const bool c0 = k < (long long)la.P * la.P;  // channel 0 (the group shares it)
+      const float o = c0 ? la.o0 : la.o1, sc = c0 ? la.s0 : la.s1;
+      v[0] = (x.x - o) * sc;
+      v[1] = (x.y - o) * sc;
+      v[2] = (x.z - o) * sc;
+      v[3] = (x.w - o) * sc;
+    } else if (m < M) {
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+        if (k + q < ke) v[q] = la(m, k + q);
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) S[r][c + q] = __float2bfloat16(v[q]);
+  }
+}
+
+// B(k = token, n = patch column) of the patch weight gradient: 4
+// consecutive n per load, stored transposed (S[n][k]).
+__device__ __forceinline__ void fill_b(__nv_bfloat16 (*S)[BK + kPad], const PatchGatherT& lb,
+                                       long long n0, long long N, long long k0, long long ke,
+                                       int tid) {
+  const PatchGather& g = lb.g;
+  if ((g.P & 3) || (g.pitch & 3) || (reinterpret_cast<uintptr_t>(g.f) & 15)) {
+    fill_tile<PatchGatherT, true>(S, lb, n0, N, k0, ke, tid);
+    return;
+  }
+  for (int i = tid; i < (64 / 4) * BK; i += kGemmThreads) {
+    const int c = i / (64 / 4), r = (i - c * (64 / 4)) * 4;  // token column c, n rows r..r+3
+    const long long k = k0 + c, n = n0 + r;
+    float v[4] = {0.f, 0.f, 0.f, 0.f};
+    if (k < ke && n + 4 <= N) {
+      const float4 x = *reinterpret_cast<const float4*>(g.f + patch_offset(g, k, (int)n));
+      const bool c0 = n < (long long)g.P * g.P;
+      const float o = c0 ? g.o0 : g.o1, sc = c0 ? g.s0 : g.s1;
+      v[0] = (x.x - o) * sc;
+      v[1] = (x.y - o) * sc;
+      v[2] = (x.z - o) * sc;
+      v[3] = (x.w - o) * sc;
+    } else if (k < ke) {
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+        if (n + q < N) v[q] = g(k, n + q);
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) S[r + q][c] = __float2bfloat16(v[q]);
+  }
 }
 
 // C(M x N) = sum over k in [k0, k1) of A(m, k) B(k, n); blockIdx.z splits k.
@@ -295,6 +363,65 @@ int32_t gemm(LA la, LB lb, ST st, long long M, long long N, long long K, int spl
   return PPF_OK;
 }
 
+// ---------------------------------------------------------------- split-k
+// Weight gradients are GEMMs over the token axis (k = tokens, thousands),
+// split across CTAs. Each split writes its partial tile to a fixed library
+// array (16 MiB) with plain stores, and one pass adds the splits into the
+// gradient: far fewer memory operations than one atomic per split and
+// element. The array is shared by every call, so weight-gradient calls must
+// not overlap on the GPU (the network's passes run on one stream).
+constexpr long long kSplitkCap = 4LL << 20;  // floats
+__device__ float g_splitk[kSplitkCap];
+
+struct StorePartial {  // part[split][m][n] = acc
+  float* part;
+  long long ld, zstride;
+  __device__ void operator()(long long m, long long n, float v) const {
+    part[blockIdx.z * zstride + m * ld + n] = v;
+  }
+};
+
+__global__ void splitk_reduce_kernel(const float* __restrict__ part, int nz, long long mn,
+                                     float* __restrict__ y) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < mn;
+       i += (long long)gridDim.x * blockDim.x) {
+    float acc = 0.f;
+    for (int z = 0; z < nz; ++z) acc += part[z * mn + i];
+    y[i] += acc;
+  }
+}
+
+float* splitk_buffer() {
+  static float* p = nullptr;
+  if (!p && cudaGetSymbolAddress((void**)&p, g_splitk) != cudaSuccess) {
+    cudaGetLastError();
+    p = nullptr;
+  }
+  return p;
+}
+
+// y[M x N] += A B with k = tokens (about 256 per split).
+template <typename LA, typename LB>
+int32_t gemm_wgrad(LA la, LB lb, float* y, long long M, long long N, long long K, cudaStream_t s) {
+  long long splits = K / 256;
+  const long long cap = kSplitkCap / (M * N);
+  if (splits > cap) splits = cap;
+  if (splits > 1024) splits = 1024;
+  float* part = splits > 1 ? splitk_buffer() : nullptr;
+  if (splits <= 1 || !part) return gemm(la, lb, StoreF32{y, nullptr, N, 1}, M, N, K, 1, s);
+  long long kchunk = (K + splits - 1) / splits;
+  kchunk = (kchunk + BK - 1) / BK * BK;
+  const int nz = (int)((K + kchunk - 1) / kchunk);
+  int32_t rc = gemm(la, lb, StorePartial{part, N, M * N}, M, N, K, (int)splits, s);
+  if (rc) return rc;
+  const long long mn = M * N;
+  long long blocks = (mn + 255) / 256;
+  if (blocks > 4096) blocks = 4096;
+  splitk_reduce_kernel<<<(unsigned)blocks, 256, 0, s>>>(part, nz, mn, y);
+  PPF_TRY_CUDA(cudaGetLastError());
+  return PPF_OK;
+}
+
 // ---------------------------------------------------------------- others
 // Depthwise 3x3 convolution over the patch grid (zero padding at each
 // sample's edge): h[t, c] = bd[c] + sum w[c][dy][dx] y[(row+dy-1, col+dx-1), c].
@@ -344,21 +471,24 @@ __global__ void dwconv_bwd_data_kernel(const float* __restrict__ dh, const float
 }
 
 // dW[c][dy][dx] += sum_t dh[t, c] y[t + off, c];  dB[c] += sum_t dh[t, c].
-// One CTA per (channel, 64-token-block chunk), block reduction, atomics.
+// Thread = channel (consecutive threads read consecutive channels of a
+// token: coalesced), CTA = a chunk of tokens; per-thread sums, then one
+// atomic per (CTA, channel, tap).
 __global__ void dwconv_bwd_weight_kernel(const float* __restrict__ dh, const float* __restrict__ y,
                                          float* __restrict__ dw, float* __restrict__ db,
                                          long long T, int C, int gh, int gw, long long chunk) {
-  __shared__ float red[10][8];
-  const int c = blockIdx.x;
-  const long long t0 = (long long)blockIdx.y * chunk;
+  const int c = blockIdx.y * blockDim.x + threadIdx.x;
+  if (c >= C) return;
+  const long long t0 = (long long)blockIdx.x * chunk;
   const long long t1 = t0 + chunk < T ? t0 + chunk : T;
   const int per = gh * gw;
   float acc[10];
 #pragma unroll
   for (int q = 0; q < 10; ++q) acc[q] = 0.f;
-  for (long long t = t0 + threadIdx.x; t < t1; t += blockDim.x) {
+  int r = (int)(t0 % per), row = r / gw, col = r - row * gw;
+#pragma unroll 4
+  for (long long t = t0; t < t1; ++t) {
     const float d = dh[t * C + c];
-    const int r = (int)(t % per), row = r / gw, col = r - row * gw;
 #pragma unroll
     for (int dy = -1; dy <= 1; ++dy)
 #pragma unroll
@@ -368,21 +498,14 @@ __global__ void dwconv_bwd_weight_kernel(const float* __restrict__ dh, const flo
           acc[(dy + 1) * 3 + (dx + 1)] += d * y[(t + (long long)dy * gw + dx) * C + c];
       }
     acc[9] += d;
+    if (++col == gw) {  // next token: (row, col) of the patch grid
+      col = 0;
+      if (++row == gh) row = 0;
+    }
   }
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
-  for (int q = 0; q < 10; ++q) {
-    float v = acc[q];
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    if (lane == 0) red[q][warp] = v;
-  }
-  __syncthreads();
-  if (threadIdx.x < 10) {
-    float v = 0.f;
-    for (int wv = 0; wv < (int)(blockDim.x >> 5); ++wv) v += red[threadIdx.x][wv];
-    if (threadIdx.x < 9) atomicAdd(dw + c * 9 + threadIdx.x, v);
-    else atomicAdd(db + c, v);
-  }
+  for (int q = 0; q < 9; ++q) atomicAdd(dw + c * 9 + q, acc[q]);
+  atomicAdd(db + c, acc[9]);
 }
 
 // db[n] += sum_m x[m * ld + n] (bias gradient), one thread per column chunk.
@@ -421,7 +544,14 @@ __global__ void mse_kernel(const float* __restrict__ out, const float* __restric
   }
   float v = d * d * inv_count;
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  if ((threadIdx.x & 31) == 0 && v != 0.f) atomicAdd(loss, (double)v);
+  __shared__ float part[8];  // blockDim.x == 256
+  if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double sum = 0.0;
+    for (int w = 0; w < 8; ++w) sum += part[w];
+    if (sum != 0.0) atomicAdd(loss, sum);  // one atomic per block, not per warp
+  }
 }
 
 // new = old + out / scale[ch] (the surrogate's k-step prediction), fields
@@ -579,11 +709,10 @@ int32_t ppf_sg_patch_bwd_weight(const PpfSgShape* s, const float* fields, const 
   StridedBf16 la{(const __nv_bfloat16*)dy_bf16, 1, s->C};  // A(m = out ch, k = token)
   PatchGatherT lb{{fields, s->P, s->H, s->W, s->pitch, gh, gw, s->in_off0, s->in_sc0,
                    s->in_off1, s->in_sc1}};
-  const int splits = (int)(T / 256 > 1 ? (T / 256 < 1024 ? T / 256 : 1024) : 1);
   cudaStream_t st = (cudaStream_t)stream;
-  if ((rc = gemm(la, lb, StoreAtomic{dw_in, K}, s->C, K, T, splits, st))) return rc;
-  dim3 cg((unsigned)((s->C + 127) / 128), (unsigned)((T + 255) / 256));
-  colsum_kernel<<<cg, 128, 0, st>>>(nullptr, (const __nv_bfloat16*)dy_bf16, db_in, T, s->C, 256);
+  if ((rc = gemm_wgrad(la, lb, dw_in, s->C, K, T, st))) return rc;
+  dim3 cg((unsigned)((s->C + 127) / 128), (unsigned)((T + 31) / 32));
+  colsum_kernel<<<cg, 128, 0, st>>>(nullptr, (const __nv_bfloat16*)dy_bf16, db_in, T, s->C, 32);
   PPF_TRY_CUDA(cudaGetLastError());
   return PPF_OK;
 }
@@ -633,12 +762,11 @@ int32_t ppf_sg_block_bwd(const PpfSgShape* s, const float* y, const void* h_bf16
   const int gh = s->H / s->P, gw = s->W / s->P;
   const long long T = (long long)s->B * gh * gw;
   cudaStream_t st = (cudaStream_t)stream;
-  const int splits = (int)(T / 256 > 1 ? (T / 256 < 1024 ? T / 256 : 1024) : 1);
   // dW2[c][e] += sum_t dy_out[t][c] act[t][e]
   StridedBf16 dyT{(const __nv_bfloat16*)dy_out_bf16, 1, s->C};
   StridedBf16 act{(const __nv_bfloat16*)act_bf16, s->E, 1};
-  if ((rc = gemm(dyT, act, StoreAtomic{dw2, s->E}, s->C, s->E, T, splits, st))) return rc;
-  const long long chunk = 256;
+  if ((rc = gemm_wgrad(dyT, act, dw2, s->C, s->E, T, st))) return rc;
+  const long long chunk = 32;
   dim3 cg((s->C + 127) / 128, (unsigned)((T + chunk - 1) / chunk));
   colsum_kernel<<<cg, 128, 0, st>>>(dy_out, nullptr, db2, T, s->C, chunk);
   PPF_TRY_CUDA(cudaGetLastError());
@@ -651,7 +779,7 @@ int32_t ppf_sg_block_bwd(const PpfSgShape* s, const float* y, const void* h_bf16
   // dW1[e][c] += sum_t dpre[t][e] h[t][c] ; db1
   StridedBf16 dpT{(const __nv_bfloat16*)dpre_bf16, 1, s->E};
   StridedBf16 hh{(const __nv_bfloat16*)h_bf16, s->C, 1};
-  if ((rc = gemm(dpT, hh, StoreAtomic{dw1, s->C}, s->E, s->C, T, splits, st))) return rc;
+  if ((rc = gemm_wgrad(dpT, hh, dw1, s->E, s->C, T, st))) return rc;
   dim3 cg1((s->E + 127) / 128, (unsigned)((T + chunk - 1) / chunk));
   colsum_kernel<<<cg1, 128, 0, st>>>(nullptr, (const __nv_bfloat16*)dpre_bf16, db1, T, s->E,
                                      chunk);
@@ -663,8 +791,9 @@ int32_t ppf_sg_block_bwd(const PpfSgShape* s, const float* y, const void* h_bf16
                  s->E, 1, st)))
     return rc;
   // depthwise: weight/bias grads, then dy = dy_out + dwconv^T(dh)
-  dim3 wg((unsigned)s->C, (unsigned)((T + 4095) / 4096));
-  dwconv_bwd_weight_kernel<<<wg, 256, 0, st>>>(dh, y, dw_dw, db_dw, T, s->C, gh, gw, 4096);
+  const long long wchunk = 32;
+  dim3 wg((unsigned)((T + wchunk - 1) / wchunk), (unsigned)((s->C + 127) / 128));
+  dwconv_bwd_weight_kernel<<<wg, 128, 0, st>>>(dh, y, dw_dw, db_dw, T, s->C, gh, gw, wchunk);
   PPF_TRY_CUDA(cudaGetLastError());
   if (dy != dy_out)
     PPF_TRY_CUDA(cudaMemcpyAsync(dy, dy_out, T * s->C * sizeof(float), cudaMemcpyDeviceToDevice,
@@ -699,13 +828,12 @@ int32_t ppf_sg_head_bwd(const PpfSgShape* s, const void* y_bf16, const void* w_o
   const int gh = s->H / s->P, gw = s->W / s->P;
   const long long T = (long long)s->B * gh * gw, K = 2LL * s->P * s->P;
   cudaStream_t st = (cudaStream_t)stream;
-  const int splits = (int)(T / 256 > 1 ? (T / 256 < 1024 ? T / 256 : 1024) : 1);
   StridedBf16 doT{(const __nv_bfloat16*)dout_bf16, 1, K};
   StridedBf16 yy{(const __nv_bfloat16*)y_bf16, s->C, 1};
-  if ((rc = gemm(doT, yy, StoreAtomic{dw_out, s->C}, K, s->C, T, splits, st))) return rc;
-  dim3 cg((unsigned)((K + 127) / 128), (unsigned)((T + 255) / 256));
+  if ((rc = gemm_wgrad(doT, yy, dw_out, K, s->C, T, st))) return rc;
+  dim3 cg((unsigned)((K + 127) / 128), (unsigned)((T + 31) / 32));
   colsum_kernel<<<cg, 128, 0, st>>>(nullptr, (const __nv_bfloat16*)dout_bf16, db_out, T, (int)K,
-                                    256);
+                                    32);
   PPF_TRY_CUDA(cudaGetLastError());
   StridedBf16 doA{(const __nv_bfloat16*)dout_bf16, K, 1};
   StridedBf16 w{(const __nv_bfloat16*)w_out_bf16, s->C, 1};  // B(k=o, n=c) = Wout[o][c]

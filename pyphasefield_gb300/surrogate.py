@@ -591,7 +591,7 @@ def main(argv=None):
     ap.add_argument("--windows", type=int, default=64)
     ap.add_argument("--tol", type=float, default=1e-2)
     ap.add_argument("--check-every", type=int, default=8)
-    ap.add_argument("--eval", type=int, default=2, help="held-out engines")
+    ap.add_argument("--eval", type=int, default=2, help="held-out engines (0: training only)")
     ap.add_argument("--save", default=None, help="write the trained parameters (.npz)")
     a = ap.parse_args(argv)
     H, k = a.grid, a.k
@@ -608,13 +608,16 @@ def main(argv=None):
     torch.cuda.synchronize()
     t_train = time.perf_counter() - t0
     del data
-    held = generate_trajectories(2, H, 1024, k, seed=77, warm_steps=64)
-    ratio = held_out_error_ratio(net, held)
-    del held
+    ratio, ev = None, None
+    if a.eval > 0:
+        held = generate_trajectories(2, H, 1024, k, seed=77, warm_steps=64)
+        ratio = held_out_error_ratio(net, held)
+        del held
     ms = time_predict(net, H)
     flops = (H // a.patch) ** 2 * net.flops_per_token()
-    ev = evaluate(net, n_eval=a.eval, H=H, windows=a.windows, k=k, tol=a.tol,
-                  check_every=a.check_every)
+    if a.eval > 0:
+        ev = evaluate(net, n_eval=a.eval, H=H, windows=a.windows, k=k, tol=a.tol,
+                      check_every=a.check_every)
     if a.save:
         net.save(a.save)
     tokens = a.batch * (H // a.patch) ** 2
