@@ -162,9 +162,9 @@ class GB300Engine:
     # ------------------------------------------------------------ lifecycle
     def just_before_simulating(self):
         t = self._temperature_type
-        if t not in (None, "ISOTHERMAL"):
-            raise NotImplementedError(f"temperature type {t!r} is not supported on the device "
-                                      "(isothermal engines only)")
+        if t not in (None, "ISOTHERMAL", "LINEAR_GRADIENT"):
+            raise NotImplementedError(f"temperature type {t!r} is not supported (XDMF input "
+                                      "needs meshio)")
         self._ppf_prepare()
         self._ppf_setup()
         fill_ghosts_host(self)
@@ -197,8 +197,19 @@ class GB300Engine:
         fill_ghosts_host(self)
 
     def update_temperature_field(self, force_cpu=False):
-        if self._temperature_type not in (None, "ISOTHERMAL"):
-            raise NotImplementedError("non-isothermal temperature on the device")
+        """One step of the temperature law (simulation.py:303-333). None of the
+        four engines reads the temperature field (Warren1995 takes the scalar
+        T of user_data), so it stays a host field that advances with the
+        step count."""
+        self._ppf_advance_temperature(1)
+
+    def _ppf_advance_temperature(self, nsteps: int):
+        t = self._temperature_type
+        if t == "LINEAR_GRADIENT" and self.temperature is not None and self._dTdt:
+            # closed form of nsteps per-step increments dTdt * dt
+            self.temperature.data += nsteps * self._dTdt * self.dt
+        elif t not in (None, "ISOTHERMAL", "LINEAR_GRADIENT"):
+            raise NotImplementedError(f"temperature type {t!r} is not supported")
 
     def simulation_loop(self):
         """Advance one step on the device (the reference's engine call)."""
@@ -220,6 +231,7 @@ class GB300Engine:
             # the step index keyed into the noise is the counter before it
             self._ppf_advance(chunk, self.time_step_counter)
             self.time_step_counter += chunk
+            self._ppf_advance_temperature(chunk)
             n -= chunk
             if rate and self.time_step_counter % rate == 0:
                 self.retrieve_fields_from_GPU()

@@ -161,3 +161,39 @@ def test_engine_rejections(cuda):
     d2._boundary_conditions_array[0][0, 3] = 0.5  # non-uniform face
     with pytest.raises(NotImplementedError, match="non-uniform"):
         d2.simulate(1)
+
+
+def test_linear_gradient_temperature_bookkeeping(cuda):
+    """LINEAR_GRADIENT (simulation.py:134-155, 313-315): the temperature
+    field starts as initial_T + gradients and advances dTdt * dt per step;
+    the engines do not read it (Warren1995 takes the scalar T), so the fields
+    equal an isothermal run bit for bit."""
+    from pyphasefield_gb300 import DiffusionGB300
+    rng = np.random.default_rng(3)
+    c0 = rng.random((40, 56))
+    runs = []
+    for ttype in ("ISOTHERMAL", "LINEAR_GRADIENT"):
+        d = DiffusionGB300(dimensions=[40, 56], dx=0.5, dt=0.05, boundary_conditions="PERIODIC",
+                           temperature_type=ttype, initial_T=1000.0, dTdx=2.0, dTdy=-1.0,
+                           dTdt=-3.0, user_data={"D": 1.0, "graph_chunk": 8})
+        d.initialize_fields_and_imported_data()
+        d.fields[0].data[1:-1, 1:-1] = c0
+        t_init = d.temperature.get_cells().copy()
+        d.simulate(37)
+        d.retrieve_fields_from_GPU()
+        runs.append((d.fields[0].get_cells().copy(), t_init, d.temperature.get_cells().copy()))
+    np.testing.assert_array_equal(runs[0][0], runs[1][0])
+    (_, t0, t1) = runs[1]
+    np.testing.assert_allclose(t1, t0 + 37 * -3.0 * 0.05, rtol=0, atol=1e-9)
+    assert t0[0, 1] - t0[0, 0] == pytest.approx(2.0 * 0.5)  # dTdx along the last axis
+    np.testing.assert_array_equal(runs[0][2], runs[0][1])  # isothermal stays put
+
+
+def test_xdmf_temperature_is_rejected(cuda):
+    from pyphasefield_gb300 import DiffusionGB300
+    d = DiffusionGB300(dimensions=[16, 16], dx=1.0, dt=0.1, boundary_conditions="PERIODIC",
+                       user_data={"D": 1.0})
+    d.initialize_fields_and_imported_data()
+    d._temperature_type = "XDMF_FILE"
+    with pytest.raises(NotImplementedError, match="meshio"):
+        d.simulate(1)
