@@ -108,6 +108,10 @@ class GB300Engine:
 
     def __del__(self):
         try:
+            self._ppf_checkpoint_wait()
+            ck = getattr(self, "_ppf_ckpt", None)
+            if ck is not None:
+                ck["pool"].shutdown(wait=True)
             self._ppf_release_graphs()
         except Exception:
             pass
@@ -234,8 +238,63 @@ class GB300Engine:
             self._ppf_advance_temperature(chunk)
             n -= chunk
             if rate and self.time_step_counter % rate == 0:
-                self.retrieve_fields_from_GPU()
-                self.save_simulation()
+                self._ppf_checkpoint()
+        self._ppf_checkpoint_wait()
+
+    # ------------------------------------------------------------ autosave
+    def _ppf_checkpoint(self):
+        """Autosave without stopping the device (simulation.py:267-271 saves
+        synchronously): the state is copied on the device into one of two
+        snapshot slots, then to pinned host memory on a copy stream, and a
+        writer thread fills Field.data and writes step_<counter>.npz while
+        the next steps run. simulate() returns after every write finished,
+        with Field.data holding the last autosaved state, as in the
+        reference."""
+        import concurrent.futures as cf
+        ck = getattr(self, "_ppf_ckpt", None)
+        g = self._ppf_grid
+        if ck is None:
+            ck = self._ppf_ckpt = {
+                "pool": cf.ThreadPoolExecutor(max_workers=1), "stream": torch.cuda.Stream(g.device),
+                "slots": [{"dev": [g.empty() for _ in range(self.NFIELDS)],
+                           "host": [torch.empty(g.alloc_shape, dtype=g.dtype, pin_memory=True)
+                                    for _ in range(self.NFIELDS)], "job": None}
+                          for _ in range(2)], "next": 0}
+        slot = ck["slots"][ck["next"]]
+        ck["next"] ^= 1
+        if slot["job"] is not None:
+            slot["job"].result()  # the slot's previous write is done with its buffers
+        s, cs = self._ppf_stream, ck["stream"]
+        with torch.cuda.stream(s):
+            for j in range(self.NFIELDS):
+                slot["dev"][j].copy_(self._ppf_bufs[self._ppf_cur][j])
+        taken = torch.cuda.Event()
+        taken.record(s)
+        cs.wait_event(taken)
+        with torch.cuda.stream(cs):
+            for j in range(self.NFIELDS):
+                slot["host"][j].copy_(slot["dev"][j], non_blocking=True)
+        done = torch.cuda.Event()
+        done.record(cs)
+        slot["job"] = ck["pool"].submit(self._ppf_write_checkpoint, slot, done,
+                                        self.time_step_counter)
+
+    def _ppf_write_checkpoint(self, slot, done, step):
+        done.synchronize()
+        g = self._ppf_grid
+        for j, f in enumerate(self.fields):
+            host = slot["host"][j][..., : g.kshape[-1]].numpy().astype(np.float64)
+            f.data[f._slice] = self._ppf_decode(j, host.reshape(g.user_shape))
+        fill_ghosts_host(self)
+        self.save_simulation(step=step)
+
+    def _ppf_checkpoint_wait(self):
+        ck = getattr(self, "_ppf_ckpt", None)
+        if ck is not None:
+            for slot in ck["slots"]:
+                if slot["job"] is not None:
+                    slot["job"].result()
+                    slot["job"] = None
 
     # ------------------------------------------------------------ stepping
     def _ppf_passes(self, nsteps: int) -> list[int]:

@@ -224,16 +224,17 @@ class Simulation:
         """Engines with a device path override this."""
 
     # ------------------------------------------------------- checkpoints
-    def save_simulation(self):
+    def save_simulation(self, step=None):
         """np.savez of every field's interior, keyed by field name, to
-        <save_path>/step_<counter>.npz (simulation.py:399-420)."""
+        <save_path>/step_<counter>.npz (simulation.py:399-420); `step`
+        overrides the counter in the file name (asynchronous autosave)."""
         if not self._save_path:
             print("self._save_path not defined, aborting save!")
             return
         loc = Path(self._save_path)
         loc.mkdir(parents=True, exist_ok=True)
-        np.savez(str(loc) + "/step_" + str(self.time_step_counter),
-                 **{f.name: f.get_cells() for f in self.fields})
+        n = self.time_step_counter if step is None else int(step)
+        np.savez(str(loc) + "/step_" + str(n), **{f.name: f.get_cells() for f in self.fields})
         return 0
 
     def load_simulation(self, file_path=None, step=-1):

@@ -78,8 +78,14 @@ def test_autosave_and_load_round_trip(cuda, tmp_path):
     sim.simulate(20)
     assert sorted(p.name for p in tmp_path.glob("*.npz")) == ["step_14.npz", "step_7.npz"]
     ref14 = restate.run_single("diffusion", c0, 14, "PERIODIC", 1.0, 0.1, D=1.0)
+    ref7 = restate.run_single("diffusion", c0, 7, "PERIODIC", 1.0, 0.1, D=1.0)
     with np.load(tmp_path / "step_14.npz") as z:
         assert rel_l2(z["c"], ref14) < 1e-5
+    with np.load(tmp_path / "step_7.npz") as z:
+        assert rel_l2(z["c"], ref7) < 1e-5
+    # the checkpoints are written while stepping on; simulate() returns with
+    # Field.data at the last autosaved step, as the reference's engines do
+    assert rel_l2(sim.fields[0].get_cells(), ref14) < 1e-5
     again = DiffusionGB300(dimensions=[30, 40], dx=1.0, dt=0.1, boundary_conditions="PERIODIC",
                            user_data={"D": 1.0})
     again.load_simulation(file_path=str(tmp_path / "step_14.npz"))
@@ -197,3 +203,24 @@ def test_xdmf_temperature_is_rejected(cuda):
     d._temperature_type = "XDMF_FILE"
     with pytest.raises(NotImplementedError, match="meshio"):
         d.simulate(1)
+
+
+def test_async_autosave_many_checkpoints(cuda, tmp_path):
+    """Checkpoints every 3 steps (snapshot slots reused while earlier writes
+    may still run): every file holds its own step."""
+    from pyphasefield_gb300 import CahnAllenGB300
+    rng = np.random.default_rng(4)
+    c0 = rng.random((48, 33))
+    sim = CahnAllenGB300(dimensions=[48, 33], dx=1.0, dt=0.1, boundary_conditions="NEUMANN",
+                         save_path=str(tmp_path), autosave=True, autosave_rate=3,
+                         user_data={"graph_chunk": 2})
+    sim.initialize_fields_and_imported_data()
+    sim.fields[0].data[1:-1, 1:-1] = c0
+    sim.simulate(16)
+    names = sorted(int(p.stem.split("_")[1]) for p in tmp_path.glob("step_*.npz"))
+    assert names == [3, 6, 9, 12, 15]
+    for n in names:
+        ref = restate.run_single("allen_cahn", c0, n, "NEUMANN", 1.0, 0.1, M=0.1, epsilon=1.0,
+                                 W=1.0)
+        with np.load(tmp_path / f"step_{n}.npz") as z:
+            assert rel_l2(z["phi"], ref) < 1e-5, n
