@@ -130,6 +130,7 @@ SIGNATURES: dict[str, list] = {
     "ppf_sg_mse": [C.POINTER(PpfSgShape), P, P, P, P, P, P],
     "ppf_sg_apply": [C.POINTER(PpfSgShape), P, P, P, P],
     "ppf_sg_cast_bf16": [P, P, C.c_longlong, P],
+    "ppf_sg_set_tensor_path": [C.c_int32],
     "ppf_sg_adam": [P, P, P, P, P, C.c_longlong, C.c_float, C.c_float, C.c_float, C.c_float,
                     I32, C.c_float, P],
     "ppf_reduce_scratch_bytes": [PG, C.POINTER(SZ)],

@@ -16,6 +16,8 @@
 #include <cuda_bf16.h>
 #include <math.h>
 
+#include <type_traits>
+
 #include "ppf_common.cuh"
 
 namespace ppf {
@@ -348,10 +350,207 @@ __global__ void __launch_bounds__(kGemmThreads)
       }
 }
 
+// ---------------------------------------------------------------- tcgen05
+// The tcgen05 path is opt-in (ppf_sg_set_tensor_path(1)): it is exact
+// against torch and the mma.sync kernel, but at the network's sizes
+// (1024-8192 tokens, N = 192-512, K = 192-512) it is still slower than the
+// mma.sync kernel (prediction 1.5 vs 0.44 ms, training step 5.9 vs 3.9 ms):
+// its two register-staged stages leave the tensor core waiting on loads.
+int g_tc_enabled = 0;
+bool tc_enabled() { return g_tc_enabled != 0; }
+
+// 5th-generation tensor-core GEMM for the GEMMs whose operands are both
+// K-contiguous bf16 (A[m][k], B stored as [n][k]): the forward 1x1
+// convolutions and the output head. One CTA (4 warps) owns a 128 x 128
+// output tile whose FP32 accumulator lives in tensor memory (128 lanes x
+// 128 columns, allocated by warp 0); k advances in 64-wide tiles staged in
+// shared memory in the canonical K-major no-swizzle layout (8 x 16-byte core
+// matrices: element (row, k) at (row / 8) * 1024 + (k / 8) * 128 +
+// (row % 8) * 16 + (k % 8) * 2 bytes). Two stages: the tile for kt + 1 is
+// loaded while the tensor core works on kt. One thread issues
+// tcgen05.mma (kind::f16, BF16 x BF16 -> F32, M = 128, N = 128, K = 16 per
+// instruction) and tcgen05.commit arrives on the stage's mbarrier; the
+// epilogue reads the accumulator with tcgen05.ld (warp w: lanes 32w..32w+31
+// = rows) and applies the storer. Every mbarrier wait is bounded; a timeout
+// sets PPF_STATUS_TIMEOUT, lets the issued MMAs finish (bounded) and frees
+// the tensor memory.
+constexpr int TCM = 128, TCN = 128, TCK = 64, kTcThreads = 128;
+constexpr int kTcStage = (TCM + TCN) * TCK * 2;  // bytes of one A + B stage
+constexpr uint32_t kTcIdesc = (1u << 4)                        // D: F32
+                              | (1u << 7) | (1u << 10)         // A, B: BF16, K-major
+                              | ((uint32_t)(TCN >> 3) << 17)   // N / 8
+                              | ((uint32_t)(TCM >> 4) << 24);  // M / 16
+
+__device__ __forceinline__ uint32_t tc_smem(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+// shared-memory matrix descriptor: no swizzle, K-major, leading (K) byte
+// offset 128, stride (M / N) byte offset 1024, descriptor version 1
+__device__ __forceinline__ uint64_t tc_desc(uint32_t addr) {
+  return (uint64_t)((addr & 0x3FFFF) >> 4) | ((uint64_t)(128 >> 4) << 16) |
+         ((uint64_t)(1024 >> 4) << 32) | ((uint64_t)1 << 46);
+}
+__device__ __forceinline__ bool tc_wait(uint64_t* bar, uint32_t parity, uint32_t limit) {
+  const uint32_t a = tc_smem(bar);
+  for (uint32_t i = 0; i < limit; ++i) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, 20000;\n"
+        " selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+// Stage one 128 x 64 operand tile: rows r0.. of x (row stride ld elements,
+// k contiguous), zero beyond R rows or K columns.
+__device__ __forceinline__ void tc_load_tile(uint8_t* dst, const __nv_bfloat16* __restrict__ x,
+                                             long long ld, long long r0, long long R,
+                                             long long k0, long long K, int tid) {
+  for (int i = tid; i < 128 * (TCK / 8); i += kTcThreads) {
+    const int row = i / (TCK / 8), k8 = (i - row * (TCK / 8)) * 8;
+    uint4 v = make_uint4(0u, 0u, 0u, 0u);
+    if (r0 + row < R && k0 + k8 < K)
+      v = *reinterpret_cast<const uint4*>(x + (r0 + row) * ld + k0 + k8);
+    *reinterpret_cast<uint4*>(dst + (row >> 3) * 1024 + (k8 >> 3) * 128 + (row & 7) * 16) = v;
+  }
+}
+
+template <typename ST>
+__global__ void __launch_bounds__(kTcThreads)
+    tc_gemm_kernel(const __nv_bfloat16* __restrict__ a, long long lda,
+                   const __nv_bfloat16* __restrict__ b, long long ldb, ST st, long long M,
+                   long long N, long long K, int* __restrict__ lib_status) {
+  extern __shared__ __align__(1024) uint8_t tc_stage[];
+  __shared__ __align__(8) uint64_t bars[2];
+  __shared__ uint32_t tmem_base;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const long long m0 = (long long)blockIdx.y * TCM, n0 = (long long)blockIdx.x * TCN;
+  uint8_t* const base = tc_stage + ((1024 - (tc_smem(tc_stage) & 1023)) & 1023);
+  auto sa = [&](int st_) { return base + st_ * kTcStage; };
+  auto sb = [&](int st_) { return base + st_ * kTcStage + TCM * TCK * 2; };
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;"
+                 ::"r"(tc_smem(&tmem_base)), "r"(TCN) : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (tid == 0) {
+    for (int i = 0; i < 2; ++i)
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(tc_smem(&bars[i])) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  pdl_wait();
+  pdl_launch_next();
+  const int nk = (int)((K + TCK - 1) / TCK);
+  tc_load_tile(sa(0), a, lda, m0, M, 0, K, tid);
+  tc_load_tile(sb(0), b, ldb, n0, N, 0, K, tid);
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = tmem_base;
+  bool ok = true;
+  for (int kt = 0; kt < nk; ++kt) {
+    const int cur = kt & 1;
+    if (tid == 0) {
+#pragma unroll
+      for (int kk = 0; kk < TCK / 16; ++kk) {
+        const uint64_t da = tc_desc(tc_smem(sa(cur)) + kk * 256);
+        const uint64_t db = tc_desc(tc_smem(sb(cur)) + kk * 256);
+        const uint32_t acc = (kt > 0 || kk > 0) ? 1u : 0u;
+        asm volatile(
+            "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+            " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n"
+            ::"r"(tmem), "l"(da), "l"(db), "r"(kTcIdesc), "r"(acc) : "memory");
+      }
+      asm volatile(
+          "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+          ::"r"(tc_smem(&bars[cur])) : "memory");
+    }
+    if (kt + 1 < nk) {
+      const int nxt = cur ^ 1;
+      // stage nxt was read by the MMAs of tile kt - 1
+      if (kt >= 1 && !tc_wait(&bars[nxt], (uint32_t)(((kt - 1) >> 1) & 1), 1u << 15)) ok = false;
+      tc_load_tile(sa(nxt), a, lda, m0, M, (long long)(kt + 1) * TCK, K, tid);
+      tc_load_tile(sb(nxt), b, ldb, n0, N, (long long)(kt + 1) * TCK, K, tid);
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    __syncthreads();
+    if (__syncthreads_or(!ok)) break;
+  }
+  // the last commit (tile nk - 1) covers every MMA issued before it
+  if (ok && !tc_wait(&bars[(nk - 1) & 1], (uint32_t)(((nk - 1) >> 1) & 1), 1u << 15)) ok = false;
+  ok = !__syncthreads_or(!ok);
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  if (ok) {
+    const long long m = m0 + warp * 32 + lane;
+#pragma unroll 1
+    for (int c0 = 0; c0 < TCN; c0 += 16) {
+      uint32_t r[16];
+      const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,"
+          "%13,%14,%15}, [%16];"
+          : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+            "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+            "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+          : "r"(taddr)
+          : "memory");
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      if (m < M) {
+#pragma unroll
+        for (int j = 0; j < 16; ++j)
+          if (n0 + c0 + j < N) st(m, n0 + c0 + j, __uint_as_float(r[j]));
+      }
+    }
+  } else {
+    if (tid == 0) atomicOr(lib_status, PPF_STATUS_TIMEOUT);
+    // let every issued MMA complete before the accumulator is freed
+    if (tid == 0)
+      for (int i = 0; i < 2; ++i)
+        for (int ph = 0; ph < 2; ++ph) tc_wait(&bars[i], (uint32_t)ph, 1u << 10);
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TCN)
+                 : "memory");
+}
+
+// Whether the tcgen05 kernel applies: both operands K-contiguous with rows
+// on 16-byte boundaries, K a multiple of 8, enough rows to fill its tiles.
+bool tc_eligible(const StridedBf16& la, const StridedBf16& lb, long long M, long long K) {
+  return la.sj == 1 && lb.si == 1 && (la.si & 7) == 0 && (lb.sj & 7) == 0 && (K & 7) == 0 &&
+         (reinterpret_cast<uintptr_t>(la.x) & 15) == 0 &&
+         (reinterpret_cast<uintptr_t>(lb.x) & 15) == 0 && M >= 2 * TCM;
+}
+
+template <typename ST>
+int32_t tc_gemm(const StridedBf16& la, const StridedBf16& lb, ST st, long long M, long long N,
+                long long K, cudaStream_t s) {
+  int* status = status_ptr();
+  if (!status) return fail(PPF_ERR_CUDA, "status word unavailable");
+  const size_t smem = 2 * (size_t)kTcStage + 1024;
+  auto kern = tc_gemm_kernel<ST>;
+  PPF_TRY_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  dim3 grid((unsigned)((N + TCN - 1) / TCN), (unsigned)((M + TCM - 1) / TCM));
+  if (grid.y > 65535) return fail(PPF_ERR_INVALID, "GEMM too large");
+  PPF_TRY_CUDA(launch(kern, grid, dim3(kTcThreads), smem, s, false, la.x, la.si, lb.x, lb.sj, st,
+                      M, N, K, status));
+  return PPF_OK;
+}
+
 template <typename LA, typename LB, typename ST>
 int32_t gemm(LA la, LB lb, ST st, long long M, long long N, long long K, int splits,
              cudaStream_t s) {
   if (M < 1 || N < 1 || K < 1) return fail(PPF_ERR_INVALID, "empty GEMM");
+  if constexpr (std::is_same<LA, StridedBf16>::value && std::is_same<LB, StridedBf16>::value) {
+    if (splits <= 1 && tc_enabled() && tc_eligible(la, lb, M, K))
+      return tc_gemm(la, lb, st, M, N, K, s);
+  }
   if (splits < 1) splits = 1;
   long long kchunk = (K + splits - 1) / splits;
   kchunk = (kchunk + BK - 1) / BK * BK;
@@ -890,6 +1089,13 @@ int32_t ppf_sg_residual(const PpfSgShape* s, const float* u, const float* pred,
   residual_kernel<<<grid, 256, 0, (cudaStream_t)stream>>>(u, pred, stepped, s->H, s->W, s->pitch,
                                                           (float)k, out);
   PPF_TRY_CUDA(cudaGetLastError());
+  return PPF_OK;
+}
+
+// 1: GEMMs with K-contiguous operands run on tcgen05 (default); 0: mma.sync.
+int32_t ppf_sg_set_tensor_path(int32_t tcgen05) {
+  clear_error();
+  g_tc_enabled = tcgen05 ? 1 : 0;
   return PPF_OK;
 }
 

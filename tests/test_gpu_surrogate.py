@@ -46,6 +46,41 @@ def test_gemm_matches_torch(cuda, M, N, K, trans_a, splits):
     assert err <= 2e-5 * K ** 0.5 * expect.abs().max().item()
 
 
+@pytest.mark.parametrize("M,N,K", [(256, 128, 64), (300, 200, 136), (1024, 384, 192),
+                                   (517, 72, 520)])
+def test_tcgen05_gemm_matches_torch_and_mma_sync(cuda, M, N, K):
+    """GEMMs with K-contiguous operands and at least 256 rows run on tcgen05
+    (accumulator in tensor memory): against torch in float64 and against the
+    mma.sync kernel (ppf_sg_set_tensor_path(0)); ragged M and N tiles."""
+    torch = _torch()
+    from pyphasefield_gb300 import _lib as L
+    g = torch.Generator().manual_seed(M + N + K)
+    a = torch.randn(M, K, generator=g).to(torch.bfloat16)
+    bt = torch.randn(N, K, generator=g).to(torch.bfloat16)  # B stored [n][k]
+    bias = torch.randn(N, generator=g)
+    expect = a.double() @ bt.double().t() + bias.double()
+    ad, bd, biasd = a.to(cuda), bt.to(cuda), bias.to(cuda)
+    s = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    outs = []
+    try:
+        for path in (1, 0):
+            L.call("ppf_sg_set_tensor_path", path)
+            y = torch.zeros(M, N, device=cuda)
+            L.call("ppf_sg_gemm", C.c_void_p(ad.data_ptr()), K, 1, C.c_void_p(bd.data_ptr()), 1, K,
+                   C.c_void_p(y.data_ptr()), N, C.c_void_p(biasd.data_ptr()), 0, M, N, K, 1, s)
+            torch.cuda.synchronize()
+            outs.append(y.cpu().double())
+    finally:
+        L.call("ppf_sg_set_tensor_path", 0)
+    for y in outs:
+        assert (y - expect).abs().max().item() <= 2e-5 * K ** 0.5 * expect.abs().max().item()
+    assert (outs[0] - outs[1]).abs().max().item() <= 1e-5 * expect.abs().max().item()
+    from pyphasefield_gb300 import _lib
+    flags = C.c_int32(0)
+    L.call("ppf_status_take", C.byref(flags))
+    assert flags.value & 2 == 0  # no wait timed out
+
+
 def test_gemm_rejects_bad_arguments(cuda):
     from pyphasefield_gb300 import _lib as L
     with pytest.raises(L.PpfError):
@@ -73,7 +108,7 @@ def _tiny(cuda, seed=0, B=2, H=16, W=20):
     f_new = f_old + 0.02 * rng.normal(size=f_old.shape)
     f_old = f_old.astype(np.float32).astype(np.float64)
     f_new = f_new.astype(np.float32).astype(np.float64)
-    pitch = 32
+    pitch = (W + 31) // 32 * 32
     def dev(f):  # noqa: E306
         t = torch.full((B, 2, H, pitch), float("nan"), dtype=torch.float32)
         t[..., :W] = torch.from_numpy(f)
@@ -81,10 +116,17 @@ def _tiny(cuda, seed=0, B=2, H=16, W=20):
     return net, params, f_old, f_new, dev(f_old), dev(f_new), (B, H, W, pitch)
 
 
-def test_forward_matches_oracle(cuda):
+@pytest.mark.parametrize("B,H,W,tc", [(2, 16, 20, 0), (1, 64, 64, 0), (1, 64, 64, 1)])
+def test_forward_matches_oracle(cuda, B, H, W, tc):
+    """tc = 1: the 256-token case runs its 1x1 convolutions on tcgen05."""
     torch = _torch()
-    net, params, f_old, _, d_old, _, shp = _tiny(cuda)
-    out = net.forward(d_old, *shp, torch.cuda.current_stream()).cpu().double().numpy()
+    from pyphasefield_gb300 import _lib as L
+    net, params, f_old, _, d_old, _, shp = _tiny(cuda, B=B, H=H, W=W)
+    L.call("ppf_sg_set_tensor_path", tc)
+    try:
+        out = net.forward(d_old, *shp, torch.cuda.current_stream()).cpu().double().numpy()
+    finally:
+        L.call("ppf_sg_set_tensor_path", 0)
     ref, _ = R.forward(params, f_old, P, NB, NORM, bf16_ops=True)
     assert np.linalg.norm(out - ref) / np.linalg.norm(ref) < 2e-3
     exact, _ = R.forward(params, f_old, P, NB, NORM, bf16_ops=False)
