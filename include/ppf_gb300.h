@@ -302,9 +302,9 @@ int32_t ppf_sg_apply(const PpfSgShape* s, const float* out, const float* f_old,
  * out[3b+1] = sum_phi pred^2, out[3b+2] = cells with a non-finite pred or stepped. */
 int32_t ppf_sg_residual(const PpfSgShape* s, const float* u, const float* pred,
                         const float* stepped, int32_t k, double* out, void* stream);
-/* 1: GEMMs whose operands are both K-contiguous (and >= 256 rows) run on the
- * tcgen05 tensor cores (accumulator in tensor memory); 0 (default): every
- * GEMM on mma.sync. */
+/* 1 (default): GEMMs whose operands are both K-contiguous, with at least 4096
+ * rows, run on the tcgen05 tensor cores (accumulator in tensor memory);
+ * 0: every GEMM on mma.sync. */
 int32_t ppf_sg_set_tensor_path(int32_t tcgen05);
 int32_t ppf_sg_cast_bf16(const float* x, void* y, long long n, void* stream);
 int32_t ppf_sg_adam(float* w, void* w_bf16, const float* g, float* m1, float* m2,

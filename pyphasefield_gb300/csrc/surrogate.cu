@@ -351,12 +351,13 @@ __global__ void __launch_bounds__(kGemmThreads)
 }
 
 // ---------------------------------------------------------------- tcgen05
-// The tcgen05 path is opt-in (ppf_sg_set_tensor_path(1)): it is exact
-// against torch and the mma.sync kernel, but at the network's sizes
-// (1024-8192 tokens, N = 192-512, K = 192-512) it is still slower than the
-// mma.sync kernel (prediction 1.5 vs 0.44 ms, training step 5.9 vs 3.9 ms):
-// its two register-staged stages leave the tensor core waiting on loads.
-int g_tc_enabled = 0;
+// The tcgen05 path is on by default for GEMMs of at least kTcMinRows rows
+// (the training batches: 8192 tokens x N 384 x K 192 runs at 74 TFLOP/s vs
+// 54 on mma.sync, 65536 tokens at 132 vs 86); below that (the 1024-token
+// prediction) its few 128 x 128 tiles leave most SMs idle and mma.sync's
+// 64 x 64 tiles win. ppf_sg_set_tensor_path(0) selects mma.sync everywhere.
+int g_tc_enabled = 1;
+constexpr long long kTcMinRows = 4096;
 bool tc_enabled() { return g_tc_enabled != 0; }
 
 // 5th-generation tensor-core GEMM for the GEMMs whose operands are both
@@ -384,11 +385,13 @@ constexpr uint32_t kTcIdesc = (1u << 4)                        // D: F32
 __device__ __forceinline__ uint32_t tc_smem(const void* p) {
   return (uint32_t)__cvta_generic_to_shared(p);
 }
-// shared-memory matrix descriptor: no swizzle, K-major, leading (K) byte
-// offset 128, stride (M / N) byte offset 1024, descriptor version 1
+// shared-memory matrix descriptor: K-major, 128-byte swizzle (8-row x
+// 128-byte atoms, stride byte offset 1024 between atoms along M / N; the
+// leading offset is implied by the swizzle), descriptor version 1, the tile
+// 1024-byte aligned. Stepping K by 16 elements moves the start by 32 bytes.
 __device__ __forceinline__ uint64_t tc_desc(uint32_t addr) {
-  return (uint64_t)((addr & 0x3FFFF) >> 4) | ((uint64_t)(128 >> 4) << 16) |
-         ((uint64_t)(1024 >> 4) << 32) | ((uint64_t)1 << 46);
+  return (uint64_t)((addr & 0x3FFFF) >> 4) | ((uint64_t)1 << 16) |
+         ((uint64_t)(1024 >> 4) << 32) | ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
 }
 __device__ __forceinline__ bool tc_wait(uint64_t* bar, uint32_t parity, uint32_t limit) {
   const uint32_t a = tc_smem(bar);
@@ -406,16 +409,20 @@ __device__ __forceinline__ bool tc_wait(uint64_t* bar, uint32_t parity, uint32_t
 }
 
 // Stage one 128 x 64 operand tile: rows r0.. of x (row stride ld elements,
-// k contiguous), zero beyond R rows or K columns.
+// k contiguous), zero beyond R rows or K columns. 128-byte swizzled K-major
+// layout: row r's 16-byte chunk j sits at (r / 8) * 1024 + (r % 8) * 128 +
+// ((j ^ (r % 8)) * 16), so the 8 threads that copy one row hit 8 different
+// bank groups.
 __device__ __forceinline__ void tc_load_tile(uint8_t* dst, const __nv_bfloat16* __restrict__ x,
                                              long long ld, long long r0, long long R,
                                              long long k0, long long K, int tid) {
+#pragma unroll 4
   for (int i = tid; i < 128 * (TCK / 8); i += kTcThreads) {
-    const int row = i / (TCK / 8), k8 = (i - row * (TCK / 8)) * 8;
+    const int row = i >> 3, j = i & 7;
     uint4 v = make_uint4(0u, 0u, 0u, 0u);
-    if (r0 + row < R && k0 + k8 < K)
-      v = *reinterpret_cast<const uint4*>(x + (r0 + row) * ld + k0 + k8);
-    *reinterpret_cast<uint4*>(dst + (row >> 3) * 1024 + (k8 >> 3) * 128 + (row & 7) * 16) = v;
+    if (r0 + row < R && k0 + j * 8 < K)
+      v = *reinterpret_cast<const uint4*>(x + (r0 + row) * ld + k0 + j * 8);
+    *reinterpret_cast<uint4*>(dst + (row >> 3) * 1024 + (row & 7) * 128 + ((j ^ (row & 7)) << 4)) = v;
   }
 }
 
@@ -458,8 +465,8 @@ __global__ void __launch_bounds__(kTcThreads)
     if (tid == 0) {
 #pragma unroll
       for (int kk = 0; kk < TCK / 16; ++kk) {
-        const uint64_t da = tc_desc(tc_smem(sa(cur)) + kk * 256);
-        const uint64_t db = tc_desc(tc_smem(sb(cur)) + kk * 256);
+        const uint64_t da = tc_desc(tc_smem(sa(cur)) + kk * 32);
+        const uint64_t db = tc_desc(tc_smem(sb(cur)) + kk * 32);
         const uint32_t acc = (kt > 0 || kk > 0) ? 1u : 0u;
         asm volatile(
             "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
@@ -486,25 +493,36 @@ __global__ void __launch_bounds__(kTcThreads)
   ok = !__syncthreads_or(!ok);
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   if (ok) {
-    const long long m = m0 + warp * 32 + lane;
+    // lane = row of the accumulator; 32 columns per round go through a
+    // per-warp 32 x 33 shared tile so that the storer runs with consecutive
+    // lanes on consecutive columns (coalesced global writes)
+    float* tile = reinterpret_cast<float*>(base) + warp * 32 * 33;
 #pragma unroll 1
-    for (int c0 = 0; c0 < TCN; c0 += 16) {
-      uint32_t r[16];
-      const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0;
-      asm volatile(
-          "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,"
-          "%13,%14,%15}, [%16];"
-          : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
-            "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
-            "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-          : "r"(taddr)
-          : "memory");
-      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-      if (m < M) {
+    for (int c0 = 0; c0 < TCN; c0 += 32) {
 #pragma unroll
-        for (int j = 0; j < 16; ++j)
-          if (n0 + c0 + j < N) st(m, n0 + c0 + j, __uint_as_float(r[j]));
+      for (int h = 0; h < 2; ++h) {
+        uint32_t r[16];
+        const uint32_t taddr = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(c0 + 16 * h);
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,"
+            "%13,%14,%15}, [%16];"
+            : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+              "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+              "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+            : "r"(taddr)
+            : "memory");
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+        for (int j = 0; j < 16; ++j) tile[lane * 33 + 16 * h + j] = __uint_as_float(r[j]);
       }
+      __syncwarp();
+      const long long n = n0 + c0 + lane;
+#pragma unroll 4
+      for (int rr = 0; rr < 32; ++rr) {
+        const long long m = m0 + warp * 32 + rr;
+        if (m < M && n < N) st(m, n, tile[rr * 33 + lane]);
+      }
+      __syncwarp();
     }
   } else {
     if (tid == 0) atomicOr(lib_status, PPF_STATUS_TIMEOUT);
@@ -521,11 +539,12 @@ __global__ void __launch_bounds__(kTcThreads)
 }
 
 // Whether the tcgen05 kernel applies: both operands K-contiguous with rows
-// on 16-byte boundaries, K a multiple of 8, enough rows to fill its tiles.
+// on 16-byte boundaries, K a multiple of 8, enough rows to fill the GPU
+// with its 128 x 128 tiles.
 bool tc_eligible(const StridedBf16& la, const StridedBf16& lb, long long M, long long K) {
   return la.sj == 1 && lb.si == 1 && (la.si & 7) == 0 && (lb.sj & 7) == 0 && (K & 7) == 0 &&
          (reinterpret_cast<uintptr_t>(la.x) & 15) == 0 &&
-         (reinterpret_cast<uintptr_t>(lb.x) & 15) == 0 && M >= 2 * TCM;
+         (reinterpret_cast<uintptr_t>(lb.x) & 15) == 0 && M >= kTcMinRows;
 }
 
 template <typename ST>

@@ -593,10 +593,11 @@ def main(argv=None):
     ap.add_argument("--check-every", type=int, default=8)
     ap.add_argument("--eval", type=int, default=2, help="held-out engines (0: training only)")
     ap.add_argument("--save", default=None, help="write the trained parameters (.npz)")
-    ap.add_argument("--tcgen05", action="store_true",
-                    help="run the K-contiguous GEMMs on the tcgen05 kernel (default mma.sync)")
+    ap.add_argument("--mma-sync", action="store_true",
+                    help="run every GEMM on mma.sync (default: tcgen05 for the large "
+                         "K-contiguous ones)")
     a = ap.parse_args(argv)
-    L.call("ppf_sg_set_tensor_path", 1 if a.tcgen05 else 0)
+    L.call("ppf_sg_set_tensor_path", 0 if a.mma_sync else 1)
     H, k = a.grid, a.k
     t0 = time.perf_counter()
     data = generate_trajectories(a.trajectories, H, a.steps, k, seed=1, warm_steps=64)
@@ -626,7 +627,7 @@ def main(argv=None):
     tokens = a.batch * (H // a.patch) ** 2
     print(json.dumps({
         "grid": H, "k": k, "params": net.n_params,
-        "tensor_path": "tcgen05 (K-contiguous GEMMs) + mma.sync" if a.tcgen05 else "mma.sync",
+        "tensor_path": "mma.sync" if a.mma_sync else "tcgen05 (K-contiguous, >= 4096 rows) + mma.sync",
         "net": {"patch": a.patch, "channels": a.channels, "expand": a.expand, "blocks": a.blocks},
         "data": {"trajectories": a.trajectories, "steps": a.steps, "seconds": round(t_data, 3),
                  "cell_updates": a.trajectories * (a.steps + 64) * H * H},
