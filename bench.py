@@ -334,7 +334,7 @@ def run_gb300(args):
         clocks = clk.summary()
         if clocks:
             line["clocks"] = clocks
-        if not args.no_cpu_baseline:
+        if not args.no_cpu_baseline and world == 1:  # the CPU baseline is an N = 1 figure
             line["cpu_baseline"] = cpu_baseline(budget_s=args.cpu_budget)
         print(json.dumps(line), flush=True)
     if world > 1:
