@@ -94,7 +94,9 @@ class ClockSampler:
     def __init__(self, index: int):
         self.index = index
         self.proc = None
-        self.path = ROOT / "gpurun_out" / f"clocks_rank{index}.csv"
+        import tempfile
+        out = os.environ.get("PPF_CLOCKS_DIR", tempfile.gettempdir())
+        self.path = Path(out) / f"ppf_clocks_rank{index}.csv"
 
     def __enter__(self):
         try:
