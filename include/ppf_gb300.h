@@ -34,7 +34,7 @@ extern "C" {
 #define PPF_OK 0
 #define PPF_ERR_INVALID (-1)     /* bad argument (shape, pitch, pointer, depth) */
 #define PPF_ERR_CUDA (-2)        /* a CUDA runtime call failed */
-#define PPF_ERR_UNSUPPORTED (-3) /* valid request this build does not implement */
+#define PPF_ERR_UNSUPPORTED (-3) /* valid request the library does not implement */
 #define PPF_ERR_TIMEOUT (-4)     /* a bounded device-side wait gave up */
 #define PPF_ERR_NONFINITE (-5)   /* a field produced NaN/Inf (status flag) */
 

@@ -1,7 +1,7 @@
 """FP64 numpy restatement of pyphasefield's explicit hot path.
 
 TEST INFRASTRUCTURE ONLY. This module is the oracle: tests, the smoke check
-and the CPU-baseline leg of the benchmark use it to judge the CUDA library.
+and the CPU-baseline leg of the benchmark use it to check the CUDA library.
 Nothing in the shipped package imports it.
 
 Every function follows the reference's own numpy code on ghost-padded arrays
@@ -227,7 +227,7 @@ def run_single(model: str, c0: np.ndarray, steps: int, boundary_conditions,
 def run_warren(phi0: np.ndarray, c0: np.ndarray, steps: int, boundary_conditions,
                dx: float, params: dict, seed: int = 0, step0: int = 0,
                values=None) -> tuple[np.ndarray, np.ndarray]:
-    """Warren1995 driver: `params` are user_data constants; dt and the derived
+    """Warren1995 run: `params` are user_data constants; dt and the derived
     constants come from warren_derived. Noise uses the project's Philox
     stream (oracle.philox.noise_uniform) keyed by (seed, step) when
     params['alpha'] != 0."""
