@@ -16,6 +16,8 @@ functions with a duck-typed simulation object:
     a caller-supplied array through a numpy proxy in the module's globals.
   * The ghost fill between steps is oracle.restate.fill_ghosts (the
     reference's apply_boundary_conditions with every axis filled).
+  * The implicit / Crank-Nicolson engines (Diffusion.py:210-633) run on an
+    interior-only field (run_implicit).
 
 Available only where the reference checkout exists (PPF_REFERENCE_ROOT or the
 default below); callers skip otherwise. Nothing here is used at run time.
@@ -200,3 +202,53 @@ def run_warren(phi0, c0, steps: int, boundary_conditions, dx: float, params: dic
     finally:
         mod.np = saved
     return sim.fields[0].get_cells().copy(), sim.fields[1].get_cells().copy()
+
+
+class _InteriorField:
+    """Field stand-in holding the interior cells only: the reference's
+    implicit engines size their matrices by get_dimensions() (the interior)
+    and solve against Field.data, so they run as written on this."""
+
+    def __init__(self, data):
+        self.data = np.array(data, dtype=np.float64)
+
+
+class _InteriorSim:
+    def __init__(self, c, dx, dt, D):
+        self.fields = [_InteriorField(c)]
+        self.dx, self.dt = dx, dt
+        self.user_data = {"D": D}
+        self._dims = list(np.shape(c))
+
+    def get_cell_spacing(self):
+        return self.dx
+
+    def get_dimensions(self):
+        return list(self._dims)
+
+
+def _gmres_legacy(A, b, atol=None, **kw):
+    """scipy.sparse.linalg.gmres with the meaning atol='legacy' had (a
+    residual bound of 1e-5 relative to |b|): scipy 1.14 and later reject
+    'legacy', which makes every *_GMRES engine raise as written."""
+    from scipy.sparse.linalg import gmres
+    return gmres(A, b, rtol=1e-5, atol=0.0)
+
+
+def run_implicit(function: str, c0, steps: int, D: float, dt: float, dx: float) -> np.ndarray:
+    """Drive one of Engines/Diffusion.py's implicit / Crank-Nicolson engine
+    functions (engine_ImplicitDiffusion2D_ADI, ...) for `steps` steps on the
+    interior array. The module global ``self`` they read (:206 and every
+    engine) is injected; the *_GMRES functions get _gmres_legacy."""
+    mod = modules()["Diffusion"]
+    sim = _InteriorSim(c0, dx, dt, D)
+    saved = mod.gmres
+    mod.self = sim
+    mod.gmres = _gmres_legacy
+    try:
+        fn = getattr(mod, function)
+        for _ in range(steps):
+            fn(sim)
+    finally:
+        mod.gmres = saved
+    return np.array(sim.fields[0].data, dtype=np.float64).reshape(np.shape(c0))

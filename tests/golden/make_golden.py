@@ -5,7 +5,8 @@ Run in a checkout that has the reference (see oracle/refshim.py):
 Each fixture stores the initial interior field(s), the run parameters, and
 the interior after `steps` steps computed by the reference's numpy engine
 (engine_ExplicitDiffusion, engine_CahnAllenExplicit,
-engine_CahnHilliardExplicit, engine_Warren1995) driven by oracle.refshim.
+engine_CahnHilliardExplicit, engine_Warren1995, and the implicit /
+Crank-Nicolson diffusion engines) driven by oracle.refshim.
 The inputs are seeded synthetic fields (numpy default_rng).
 """
 from __future__ import annotations
@@ -69,6 +70,29 @@ def main():
     single("cahn_hilliard_3d_mixed", "cahn_hilliard",
            0.5 + rng.uniform(-0.2, 0.2, (9, 12, 10)), 2, ["PERIODIC", "NEUMANN", "PERIODIC"],
            1.0, 0.01, M=1.0, epsilon=1.0)
+
+    # implicit / Crank-Nicolson diffusion (Engines/Diffusion.py:210-633);
+    # their own generator keeps the fixtures below unchanged
+    irng = np.random.default_rng(20240602)
+    for name, fn, shape, steps, D, dt, dx_ in [
+        ("implicit_1d", "engine_ImplicitDiffusion1D", (40,), 3, 1.0, 0.5, 1.0),
+        ("crank_nicolson_1d", "engine_CrankNicolsonDiffusion1D", (37,), 3, 1.0, 2.0, 1.0),
+        ("implicit_2d", "engine_ImplicitDiffusion2D", (12, 10), 2, 0.7, 1.0, 1.0),
+        ("crank_nicolson_2d", "engine_CrankNicolsonDiffusion2D", (9, 14), 2, 1.0, 3.0, 1.0),
+        ("implicit_3d", "engine_ImplicitDiffusion3D", (6, 7, 5), 2, 0.5, 1.0, 0.8),
+        ("crank_nicolson_3d", "engine_CrankNicolsonDiffusion3D", (5, 6, 8), 2, 1.0, 0.4, 1.0),
+        ("implicit_2d_adi", "engine_ImplicitDiffusion2D_ADI", (24, 20), 3, 1.0, 2.0, 1.0),
+        ("crank_nicolson_2d_adi", "engine_CrankNicolsonDiffusion2D_ADI", (19, 23), 3, 1.0, 0.8, 1.0),
+        ("implicit_3d_adi", "engine_ImplicitDiffusion3D_ADI", (8, 10, 12), 2, 1.0, 5.0, 1.0),
+        ("crank_nicolson_3d_adi", "engine_CrankNicolsonDiffusion3D_ADI", (9, 7, 11), 2, 0.3, 1.0, 0.5),
+        ("implicit_2d_adi_gmres", "engine_ImplicitDiffusion2D_ADI_GMRES", (16, 12), 2, 1.0, 1.0, 1.0),
+    ]:
+        c0 = irng.random(shape)
+        out = refshim.run_implicit(fn, c0, steps, D, dt, dx_)
+        meta = dict(model="diffusion_implicit", function=fn, steps=steps, D=D, dt=dt, dx=dx_,
+                    solver="crank-nicolson" if "CrankNicolson" in fn else "implicit",
+                    adi="ADI" in fn, gmres="GMRES" in fn)
+        save(name, meta, c0=c0, out=out)
 
     dx = 4.6e-8
     prm = dict(restate.WARREN_DEFAULTS)
