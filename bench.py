@@ -367,6 +367,18 @@ SWEEP = {
     "cahn_hilliard_384": ("cahn_hilliard", (384, 384, 384), 1, 100),
     "cahn_hilliard_512": ("cahn_hilliard", (512, 512, 512), 1, 100),
     "ensemble_64": ("ensemble", None, 1, 2000),
+    # implicit / Crank-Nicolson diffusion (periodic line solves or the full
+    # system), D dt / dx^2 = 5
+    "implicit_adi_8192": ("diffusion", (8192, 8192), 1, 50,
+                          {"solver": "implicit", "adi": True, "dt": 5.0}),
+    "crank_nicolson_adi_8192": ("diffusion", (8192, 8192), 1, 50,
+                                {"solver": "crank-nicolson", "adi": True, "dt": 5.0}),
+    "implicit_adi3d_512": ("diffusion", (512, 512, 512), 1, 20,
+                           {"solver": "implicit", "adi": True, "dt": 5.0}),
+    "crank_nicolson_adi3d_512": ("diffusion", (512, 512, 512), 1, 20,
+                                 {"solver": "crank-nicolson", "adi": True, "dt": 5.0}),
+    "implicit_full_4096": ("diffusion", (4096, 4096), 1, 5,
+                           {"solver": "implicit", "adi": False, "dt": 5.0}),
 }
 SWEEP_B_ALG = {"diffusion": 8, "allen_cahn": 8, "cahn_hilliard": 8, "warren1995": 16}
 
@@ -375,9 +387,11 @@ def sweep_engine(model, grid, depth, steps, rng, extra=None):
     """An engine of `model` on `grid` with seeded synthetic fields."""
     from pyphasefield_gb300 import (CahnAllenGB300, CahnHilliardGB300, DiffusionGB300,
                                     Warren1995GB300)
-    ud = dict({"graph_chunk": min(steps, 100), "temporal_depth": depth}, **(extra or {}))
+    extra = dict(extra or {})
+    dt = extra.pop("dt", None)
+    ud = dict({"graph_chunk": min(steps, 100), "temporal_depth": depth}, **extra)
     if model == "diffusion":
-        sim = DiffusionGB300(dimensions=list(grid), dx=1.0, dt=0.2,
+        sim = DiffusionGB300(dimensions=list(grid), dx=1.0, dt=dt or 0.2,
                              boundary_conditions="PERIODIC", user_data=dict(ud, D=1.0))
         init = [0.5 + 0.01 * rng.standard_normal(grid)]
     elif model == "allen_cahn":
@@ -399,6 +413,19 @@ def sweep_engine(model, grid, depth, steps, rng, extra=None):
     for f, v in zip(sim.fields, init):
         f.data[sl] = v
     return sim
+
+
+def sweep_bytes_per_cell(model, sim) -> int:
+    """Algorithmic bytes per cell and step: every field read and written once
+    per step; for the implicit solvers once per line sweep (ADI: one sweep per
+    axis) or per Chebyshev iteration (iterate, previous iterate and the
+    right-hand side read, the new iterate written: 16 B in float)."""
+    ud = sim.user_data
+    if model == "diffusion" and ud.get("solver", "explicit") != "explicit":
+        if ud.get("adi") or len(sim.dimensions) == 1:
+            return 8 * len(sim.dimensions)
+        return 16 * sim._ppf_iterations
+    return SWEEP_B_ALG[model]
 
 
 def run_sweep(args):
@@ -426,9 +453,10 @@ def run_sweep(args):
         else:
             sim = sweep_engine(model, grid, depth, steps, rng, extra)
             cells = int(np.prod(grid))
-            bytes_per_step = SWEEP_B_ALG[model] * cells
             advance = sim.simulate
         advance(min(steps, 100))  # set-up, upload, graph capture, warm-up
+        if model != "ensemble":
+            bytes_per_step = sweep_bytes_per_cell(model, sim) * cells
         if model != "ensemble":
             stream = sim._ppf_stream
         torch.cuda.synchronize()
@@ -577,6 +605,8 @@ def profile_case(name: str):
     diff4096    Diffusion 2-D 4096^2 periodic, 5 steps (temporal depth from PPF_DEPTH, default 1)
     diff3d384   Diffusion 3-D 384^3 periodic, 5 steps
     diff16384   Diffusion 2-D 16384^2 periodic, 5 steps (2 GiB of fields: beyond L2)
+    adi4096     implicit ADI Diffusion 2-D 4096^2 (Crank-Nicolson with PPF_CN=1), D dt = 5,
+                3 steps: line solves along x and y
     """
     import torch
     from pyphasefield_gb300 import CahnHilliardGB300, DiffusionGB300
@@ -607,6 +637,15 @@ def profile_case(name: str):
         sim.initialize_fields_and_imported_data()
         sim.fields[0].data[1:-1, 1:-1] = 0.5 + 0.01 * rng.standard_normal((16384, 16384))
         sim.simulate(5)
+    elif name == "adi4096":
+        solver = "crank-nicolson" if os.environ.get("PPF_CN") == "1" else "implicit"
+        sim = DiffusionGB300(dimensions=[4096, 4096], dx=1.0, dt=5.0,
+                             boundary_conditions="PERIODIC",
+                             user_data={"D": 1.0, "use_graph": False, "solver": solver,
+                                        "adi": True})
+        sim.initialize_fields_and_imported_data()
+        sim.fields[0].data[1:-1, 1:-1] = rng.random((4096, 4096))
+        sim.simulate(3)
     elif name == "diff3d384":
         sim = DiffusionGB300(dimensions=[384, 384, 384], dx=1.0, dt=0.1,
                              boundary_conditions="PERIODIC", user_data={"D": 1.0, "use_graph": False})

@@ -203,6 +203,74 @@ int32_t ppf_warren1995_step_f64(const PpfWarren1995Params* p, const PpfGrid* g,
                                 const uint64_t* step_base,
                                 const PpfTiling* tiling, void* stream);
 
+/* ---- implicit and Crank-Nicolson diffusion ------------------------------ */
+
+/* Solver choice of the Diffusion engine's user_data["solver"]
+ * (Diffusion.simulation_loop, Engines/Diffusion.py:671-720). */
+#define PPF_SOLVER_EXPLICIT 0
+#define PPF_SOLVER_IMPLICIT 1
+#define PPF_SOLVER_CRANK_NICOLSON 2
+
+/* One step of engine_ImplicitDiffusion{1,2,3}D[_ADI][_GMRES] or
+ * engine_CrankNicolsonDiffusion{1,2,3}D[_ADI][_GMRES]
+ * (Engines/Diffusion.py:210-633). Every axis is periodic, whatever the
+ * simulation's boundary conditions: the reference's matrices are
+ * (diffusion_matrix_1d/_2d/_3d, :18-196). a = D dt / dx^2 (implicit) or
+ * D dt / (2 dx^2) (Crank-Nicolson).
+ * adi = 1: 1-D solves axis by axis in the reference's order; exact up to
+ *   rounding. adi = 0 (2-D / 3-D): the full (1 + 2 d a) I - a sum(S + S^-1)
+ *   system by Chebyshev semi-iteration with the iteration count that bounds
+ *   the error by tol relative to the field (tol = 0: 1e-7 float, 1e-14
+ *   double). The *_GMRES engines solve the same systems approximately
+ *   (scipy gmres, residual 1e-5 relative); they map to the same call.
+ * A 2-D grid with shape[0] = 1 is the 1-D engine. */
+typedef struct PpfImplicitDiffusionParams {
+  double dx, dt, D;
+  double tol;
+  int32_t solver; /* PPF_SOLVER_IMPLICIT or PPF_SOLVER_CRANK_NICOLSON */
+  int32_t adi;
+} PpfImplicitDiffusionParams;
+
+/* Bytes of device scratch a line solve along any axis of g needs. */
+int32_t ppf_implicit_scratch_bytes(const PpfGrid* g, int32_t elem_bytes, size_t* bytes);
+/* in and out must differ. tmp: a third field of g's geometry, needed by
+ * Crank-Nicolson with adi = 1 and by every adi = 0 solve in 2-D / 3-D
+ * (may be NULL otherwise). iterations (nullable) receives the Chebyshev
+ * iteration count (0 for line solves). */
+int32_t ppf_diffusion_implicit_step_f32(const PpfImplicitDiffusionParams* p,
+                                        const PpfGrid* g, const float* in,
+                                        float* out, float* tmp, void* scratch,
+                                        size_t scratch_bytes, int32_t* iterations,
+                                        void* stream);
+int32_t ppf_diffusion_implicit_step_f64(const PpfImplicitDiffusionParams* p,
+                                        const PpfGrid* g, const double* in,
+                                        double* out, double* tmp, void* scratch,
+                                        size_t scratch_bytes, int32_t* iterations,
+                                        void* stream);
+/* The building blocks. Line solve along `axis` (C order) of every line:
+ * (1 + 2 alpha) x_i - alpha (x_{i-1} + x_{i+1}) = d_i, periodic, with
+ * d = in (expl_axis < 0) or d = (1 - 2 expl_alpha) in + expl_alpha
+ * (in[-1] + in[+1]) along expl_axis (the explicit half steps of the
+ * Crank-Nicolson ADI engines, Diffusion.py:527, 580-590). In place
+ * (in == out) only without an explicit part. >= 3 cells along the axis. */
+int32_t ppf_line_solve_f32(const PpfGrid* g, int32_t axis, double alpha,
+                           int32_t expl_axis, double expl_alpha, const float* in,
+                           float* out, void* scratch, size_t scratch_bytes,
+                           void* stream);
+int32_t ppf_line_solve_f64(const PpfGrid* g, int32_t axis, double alpha,
+                           int32_t expl_axis, double expl_alpha, const double* in,
+                           double* out, void* scratch, size_t scratch_bytes,
+                           void* stream);
+/* Full periodic solve (1 + 2 d alpha) x - alpha sum(neighbours of x) = b,
+ * b = in (rhs_alpha = 0) or (1 - 2 d rhs_alpha) in + rhs_alpha
+ * sum(neighbours of in); in, out, tmp distinct. */
+int32_t ppf_periodic_solve_f32(const PpfGrid* g, double alpha, double rhs_alpha,
+                               double tol, const float* in, float* out, float* tmp,
+                               int32_t* iterations, void* stream);
+int32_t ppf_periodic_solve_f64(const PpfGrid* g, double alpha, double rhs_alpha,
+                               double tol, const double* in, double* out,
+                               double* tmp, int32_t* iterations, void* stream);
+
 /* ---- batched ensemble ------------------------------------------------- */
 
 #define PPF_MODEL_WARREN1995 1

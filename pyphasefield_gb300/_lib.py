@@ -74,6 +74,16 @@ class PpfWarren1995Params(C.Structure):
     _fields_ = [(n, C.c_double) for n in WARREN_PARAM_NAMES]
 
 
+PPF_SOLVER_EXPLICIT = 0
+PPF_SOLVER_IMPLICIT = 1
+PPF_SOLVER_CRANK_NICOLSON = 2
+
+
+class PpfImplicitDiffusionParams(C.Structure):
+    _fields_ = [(n, C.c_double) for n in ("dx", "dt", "D", "tol")] + [
+        ("solver", C.c_int32), ("adi", C.c_int32)]
+
+
 PPF_MODEL_WARREN1995 = 1
 PPF_MODEL_ALLEN_CAHN = 2
 
@@ -115,6 +125,17 @@ SIGNATURES: dict[str, list] = {
     "ppf_cahn_hilliard_step_f64": [C.POINTER(PpfCahnHilliardParams), PG, PB, P, P, P, P, PT, P],
     "ppf_warren1995_step_f32": [C.POINTER(PpfWarren1995Params), PG, PB, P, P, P, P, U64, U64, P, PT, P],
     "ppf_warren1995_step_f64": [C.POINTER(PpfWarren1995Params), PG, PB, P, P, P, P, U64, U64, P, PT, P],
+    "ppf_implicit_scratch_bytes": [PG, I32, C.POINTER(SZ)],
+    "ppf_diffusion_implicit_step_f32": [C.POINTER(PpfImplicitDiffusionParams), PG, P, P, P, P,
+                                        SZ, C.POINTER(I32), P],
+    "ppf_diffusion_implicit_step_f64": [C.POINTER(PpfImplicitDiffusionParams), PG, P, P, P, P,
+                                        SZ, C.POINTER(I32), P],
+    "ppf_line_solve_f32": [PG, I32, C.c_double, I32, C.c_double, P, P, P, SZ, P],
+    "ppf_line_solve_f64": [PG, I32, C.c_double, I32, C.c_double, P, P, P, SZ, P],
+    "ppf_periodic_solve_f32": [PG, C.c_double, C.c_double, C.c_double, P, P, P,
+                               C.POINTER(I32), P],
+    "ppf_periodic_solve_f64": [PG, C.c_double, C.c_double, C.c_double, P, P, P,
+                               C.POINTER(I32), P],
     "ppf_ensemble_plan_bytes": [C.POINTER(PpfMember), I32, PT, C.POINTER(SZ)],
     "ppf_ensemble_build": [C.POINTER(PpfMember), I32, PT, P, SZ, C.POINTER(PpfEnsemblePlan), P],
     "ppf_ensemble_step_f32": [C.POINTER(PpfEnsemblePlan), I32, U64, P, PT, P],

@@ -1,10 +1,11 @@
-"""The four explicit engines, as drop-in Simulation subclasses.
+"""The four engines, as drop-in Simulation subclasses.
 
 Each keeps the reference engine's user_data keys and defaults, its field
 names and its initial condition, and advances the fields with the CUDA
 library instead of numpy:
 
-  DiffusionGB300      <- Engines/Diffusion.py:635-733 (explicit solver)
+  DiffusionGB300      <- Engines/Diffusion.py:635-733 (explicit, implicit,
+                         Crank-Nicolson, ADI)
   CahnAllenGB300      <- Engines/CahnAllen.py:289-361 (explicit solver)
   CahnHilliardGB300   <- Engines/CahnHilliard.py:347-421 (explicit solver)
   Warren1995GB300     <- Engines/Warren1995.py:133-207
@@ -45,8 +46,20 @@ def _stencil_candidates(sim) -> list:
         [{"tile": t} for t in ((64, 16), (32, 16), (128, 8))]
 
 
+_SOLVERS = {"explicit": L.PPF_SOLVER_EXPLICIT, "implicit": L.PPF_SOLVER_IMPLICIT,
+            "crank-nicolson": L.PPF_SOLVER_CRANK_NICOLSON}
+
+
 class _DiffusionMixin(GB300Engine):
-    """c += dt*D*lap(c) (engine_ExplicitDiffusion, Engines/Diffusion.py:198-208)."""
+    """c += dt*D*lap(c) (engine_ExplicitDiffusion, Engines/Diffusion.py:198-208),
+    or one implicit / Crank-Nicolson step (Diffusion.py:210-633) chosen by
+    user_data["solver"] ("explicit" | "implicit" | "crank-nicolson") and
+    user_data["adi"], as in Diffusion.simulation_loop (:671-720). The
+    implicit solvers are periodic on every axis, as the reference's matrices
+    are (:18-196); user_data["gmres"] selects the reference's approximate
+    GMRES twins, which solve the same systems, so it maps to the same solve.
+    user_data["implicit_tol"] bounds the error of the non-ADI 2-D / 3-D
+    solves (0: the library default)."""
 
     NFIELDS = 1
 
@@ -56,6 +69,7 @@ class _DiffusionMixin(GB300Engine):
         self.user_data.setdefault("solver", "explicit")
         self.user_data.setdefault("gmres", False)
         self.user_data.setdefault("adi", False)
+        self.user_data.setdefault("implicit_tol", 0.0)
         self._ppf_defaults()
 
     def init_fields(self):
@@ -65,23 +79,68 @@ class _DiffusionMixin(GB300Engine):
         c[tuple(slice(n // 4, 3 * n // 4) for n in dim)] = 1
         self.add_field(c, "c")
 
+    @property
+    def _ppf_solver(self) -> int:
+        solver = self.user_data.get("solver", "explicit")
+        if solver not in _SOLVERS:
+            raise ValueError(f"Diffusion: solver must be one of {sorted(_SOLVERS)}, "
+                             f"got {solver!r}")
+        return _SOLVERS[solver]
+
     def _ppf_prepare(self):
-        _explicit_only(self.user_data, "Diffusion")
         if self.dt is None or self.dx is None:
             raise ValueError("Diffusion needs dx and dt")
+        if self._ppf_solver != L.PPF_SOLVER_EXPLICIT and min(self.dimensions) < 3:
+            raise ValueError("the implicit solvers need >= 3 cells per axis (the reference's "
+                             "periodic matrices are malformed below that)")
+
+    def _ppf_setup(self):
+        if self._ppf_solver != L.PPF_SOLVER_EXPLICIT and self._boundary_conditions_type is None:
+            # the implicit solvers are periodic; the host ghost cells follow
+            self._boundary_conditions_type = "PERIODIC"
+        super()._ppf_setup()
+        self._ppf_tmp = self._ppf_scratch = None
+        if self._ppf_solver != L.PPF_SOLVER_EXPLICIT:
+            g = self._ppf_grid
+            self._ppf_tmp = g.empty()
+            nbytes = C.c_size_t()
+            L.call("ppf_implicit_scratch_bytes", C.byref(g.grid),
+                   4 if self._ppf_dtype == torch.float32 else 8, C.byref(nbytes))
+            self._ppf_scratch = torch.empty(max(16, nbytes.value), dtype=torch.uint8,
+                                            device=g.device)
 
     def _ppf_max_depth(self):
+        if self._ppf_solver != L.PPF_SOLVER_EXPLICIT:
+            return 1
         return 8 if len(self._ppf_grid.kshape) == 2 else 1
 
     def _ppf_tune_candidates(self):
+        if self._ppf_solver != L.PPF_SOLVER_EXPLICIT:
+            return []
         return _stencil_candidates(self)
 
     def _ppf_params(self):
         return L.PpfDiffusionParams(float(self.dx), float(self.dt), float(self.user_data["D"]))
 
+    def _ppf_implicit_params(self):
+        ud = self.user_data
+        return L.PpfImplicitDiffusionParams(float(self.dx), float(self.dt), float(ud["D"]),
+                                            float(ud.get("implicit_tol", 0.0)), self._ppf_solver,
+                                            1 if ud.get("adi", False) else 0)
+
     def _ppf_step(self, src, dst, depth, step, step_base, sp):
+        f = _F[self._ppf_dtype]
+        if self._ppf_solver != L.PPF_SOLVER_EXPLICIT:
+            p = self._ppf_implicit_params()
+            it = C.c_int32()
+            sc = self._ppf_scratch
+            L.call(f"ppf_diffusion_implicit_step_{f}", C.byref(p), C.byref(self._ppf_grid.grid),
+                   ptr(src[0]), ptr(dst[0]), ptr(self._ppf_tmp), ptr(sc), sc.numel(),
+                   C.byref(it), sp)
+            self._ppf_iterations = it.value
+            return
         p = self._ppf_params()
-        L.call(f"ppf_diffusion_step_{_F[self._ppf_dtype]}", C.byref(p),
+        L.call(f"ppf_diffusion_step_{f}", C.byref(p),
                C.byref(self._ppf_grid.grid), C.byref(self._ppf_bc), ptr(src[0]), ptr(dst[0]),
                C.byref(self._ppf_tiling(depth)), sp)
 
