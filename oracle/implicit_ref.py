@@ -261,3 +261,147 @@ def chebyshev_solve(rhs: np.ndarray, x0: np.ndarray, alpha: float, tol: float) -
             nxt = prev + om[j] * (nxt - prev)
         prev, cur = cur, nxt
     return cur
+
+
+# ---------------------------------------------------------------------------
+# Allen-Cahn ("CahnAllen") and Cahn-Hilliard implicit engines
+# (Engines/CahnAllen.py:137-280, Engines/CahnHilliard.py:148-341): periodic
+# systems whose diagonal varies per cell.
+
+def var_line_solve(b: np.ndarray, diag: np.ndarray, alpha: float, axis: int) -> np.ndarray:
+    """Solve diag_i x_i - alpha (x_{i-1} + x_{i+1}) = b_i, periodic, along
+    `axis` for every line; diag has b's shape, or is 1-D (the same diagonal
+    for every line, indexed by the position along the line)."""
+    n = b.shape[axis]
+    if n < 3:
+        raise ValueError("periodic line solves need >= 3 cells per axis")
+    bm = np.moveaxis(np.asarray(b, dtype=np.float64), axis, 0)
+    flat_b = bm.reshape(n, -1)
+    if np.ndim(diag) == 1:
+        m = periodic_matrix_1d(n, 0.0, -alpha)
+        m[np.arange(n), np.arange(n)] = diag
+        x = np.linalg.solve(m, flat_b)
+    else:
+        dm = np.moveaxis(np.asarray(diag, dtype=np.float64), axis, 0).reshape(n, -1)
+        x = np.empty_like(flat_b)
+        base = periodic_matrix_1d(n, 0.0, -alpha)
+        for j in range(flat_b.shape[1]):
+            m = base.copy()
+            m[np.arange(n), np.arange(n)] = dm[:, j]
+            x[:, j] = np.linalg.solve(m, flat_b[:, j])
+    return np.moveaxis(x.reshape(bm.shape), 0, axis)
+
+
+def well_slope(phi):
+    """4 phi^2 - 6 phi + 2: the double well's g'(phi) / phi."""
+    return 4.0 * phi * phi - 6.0 * phi + 2.0
+
+
+def allen_cahn_implicit_step(phi, solver: str, M: float, W: float, eps: float, dt: float,
+                             dx: float, adi: bool, gmres: bool) -> np.ndarray:
+    """One step of CahnAllen.simulation_loop for the non-explicit solvers
+    (CahnAllen.py:325-361), each branch restating the engine function it
+    calls. Branches the reference leaves empty (Crank-Nicolson in 1-D and
+    3-D, IMEX beyond 1-D) return the field unchanged, as it does."""
+    phi = np.asarray(phi, dtype=np.float64)
+    a = M * dt * eps ** 2 / dx ** 2
+    nd = phi.ndim
+    if solver == "implicit":
+        if nd == 1:  # engine_CahnAllenImplicit1D[_GMRES] :137-162
+            return var_line_solve(phi, 1 + 2 * a + 16 * W * M * dt * well_slope(phi), a, 0)
+        if nd == 2:
+            if gmres and not adi:  # engine_CahnAllenImplicit2D_GMRES :163-175
+                diag = 1 + 4 * a + 16 * W * M * dt * well_slope(phi)
+                m = periodic_matrix_nd(phi.shape, 0.0, -a)
+                m[np.arange(phi.size), np.arange(phi.size)] = diag.ravel()
+                return np.linalg.solve(m, phi.ravel()).reshape(phi.shape)
+            # engine_CahnAllenImplicit2D_ADI[_GMRES] :176-186, :209-224: rows, then columns,
+            # each with the source term of the field as it stands
+            phi = var_line_solve(phi, 1 + 2 * a + 8 * W * M * dt * well_slope(phi), a, 1)
+            return var_line_solve(phi, 1 + 2 * a + 8 * W * M * dt * well_slope(phi), a, 0)
+        # engine_CahnAllenImplicit3D_ADI :225-251: np.fill_diagonal takes the first
+        # n entries of the flattened 3-D source term, so every line of an axis
+        # shares the diagonal 1 + 2a + s.flat[:n]
+        s = (16 * W * M * dt * well_slope(phi) / 3).ravel()
+        for ax in (2, 1, 0):
+            phi = var_line_solve(phi, 1 + 2 * a + s[:phi.shape[ax]], a, ax)
+        return phi
+    if solver == "imex":
+        if nd != 1:
+            return phi
+        # engine_CahnAllenIMEX1D :252-267 (its -2 phi term as written)
+        rhs = phi - 16 * W * M * dt * (4 * phi ** 3 - 6 * phi ** 2 - 2 * phi)
+        return line_solve(rhs, a, 0)
+    if solver == "crank-nicolson":
+        if nd != 2:
+            return phi
+        # engine_CahnAllenCrankNicolson2D_ADI :187-208: explicit half along
+        # axis 1, rows; explicit half along axis 0, columns; the source term
+        # keeps the full dt
+        h = 0.5 * a
+        phi = explicit_half(phi, h, 1)
+        phi = var_line_solve(phi, 1 + 2 * h + 8 * W * M * dt * well_slope(phi), h, 1)
+        phi = explicit_half(phi, h, 0)
+        return var_line_solve(phi, 1 + 2 * h + 8 * W * M * dt * well_slope(phi), h, 0)
+    raise ValueError(solver)
+
+
+def cahn_hilliard_matrix_1d(c, M: float, eps: float, dt: float, dx: float) -> np.ndarray:
+    """implicit_matrix_1d of CahnHilliard.py:20-71 with the coefficients of
+    engine_CahnHilliardImplicit1D (:148-163): row j holds
+    1 + a (2 s_j + 6 e2/dx^2) on the diagonal, -a (s_j + 4 e2/dx^2) at
+    j -/+ 1 and a e2/dx^2 at j -/+ 2 (periodic), a = M dt / dx^2,
+    s = 4c^2 - 6c + 2."""
+    n = c.size
+    if n < 5:
+        raise ValueError("the periodic pentadiagonal solve needs >= 5 cells")
+    idx2 = 1.0 / dx ** 2
+    e2 = eps ** 2
+    a = M * dt * idx2
+    s = well_slope(c)
+    m = np.zeros((n, n))
+    j = np.arange(n)
+    m[j, j] = 1 + a * (2 * s + 6 * e2 * idx2)
+    nb = -a * (s + 4 * e2 * idx2)
+    m[j, (j - 1) % n] = nb
+    m[j, (j + 1) % n] = nb
+    m[j, (j - 2) % n] = a * e2 * idx2
+    m[j, (j + 2) % n] = a * e2 * idx2
+    return m
+
+
+def cahn_hilliard_implicit_step(c, solver: str, M: float, W: float, eps: float, dt: float,
+                                dx: float, adi: bool, gmres: bool) -> np.ndarray:
+    """One step of CahnHilliard.simulation_loop for the non-explicit solvers
+    (CahnHilliard.py:382-421). 1-D implicit (:148-179) and Crank-Nicolson
+    (:180-227: an explicit step of M times the Laplacian of mu, without dt as
+    written, then the implicit solve with dt/2). The
+    2-D / 3-D engines and IMEX call the three-argument matrix builder of the
+    Allen-Cahn module, which CahnHilliard.py does not define (TypeError in the
+    reference); their evident intent, the Allen-Cahn formulas they copy
+    (:228-341), is what runs here."""
+    c = np.asarray(c, dtype=np.float64)
+    if c.ndim == 1 and solver in ("implicit", "crank-nicolson"):
+        h = dt
+        if solver == "crank-nicolson":
+            h = dt / 2
+            mu = -eps ** 2 * lap_periodic(c, dx) + (4 * c ** 3 - 6 * c ** 2 + 2 * c)
+            c = c + M * (np.roll(mu, 1) + np.roll(mu, -1) - 2 * mu) / dx ** 2
+        return np.linalg.solve(cahn_hilliard_matrix_1d(c, M, eps, h, dx), c)
+    return allen_cahn_implicit_step(c, solver, M, W, eps, dt, dx, adi, gmres)
+
+
+def lap_periodic(x, dx):
+    out = np.zeros_like(x)
+    for ax in range(x.ndim):
+        out += np.roll(x, 1, ax) + np.roll(x, -1, ax) - 2 * x
+    return out / dx ** 2
+
+
+def run_phase(model: str, c0, steps: int, solver: str, M: float, W: float, eps: float,
+              dt: float, dx: float, adi: bool, gmres: bool) -> np.ndarray:
+    fn = allen_cahn_implicit_step if model == "allen_cahn" else cahn_hilliard_implicit_step
+    c = np.asarray(c0, dtype=np.float64)
+    for _ in range(steps):
+        c = fn(c, solver, M, W, eps, dt, dx, adi, gmres)
+    return c

@@ -204,18 +204,17 @@ def run_warren(phi0, c0, steps: int, boundary_conditions, dx: float, params: dic
     return sim.fields[0].get_cells().copy(), sim.fields[1].get_cells().copy()
 
 
-class _InteriorField:
-    """Field stand-in holding the interior cells only: the reference's
-    implicit engines size their matrices by get_dimensions() (the interior)
-    and solve against Field.data, so they run as written on this."""
-
-    def __init__(self, data):
-        self.data = np.array(data, dtype=np.float64)
-
-
 class _InteriorSim:
-    def __init__(self, c, dx, dt, D):
-        self.fields = [_InteriorField(c)]
+    """A simulation whose one Field holds the interior cells only: the
+    reference's implicit engines size their matrices by get_dimensions()
+    (the interior) and solve against Field.data, so they run as written on
+    it; Field.laplacian then wraps periodically, as the matrices do."""
+
+    def __init__(self, c, dx, dt, D=None):
+        Field = modules()["field"].Field
+        f = Field(data=np.asarray(c, dtype=np.float64), simulation=self, name="c")
+        f.data = np.array(c, dtype=np.float64)
+        self.fields = [f]
         self.dx, self.dt = dx, dt
         self.user_data = {"D": D}
         self._dims = list(np.shape(c))
@@ -235,15 +234,19 @@ def _gmres_legacy(A, b, atol=None, **kw):
     return gmres(A, b, rtol=1e-5, atol=0.0)
 
 
-def run_implicit(function: str, c0, steps: int, D: float, dt: float, dx: float) -> np.ndarray:
-    """Drive one of Engines/Diffusion.py's implicit / Crank-Nicolson engine
-    functions (engine_ImplicitDiffusion2D_ADI, ...) for `steps` steps on the
-    interior array. The module global ``self`` they read (:206 and every
-    engine) is injected; the *_GMRES functions get _gmres_legacy."""
-    mod = modules()["Diffusion"]
+def run_implicit(function: str, c0, steps: int, D: float, dt: float, dx: float,
+                 module: str = "Diffusion", user_data=None) -> np.ndarray:
+    """Drive one of the reference's implicit / Crank-Nicolson / IMEX engine
+    functions (Diffusion.py:210-633, CahnAllen.py:137-267,
+    CahnHilliard.py:148-341) for `steps` steps on the interior array. The
+    module globals they read (``self`` in Diffusion.py, ``user_data`` in the
+    other two) are injected; the *_GMRES functions get _gmres_legacy."""
+    mod = modules()[module]
     sim = _InteriorSim(c0, dx, dt, D)
     saved = mod.gmres
     mod.self = sim
+    if user_data is not None:
+        mod.user_data = dict(user_data)
     mod.gmres = _gmres_legacy
     try:
         fn = getattr(mod, function)

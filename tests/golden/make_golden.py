@@ -94,6 +94,40 @@ def main():
                     adi="ADI" in fn, gmres="GMRES" in fn)
         save(name, meta, c0=c0, out=out)
 
+    # implicit / Crank-Nicolson / IMEX Allen-Cahn and Cahn-Hilliard
+    # (CahnAllen.py:137-267, CahnHilliard.py:148-227)
+    prng = np.random.default_rng(20240603)
+    ud = dict(M=0.7, W=1.3, epsilon=1.1)
+    for name, module, fn, shape, solver, adi, gm in [
+        ("phase_implicit_ac_1d", "CahnAllen", "engine_CahnAllenImplicit1D", (40,), "implicit",
+         False, False),
+        ("phase_implicit_ac_1d_gmres", "CahnAllen", "engine_CahnAllenImplicit1D_GMRES", (40,),
+         "implicit", False, True),
+        ("phase_implicit_ac_2d_gmres", "CahnAllen", "engine_CahnAllenImplicit2D_GMRES", (9, 8),
+         "implicit", False, True),
+        ("phase_implicit_ac_2d_adi", "CahnAllen", "engine_CahnAllenImplicit2D_ADI", (20, 24),
+         "implicit", True, False),
+        ("phase_implicit_ac_2d_adi_gmres", "CahnAllen", "engine_CahnAllenImplicit2D_ADI_GMRES",
+         (12, 10), "implicit", True, True),
+        ("phase_implicit_ac_2d_cn_adi", "CahnAllen", "engine_CahnAllenCrankNicolson2D_ADI",
+         (19, 21), "crank-nicolson", True, False),
+        ("phase_implicit_ac_3d_adi", "CahnAllen", "engine_CahnAllenImplicit3D_ADI", (6, 8, 10),
+         "implicit", True, False),
+        ("phase_implicit_ac_1d_imex", "CahnAllen", "engine_CahnAllenIMEX1D", (40,), "imex",
+         False, False),
+        ("phase_implicit_ch_1d", "CahnHilliard", "engine_CahnHilliardImplicit1D", (40,),
+         "implicit", False, False),
+        ("phase_implicit_ch_1d_cn", "CahnHilliard", "engine_CahnHilliardCrankNicolson1D", (36,),
+         "crank-nicolson", False, False),
+    ]:
+        c0 = 0.5 + 0.4 * (prng.random(shape) - 0.5)
+        dt, dx_ = 0.3, 1.2
+        out = refshim.run_implicit(fn, c0, 3, None, dt, dx_, module=module, user_data=ud)
+        meta = dict(model="allen_cahn" if module == "CahnAllen" else "cahn_hilliard",
+                    function=fn, steps=3, dt=dt, dx=dx_, solver=solver, adi=adi, gmres=gm,
+                    params=ud)
+        save(name, meta, c0=c0, out=out)
+
     dx = 4.6e-8
     prm = dict(restate.WARREN_DEFAULTS)
     for name, shape, center, r, bc, steps, alpha, seed in [

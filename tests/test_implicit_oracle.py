@@ -78,3 +78,33 @@ def test_reference_degenerate_short_axes_rejected():
         I.line_solve(np.ones(2), 1.0, 0)
     with pytest.raises(ValueError):
         I.full_solve_dense(np.ones((2, 5)), 1.0)
+
+
+PHASE = sorted(p.stem for p in GOLDEN.glob("phase_implicit_*.npz"))
+
+
+def test_phase_fixture_set_complete():
+    assert len(PHASE) == 10
+
+
+@pytest.mark.parametrize("name", PHASE)
+def test_phase_oracle_matches_reference_fixture(name):
+    z = np.load(GOLDEN / f"{name}.npz")
+    m = json.loads(str(z["meta"]))
+    p = m["params"]
+    got = I.run_phase(m["model"], z["c0"], m["steps"], m["solver"], p["M"], p["W"],
+                      p["epsilon"], m["dt"], m["dx"], m["adi"], m["gmres"])
+    err = np.abs(got - z["out"]).max() / np.abs(z["out"]).max()
+    assert err <= (1e-3 if m["gmres"] else 1e-13), err
+
+
+def test_var_line_solve_shared_and_per_cell_diagonals():
+    rng = np.random.default_rng(6)
+    b = rng.random((7, 9))
+    d1 = 3.0 + rng.random(9)
+    x = I.var_line_solve(b, d1, 1.0, 1)
+    full = np.broadcast_to(d1, b.shape)
+    np.testing.assert_allclose(I.var_line_solve(b, full, 1.0, 1), x, rtol=1e-14)
+    # residual of every row
+    r = d1 * x - 1.0 * (np.roll(x, 1, 1) + np.roll(x, -1, 1)) - b
+    assert np.abs(r).max() < 1e-13
