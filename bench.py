@@ -379,6 +379,16 @@ SWEEP = {
                                  {"solver": "crank-nicolson", "adi": True, "dt": 5.0}),
     "implicit_full_4096": ("diffusion", (4096, 4096), 1, 5,
                            {"solver": "implicit", "adi": False, "dt": 5.0}),
+    # semi-implicit Allen-Cahn (a diagonal that varies per cell): M eps^2 dt / dx^2 = 0.1,
+    # 16 W M dt = 1.6
+    "allen_cahn_implicit_adi_8192": ("allen_cahn", (8192, 8192), 1, 50,
+                                     {"solver": "implicit", "adi": True, "dt": 1.0}),
+    "allen_cahn_cn_adi_8192": ("allen_cahn", (8192, 8192), 1, 50,
+                               {"solver": "crank-nicolson", "adi": True, "dt": 1.0}),
+    "allen_cahn_implicit_adi3d_512": ("allen_cahn", (512, 512, 512), 1, 20,
+                                      {"solver": "implicit", "adi": True, "dt": 1.0}),
+    "allen_cahn_full_4096": ("allen_cahn", (4096, 4096), 1, 5,
+                             {"solver": "implicit", "adi": False, "gmres": True, "dt": 1.0}),
 }
 SWEEP_B_ALG = {"diffusion": 8, "allen_cahn": 8, "cahn_hilliard": 8, "warren1995": 16}
 
@@ -395,7 +405,7 @@ def sweep_engine(model, grid, depth, steps, rng, extra=None):
                              boundary_conditions="PERIODIC", user_data=dict(ud, D=1.0))
         init = [0.5 + 0.01 * rng.standard_normal(grid)]
     elif model == "allen_cahn":
-        sim = CahnAllenGB300(dimensions=list(grid), dx=1.0, dt=0.1,
+        sim = CahnAllenGB300(dimensions=list(grid), dx=1.0, dt=dt or 0.1,
                              boundary_conditions="NEUMANN", user_data=dict(ud))
         init = [rng.random(grid)]
     elif model == "cahn_hilliard":
@@ -421,7 +431,7 @@ def sweep_bytes_per_cell(model, sim) -> int:
     axis) or per Chebyshev iteration (iterate, previous iterate and the
     right-hand side read, the new iterate written: 16 B in float)."""
     ud = sim.user_data
-    if model == "diffusion" and ud.get("solver", "explicit") != "explicit":
+    if model in ("diffusion", "allen_cahn") and ud.get("solver", "explicit") != "explicit":
         if ud.get("adi") or len(sim.dimensions) == 1:
             return 8 * len(sim.dimensions)
         return 16 * sim._ppf_iterations

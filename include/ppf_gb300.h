@@ -210,6 +210,7 @@ int32_t ppf_warren1995_step_f64(const PpfWarren1995Params* p, const PpfGrid* g,
 #define PPF_SOLVER_EXPLICIT 0
 #define PPF_SOLVER_IMPLICIT 1
 #define PPF_SOLVER_CRANK_NICOLSON 2
+#define PPF_SOLVER_IMEX 3
 
 /* One step of engine_ImplicitDiffusion{1,2,3}D[_ADI][_GMRES] or
  * engine_CrankNicolsonDiffusion{1,2,3}D[_ADI][_GMRES]
@@ -270,6 +271,55 @@ int32_t ppf_periodic_solve_f32(const PpfGrid* g, double alpha, double rhs_alpha,
 int32_t ppf_periodic_solve_f64(const PpfGrid* g, double alpha, double rhs_alpha,
                                double tol, const double* in, double* out,
                                double* tmp, int32_t* iterations, void* stream);
+
+/* One step of the Allen-Cahn ("CahnAllen") or Cahn-Hilliard engines with
+ * user_data solver "implicit", "crank-nicolson" or "imex"
+ * (Engines/CahnAllen.py:137-267, dispatch :325-361;
+ * Engines/CahnHilliard.py:148-341, dispatch :382-421). Periodic on every
+ * axis, as the reference's matrices are. a = M dt eps^2 / dx^2.
+ *  Allen-Cahn, 1-D implicit: (1 + 2a + 16 W M dt g(phi)) on the diagonal,
+ *    g(phi) = 4 phi^2 - 6 phi + 2; 2-D implicit: rows then columns with
+ *    8 W M dt g (ADI; gmres without adi: the full 2-D system by Chebyshev
+ *    with Jacobi scaling, error bound tol, needs 4 W M dt < 1); 3-D implicit:
+ *    x, y, z solves whose diagonal is the first n entries of the flattened
+ *    source term, as np.fill_diagonal gives the reference; Crank-Nicolson
+ *    (2-D): explicit half and solve along x, then along y; IMEX (1-D).
+ *    Branches the reference leaves empty return the field unchanged.
+ *  Cahn-Hilliard, 1-D implicit and Crank-Nicolson: the cyclic pentadiagonal
+ *    system of CahnHilliard.py:20-71. Its 2-D / 3-D and IMEX engines call
+ *    an Allen-Cahn matrix builder the module lacks (TypeError in the
+ *    reference); they run the Allen-Cahn formulas they copy.
+ * tmp: a third field (Crank-Nicolson, IMEX, the full 2-D solve). */
+#define PPF_MODEL_CAHN_HILLIARD 3
+typedef struct PpfImplicitPhaseParams {
+  double dx, dt, M, W, epsilon;
+  double tol;
+  int32_t model;  /* PPF_MODEL_ALLEN_CAHN or PPF_MODEL_CAHN_HILLIARD */
+  int32_t solver; /* PPF_SOLVER_IMPLICIT, _CRANK_NICOLSON or _IMEX */
+  int32_t adi, gmres;
+} PpfImplicitPhaseParams;
+
+int32_t ppf_phase_implicit_scratch_bytes(const PpfGrid* g, int32_t elem_bytes, size_t* bytes);
+int32_t ppf_phase_implicit_step_f32(const PpfImplicitPhaseParams* p, const PpfGrid* g,
+                                    const float* in, float* out, float* tmp, void* scratch,
+                                    size_t scratch_bytes, int32_t* iterations, void* stream);
+int32_t ppf_phase_implicit_step_f64(const PpfImplicitPhaseParams* p, const PpfGrid* g,
+                                    const double* in, double* out, double* tmp, void* scratch,
+                                    size_t scratch_bytes, int32_t* iterations, void* stream);
+/* Periodic line solve along `axis` with a diagonal that varies:
+ * d_i x_i - alpha (x_{i-1} + x_{i+1}) = b_i, d_i = dvec[i] (dvec non-NULL:
+ * one diagonal for every line, indexed by the position along it) or
+ * dbase + dcoef (4 b_i^2 - 6 b_i + 2); b = in, or with expl = 1 the
+ * explicit half step (1 - 2 expl_alpha) in + expl_alpha (in[-1] + in[+1])
+ * along the same axis. In place (in == out) only without expl. */
+int32_t ppf_var_line_solve_f32(const PpfGrid* g, int32_t axis, double alpha, double dbase,
+                               double dcoef, const float* dvec, int32_t expl,
+                               double expl_alpha, const float* in, float* out, void* scratch,
+                               size_t scratch_bytes, void* stream);
+int32_t ppf_var_line_solve_f64(const PpfGrid* g, int32_t axis, double alpha, double dbase,
+                               double dcoef, const double* dvec, int32_t expl,
+                               double expl_alpha, const double* in, double* out, void* scratch,
+                               size_t scratch_bytes, void* stream);
 
 /* ---- batched ensemble ------------------------------------------------- */
 

@@ -77,6 +77,13 @@ class PpfWarren1995Params(C.Structure):
 PPF_SOLVER_EXPLICIT = 0
 PPF_SOLVER_IMPLICIT = 1
 PPF_SOLVER_CRANK_NICOLSON = 2
+PPF_SOLVER_IMEX = 3
+PPF_MODEL_CAHN_HILLIARD = 3
+
+
+class PpfImplicitPhaseParams(C.Structure):
+    _fields_ = [(n, C.c_double) for n in ("dx", "dt", "M", "W", "epsilon", "tol")] + [
+        (n, C.c_int32) for n in ("model", "solver", "adi", "gmres")]
 
 
 class PpfImplicitDiffusionParams(C.Structure):
@@ -130,6 +137,15 @@ SIGNATURES: dict[str, list] = {
                                         SZ, C.POINTER(I32), P],
     "ppf_diffusion_implicit_step_f64": [C.POINTER(PpfImplicitDiffusionParams), PG, P, P, P, P,
                                         SZ, C.POINTER(I32), P],
+    "ppf_phase_implicit_scratch_bytes": [PG, I32, C.POINTER(SZ)],
+    "ppf_phase_implicit_step_f32": [C.POINTER(PpfImplicitPhaseParams), PG, P, P, P, P, SZ,
+                                    C.POINTER(I32), P],
+    "ppf_phase_implicit_step_f64": [C.POINTER(PpfImplicitPhaseParams), PG, P, P, P, P, SZ,
+                                    C.POINTER(I32), P],
+    "ppf_var_line_solve_f32": [PG, I32, C.c_double, C.c_double, C.c_double, P, I32, C.c_double,
+                               P, P, P, SZ, P],
+    "ppf_var_line_solve_f64": [PG, I32, C.c_double, C.c_double, C.c_double, P, I32, C.c_double,
+                               P, P, P, SZ, P],
     "ppf_line_solve_f32": [PG, I32, C.c_double, I32, C.c_double, P, P, P, SZ, P],
     "ppf_line_solve_f64": [PG, I32, C.c_double, I32, C.c_double, P, P, P, SZ, P],
     "ppf_periodic_solve_f32": [PG, C.c_double, C.c_double, C.c_double, P, P, P,

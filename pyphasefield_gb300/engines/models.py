@@ -6,8 +6,10 @@ library instead of numpy:
 
   DiffusionGB300      <- Engines/Diffusion.py:635-733 (explicit, implicit,
                          Crank-Nicolson, ADI)
-  CahnAllenGB300      <- Engines/CahnAllen.py:289-361 (explicit solver)
-  CahnHilliardGB300   <- Engines/CahnHilliard.py:347-421 (explicit solver)
+  CahnAllenGB300      <- Engines/CahnAllen.py:289-361 (explicit, implicit,
+                         Crank-Nicolson, IMEX)
+  CahnHilliardGB300   <- Engines/CahnHilliard.py:347-421 (explicit, implicit,
+                         Crank-Nicolson, IMEX)
   Warren1995GB300     <- Engines/Warren1995.py:133-207
 
 ``make_engines(Base)`` builds the same four classes on any Simulation base
@@ -28,11 +30,68 @@ from .base import GB300Engine
 _F = {torch.float32: "f32", torch.float64: "f64"}
 
 
-def _explicit_only(ud, name):
-    solver = ud.get("solver", "explicit")
-    if solver != "explicit":
-        raise NotImplementedError(f"{name}: only the explicit solver runs on the GB300 "
-                                  f"path (got solver={solver!r})")
+_PHASE_SOLVERS = {"implicit": L.PPF_SOLVER_IMPLICIT, "crank-nicolson": L.PPF_SOLVER_CRANK_NICOLSON,
+                  "imex": L.PPF_SOLVER_IMEX}
+
+
+class _ImplicitPhase:
+    """user_data["solver"] of the Allen-Cahn and Cahn-Hilliard engines:
+    "explicit" (the stencil kernels) or "implicit" / "crank-nicolson" /
+    "imex" with "adi" and "gmres", dispatched as CahnAllen.simulation_loop
+    (Engines/CahnAllen.py:325-361) and CahnHilliard.simulation_loop
+    (Engines/CahnHilliard.py:382-421) do; periodic, as the reference's
+    matrices are. user_data["implicit_tol"] bounds the error of the full 2-D
+    solve (0: the library default)."""
+
+    PHASE_MODEL = 0
+
+    @property
+    def _ppf_phase_solver(self):
+        solver = self.user_data.get("solver", "explicit")
+        if solver == "explicit":
+            return None
+        if solver not in _PHASE_SOLVERS:
+            raise ValueError(f"{type(self).__name__}: solver must be 'explicit', "
+                             f"{', '.join(repr(k) for k in _PHASE_SOLVERS)}; got {solver!r}")
+        return _PHASE_SOLVERS[solver]
+
+    def _ppf_phase_prepare(self):
+        if self._ppf_phase_solver is None:
+            return
+        if self.dt is None or self.dx is None:
+            raise ValueError(f"{type(self).__name__}: the implicit solvers need dx and dt")
+        if min(self.dimensions) < 3:
+            raise ValueError("the implicit solvers need >= 3 cells per axis")
+
+    def _ppf_phase_setup(self):
+        self._ppf_tmp = self._ppf_scratch = None
+        if self._ppf_phase_solver is None:
+            return
+        g = self._ppf_grid
+        self._ppf_tmp = g.empty()
+        nbytes = C.c_size_t()
+        L.call("ppf_phase_implicit_scratch_bytes", C.byref(g.grid),
+               4 if self._ppf_dtype == torch.float32 else 8, C.byref(nbytes))
+        self._ppf_scratch = torch.empty(max(16, nbytes.value), dtype=torch.uint8,
+                                        device=g.device)
+
+    def _ppf_phase_step(self, src, dst, sp):
+        ud = self.user_data
+        p = L.PpfImplicitPhaseParams(float(self.dx), float(self.dt), float(ud["M"]),
+                                     float(ud["W"]), float(ud["epsilon"]),
+                                     float(ud.get("implicit_tol", 0.0)), self.PHASE_MODEL,
+                                     self._ppf_phase_solver, 1 if ud.get("adi") else 0,
+                                     1 if ud.get("gmres") else 0)
+        it = C.c_int32()
+        sc = self._ppf_scratch
+        L.call(f"ppf_phase_implicit_step_{_F[self._ppf_dtype]}", C.byref(p),
+               C.byref(self._ppf_grid.grid), ptr(src[0]), ptr(dst[0]), ptr(self._ppf_tmp),
+               ptr(sc), sc.numel(), C.byref(it), sp)
+        self._ppf_iterations = it.value
+
+    def _ppf_phase_bc(self):
+        if self._ppf_phase_solver is not None and self._boundary_conditions_type is None:
+            self._boundary_conditions_type = "PERIODIC"
 
 
 def _stencil_candidates(sim) -> list:
@@ -145,11 +204,14 @@ class _DiffusionMixin(GB300Engine):
                C.byref(self._ppf_tiling(depth)), sp)
 
 
-class _CahnAllenMixin(GB300Engine):
+class _CahnAllenMixin(_ImplicitPhase, GB300Engine):
     """phi += dt*M*(eps^2 lap(phi) - 16 W g'(phi))
-    (engine_CahnAllenExplicit, Engines/CahnAllen.py:128-135)."""
+    (engine_CahnAllenExplicit, Engines/CahnAllen.py:128-135), or the
+    implicit, Crank-Nicolson and IMEX engines (:137-267) by user_data
+    "solver" / "adi" / "gmres"."""
 
     NFIELDS = 1
+    PHASE_MODEL = L.PPF_MODEL_ALLEN_CAHN
 
     def __init__(self, **kwargs):
         super().__init__(**kwargs)
@@ -165,15 +227,22 @@ class _CahnAllenMixin(GB300Engine):
         self.add_field(0.001 * rng.random(self.dimensions) + 0.4995, "phi")
 
     def _ppf_prepare(self):
-        _explicit_only(self.user_data, "CahnAllen")
         if self.dt is None or self.dx is None:
             raise ValueError("CahnAllen needs dx and dt")
+        self._ppf_phase_prepare()
+
+    def _ppf_setup(self):
+        self._ppf_phase_bc()
+        super()._ppf_setup()
+        self._ppf_phase_setup()
 
     def _ppf_max_depth(self):
+        if self._ppf_phase_solver is not None:
+            return 1
         return 8 if len(self._ppf_grid.kshape) == 2 else 1
 
     def _ppf_tune_candidates(self):
-        return _stencil_candidates(self)
+        return [] if self._ppf_phase_solver is not None else _stencil_candidates(self)
 
     def _ppf_params(self):
         ud = self.user_data
@@ -181,6 +250,8 @@ class _CahnAllenMixin(GB300Engine):
                                     float(ud["epsilon"]), float(ud["W"]))
 
     def _ppf_step(self, src, dst, depth, step, step_base, sp):
+        if self._ppf_phase_solver is not None:
+            return self._ppf_phase_step(src, dst, sp)
         p = self._ppf_params()
         L.call(f"ppf_allen_cahn_step_{_F[self._ppf_dtype]}", C.byref(p),
                C.byref(self._ppf_grid.grid), C.byref(self._ppf_bc), ptr(src[0]), ptr(dst[0]),
@@ -190,7 +261,7 @@ class _CahnAllenMixin(GB300Engine):
 CH_QUANTUM_F32 = 2.0 ** -24
 
 
-class _CahnHilliardMixin(GB300Engine):
+class _CahnHilliardMixin(_ImplicitPhase, GB300Engine):
     """mu = -eps^2 lap(c) + 4c^3 - 6c^2 + 2c; c += dt*M*lap(mu)
     (engine_CahnHilliardExplicit, Engines/CahnHilliard.py:134-146, with dt;
     dt=None keeps the reference's dt-free update, i.e. dt = 1).
@@ -199,9 +270,14 @@ class _CahnHilliardMixin(GB300Engine):
     every face flux is rounded to a multiple of 2^-24 and the initial field
     is rounded to that grid on upload, so the float field's sum is conserved
     exactly. With track_mass (default) the FP64 total mass sum(c) of every
-    step is kept in ``mass_history`` (fused into the step kernel)."""
+    step is kept in ``mass_history`` (fused into the step kernel).
+
+    user_data "solver" = "implicit" / "crank-nicolson" / "imex" selects the
+    reference's other engines (Engines/CahnHilliard.py:148-341); those store
+    c itself and track no mass."""
 
     NFIELDS = 1
+    PHASE_MODEL = L.PPF_MODEL_CAHN_HILLIARD
 
     def __init__(self, **kwargs):
         super().__init__(**kwargs)
@@ -222,26 +298,33 @@ class _CahnHilliardMixin(GB300Engine):
         return 0.0
 
     def _ppf_prepare(self):
-        _explicit_only(self.user_data, "CahnHilliard")
         if self.dx is None:
             raise ValueError("CahnHilliard needs dx")
+        self._ppf_phase_prepare()
         self._ch_k = 0
         self._ch_mass_parts = []
 
     def _ppf_setup(self):
+        self._ppf_phase_bc()
         super()._ppf_setup()
+        self._ppf_phase_setup()
         chunk = max(2, int(self.user_data.get("graph_chunk", 64)))
         self._ch_mass = torch.zeros(max(chunk, 1024), dtype=torch.float64,
                                     device=self._ppf_grid.device)
         self._ch_status = torch.zeros(1, dtype=torch.int32, device=self._ppf_grid.device)
 
     def _ppf_encode(self, j, x):
+        if self._ppf_phase_solver is not None:
+            return x
         u = np.asarray(x, dtype=np.float64) - 0.5
         q = self._ppf_quantum()
         return np.rint(u / q) * q if q else u
 
     def _ppf_decode(self, j, x):
-        return x + 0.5
+        return x if self._ppf_phase_solver is not None else x + 0.5
+
+    def _ppf_max_depth(self):
+        return 1
 
     def _ppf_params(self):
         ud = self.user_data
@@ -252,20 +335,25 @@ class _CahnHilliardMixin(GB300Engine):
         p.reserved = 0
         return p
 
+    def _ppf_tracks_mass(self):
+        return self._ppf_phase_solver is None and self.user_data.get("track_mass", True)
+
     def _ppf_segment_begin(self, nsteps, stream):
         self._ch_k = 0
-        if self.user_data.get("track_mass", True):
+        if self._ppf_tracks_mass():
             if nsteps > self._ch_mass.numel():
                 self._ch_mass = torch.zeros(nsteps, dtype=torch.float64,
                                             device=self._ppf_grid.device)
             self._ch_mass[:nsteps].zero_()
 
     def _ppf_segment_end(self, nsteps, stream):
-        if self.user_data.get("track_mass", True):
+        if self._ppf_tracks_mass():
             with torch.cuda.stream(stream):
                 self._ch_mass_parts.append(self._ch_mass[:nsteps].clone())
 
     def _ppf_step(self, src, dst, depth, step, step_base, sp):
+        if self._ppf_phase_solver is not None:
+            return self._ppf_phase_step(src, dst, sp)
         p = self._ppf_params()
         mass = None
         if self.user_data.get("track_mass", True):

@@ -225,3 +225,153 @@ def test_engine_solver_keys(cuda, solver, adi, shape):
     ref = I.run(c0, 10, solver, 0.5, 2.0, 1.0, adi)
     assert rel_l2(sim.fields[0].get_cells(), ref) < F64_TOL
     assert sim.time_step_counter == 10
+
+
+# ---------------------------------------------------------------------------
+# Allen-Cahn / Cahn-Hilliard implicit engines (CahnAllen.py:137-267,
+# CahnHilliard.py:148-341)
+
+PHASE = golden_names("phase_implicit_")
+_PSOLVER = {"implicit": 1, "crank-nicolson": 2, "imex": 3}
+
+
+def run_phase_gpu(model, c0, steps, solver, M, W, eps, dt, dx, adi, gmres, precision="fp64"):
+    import torch
+    from pyphasefield_gb300 import _lib as L
+    c0 = np.asarray(c0, dtype=np.float64)
+    g, _, kshape, pitch = make_structs(c0.shape, "PERIODIC")
+    dtype = torch.float64 if precision == "fp64" else torch.float32
+    nbytes = C.c_size_t()
+    L.call("ppf_phase_implicit_scratch_bytes", C.byref(g), 8 if precision == "fp64" else 4,
+           C.byref(nbytes))
+    scratch = torch.empty(max(16, nbytes.value), dtype=torch.uint8, device="cuda")
+    a = to_dev(c0, kshape, pitch, dtype, "cuda")
+    o, tmp = torch.zeros_like(a), torch.zeros_like(a)
+    p = L.PpfImplicitPhaseParams(dx, dt, M, W, eps, 0.0,
+                                 L.PPF_MODEL_ALLEN_CAHN if model == "allen_cahn"
+                                 else L.PPF_MODEL_CAHN_HILLIARD, _PSOLVER[solver],
+                                 1 if adi else 0, 1 if gmres else 0)
+    it = C.c_int32()
+    sfx = "f64" if precision == "fp64" else "f32"
+    s = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    for _ in range(steps):
+        L.call(f"ppf_phase_implicit_step_{sfx}", C.byref(p), C.byref(g),
+               C.c_void_p(a.data_ptr()), C.c_void_p(o.data_ptr()), C.c_void_p(tmp.data_ptr()),
+               C.c_void_p(scratch.data_ptr()), scratch.numel(), C.byref(it), s)
+        a, o = o, a
+    torch.cuda.synchronize()
+    return from_dev(a, kshape, c0.shape)
+
+
+def test_phase_fixture_count():
+    assert len(PHASE) == 10
+
+
+@pytest.mark.parametrize("name", PHASE)
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_phase_reference_fixtures(cuda, name, precision):
+    d = load_golden(name)
+    m = d["meta"]
+    p = m["params"]
+    args = (m["model"], d["c0"], m["steps"], m["solver"], p["M"], p["W"], p["epsilon"], m["dt"],
+            m["dx"], m["adi"], m["gmres"])
+    out = run_phase_gpu(*args, precision=precision)
+    exact = I.run_phase(*args)
+    tol = F64_TOL if precision == "fp64" else F32_TOL
+    assert rel_l2(out, exact) < tol
+    assert rel_l2(out, d["out"]) < (1e-3 if m["gmres"] else max(tol, 1e-12))
+
+
+def _var_line(shape, axis, alpha, shared, expl, precision, seed=0):
+    import torch
+    from pyphasefield_gb300 import _lib as L
+    rng = np.random.default_rng(seed)
+    c0 = rng.random(shape)
+    g, kshape, pitch, dtype, _ = _setup(shape, precision)
+    nbytes = C.c_size_t()
+    L.call("ppf_phase_implicit_scratch_bytes", C.byref(g), 8 if precision == "fp64" else 4,
+           C.byref(nbytes))
+    scratch = torch.empty(max(16, nbytes.value), dtype=torch.uint8, device="cuda")
+    a = to_dev(c0, kshape, pitch, dtype, "cuda")
+    o = torch.zeros_like(a)
+    n = shape[axis]
+    dbase, dcoef = 1 + 2 * alpha, 0.3
+    dv = None
+    dvec = None
+    if shared:
+        dv = 1 + 2 * alpha + 0.5 * rng.random(n)
+        dvec = torch.tensor(dv, dtype=dtype, device="cuda")
+    sfx = "f64" if precision == "fp64" else "f32"
+    kax = axis + (len(kshape) - len(shape))
+    L.call(f"ppf_var_line_solve_{sfx}", C.byref(g), kax, alpha, dbase, dcoef,
+           C.c_void_p(dvec.data_ptr()) if shared else None, 1 if expl else 0, 0.6 * alpha,
+           C.c_void_p(a.data_ptr()), C.c_void_p(o.data_ptr()), C.c_void_p(scratch.data_ptr()),
+           scratch.numel(), C.c_void_p(torch.cuda.current_stream().cuda_stream))
+    torch.cuda.synchronize()
+    rhs = I.explicit_half(c0, 0.6 * alpha, axis) if expl else c0
+    diag = dv if shared else dbase + dcoef * I.well_slope(rhs)
+    return from_dev(o, kshape, shape), I.var_line_solve(rhs, diag, alpha, axis)
+
+
+@pytest.mark.parametrize("shape,axis", [((3,), 0), ((33,), 0), ((34,), 0), ((1000,), 0),
+                                        ((65, 20), 0), ((20, 65), 1), ((64, 9), 0),
+                                        ((7, 40, 97), 0), ((7, 40, 97), 1), ((7, 40, 97), 2)])
+@pytest.mark.parametrize("alpha", [0.05, 3.0, 400.0])
+@pytest.mark.parametrize("variant", ["cell", "shared", "expl"])
+def test_var_line_solve(cuda, shape, axis, alpha, variant):
+    for precision in ("fp64", "fp32"):
+        got, ref = _var_line(shape, axis, alpha, variant == "shared", variant == "expl",
+                             precision, seed=len(shape) + axis)
+        # float: the system's condition number grows like alpha (its smallest
+        # eigenvalue stays near 1, its largest is about 1 + 4 alpha)
+        tol = F64_TOL if precision == "fp64" else 2e-6 * max(1.0, alpha / 20)
+        assert rel_l2(got, ref) < tol, precision
+
+
+def test_full_allen_cahn_system_outside_the_bound_rejected(cuda):
+    """16 W M dt >= 4: the Chebyshev bound of the full 2-D solve does not
+    hold; the library refuses instead of returning an unconverged field."""
+    from pyphasefield_gb300 import _lib as L
+    with pytest.raises(L.PpfError, match="diagonally dominant"):
+        run_phase_gpu("allen_cahn", np.full((8, 8), 0.5), 1, "implicit", 0.7, 1.3, 1.1, 0.3, 1.2,
+                      False, True)
+
+
+def test_cahn_hilliard_1d_pentadiagonal_large(cuda):
+    rng = np.random.default_rng(12)
+    c0 = 0.5 + 0.3 * (rng.random(2000) - 0.5)
+    args = ("cahn_hilliard", c0, 2, "implicit", 1.0, 1.0, 1.0, 0.5, 1.0, False, False)
+    exact = I.run_phase(*args)
+    assert rel_l2(run_phase_gpu(*args, precision="fp64"), exact) < F64_TOL
+    assert rel_l2(run_phase_gpu(*args, precision="fp32"), exact) < F32_TOL
+
+
+@pytest.mark.parametrize("cls,solver,adi,gmres,shape", [
+    ("CahnAllenGB300", "implicit", True, False, (40, 36)),
+    ("CahnAllenGB300", "implicit", False, True, (24, 20)),
+    ("CahnAllenGB300", "crank-nicolson", True, False, (30, 34)),
+    ("CahnAllenGB300", "implicit", True, False, (10, 12, 14)),
+    ("CahnAllenGB300", "imex", False, False, (90,)),
+    ("CahnHilliardGB300", "crank-nicolson", False, False, (80,))])
+def test_phase_engine_solver_keys(cuda, cls, solver, adi, gmres, shape):
+    """The Allen-Cahn / Cahn-Hilliard engines with solver / adi / gmres keys,
+    through captured graphs, equal the oracle."""
+    import pyphasefield_gb300 as P
+    rng = np.random.default_rng(4)
+    c0 = 0.5 + 0.4 * (rng.random(shape) - 0.5)
+    ud = {"M": 0.7, "W": 1.3, "epsilon": 1.1, "solver": solver, "adi": adi, "gmres": gmres,
+          "precision": "fp64", "graph_chunk": 4}
+    # the full 2-D solve needs 16 W M dt < 4; the IMEX engine's -2 phi term
+    # (as the reference writes it) makes larger steps run away
+    dt = 0.005 if solver == "imex" else (0.1 if gmres and not adi else 0.3)
+    sim = getattr(P, cls)(dimensions=list(shape), dx=1.2, dt=dt, user_data=ud)
+    sim.initialize_fields_and_imported_data()
+    sim.fields[0].data[sim.fields[0]._slice] = c0
+    sim.simulate(9)
+    sim.retrieve_fields_from_GPU()
+    model = "allen_cahn" if cls == "CahnAllenGB300" else "cahn_hilliard"
+    ref = I.run_phase(model, c0, 9, solver, 0.7, 1.3, 1.1, dt, 1.2, adi, gmres)
+    assert np.isfinite(ref).all()
+    # nine steps of a stiff nonlinear map (16 W M dt = 4.4) amplify the
+    # rounding-order differences of each solve (1e-15) to about 1e-10
+    assert rel_l2(sim.fields[0].get_cells(), ref) < 1e-9
