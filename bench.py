@@ -617,6 +617,8 @@ def profile_case(name: str):
     diff16384   Diffusion 2-D 16384^2 periodic, 5 steps (2 GiB of fields: beyond L2)
     adi4096     implicit ADI Diffusion 2-D 4096^2 (Crank-Nicolson with PPF_CN=1), D dt = 5,
                 3 steps: line solves along x and y
+    acadi4096   semi-implicit ADI Allen-Cahn 2-D 4096^2, dt = 1, 3 steps: variable-diagonal
+                line solves along x and y
     """
     import torch
     from pyphasefield_gb300 import CahnHilliardGB300, DiffusionGB300
@@ -653,6 +655,14 @@ def profile_case(name: str):
                              boundary_conditions="PERIODIC",
                              user_data={"D": 1.0, "use_graph": False, "solver": solver,
                                         "adi": True})
+        sim.initialize_fields_and_imported_data()
+        sim.fields[0].data[1:-1, 1:-1] = rng.random((4096, 4096))
+        sim.simulate(3)
+    elif name == "acadi4096":
+        from pyphasefield_gb300 import CahnAllenGB300
+        sim = CahnAllenGB300(dimensions=[4096, 4096], dx=1.0, dt=1.0,
+                             boundary_conditions="PERIODIC",
+                             user_data={"use_graph": False, "solver": "implicit", "adi": True})
         sim.initialize_fields_and_imported_data()
         sim.fields[0].data[1:-1, 1:-1] = rng.random((4096, 4096))
         sim.simulate(3)

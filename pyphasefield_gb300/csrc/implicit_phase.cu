@@ -91,6 +91,56 @@ __device__ __forceinline__ T rhs_val(const T* __restrict__ row, const PLines& L,
   return k.w0 * c + k.w1 * (__ldg(row + (int64_t)im * L.stride) + __ldg(row + (int64_t)ip * L.stride));
 }
 
+// Correctly rounded reciprocal (the pivots of the eliminations).
+__device__ __forceinline__ float rcp(float x) { return __frcp_rn(x); }
+__device__ __forceinline__ double rcp(double x) { return __drcp_rn(x); }
+
+// The segment's cells as 16-byte vectors (rows are 16-byte aligned, a
+// segment starts at a multiple of 32 cells); x lines without explicit part.
+template <typename T>
+__device__ __forceinline__ void load_seg_x(const T* __restrict__ row, int p, int cnt,
+                                           T (&b)[kPSeg - 1]) {
+  constexpr int V = 16 / sizeof(T);
+#pragma unroll
+  for (int q = 0; q < (kPSeg - 1 + V - 1) / V; ++q) {
+    if (q * V < cnt) {
+      T v[V];
+      if constexpr (sizeof(T) == 4) {
+        const float4 t = __ldg(reinterpret_cast<const float4*>(row + p) + q);
+        v[0] = t.x, v[1] = t.y, v[2] = t.z, v[3] = t.w;
+      } else {
+        const double2 t = __ldg(reinterpret_cast<const double2*>(row + p) + q);
+        v[0] = t.x, v[1] = t.y;
+      }
+#pragma unroll
+      for (int e = 0; e < V; ++e)
+        if (q * V + e < kPSeg - 1) b[q * V + e] = v[e];
+    }
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ T diag_val(const PCoef<T>& k, int i, T b);
+
+// Right-hand side of the K interior cells of a segment starting at p: all
+// loads issued before any use (a full segment takes the unguarded path).
+template <typename T>
+__device__ __forceinline__ void load_interior(const T* __restrict__ row, const PLines& L,
+                                              const PCoef<T>& k, int p, int K,
+                                              T (&b)[kPSeg - 1]) {
+  if (K == kPSeg - 1) {
+    if (L.stride == 1 && !k.expl) {
+      load_seg_x(row, p, K, b);
+    } else {
+#pragma unroll
+      for (int j = 0; j < kPSeg - 1; ++j) b[j] = rhs_val(row, L, k, p + j);
+    }
+    return;
+  }
+#pragma unroll
+  for (int j = 0; j < kPSeg - 1; ++j) b[j] = j < K ? rhs_val(row, L, k, p + j) : T(0);
+}
+
 template <typename T>
 __device__ __forceinline__ T diag_val(const PCoef<T>& k, int i, T b) {
   if (k.dvec) return __ldg(k.dvec + i);
@@ -112,45 +162,55 @@ __global__ void __launch_bounds__(kPThreads)
   const int p = s * kPSeg;
   const int len = min(kPSeg, L.n - p);
   const int K = len - 1;
-  T b[kPSeg - 1], d[kPSeg - 1];
-#pragma unroll
-  for (int j = 0; j < kPSeg - 1; ++j) {
-    if (j < K) {
-      b[j] = rhs_val(row, L, k, p + j);
-      d[j] = diag_val(k, p + j, b[j]);
-    }
-  }
+  T b[kPSeg - 1];
+  load_interior(row, L, k, p, K, b);
   const T a = k.a;
   T uf = 0, ul = 0, vf = 0, vl = 1, wl = 0;  // K = 0: the neighbours are the separators
   if (K > 0) {
-    // forward elimination: pivots piv_j, u and v right-hand sides, product of -c'
+    // forward elimination (u, v, w right-hand sides; the last values) and
+    // backward elimination from the last interior cell (u, v; the first
+    // values), interleaved: two independent chains of pivots; the
+    // diagonal is recomputed from b where it is needed
     T cp = 0, yu = 0, yv = 0, yw = 0;
+    T cb = 0, zu = 0, zv = 0;
+    if (K == kPSeg - 1) {
 #pragma unroll
-    for (int j = 0; j < kPSeg - 1; ++j) {
-      if (j < K) {
-        const T piv = d[j] + a * cp;  // d_j - (-a) c'_{j-1}
-        const T inv = T(1) / piv;
+      for (int j = 0; j < kPSeg - 1; ++j) {
+        const int jb = kPSeg - 2 - j;  // the same step of the backward chain
+        const T inv = rcp(diag_val(k, p + j, b[j]) + a * cp);  // d_j - (-a) c'_{j-1}
+        const T invb = rcp(diag_val(k, p + jb, b[jb]) + a * cb);
         yu = (b[j] + a * yu) * inv;
         yv = ((j == 0 ? a : T(0)) + a * yv) * inv;
-        yw = ((j == K - 1 ? a : T(0)) + a * yw) * inv;
+        yw = ((j == kPSeg - 2 ? a : T(0)) + a * yw) * inv;
         cp = -a * inv;
+        zu = (b[jb] + a * zu) * invb;
+        zv = ((jb == 0 ? a : T(0)) + a * zv) * invb;
+        cb = -a * invb;
+      }
+    } else {  // the short last segment of a line
+#pragma unroll
+      for (int j = 0; j < kPSeg - 1; ++j) {
+        if (j < K) {
+          const T inv = rcp(diag_val(k, p + j, b[j]) + a * cp);
+          yu = (b[j] + a * yu) * inv;
+          yv = ((j == 0 ? a : T(0)) + a * yv) * inv;
+          yw = ((j == K - 1 ? a : T(0)) + a * yw) * inv;
+          cp = -a * inv;
+        }
+      }
+#pragma unroll
+      for (int j = kPSeg - 2; j >= 0; --j) {
+        if (j < K) {
+          const T invb = rcp(diag_val(k, p + j, b[j]) + a * cb);
+          zu = (b[j] + a * zu) * invb;
+          zv = ((j == 0 ? a : T(0)) + a * zv) * invb;
+          cb = -a * invb;
+        }
       }
     }
     ul = yu;
     vl = yv;
     wl = yw;
-    // backward elimination from the last interior cell gives the first values
-    T cb = 0, zu = 0, zv = 0;
-#pragma unroll
-    for (int j = kPSeg - 2; j >= 0; --j) {
-      if (j < K) {
-        const T piv = d[j] + a * cb;
-        const T inv = T(1) / piv;
-        zu = (b[j] + a * zu) * inv;
-        zv = ((j == 0 ? a : T(0)) + a * zv) * inv;
-        cb = -a * inv;
-      }
-    }
     uf = zu;
     vf = zv;
   }
@@ -216,39 +276,71 @@ __global__ void __launch_bounds__(kPThreads)
   coef(m - 1, loL, diL, upL, rhL);
   const T gamma = -di0;
   // forward sweep of T y = rhs and T z = (gamma, 0, ..., 0, upL), with the
-  // modified first and last diagonals
+  // modified first and last diagonals; records are read kPre at a time so
+  // that their loads overlap (the sweep itself is sequential)
+  constexpr int kPre = 4;
   T cprev = 0, yprev = 0, zprev = 0;
-  for (int s = 0; s < m; ++s) {
-    T lo, di, up, rh;
-    if (s == 0) {
-      lo = lo0, di = di0 - gamma, up = up0, rh = rh0;
-    } else if (s == m - 1) {
-      lo = loL, di = diL - lo0 * upL / gamma, up = upL, rh = rhL;
-    } else {
-      coef(s, lo, di, up, rh);
+  for (int s0 = 0; s0 < m; s0 += kPre) {
+    T f0[kPre + 1], f2[kPre + 1], f3[kPre + 1], g1[kPre + 1], g4[kPre + 1], g5[kPre + 1],
+        g6[kPre + 1];
+#pragma unroll
+    for (int q = 0; q <= kPre; ++q) {
+      const int s = s0 + q;
+      if (s <= m) {
+        const T* r = R(s == m ? 0 : s);
+        f0[q] = r[0], f2[q] = r[2], f3[q] = r[3];
+        g1[q] = r[1], g4[q] = r[4], g5[q] = r[5], g6[q] = r[6];
+      }
     }
-    const T zr = s == 0 ? gamma : (s == m - 1 ? upL : T(0));
-    const T inv = T(1) / (di - lo * cprev);
-    const T c = up * inv;
-    const T y = (rh - lo * yprev) * inv;
-    const T z = (zr - lo * zprev) * inv;
-    T* r = R(s);
-    r[5] = c;  // slot 5 (d_q) and 6 (b_q) are no longer needed by rows > s
-    r[6] = y;
-    r[7] = z;
-    cprev = c, yprev = y, zprev = z;
+#pragma unroll
+    for (int q = 0; q < kPre; ++q) {
+      const int s = s0 + q;
+      if (s < m) {
+        T lo = -a * f3[q];
+        T up = -a * f3[q + 1];
+        T di = g5[q] - a * g4[q] - a * f2[q + 1];
+        const T rh = g6[q] + a * (g1[q] + f0[q + 1]);
+        if (s == 0) di = di - gamma;
+        if (s == m - 1) di = di - lo0 * upL / gamma;
+        const T zr = s == 0 ? gamma : (s == m - 1 ? upL : T(0));
+        const T inv = rcp(di - lo * cprev);
+        const T c = up * inv;
+        const T y = (rh - lo * yprev) * inv;
+        const T z = (zr - lo * zprev) * inv;
+        T* r = R(s);
+        r[5] = c;  // slots 5 (d_q) and 6 (b_q) are no longer needed
+        r[6] = y;
+        r[7] = z;
+        cprev = c, yprev = y, zprev = z;
+      }
+    }
   }
   // back substitution of both systems
   T ynext = 0, znext = 0, y0 = 0, z0 = 0, yL = 0, zL = 0;
-  for (int s = m - 1; s >= 0; --s) {
-    T* r = R(s);
-    const T y = r[6] - r[5] * ynext;
-    const T z = r[7] - r[5] * znext;
-    r[6] = y;
-    r[7] = z;
-    if (s == m - 1) yL = y, zL = z;
-    if (s == 0) y0 = y, z0 = z;
-    ynext = y, znext = z;
+  for (int s1 = m - 1; s1 >= 0; s1 -= kPre) {
+    T c5[kPre], c6[kPre], c7[kPre];
+#pragma unroll
+    for (int q = 0; q < kPre; ++q) {
+      const int s = s1 - q;
+      if (s >= 0) {
+        const T* r = R(s);
+        c5[q] = r[5], c6[q] = r[6], c7[q] = r[7];
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < kPre; ++q) {
+      const int s = s1 - q;
+      if (s >= 0) {
+        const T y = c6[q] - c5[q] * ynext;
+        const T z = c7[q] - c5[q] * znext;
+        T* r = R(s);
+        r[6] = y;
+        r[7] = z;
+        if (s == m - 1) yL = y, zL = z;
+        if (s == 0) y0 = y, z0 = z;
+        ynext = y, znext = z;
+      }
+    }
   }
   const T fac = (y0 + lo0 * yL / gamma) / (T(1) + z0 + lo0 * zL / gamma);
   for (int s = 0; s < m; ++s) {
@@ -275,13 +367,7 @@ __global__ void __launch_bounds__(kPThreads)
   const int sl = s == 0 ? L.nseg - 1 : s - 1;
   const T sep_l = rec[((int64_t)sl * L.nlines + line) * kRec + 7];
   T b[kPSeg - 1], d[kPSeg - 1];
-#pragma unroll 31
-  for (int j = 0; j < kPSeg - 1; ++j) {
-    if (j < K) {
-      b[j] = rhs_val(row, L, k, p + j);
-      d[j] = diag_val(k, p + j, b[j]);
-    }
-  }
+  load_interior(row, L, k, p, K, b);
   const T a = k.a;
   // forward elimination, pivots and right-hand sides kept in d and b
   T cp = 0, y = 0;
@@ -289,7 +375,7 @@ __global__ void __launch_bounds__(kPThreads)
   for (int j = 0; j < kPSeg - 1; ++j) {
     if (j < K) {
       const T rj = b[j] + (j == 0 ? a * sep_l : T(0)) + (j == K - 1 ? a * sep_r : T(0));
-      const T inv = T(1) / (d[j] + a * cp);
+      const T inv = rcp(diag_val(k, p + j, b[j]) + a * cp);
       y = (rj + a * y) * inv;
       cp = -a * inv;
       d[j] = cp;
@@ -368,8 +454,9 @@ int32_t var_sweep(const Geo& g, int axis, double a, double dbase, double dc, con
   const int64_t threads = (int64_t)L.nlines * L.nseg;
   const dim3 grid((unsigned)((threads + kPThreads - 1) / kPThreads));
   PPF_TRY_CUDA(launch(part_sums<T>, grid, dim3(kPThreads), 0, st, true, L, k, in, rec));
-  PPF_TRY_CUDA(launch(part_reduce<T>, dim3((L.nlines + kPThreads - 1) / kPThreads),
-                      dim3(kPThreads), 0, st, true, L, (T)a, rec));
+  // one warp per block: the lines' sequential sweeps spread over every SM
+  PPF_TRY_CUDA(launch(part_reduce<T>, dim3((L.nlines + 31) / 32), dim3(32), 0, st, true, L,
+                      (T)a, rec));
   PPF_TRY_CUDA(launch(part_solve<T>, grid, dim3(kPThreads), 0, st, true, L, k, in,
                       (const T*)rec, out));
   return PPF_OK;
