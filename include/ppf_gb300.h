@@ -321,6 +321,38 @@ int32_t ppf_var_line_solve_f64(const PpfGrid* g, int32_t axis, double alpha, dou
                                double expl_alpha, const double* in, double* out, void* scratch,
                                size_t scratch_bytes, void* stream);
 
+/* ---- NCGPU (multi-component solidification with orientation) ----------- */
+
+/* One step of the NCGPU engine (Engines/NCGPU.py:37-303, simulation_loop
+ * :499-532), binary systems, 2-D: fields phi, q1, q4 and c (the first
+ * component's fraction; the second is 1 - c). Parameters as
+ * NCGPU.init_tdb_params derives them (:336-373): ebar2 = 6 sqrt(2) S[1] d /
+ * T_M[1], W and M per component (components sorted). gibbs[phase][comp]
+ * holds up to 4 temperature ranges of the pure element's Gibbs energy in
+ * J/mol, {T_lo, T_hi, c_1, c_T, c_TlnT, c_T^2, c_T^3, c_T^7, c_1/T, c_T^-9}
+ * (phase 0 = the solid, the first phase name in sorted order; 1 = liquid);
+ * the molar Gibbs energy adds R T (x ln x + (1-x) ln(1-x)), R = 8.3145.
+ * noise_scale multiplies the Langevin term of dF/dc (1 = the reference);
+ * its N(0,1) numbers come from Philox4x32-10 keyed by (seed, step
+ * (+ *step_base), cell). temperature: a field of the grid's layout.
+ * transfer: device scratch of 3 fields of the grid's layout. Boundaries:
+ * periodic or zero-gradient Neumann. */
+typedef struct PpfNcgpuParams {
+  double dx, dt, v_m, D_L, D_S, M_qmax, H, y_e, beta, ebar2, noise_scale;
+  double W[2], M[2];
+  double gibbs[2][2][4][10];
+  int32_t npieces[2][2];
+} PpfNcgpuParams;
+
+int32_t ppf_ncgpu_step_f32(const PpfNcgpuParams* p, const PpfGrid* g, const PpfBoundary* bc,
+                           const float* const* fields_in, float* const* fields_out,
+                           const float* temperature, float* transfer, uint64_t seed,
+                           uint64_t step, const uint64_t* step_base, void* stream);
+int32_t ppf_ncgpu_step_f64(const PpfNcgpuParams* p, const PpfGrid* g, const PpfBoundary* bc,
+                           const double* const* fields_in, double* const* fields_out,
+                           const double* temperature, double* transfer, uint64_t seed,
+                           uint64_t step, const uint64_t* step_base, void* stream);
+
 /* ---- batched ensemble ------------------------------------------------- */
 
 #define PPF_MODEL_WARREN1995 1

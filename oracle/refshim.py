@@ -255,3 +255,99 @@ def run_implicit(function: str, c0, steps: int, D: float, dt: float, dx: float,
     finally:
         mod.gmres = saved
     return np.array(sim.fields[0].data, dtype=np.float64).reshape(np.shape(c0))
+
+
+# ---------------------------------------------------------------------------
+# NCGPU (Engines/NCGPU.py): its kernels are numba CUDA kernels written as
+# grid-stride loops, so with a stand-in numba module (cuda.jit = the plain
+# function, cuda.grid = 0, cuda.gridsize = 1) each runs as one Python loop
+# over the whole grid: the reference's own arithmetic, serially.
+
+def _install_numba_standin(normal_source):
+    import types as _t
+
+    def jit(*a, **k):
+        if a and callable(a[0]):
+            return a[0]
+        return lambda f: f
+
+    numba = _t.ModuleType("numba")
+    cuda = _t.ModuleType("numba.cuda")
+    rnd = _t.ModuleType("numba.cuda.random")
+    numba.jit = jit
+    cuda.jit = jit
+    cuda.grid = lambda n: (0, 0) if n == 2 else 0
+    cuda.gridsize = lambda n: (1, 1) if n == 2 else 1
+    cuda.synchronize = lambda: None
+    rnd.create_xoroshiro128p_states = lambda n, seed=0: None
+    rnd.xoroshiro128p_uniform_float32 = lambda states, tid: 0.5
+    rnd.xoroshiro128p_normal_float32 = lambda states, tid: normal_source()
+    cuda.random = rnd
+    numba.cuda = cuda
+    sys.modules["numba"] = numba
+    sys.modules["numba.cuda"] = cuda
+    sys.modules["numba.cuda.random"] = rnd
+
+
+_NC = {"queue": None}
+
+
+def ncgpu_module():
+    """Import Engines/NCGPU.py with the numba stand-in (test use only)."""
+    mod = sys.modules.get("pyphasefield.Engines.NCGPU")
+    if mod is not None and getattr(mod, "_ppf_standin", False):
+        return mod
+
+    def normal():
+        q = _NC["queue"]
+        return next(q) if q is not None else 0.0
+
+    saved = {k: sys.modules.get(k) for k in ("numba", "numba.cuda", "numba.cuda.random")}
+    modules()
+    _install_numba_standin(normal)
+    try:
+        import importlib
+        sys.modules.pop("pyphasefield.Engines.NCGPU", None)
+        mod = importlib.import_module("pyphasefield.Engines.NCGPU")
+        mod._ppf_standin = True
+    finally:
+        for k, v in saved.items():
+            if v is None:
+                sys.modules.pop(k, None)
+            else:
+                sys.modules[k] = v
+    return mod
+
+
+def run_ncgpu(phi, q1, q4, c, T, steps: int, p: dict, tdb, noise_fields, bc="PERIODIC"):
+    """Drive NComponent_helper_kernel and NComponent_kernel (binary system)
+    for `steps` steps. noise_fields[s] is the interior N(0,1) field of step
+    s; ghost cells take the noise of the cell the boundary rule maps them
+    to. Ghost cells of every field and of T follow `bc` (PERIODIC or
+    zero-gradient NEUMANN), as ppf_gpu_utils.apply_boundary_conditions fills
+    them between steps."""
+    mod = ncgpu_module()
+    mode = "wrap" if bc == "PERIODIC" else "symmetric"
+    pad = lambda a: np.pad(np.asarray(a, dtype=np.float64), 1, mode=mode)  # noqa: E731
+    ph, a1, a4, cc = (np.array(a, dtype=np.float64) for a in (phi, q1, q4, c))
+    ny, nx = ph.shape
+    Tp = pad(T)
+    params = np.array([p["dx"], p["d"], p["v_m"], p["M_qmax"], p["H"], p["y_e"], p["beta"],
+                       p["D_L"], p["D_S"], p["dt"]])
+    c_params = np.array([p["L"], p["T_M"], p["S"], p["B"], p["W"], p["M"]])
+    phases = tdb.phases
+    mod.ufunc_g_l = lambda arr: tdb.gibbs(phases[1], [arr[0], arr[1]], arr[2])
+    mod.ufunc_g_s = lambda arr: tdb.gibbs(phases[0], [arr[0], arr[1]], arr[2])
+    for s in range(steps):
+        fields = np.stack([pad(ph), pad(a1), pad(a4), pad(cc)])
+        out = np.zeros_like(fields)
+        transfer = np.zeros((4,) + fields.shape[1:])
+        ufunc_array = np.zeros(fields.shape[1:] + (3,))
+        nz = pad(noise_fields[s])
+        _NC["queue"] = iter(nz.ravel().tolist())
+        mod.NComponent_helper_kernel(fields, Tp, transfer, None, ufunc_array, params, c_params)
+        _NC["queue"] = iter([0.0] * (ny * nx))
+        mod.NComponent_kernel(fields, Tp, transfer, out, None, params, c_params)
+        ph, a1, a4, cc = (out[k, 1:-1, 1:-1].copy() for k in range(4))
+    _NC["queue"] = None
+    return ph, a1, a4, cc

@@ -91,6 +91,13 @@ class PpfImplicitDiffusionParams(C.Structure):
         ("solver", C.c_int32), ("adi", C.c_int32)]
 
 
+class PpfNcgpuParams(C.Structure):
+    _fields_ = [(n, C.c_double) for n in ("dx", "dt", "v_m", "D_L", "D_S", "M_qmax", "H",
+                                          "y_e", "beta", "ebar2", "noise_scale")] + [
+        ("W", C.c_double * 2), ("M", C.c_double * 2),
+        ("gibbs", (((C.c_double * 10) * 4) * 2) * 2), ("npieces", (C.c_int32 * 2) * 2)]
+
+
 PPF_MODEL_WARREN1995 = 1
 PPF_MODEL_ALLEN_CAHN = 2
 
@@ -137,6 +144,8 @@ SIGNATURES: dict[str, list] = {
                                         SZ, C.POINTER(I32), P],
     "ppf_diffusion_implicit_step_f64": [C.POINTER(PpfImplicitDiffusionParams), PG, P, P, P, P,
                                         SZ, C.POINTER(I32), P],
+    "ppf_ncgpu_step_f32": [C.POINTER(PpfNcgpuParams), PG, PB, P, P, P, P, U64, U64, P, P],
+    "ppf_ncgpu_step_f64": [C.POINTER(PpfNcgpuParams), PG, PB, P, P, P, P, U64, U64, P, P],
     "ppf_phase_implicit_scratch_bytes": [PG, I32, C.POINTER(SZ)],
     "ppf_phase_implicit_step_f32": [C.POINTER(PpfImplicitPhaseParams), PG, P, P, P, P, SZ,
                                     C.POINTER(I32), P],

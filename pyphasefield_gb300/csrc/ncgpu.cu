@@ -1,0 +1,338 @@
+// NCGPU: the multi-component solidification engine with quaternion
+// orientation fields (pyphasefield Engines/NCGPU.py), binary systems.
+//
+//   ncgpu_thermo_kernel  (NComponent_helper_kernel, :248-303): per cell the
+//       molar Gibbs energies of the solid (first phase, sorted) and liquid,
+//       from the pure-element energies of the TDB (piecewise in T, basis
+//       1, T, T ln T, T^2, T^3, T^7, 1/T, T^-9) plus R T sum x ln x, in
+//       double; dG/dc by the reference's forward difference (step 1e-7);
+//       stores G_S - G_L, the mobility M_c and dF/dc (with the Langevin
+//       noise) for the update.
+//   ncgpu_kernel (NComponent_kernel, :37-242): phi (anisotropic through the
+//       quaternion-rotated gradient psi), q1 and q4 (orientation diffusion
+//       normalised to unit length), c (div M_c grad dF/dc minus the
+//       c-weighted term), phi clamped to [1e-6, 1 - 1e-6].
+// Ghost cells follow the boundary rule while the tiles are read (periodic
+// or zero-gradient), for the fields, the temperature and the per-cell
+// thermodynamic terms alike.
+#include <math.h>
+#include <string.h>
+
+#include "ppf_common.cuh"
+
+namespace ppf {
+namespace {
+
+template <typename T>
+struct NcCoef {
+  T idx, dt, v_m, D_L, D_S, M_qmax, H, y_e, beta, ebar2, eqbar2, noise;
+  T W0, W1, M0, M1;
+};
+
+struct NcGibbs {
+  double piece[2][2][4][10];  // [phase][component][piece] {lo, hi, 8 coefficients}
+  int npieces[2][2];
+};
+
+__device__ __forceinline__ double g_pure(const NcGibbs& g, int ph, int comp, double T,
+                                         double lnT) {
+  for (int k = 0; k < g.npieces[ph][comp]; ++k) {
+    const double* c = g.piece[ph][comp][k];
+    if (T >= c[0] && T < c[1]) {
+      const double T2 = T * T, T3 = T2 * T, T7 = T3 * T3 * T, iT = 1.0 / T;
+      const double iT3 = iT * iT * iT, iT9 = iT3 * iT3 * iT3;
+      return c[2] + c[3] * T + c[4] * T * lnT + c[5] * T2 + c[6] * T3 + c[7] * T7 +
+             c[8] * iT + c[9] * iT9;
+    }
+  }
+  return 0.0;  // outside every range, as a piecewise TDB function gives
+}
+
+// Molar Gibbs energy of phase ph at (x0, x1) (x1 = 1 - x0 passed apart, as
+// the reference's perturbed argument is), pycalphad's ideal solution.
+__device__ __forceinline__ double gibbs(const NcGibbs& g, int ph, double x0, double x1,
+                                        double T, double lnT, double G0, double G1) {
+  double mix = 0.0;
+  if (x0 > 0) mix += x0 * log(x0);
+  if (x1 > 0) mix += x1 * log(x1);
+  return x0 * G0 + x1 * G1 + 8.3145 * T * mix;
+}
+
+// N(0,1) of cell (row, col) at a step: Box-Muller on two uniforms from a
+// Philox4x32-10 block (counter (col / 2, row, step), key seed ^ 0x5eed0000),
+// pair col % 2.
+template <typename T>
+__device__ __forceinline__ T noise_normal(uint64_t seed, uint64_t step, int row, int col) {
+  const U4 w = philox4x32_10(U4{(uint32_t)(col >> 1), (uint32_t)row, (uint32_t)step,
+                                (uint32_t)(step >> 32)},
+                             (uint32_t)seed ^ 0x5EED0000u, (uint32_t)(seed >> 32));
+  const uint32_t a = (col & 1) ? w.z : w.x, b = (col & 1) ? w.w : w.y;
+  const double u1 = ((double)(a >> 8) + 0.5) * (1.0 / 16777216.0);
+  const double u2 = (double)(b >> 8) * (1.0 / 16777216.0);
+  return (T)(sqrt(-2.0 * log(u1)) * cospi(2.0 * u2));
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256)
+    ncgpu_thermo_kernel(Geo g, NcCoef<T> k, NcGibbs gb, const T* __restrict__ phi,
+                        const T* __restrict__ c, const T* __restrict__ temp, T* __restrict__ dG,
+                        T* __restrict__ Mc, T* __restrict__ dF, uint64_t seed, uint64_t step,
+                        const uint64_t* step_base) {
+  pdl_wait();
+  pdl_launch_next();
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y;
+  if (x >= g.n[1]) return;
+  const int64_t i = (int64_t)y * g.pitch + x;
+  const uint64_t st = step + (step_base ? *step_base : 0);
+  const double t = (double)temp[i];
+  const double lnT = log(t);
+  const double x0 = (double)c[i], x1 = 1.0 - x0;
+  double G[2][2];
+#pragma unroll
+  for (int ph = 0; ph < 2; ++ph)
+#pragma unroll
+    for (int cp = 0; cp < 2; ++cp) G[ph][cp] = g_pure(gb, ph, cp, t, lnT);
+  const double gs = gibbs(gb, 0, x0, x1, t, lnT, G[0][0], G[0][1]);
+  const double gl = gibbs(gb, 1, x0, x1, t, lnT, G[1][0], G[1][1]);
+  // the reference's forward difference (NCGPU.py:282-286)
+  const double xp1 = x1 - 0.0000001, xp0 = x0 + 0.0000001;
+  const double dgl = 10000000.0 * (gibbs(gb, 1, xp0, xp1, t, lnT, G[1][0], G[1][1]) - gl);
+  const double dgs = 10000000.0 * (gibbs(gb, 0, xp0, xp1, t, lnT, G[0][0], G[0][1]) - gs);
+  const T p = phi[i];
+  const T gg = p * p * (T(1) - p) * (T(1) - p);
+  const T h = p * p * p * (T(6) * p * p - T(15) * p + T(10));
+  const T tt = (T)t;
+  const T nz = k.noise > T(0)
+                   ? k.noise * sqrt(T(2) * T(8.314) * tt / k.v_m) * noise_normal<T>(seed, st, y, x)
+                   : T(0);
+  dG[i] = (T)(gs - gl);
+  Mc[i] = k.v_m * (T)x0 * (k.D_L + h * (k.D_S - k.D_L)) / (T(8.314) * tt);
+  dF[i] = (T)((dgl + (double)h * (dgs - dgl)) / (double)k.v_m) + (k.W0 - k.W1) * gg * tt + nz;
+}
+
+template <typename T>
+__device__ __forceinline__ T divagradb(T a, T axp, T axm, T ayp, T aym, T b, T bxp, T bxm,
+                                       T byp, T bym, T idx) {
+  return T(0.5) * idx * idx *
+         ((axp + a) * (bxp - b) - (a + axm) * (b - bxm) + (ayp + a) * (byp - b) -
+          (a + aym) * (b - bym));
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256)
+    ncgpu_kernel(Geo g, Bc<T> bc, NcCoef<T> k, const T* __restrict__ phi,
+                 const T* __restrict__ q1, const T* __restrict__ q4, const T* __restrict__ c,
+                 const T* __restrict__ temp, const T* __restrict__ dG, const T* __restrict__ Mc,
+                 const T* __restrict__ dF, T* __restrict__ phi_o, T* __restrict__ q1_o,
+                 T* __restrict__ q4_o, T* __restrict__ c_o) {
+  pdl_wait();
+  pdl_launch_next();
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y;
+  if (x >= g.n[1]) return;
+  const int64_t i = (int64_t)y * g.pitch + x;
+  auto F = [&](const T* f, int dy, int dx) { return fetch<T, 2>(f, g, bc, 0, y + dy, x + dx); };
+  const T idx = k.idx;
+  const T ph = phi[i];
+  const T gg = ph * ph * (T(1) - ph) * (T(1) - ph);
+  const T h = ph * ph * ph * (T(6) * ph * ph - T(15) * ph + T(10));
+  const T hprime = T(30) * gg;
+  const T gprime = T(4) * ph * ph * ph - T(6) * ph * ph + T(2) * ph;
+  const T pxp = F(phi, 0, 1), pxm = F(phi, 0, -1), pyp = F(phi, 1, 0), pym = F(phi, -1, 0);
+  const T dpx = T(0.5) * (pxp - pxm) * idx, dpy = T(0.5) * (pyp - pym) * idx;
+  const T dpx2 = dpx * dpx, dpy2 = dpy * dpy;
+  const T t = temp[i];
+  const T txp = F(temp, 0, 1), txm = F(temp, 0, -1), typ = F(temp, 1, 0), tym = F(temp, -1, 0);
+  const T dTx = T(0.5) * idx * (txp - txm), dTy = T(0.5) * idx * (typ - tym);
+  const T pxx = (pxp + pxm - T(2) * ph) * idx * idx;
+  const T pyy = (pyp + pym - T(2) * ph) * idx * idx;
+  const T lphi = pxx + pyy;
+  const T pxy = T(0.25) * (F(phi, 1, 1) - F(phi, 1, -1) - F(phi, -1, 1) + F(phi, -1, -1)) *
+                idx * idx;
+  T mg2 = dpx2 + dpy2;
+  if (mg2 < T(1e-6)) mg2 = T(1e-6);
+  const T a1 = q1[i], a4 = q4[i];
+  const T q1xp = F(q1, 0, 1), q1xm = F(q1, 0, -1), q1yp = F(q1, 1, 0), q1ym = F(q1, -1, 0);
+  const T q4xp = F(q4, 0, 1), q4xm = F(q4, 0, -1), q4yp = F(q4, 1, 0), q4ym = F(q4, -1, 0);
+  const T dq1x = T(0.5) * idx * (q1xp - q1xm), dq1y = T(0.5) * idx * (q1yp - q1ym);
+  const T dq4x = T(0.5) * idx * (q4xp - q4xm), dq4y = T(0.5) * idx * (q4yp - q4ym);
+  T gxp = idx * sqrt((q1xp - a1) * (q1xp - a1) + (q4xp - a4) * (q4xp - a4));
+  T gxm = idx * sqrt((q1xm - a1) * (q1xm - a1) + (q4xm - a4) * (q4xm - a4));
+  T gyp = idx * sqrt((q1yp - a1) * (q1yp - a1) + (q4yp - a4) * (q4yp - a4));
+  T gym = idx * sqrt((q1ym - a1) * (q1ym - a1) + (q4ym - a4) * (q4ym - a4));
+  const T mgq = T(0.5) * (gxp + gxm + gyp + gym);
+  gxp = gxp < k.beta ? k.beta : gxp;
+  gxm = gxm < k.beta ? k.beta : gxm;
+  gyp = gyp < k.beta ? k.beta : gyp;
+  gym = gym < k.beta ? k.beta : gym;
+  // psi: the phi gradient rotated by the orientation. The anisotropy terms
+  // divide powers of psi by powers of |grad phi|^2 (up to the 8th); they are
+  // evaluated here on the unit vectors u = grad phi / m, s = psi / m
+  // (m = |grad phi|, clamped as the reference clamps |grad phi|^2 to 1e-6):
+  // the same expressions, without the float overflow of |grad phi|^8 at
+  // centimetre cell sizes
+  const T q2q2 = a1 * a1 - a4 * a4, qq2 = T(2) * a1 * a4;
+  const T m = sqrt(mg2), im = T(1) / m;
+  const T ux = dpx * im, uy = dpy * im;
+  const T sx = (q2q2 * dpx - qq2 * dpy) * im, sy = (qq2 * dpx + q2q2 * dpy) * im;
+  const T sx2 = sx * sx, sy2 = sy * sy;
+  const T sx3 = sx2 * sx, sy3 = sy2 * sy;
+  const T s4 = sx2 * sx2 + sy2 * sy2;
+  const T dq2q2dx = T(2) * a1 * dq1x - T(2) * a4 * dq4x;
+  const T dqq2dx = T(2) * a4 * dq1x + T(2) * a1 * dq4x;
+  const T dq2q2dy = T(2) * a1 * dq1y - T(2) * a4 * dq4y;
+  const T dqq2dy = T(2) * a4 * dq1y + T(2) * a1 * dq4y;
+  const T dpsxdx = dq2q2dx * dpx + q2q2 * pxx - dqq2dx * dpy - qq2 * pxy;
+  const T dpsxdy = dq2q2dy * dpx + q2q2 * pxy - dqq2dy * dpy - qq2 * pyy;
+  const T dpsydx = dq2q2dx * dpy + q2q2 * pxy + dqq2dx * dpx + qq2 * pxx;
+  const T dpsydy = dq2q2dy * dpy + q2q2 * pyy + dqq2dy * dpx + qq2 * pxy;
+  const T ux2 = ux * ux, uy2 = uy * uy;
+  T tx = dTx * m * (T(2) * sx3 * q2q2 + T(2) * sy3 * qq2 - ux * s4);
+  tx += t * (T(6) * sx2 * dpsxdx * q2q2 + T(2) * sx3 * m * dq2q2dx + T(6) * sy2 * dpsydx * qq2 +
+             T(2) * sy3 * m * dqq2dx);
+  tx -= t * (T(2) * sx3 * q2q2 + T(2) * sy3 * qq2) * (T(2) * ux * pxx + T(2) * uy * pxy);
+  tx -= t * (pxx * s4 + ux * (T(4) * sx3 * dpsxdx + T(4) * sy3 * dpsydx));
+  tx += t * (ux * s4 * (T(4) * ux2 * ux * pxx + T(4) * ux * pxx * uy2 + T(4) * uy * pxy * ux2 +
+                        T(4) * uy2 * uy * pxy));
+  tx *= T(4) * k.y_e * k.ebar2;
+  T ty = dTy * m * (-T(2) * sx3 * qq2 + T(2) * sy3 * q2q2 - uy * s4);
+  ty += t * (-T(6) * sx2 * dpsxdy * qq2 - T(2) * sx3 * m * dqq2dy + T(6) * sy2 * dpsydy * q2q2 +
+             T(2) * sy3 * m * dq2q2dy);
+  ty -= t * (-T(2) * sx3 * qq2 + T(2) * sy3 * q2q2) * (T(2) * ux * pxy + T(2) * uy * pyy);
+  ty -= t * (pyy * s4 + uy * (T(4) * sx3 * dpsxdy + T(4) * sy3 * dpsydy));
+  ty += t * (uy * s4 * (T(4) * ux2 * ux * pxy + T(4) * ux * pxy * uy2 + T(4) * uy * pyy * ux2 +
+                        T(4) * uy2 * uy * pyy));
+  ty *= T(4) * k.y_e * k.ebar2;
+  const T ci = c[i];
+  const T cW = ci * k.W0 + (T(1) - ci) * k.W1;
+  const T M_phi = ci * k.M0 + (T(1) - ci) * k.M1;
+  const T M_q = k.M_qmax + (T(1e-6) - k.M_qmax) * h;
+  T dphidt = k.ebar2 * (T(1) - T(3) * k.y_e) * (t * lphi + dTx * dpx + dTy * dpy);
+  dphidt += tx + ty;
+  dphidt -= hprime * dG[i] / k.v_m;
+  dphidt -= gprime * t * cW;
+  dphidt -= T(4) * k.H * t * ph * mgq;
+  dphidt *= M_phi;
+  // c: div(M_c grad dF/dc) - div(M_c c grad dF/dc)
+  const T m0 = Mc[i], mxp = F(Mc, 0, 1), mxm = F(Mc, 0, -1), myp = F(Mc, 1, 0),
+          mym = F(Mc, -1, 0);
+  const T f0 = dF[i], fxp = F(dF, 0, 1), fxm = F(dF, 0, -1), fyp = F(dF, 1, 0),
+          fym = F(dF, -1, 0);
+  const T cxp = F(c, 0, 1), cxm = F(c, 0, -1), cyp = F(c, 1, 0), cym = F(c, -1, 0);
+  T dc = divagradb(m0, mxp, mxm, myp, mym, f0, fxp, fxm, fyp, fym, idx);
+  dc -= divagradb(m0 * ci, mxp * cxp, mxm * cxm, myp * cyp, mym * cym, f0, fxp, fxm, fyp, fym,
+                  idx);
+  // orientation
+  const T Dq = T(2) * k.H * t * ph * ph;
+  const T Dxp = T(2) * k.H * txp * pxp * pxp, Dxm = T(2) * k.H * txm * pxm * pxm;
+  const T Dyp = T(2) * k.H * typ * pyp * pyp, Dym = T(2) * k.H * tym * pym * pym;
+  auto fori = [&](T q, T qxp, T qxm, T qyp, T qym) {
+    return T(0.5) * idx * idx *
+           ((Dq + Dxp) * (qxp - q) / gxp - (Dq + Dxm) * (q - qxm) / gxm +
+            (Dq + Dyp) * (qyp - q) / gyp - (Dq + Dym) * (q - qym) / gym);
+  };
+  const T f1 = fori(a1, q1xp, q1xm, q1yp, q1ym);
+  const T f4 = fori(a4, q4xp, q4xm, q4yp, q4ym);
+  const T lq1 = (q1xp + q1xm + q1yp + q1ym - T(4) * a1) * idx * idx;
+  const T lq4 = (q4xp + q4xm + q4yp + q4ym - T(4) * a4) * idx * idx;
+  const T dq1 = M_q * ((T(1) - a1 * a1) * (f1 + lq1 * k.eqbar2) - a1 * a4 * (f4 + lq4 * k.eqbar2));
+  const T dq4 = M_q * ((T(1) - a4 * a4) * (f4 + lq4 * k.eqbar2) - a1 * a4 * (f1 + lq1 * k.eqbar2));
+  T pn = ph + k.dt * dphidt;
+  pn = pn < T(0.000001) ? T(0.000001) : pn;
+  pn = pn > T(0.999999) ? T(0.999999) : pn;
+  const T n1 = a1 + k.dt * dq1, n4 = a4 + k.dt * dq4;
+  const T rn = sqrt(n1 * n1 + n4 * n4);
+  phi_o[i] = pn;
+  q1_o[i] = n1 / rn;
+  q4_o[i] = n4 / rn;
+  c_o[i] = ci + k.dt * dc;
+}
+
+template <typename T>
+int32_t ncgpu_step(const PpfNcgpuParams* p, const PpfGrid* grid, const PpfBoundary* bcin,
+                   const T* const* in, T* const* out, const T* temp, T* transfer, uint64_t seed,
+                   uint64_t step, const uint64_t* step_base, void* stream) {
+  clear_error();
+  if (!p || !in || !out) return fail(PPF_ERR_INVALID, "NULL argument");
+  Geo g;
+  int32_t rc = make_geo(grid, 2, 2, &g);
+  if (rc) return rc;
+  for (int f = 0; f < 4; ++f)
+    if (!in[f] || !out[f]) return fail(PPF_ERR_INVALID, "NULL field pointer");
+  if (!temp || !transfer) return fail(PPF_ERR_INVALID, "NULL temperature or transfer buffer");
+  if (g.n[0] > 65535) return fail(PPF_ERR_INVALID, "more than 65535 rows");
+  Bc<T> bc;
+  if ((rc = make_bc<T>(bcin, g, p->dx, 1, 1, &bc))) return rc;
+  for (int a = 0; a < 2; ++a) {
+    if (bcin && bcin->type[a] == PPF_BC_DIRCHLET)
+      return fail(PPF_ERR_UNSUPPORTED,
+                  "NCGPU: periodic or zero-gradient boundaries only (the per-cell "
+                  "thermodynamic terms of ghost cells follow their fields)");
+    for (int s = 0; s < 2; ++s)
+      if (bcin && bcin->type[a] == PPF_BC_NEUMANN && bcin->value[0][a][s] != 0.0)
+        return fail(PPF_ERR_UNSUPPORTED, "NCGPU: Neumann boundaries with zero gradient only");
+  }
+  for (int ph = 0; ph < 2; ++ph)
+    for (int cp = 0; cp < 2; ++cp)
+      if (p->npieces[ph][cp] < 0 || p->npieces[ph][cp] > 4)
+        return fail(PPF_ERR_INVALID, "npieces must be 0..4");
+  NcCoef<T> k;
+  k.idx = (T)(1.0 / p->dx);
+  k.dt = (T)p->dt;
+  k.v_m = (T)p->v_m;
+  k.D_L = (T)p->D_L;
+  k.D_S = (T)p->D_S;
+  k.M_qmax = (T)p->M_qmax;
+  k.H = (T)p->H;
+  k.y_e = (T)p->y_e;
+  k.beta = (T)p->beta;
+  k.ebar2 = (T)p->ebar2;
+  k.eqbar2 = (T)(0.25 * p->ebar2);
+  k.noise = (T)p->noise_scale;
+  k.W0 = (T)p->W[0];
+  k.W1 = (T)p->W[1];
+  k.M0 = (T)p->M[0];
+  k.M1 = (T)p->M[1];
+  NcGibbs gb;
+  static_assert(sizeof(gb.piece) == sizeof(p->gibbs), "Gibbs table layout");
+  memcpy(gb.piece, p->gibbs, sizeof(gb.piece));
+  memcpy(gb.npieces, p->npieces, sizeof(gb.npieces));
+  const int64_t fsz = (int64_t)g.n[0] * g.pitch;
+  T* dG = transfer;
+  T* Mc = transfer + fsz;
+  T* dF = transfer + 2 * fsz;
+  cudaStream_t st = (cudaStream_t)stream;
+  const dim3 grid2((g.n[1] + 255) / 256, g.n[0]);
+  PPF_TRY_CUDA(launch(ncgpu_thermo_kernel<T>, grid2, dim3(256), 0, st, true, g, k, gb, in[0],
+                      in[3], temp, dG, Mc, dF, seed, step, step_base));
+  PPF_TRY_CUDA(launch(ncgpu_kernel<T>, grid2, dim3(256), 0, st, true, g, bc, k, in[0], in[1],
+                      in[2], in[3], temp, (const T*)dG, (const T*)Mc, (const T*)dF, out[0],
+                      out[1], out[2], out[3]));
+  return PPF_OK;
+}
+
+}  // namespace
+}  // namespace ppf
+
+using namespace ppf;
+
+extern "C" {
+
+int32_t ppf_ncgpu_step_f32(const PpfNcgpuParams* p, const PpfGrid* g, const PpfBoundary* bc,
+                           const float* const* fields_in, float* const* fields_out,
+                           const float* temperature, float* transfer, uint64_t seed,
+                           uint64_t step, const uint64_t* step_base, void* stream) {
+  return ncgpu_step<float>(p, g, bc, fields_in, fields_out, temperature, transfer, seed, step,
+                           step_base, stream);
+}
+
+int32_t ppf_ncgpu_step_f64(const PpfNcgpuParams* p, const PpfGrid* g, const PpfBoundary* bc,
+                           const double* const* fields_in, double* const* fields_out,
+                           const double* temperature, double* transfer, uint64_t seed,
+                           uint64_t step, const uint64_t* step_base, void* stream) {
+  return ncgpu_step<double>(p, g, bc, fields_in, fields_out, temperature, transfer, seed, step,
+                            step_base, stream);
+}
+
+}  // extern "C"

@@ -2,6 +2,7 @@
 (Engines/__init__.py:8-23 exports every class of every engine module)."""
 from .models import (AllenCahnGB300, CahnAllenGB300, CahnHilliardGB300, DiffusionGB300,
                      Warren1995GB300, make_engines)
+from .ncgpu import NCGPUGB300, make_ncgpu
 
 __all__ = ["DiffusionGB300", "CahnAllenGB300", "AllenCahnGB300", "CahnHilliardGB300",
-           "Warren1995GB300", "make_engines"]
+           "Warren1995GB300", "NCGPUGB300", "make_engines", "make_ncgpu"]

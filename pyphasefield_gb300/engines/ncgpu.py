@@ -1,0 +1,195 @@
+"""NCGPUGB300: the reference's NCGPU engine (Engines/NCGPU.py:329-532) on the
+CUDA library: binary alloy solidification with a phase field, two quaternion
+orientation fields and the first component's fraction, thermodynamics from
+a TDB file (read by pyphasefield_gb300.tdb instead of pycalphad).
+
+Fields, in the reference's order: phi (1 = solid), q1, q4, c_<first
+component>. user_data keys as the reference: d_ratio (4), sim_type ("seed"
+places one seed at the centre; anything else leaves the melt), melt_angle,
+seed_angle, initial_concentration_array; added: seed (noise stream),
+noise_scale (1 = the reference's Langevin term on dF/dc, 0 = none).
+dt is the reference's dx^2 / 5 / D_L / 8. precision defaults to "fp64"
+(float32 runs; its threshold branches part from float64 within a few
+steps). Periodic or zero-gradient
+boundaries; the temperature field must be ISOTHERMAL or a LINEAR_GRADIENT
+without dTdt (the device copy of the field is fixed during a run).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+import torch
+
+from .. import _lib as L
+from ..device import ptr
+from ..simulation import Simulation
+from ..tdb import Database
+from .base import GB300Engine
+
+_F = {torch.float32: "f32", torch.float64: "f64"}
+
+
+def ncgpu_parameters(db: Database, dx: float, d_ratio: float = 4.0) -> dict:
+    """NCGPU.init_tdb_params (NCGPU.py:336-373): per-component latent heat,
+    melting point, surface energy and kinetic coefficient from the TDB's
+    <COMP>_L / _TM / _S / _B functions, the derived W and M, and the scalar
+    functions D_S, D_L, V_M, M_Q, H, Y_E."""
+    comps = db.elements
+    if len(comps) != 2:
+        raise NotImplementedError(f"NCGPU: binary systems only (the TDB lists {comps})")
+    d = dx * d_ratio
+    ud = {"d": d, "R": 8.314}
+    for key, fn in (("L", "_L"), ("T_M", "_TM"), ("S", "_S"), ("B", "_B")):
+        ud[key] = [db.scalar(c + fn) for c in comps]
+    ud["W"] = [3 * s / (np.sqrt(2) * tm * d) for s, tm in zip(ud["S"], ud["T_M"])]
+    # the reference divides the mobility by a fixed 1574 (NCGPU.py:362)
+    ud["M"] = [tm ** 2 * b / (6 * np.sqrt(2) * lat * d) / 1574.0
+               for tm, b, lat in zip(ud["T_M"], ud["B"], ud["L"])]
+    for key, fn in (("D_S", "D_S"), ("D_L", "D_L"), ("v_m", "V_M"), ("M_qmax", "M_Q"),
+                    ("H", "H"), ("y_e", "Y_E")):
+        ud[key] = db.scalar(fn)
+    ud["ebar"] = float(np.sqrt(6 * np.sqrt(2) * ud["S"][1] * d / ud["T_M"][1]))
+    ud["eqbar"] = 0.5 * ud["ebar"]
+    ud["beta"] = 1.5
+    ud["dt"] = dx ** 2 / 5.0 / ud["D_L"] / 8
+    return ud
+
+
+def gibbs_table(db: Database):
+    """(gibbs[2][2][4][10], npieces[2][2]) for PpfNcgpuParams: phase 0 the
+    solid (first phase in sorted order), 1 the liquid; components sorted."""
+    if len(db.phases) != 2:
+        raise NotImplementedError(f"NCGPU: two phases expected (the TDB lists {db.phases})")
+    table = np.zeros((2, 2, 4, 10))
+    npieces = np.zeros((2, 2), dtype=np.int32)
+    for ph, phase in enumerate(db.phases):
+        for cp, comp in enumerate(db.elements):
+            pieces = db.params.get((phase, comp))
+            if pieces is None:
+                raise ValueError(f"TDB has no G({phase}, {comp}; 0)")
+            if len(pieces) > 4:
+                raise NotImplementedError("more than 4 temperature ranges")
+            for k, (lo, hi, coefs) in enumerate(pieces):
+                table[ph, cp, k, 0], table[ph, cp, k, 1] = lo, hi
+                table[ph, cp, k, 2:] = coefs
+            npieces[ph, cp] = len(pieces)
+    return table, npieces
+
+
+def make_seed(phi, q1, q4, x, y, angle, seed_radius):
+    """phi = 1 within seed_radius of (x, y), the quaternion at `angle` within
+    seed_radius + 5 (NCGPU.make_seed, :305-320; half angles, periodic wrap)."""
+    ny, nx = phi.shape
+    qrad = seed_radius + 5
+    yy, xx = np.mgrid[int(y - qrad):int(y + qrad), int(x - qrad):int(x + qrad)]
+    r2 = (yy - y) ** 2 + (xx - x) ** 2
+    inner = (yy >= int(y - seed_radius)) & (yy < int(y + seed_radius)) & \
+        (xx >= int(x - seed_radius)) & (xx < int(x + seed_radius)) & (r2 < seed_radius ** 2)
+    phi[yy[inner] % ny, xx[inner] % nx] = 1
+    outer = r2 < qrad ** 2
+    q1[yy[outer] % ny, xx[outer] % nx] = np.cos(0.5 * angle)
+    q4[yy[outer] % ny, xx[outer] % nx] = np.sin(0.5 * angle)
+    return phi, q1, q4
+
+
+class _NcgpuMixin(GB300Engine):
+    NFIELDS = 4
+
+    def __init__(self, **kwargs):
+        super().__init__(**kwargs)
+        self.user_data.setdefault("d_ratio", 4.0)
+        self.user_data.setdefault("seed", 0)
+        self.user_data.setdefault("noise_scale", 1.0)
+        # float64 by default: the kernel's thresholds (|grad q| >= beta, the
+        # phi clamp) flip for some cells in float32 within a few steps
+        self.user_data.setdefault("precision", "fp64")
+        self._ppf_defaults()
+        self._ppf_db = None
+
+    def init_tdb_params(self):
+        if self._tdb_path is None:
+            raise ValueError("NCGPU needs tdb_path (a thermodynamic database)")
+        self._ppf_db = Database(self._tdb_path)
+        if self.dx is None:
+            raise ValueError("NCGPU needs dx")
+        self.user_data.update(ncgpu_parameters(self._ppf_db, float(self.dx),
+                                               float(self.user_data["d_ratio"])))
+        self._tdb_components = list(self._ppf_db.elements)
+        self._tdb_phases = list(self._ppf_db.phases)
+        self.dt = self.user_data["dt"]  # set_time_step_length (:367)
+
+    def init_fields(self):
+        dim = self.dimensions
+        if len(dim) != 2:
+            raise NotImplementedError("NCGPU runs 2-D grids (the reference's 1-D / 3-D paths "
+                                      "launch its 2-D kernels)")
+        ud = self.user_data
+        comps = self._tdb_components
+        phi = np.zeros(dim)
+        melt = float(ud.get("melt_angle", 0.0)) if ud.get("sim_type") == "seed" else 0.0
+        q1 = np.full(dim, np.cos(0.5 * melt))
+        q4 = np.full(dim, np.sin(0.5 * melt))
+        if ud.get("sim_type") == "seed":
+            seed_angle = float(ud.get("seed_angle", np.pi / 4))
+            phi, q1, q4 = make_seed(phi, q1, q4, dim[1] / 2, dim[0] / 2, seed_angle, 5)
+        self.add_field(phi, "phi")
+        self.add_field(q1, "q1")
+        self.add_field(q4, "q4")
+        c0 = ud.get("initial_concentration_array")
+        val = float(c0[0]) if c0 is not None else 1.0 / len(comps)
+        self.add_field(np.full(dim, val), "c_" + comps[0])
+
+    def _ppf_prepare(self):
+        t = self._temperature_type
+        if self.temperature is None or t not in ("ISOTHERMAL", "LINEAR_GRADIENT"):
+            raise ValueError("NCGPU needs an ISOTHERMAL or LINEAR_GRADIENT temperature field")
+        if t == "LINEAR_GRADIENT" and self._dTdt:
+            raise NotImplementedError("NCGPU: a temperature that changes in time (dTdt) is not "
+                                      "supported")
+        if self._boundary_conditions_type is None:
+            self._boundary_conditions_type = "PERIODIC"
+
+    def _ppf_setup(self):
+        super()._ppf_setup()
+        g = self._ppf_grid
+        self._nc_temp = g.empty()
+        self._nc_transfer = torch.zeros((3,) + tuple(g.alloc_shape), dtype=g.dtype,
+                                        device=g.device)
+        # the pinned staging copy must outlive the asynchronous upload
+        self._nc_temp_staging = self._ppf_grid.upload(self._nc_temp, self.temperature.get_cells(),
+                                                      self._ppf_stream)
+        table, npieces = gibbs_table(self._ppf_db)
+        ud = self.user_data
+        p = L.PpfNcgpuParams()
+        for name in ("dt", "v_m", "D_L", "D_S", "M_qmax", "H", "y_e", "beta"):
+            setattr(p, name, float(ud[name]))
+        p.dx = float(self.dx)
+        p.ebar2 = float(ud["ebar"]) ** 2
+        p.noise_scale = float(ud.get("noise_scale", 1.0))
+        for j in range(2):
+            p.W[j] = float(ud["W"][j])
+            p.M[j] = float(ud["M"][j])
+        flat = table.reshape(-1)
+        for k in range(flat.size):
+            p.gibbs[k // 80][(k // 40) % 2][(k // 10) % 4][k % 10] = float(flat[k])
+        for ph in range(2):
+            for cp in range(2):
+                p.npieces[ph][cp] = int(npieces[ph, cp])
+        self._nc_params = p
+
+    def _ppf_step(self, src, dst, depth, step, step_base, sp):
+        fin = (C.c_void_p * 4)(*[ptr(t) for t in src])
+        fout = (C.c_void_p * 4)(*[ptr(t) for t in dst])
+        L.call(f"ppf_ncgpu_step_{_F[self._ppf_dtype]}", C.byref(self._nc_params),
+               C.byref(self._ppf_grid.grid), C.byref(self._ppf_bc), fin, fout,
+               ptr(self._nc_temp), ptr(self._nc_transfer), C.c_uint64(int(self.user_data["seed"])),
+               C.c_uint64(int(step)), ptr(step_base), sp)
+
+
+def make_ncgpu(base=Simulation):
+    return type("NCGPUGB300", (_NcgpuMixin, base), {"__module__": __name__,
+                                                   "__doc__": __doc__})
+
+
+NCGPUGB300 = make_ncgpu(Simulation)

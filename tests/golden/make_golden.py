@@ -36,6 +36,29 @@ def save(name, meta, **arrays):
     print(name, {k: v.shape for k, v in arrays.items()})
 
 
+def write_tdb(tdb, path):
+    """The FUNCTION and PARAMETER records the NCGPU fixtures use, re-emitted
+    from the parsed database (so the GPU machine, which has no reference
+    checkout, reads the same thermodynamic data)."""
+    lines = ["$ Ni-Cu ideal solution records used by the NCGPU fixtures "
+             "(written by tests/golden/make_golden.py)"]
+    for el in tdb.elements:
+        lines.append(f"ELEMENT {el} FCC_A1 0 0 0 !")
+    for name, pieces in tdb.functions.items():
+        body = f"{pieces[0][0]!r} {pieces[0][2]}"
+        for k, (lo, hi, expr) in enumerate(pieces):
+            more = k + 1 < len(pieces)
+            body += f"; {hi!r} " + (f"Y {pieces[k + 1][2]}" if more else "N")
+        lines.append(f"FUNCTION {name} {body} !")
+    for ph in tdb.phases:
+        lines.append(f"PHASE {ph} % 1 1 !")
+        for (pph, comp), pieces in tdb.params.items():
+            if pph == ph:
+                lo, hi, expr = pieces[0]
+                lines.append(f"PARAMETER G({ph},{comp};0) {lo!r} {expr}; {hi!r} N !")
+    Path(path).write_text("\n".join(lines) + "\n")
+
+
 def single(name, model, c0, steps, bc, dx, dt, values=None, **params):
     if model == "cahn_hilliard":
         out = refshim.run_cahn_hilliard_extended(c0, steps, bc, dx, dt, params["M"],
@@ -130,6 +153,27 @@ def main():
                     function=fn, steps=3, dt=dt, dx=dx_, solver=solver, adi=adi, gmres=gm,
                     params=ud)
         save(name, meta, c0=c0, out=out)
+
+    # NCGPU (Engines/NCGPU.py): the reference's numba kernels run serially
+    # under a stand-in numba module, Ni-Cu ideal TDB of the reference
+    from oracle import ncgpu_ref
+    tdb_path = refshim.reference_root() / "pyphasefield" / "examples" / "Ni-Cu_Ideal.tdb"
+    tdb = ncgpu_ref.Tdb(tdb_path)
+    write_tdb(tdb, HERE / "ncgpu_nicu.tdb")
+    tdb = ncgpu_ref.Tdb(HERE / "ncgpu_nicu.tdb")
+    nrng = np.random.default_rng(20240604)
+    for name, shape, bc, steps, seed in [("ncgpu_periodic", (24, 20), "PERIODIC", 4, 7),
+                                         ("ncgpu_neumann", (20, 22), "NEUMANN", 3, 11)]:
+        p = ncgpu_ref.tdb_params(tdb, 4.6e-6)
+        phi0, q10, q40, c0 = ncgpu_ref.seed_fields(shape, c0=0.40831)
+        c0 = c0 + nrng.uniform(-1e-3, 1e-3, shape)
+        T = np.full(shape, 1574.0)
+        noise = [ncgpu_ref.noise_normal(seed, s, shape) for s in range(steps)]
+        out = refshim.run_ncgpu(phi0, q10, q40, c0, T, steps, p, tdb, noise, bc)
+        meta = dict(model="ncgpu", steps=steps, bc=bc, seed=seed, dx=4.6e-6, T=1574.0,
+                    tdb="ncgpu_nicu.tdb")
+        save(name, meta, phi0=phi0, q10=q10, q40=q40, c0=c0, phi=out[0], q1=out[1], q4=out[2],
+             c=out[3])
 
     dx = 4.6e-8
     prm = dict(restate.WARREN_DEFAULTS)

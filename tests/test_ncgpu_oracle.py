@@ -1,0 +1,75 @@
+"""NCGPU on the CPU: the oracle (oracle/ncgpu_ref.py) against the fixtures
+made by running the reference's own numba kernels serially
+(tests/golden/ncgpu_*), and the package's TDB reader, parameters and seed
+against the oracle's."""
+import json
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from oracle import ncgpu_ref as N
+from pyphasefield_gb300.engines.ncgpu import gibbs_table, make_seed, ncgpu_parameters
+from pyphasefield_gb300.tdb import Database, g_eval
+
+GOLDEN = Path(__file__).resolve().parent / "golden"
+TDB = GOLDEN / "ncgpu_nicu.tdb"
+
+
+@pytest.mark.parametrize("name", ["ncgpu_periodic", "ncgpu_neumann"])
+def test_oracle_matches_reference_kernels(name):
+    z = np.load(GOLDEN / f"{name}.npz")
+    m = json.loads(str(z["meta"]))
+    tdb = N.Tdb(GOLDEN / m["tdb"])
+    p = N.tdb_params(tdb, m["dx"])
+    T = np.full(z["phi0"].shape, m["T"])
+    out = N.run([z["phi0"], z["q10"], z["q40"], z["c0"]], T, m["steps"], p, tdb, seed=m["seed"],
+                bc=m["bc"])
+    # c: the reference's dG/dc is a forward difference with step 1e-7, which
+    # turns a rounding-level change of c (1e-17, from the order of the
+    # operations) into 1e-11 .. 1e-10 after a few steps
+    for got, key, tol in zip(out, ("phi", "q1", "q4", "c"), (1e-12, 1e-12, 1e-12, 1e-8)):
+        ref = z[key]
+        assert np.abs(got - ref).max() <= tol * max(1.0, np.abs(ref).max()), key
+
+
+def test_tdb_reader_matches_oracle_evaluation():
+    db, tdb = Database(TDB), N.Tdb(TDB)
+    assert db.elements == tdb.elements == ["CU", "NI"]
+    assert db.phases == tdb.phases == ["FCC_A1", "LIQUID"]
+    for (ph, comp), pieces in db.params.items():
+        for T in (300.0, 900.0, 1357.0, 1357.77, 1574.0, 1727.99, 1728.0, 2500.0, 3500.0):
+            mine = 0.0
+            for lo, hi, c in pieces:
+                if lo <= T < hi:
+                    mine = g_eval(c, T)
+            assert mine == pytest.approx(tdb.g_pure(ph, comp, T), rel=1e-13, abs=1e-9)
+    table, npieces = gibbs_table(db)
+    assert table.shape == (2, 2, 4, 10) and (npieces == 2).all()
+
+
+def test_parameters_match_oracle():
+    db, tdb = Database(TDB), N.Tdb(TDB)
+    mine = ncgpu_parameters(db, 4.6e-6)
+    ref = N.tdb_params(tdb, 4.6e-6)
+    for k in ("d", "D_S", "D_L", "v_m", "M_qmax", "H", "y_e", "beta", "dt", "ebar"):
+        assert mine[k] == pytest.approx(ref[k], rel=1e-14), k
+    for k in ("L", "T_M", "S", "B", "W", "M"):
+        np.testing.assert_allclose(mine[k], ref[k], rtol=1e-14)
+
+
+@pytest.mark.parametrize("shape", [(40, 50), (21, 17), (12, 12)])
+def test_seed_matches_oracle(shape):
+    phi = np.zeros(shape)
+    q1 = np.ones(shape)
+    q4 = np.zeros(shape)
+    make_seed(phi, q1, q4, shape[1] / 2, shape[0] / 2, np.pi / 4, 5)
+    rphi, rq1, rq4, _ = N.seed_fields(shape)
+    np.testing.assert_array_equal(phi, rphi)
+    np.testing.assert_array_equal(q1, rq1)
+    np.testing.assert_array_equal(q4, rq4)
+
+
+def test_noise_is_standard_normal():
+    z = N.noise_normal(3, 5, (300, 400))
+    assert abs(z.mean()) < 0.01 and abs(z.std() - 1) < 0.01

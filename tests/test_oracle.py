@@ -16,7 +16,7 @@ from oracle.philox import noise_uniform, philox4x32_10
 from tests.helpers import golden_names, load_golden, rel_l2
 
 
-EXPLICIT_GOLDEN = [n for n in golden_names() if not n.startswith(("implicit_", "crank_nicolson_", "phase_implicit_"))]
+EXPLICIT_GOLDEN = [n for n in golden_names() if not n.startswith(("implicit_", "crank_nicolson_", "phase_implicit_", "ncgpu_"))]
 
 
 @pytest.mark.parametrize("name", EXPLICIT_GOLDEN)
