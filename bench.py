@@ -389,8 +389,13 @@ SWEEP = {
                                       {"solver": "implicit", "adi": True, "dt": 1.0}),
     "allen_cahn_full_4096": ("allen_cahn", (4096, 4096), 1, 5,
                              {"solver": "implicit", "adi": False, "gmres": True, "dt": 1.0}),
+    # NCGPU (Ni-Cu, 1574 K, one seed at the centre, dx = 4.6e-6 cm): float64 (the engine's
+    # default) and float32
+    "ncgpu_2048": ("ncgpu", (2048, 2048), 1, 100, {"precision": "fp64"}),
+    "ncgpu_2048_fp32": ("ncgpu", (2048, 2048), 1, 100, {"precision": "fp32"}),
 }
 SWEEP_B_ALG = {"diffusion": 8, "allen_cahn": 8, "cahn_hilliard": 8, "warren1995": 16}
+NCGPU_TDB = ROOT / "tests" / "golden" / "ncgpu_nicu.tdb"
 
 
 def sweep_engine(model, grid, depth, steps, rng, extra=None):
@@ -413,6 +418,15 @@ def sweep_engine(model, grid, depth, steps, rng, extra=None):
                                 boundary_conditions="PERIODIC",
                                 user_data=dict(ud, M=1.0, epsilon=1.0))
         init = [0.5 + rng.uniform(-0.05, 0.05, grid)]
+    elif model == "ncgpu":
+        from pyphasefield_gb300 import NCGPUGB300
+        sim = NCGPUGB300(dimensions=list(grid), dx=4.6e-6, tdb_path=str(NCGPU_TDB),
+                         temperature_type="ISOTHERMAL", initial_T=1574.0,
+                         boundary_conditions="PERIODIC",
+                         user_data=dict(ud, sim_type="seed", initial_concentration_array=[0.40831],
+                                        seed=SEED))
+        sim.initialize_fields_and_imported_data()
+        return sim
     else:
         sim = Warren1995GB300(dimensions=list(grid), dx=DX, boundary_conditions="NEUMANN",
                               user_data=dict(ud, seed=SEED, alpha=0.3))
@@ -431,6 +445,9 @@ def sweep_bytes_per_cell(model, sim) -> int:
     axis) or per Chebyshev iteration (iterate, previous iterate and the
     right-hand side read, the new iterate written: 16 B in float)."""
     ud = sim.user_data
+    if model == "ncgpu":
+        # phi, q1, q4, c read and written, the temperature read
+        return 9 * (8 if ud.get("precision", "fp64") == "fp64" else 4)
     if model in ("diffusion", "allen_cahn") and ud.get("solver", "explicit") != "explicit":
         if ud.get("adi") or len(sim.dimensions) == 1:
             return 8 * len(sim.dimensions)

@@ -158,9 +158,9 @@ def test_engine_rejections(cuda):
     with pytest.raises(RuntimeError, match="PERIODIC and NEUMANN"):
         ch.simulate(1)
     d = DiffusionGB300(dimensions=[16, 16], dx=1.0, dt=0.1, boundary_conditions="NEUMANN",
-                       user_data={"solver": "implicit"})
+                       user_data={"solver": "multigrid"})
     d.initialize_fields_and_imported_data()
-    with pytest.raises(NotImplementedError):
+    with pytest.raises(ValueError, match="solver must be one of"):
         d.simulate(1)
     d2 = DiffusionGB300(dimensions=[16, 16], dx=1.0, dt=0.1, boundary_conditions="NEUMANN")
     d2.initialize_fields_and_imported_data()
