@@ -324,8 +324,9 @@ int32_t ppf_var_line_solve_f64(const PpfGrid* g, int32_t axis, double alpha, dou
 /* ---- NCGPU (multi-component solidification with orientation) ----------- */
 
 /* One step of the NCGPU engine (Engines/NCGPU.py:37-303, simulation_loop
- * :499-532), binary systems, 2-D: fields phi, q1, q4 and c (the first
- * component's fraction; the second is 1 - c). Parameters as
+ * :499-532), 2 or 3 components (ncomp), 2-D: fields phi, q1, q4 and the
+ * fractions c_1 .. c_{ncomp-1} of all but the last component (the last is
+ * 1 - sum c), 3 + ncomp - 1 pointers in fields_in / fields_out. Parameters as
  * NCGPU.init_tdb_params derives them (:336-373): ebar2 = 6 sqrt(2) S[1] d /
  * T_M[1], W and M per component (components sorted). gibbs[phase][comp]
  * holds up to 4 temperature ranges of the pure element's Gibbs energy in
@@ -335,13 +336,17 @@ int32_t ppf_var_line_solve_f64(const PpfGrid* g, int32_t axis, double alpha, dou
  * noise_scale multiplies the Langevin term of dF/dc (1 = the reference);
  * its N(0,1) numbers come from Philox4x32-10 keyed by (seed, step
  * (+ *step_base), cell). temperature: a field of the grid's layout.
- * transfer: device scratch of 3 fields of the grid's layout. Boundaries:
- * periodic or zero-gradient Neumann. */
+ * transfer: device scratch of 2 ncomp - 1 fields of the grid's layout.
+ * Boundaries: periodic or zero-gradient Neumann. As the reference, dG/dc is
+ * one forward difference per cell (the first component up, the last down)
+ * shared by every component. */
 typedef struct PpfNcgpuParams {
   double dx, dt, v_m, D_L, D_S, M_qmax, H, y_e, beta, ebar2, noise_scale;
-  double W[2], M[2];
-  double gibbs[2][2][4][10];
-  int32_t npieces[2][2];
+  double W[3], M[3];
+  double gibbs[2][3][4][10];
+  int32_t npieces[2][3];
+  int32_t ncomp;
+  int32_t reserved;
 } PpfNcgpuParams;
 
 int32_t ppf_ncgpu_step_f32(const PpfNcgpuParams* p, const PpfGrid* g, const PpfBoundary* bc,

@@ -167,7 +167,7 @@ def tdb_params(tdb: Tdb, dx: float, d_ratio: float = 4.0) -> dict:
     return p
 
 
-def seed_fields(shape, melt_angle=0.0, seed_angle=np.pi / 4, radius=5, c0=None):
+def seed_fields(shape, melt_angle=0.0, seed_angle=np.pi / 4, radius=5, c0=None, ncomp=2):
     """NCGPU.init_fields with sim_type "seed" (:375-415) and make_seed
     (:305-320): phi = 1 in a disk of `radius` at the centre, quaternion
     angle seed_angle within radius + 5, melt_angle elsewhere; c = c0 (or
@@ -187,8 +187,10 @@ def seed_fields(shape, melt_angle=0.0, seed_angle=np.pi / 4, radius=5, c0=None):
             if (i - y) ** 2 + (j - x) ** 2 < qr ** 2:
                 q1[i % ny, j % nx] = np.cos(0.5 * seed_angle)
                 q4[i % ny, j % nx] = np.sin(0.5 * seed_angle)
-    c = np.full(shape, 0.5 if c0 is None else c0)
-    return phi, q1, q4, c
+    if ncomp == 2 and not isinstance(c0, (list, tuple)):
+        return phi, q1, q4, np.full(shape, 0.5 if c0 is None else c0)
+    vals = list(c0) if c0 is not None else [1.0 / ncomp] * (ncomp - 1)
+    return (phi, q1, q4) + tuple(np.full(shape, v) for v in vals)
 
 
 def noise_normal(seed: int, step: int, shape) -> np.ndarray:
@@ -222,9 +224,14 @@ def _pad(a, bc):
 
 def step(fields, T, p: dict, tdb: Tdb, noise, bc: str = "PERIODIC", noise_scale: float = 1.0):
     """One NCGPU step (helper kernel, then main kernel) on interior arrays
-    (phi, q1, q4, c), binary system; T an interior array. `bc`: PERIODIC or
-    NEUMANN (zero gradient), applied to every field as ghost cells."""
-    phi, q1, q4, c = fields
+    (phi, q1, q4, c_1 .. c_{N-1}); the last component's fraction is 1 - sum
+    c. T an interior array. `bc`: PERIODIC or NEUMANN (zero gradient),
+    applied to every field as ghost cells. As the reference, dG/dc is taken
+    once per cell (first component up, last one down, :282-286) and used for
+    every component."""
+    phi, q1, q4 = fields[:3]
+    cs = list(fields[3:])
+    nc = len(cs)
     phases = tdb.phases  # sorted: FCC_A1 (solid), LIQUID
     idx = 1.0 / p["dx"]
     v_m, D_L, D_S = p["v_m"], p["D_L"], p["D_S"]
@@ -236,15 +243,18 @@ def step(fields, T, p: dict, tdb: Tdb, noise, bc: str = "PERIODIC", noise_scale:
     # helper: thermodynamics per interior cell
     GL = np.empty_like(phi)
     GS = np.empty_like(phi)
-    Mc = np.empty_like(phi)
-    dF = np.empty_like(phi)
+    Mcs = [np.empty_like(phi) for _ in range(nc)]
+    dFs = [np.empty_like(phi) for _ in range(nc)]
     for i in range(ny):
         for j in range(nx):
-            x0, t = c[i, j], T[i, j]
-            xs = [x0, 1.0 - x0]
+            t = T[i, j]
+            xs = [c[i, j] for c in cs]
+            xs.append(1.0 - sum(xs))
             gl = tdb.gibbs(phases[1], xs, t)
             gs = tdb.gibbs(phases[0], xs, t)
-            xp = [x0 + 1e-7, (1.0 - x0) - 1e-7]
+            xp = list(xs)
+            xp[nc] -= 1e-7
+            xp[0] += 1e-7
             dgl = 1e7 * (tdb.gibbs(phases[1], xp, t) - gl)
             dgs = 1e7 * (tdb.gibbs(phases[0], xp, t) - gs)
             ph = phi[i, j]
@@ -252,10 +262,23 @@ def step(fields, T, p: dict, tdb: Tdb, noise, bc: str = "PERIODIC", noise_scale:
             h = ph ** 3 * (6 * ph * ph - 15 * ph + 10)
             nz = noise_scale * math.sqrt(2.0 * R_KERNEL * t / v_m) * noise[i, j]
             GL[i, j], GS[i, j] = gl, gs
-            Mc[i, j] = v_m * x0 * (D_L + h * (D_S - D_L)) / (R_KERNEL * t)
-            dF[i, j] = (dgl + h * (dgs - dgl)) / v_m + (W[0] - W[1]) * g * t + nz
-    P, Q1, Q4, Cc, TT, MC, DF = (_pad(a, bc) for a in (phi, q1, q4, c, T, Mc, dF))
-    out = [np.empty_like(phi) for _ in range(4)]
+            for l in range(nc):
+                Mcs[l][i, j] = v_m * xs[l] * (D_L + h * (D_S - D_L)) / (R_KERNEL * t)
+                dFs[l][i, j] = (dgl + h * (dgs - dgl)) / v_m + (W[l] - W[nc]) * g * t + nz
+    P, Q1, Q4, TT = (_pad(a, bc) for a in (phi, q1, q4, T))
+    CC = [_pad(a, bc) for a in cs]
+    MC = [_pad(a, bc) for a in Mcs]
+    DF = [_pad(a, bc) for a in dFs]
+    return _update(P, Q1, Q4, CC, TT, GL, GS, MC, DF, p, ebar2, eqbar2, idx)
+
+
+def _update(P, Q1, Q4, CC, TT, GL, GS, MC, DF, p, ebar2, eqbar2, idx):
+    """NComponent_kernel (:37-242) on padded arrays."""
+    v_m, W, M = p["v_m"], p["W"], p["M"]
+    y_e, H, beta, M_qmax, dt = p["y_e"], p["H"], p["beta"], p["M_qmax"], p["dt"]
+    nc = len(CC)
+    ny, nx = P.shape[0] - 2, P.shape[1] - 2
+    out = [np.empty((ny, nx)) for _ in range(3 + nc)]
     for i in range(1, ny + 1):
         for j in range(1, nx + 1):
             ph = P[i, j]
@@ -318,9 +341,14 @@ def step(fields, T, p: dict, tdb: Tdb, noise, bc: str = "PERIODIC", noise_scale:
             ty += t * (dpy * s4 * (4 * dpx ** 3 * pxy + 4 * dpx * pxy * dpy ** 2
                                    + 4 * dpy * pyy * dpx ** 2 + 4 * dpy ** 3 * pyy)) / mg8
             ty *= 4 * y_e * ebar2
-            ci = Cc[i, j]
-            cW = ci * W[0] + (1 - ci) * W[1]
-            M_phi = ci * M[0] + (1 - ci) * M[1]
+            cW, c_N, M_phi = 0.0, 1.0, 0.0
+            for l in range(nc):
+                cl = CC[l][i, j]
+                cW += cl * W[l]
+                c_N -= cl
+                M_phi += cl * M[l]
+            cW += c_N * W[nc]
+            M_phi += c_N * M[nc]
             M_q = M_qmax + (1e-6 - M_qmax) * h
             dphidt = ebar2 * (1 - 3 * y_e) * (t * lphi + dTx * dpx + dTy * dpy)
             dphidt += tx + ty
@@ -333,11 +361,18 @@ def step(fields, T, p: dict, tdb: Tdb, noise, bc: str = "PERIODIC", noise_scale:
                 return 0.5 * idx * idx * ((axp + a) * (bxp - b) - (a + axm) * (b - bxm)
                                           + (ayp + a) * (byp - b) - (a + aym) * (b - bym))
 
-            m, mxp, mxm, myp, mym = MC[i, j], MC[i, j + 1], MC[i, j - 1], MC[i + 1, j], MC[i - 1, j]
-            f, fxp, fxm, fyp, fym = DF[i, j], DF[i, j + 1], DF[i, j - 1], DF[i + 1, j], DF[i - 1, j]
-            dc = divagradb(m, mxp, mxm, myp, mym, f, fxp, fxm, fyp, fym)
-            dc -= divagradb(m * Cc[i, j], mxp * Cc[i, j + 1], mxm * Cc[i, j - 1],
-                            myp * Cc[i + 1, j], mym * Cc[i - 1, j], f, fxp, fxm, fyp, fym)
+            def nb5(A):
+                return A[i, j], A[i, j + 1], A[i, j - 1], A[i + 1, j], A[i - 1, j]
+
+            dcs = []
+            for l in range(nc):
+                m, mxp, mxm, myp, mym = nb5(MC[l])
+                dc = divagradb(m, mxp, mxm, myp, mym, *nb5(DF[l]))
+                for k in range(nc):
+                    c0_, cxp, cxm, cyp, cym = nb5(CC[k])
+                    dc -= divagradb(m * c0_, mxp * cxp, mxm * cxm, myp * cyp, mym * cym,
+                                    *nb5(DF[k]))
+                dcs.append(dc)
             Dq = 2 * H * t * ph * ph
             Dxp = 2 * H * TT[i, j + 1] * P[i, j + 1] ** 2
             Dxm = 2 * H * TT[i, j - 1] * P[i, j - 1] ** 2
@@ -360,7 +395,8 @@ def step(fields, T, p: dict, tdb: Tdb, noise, bc: str = "PERIODIC", noise_scale:
             out[0][i - 1, j - 1] = pn
             out[1][i - 1, j - 1] = n1 / rn
             out[2][i - 1, j - 1] = n4 / rn
-            out[3][i - 1, j - 1] = ci + dt * dc
+            for l in range(nc):
+                out[3 + l][i - 1, j - 1] = CC[l][i, j] + dt * dcs[l]
     return out
 
 

@@ -320,34 +320,36 @@ def ncgpu_module():
 
 
 def run_ncgpu(phi, q1, q4, c, T, steps: int, p: dict, tdb, noise_fields, bc="PERIODIC"):
-    """Drive NComponent_helper_kernel and NComponent_kernel (binary system)
-    for `steps` steps. noise_fields[s] is the interior N(0,1) field of step
-    s; ghost cells take the noise of the cell the boundary rule maps them
-    to. Ghost cells of every field and of T follow `bc` (PERIODIC or
-    zero-gradient NEUMANN), as ppf_gpu_utils.apply_boundary_conditions fills
-    them between steps."""
+    """Drive NComponent_helper_kernel and NComponent_kernel for `steps`
+    steps; c is one concentration field (binary) or a list of N - 1 of them.
+    noise_fields[s] is the interior N(0,1) field of step s; ghost cells take
+    the noise of the cell the boundary rule maps them to. Ghost cells of
+    every field and of T follow `bc` (PERIODIC or zero-gradient NEUMANN), as
+    ppf_gpu_utils.apply_boundary_conditions fills them between steps."""
     mod = ncgpu_module()
     mode = "wrap" if bc == "PERIODIC" else "symmetric"
     pad = lambda a: np.pad(np.asarray(a, dtype=np.float64), 1, mode=mode)  # noqa: E731
-    ph, a1, a4, cc = (np.array(a, dtype=np.float64) for a in (phi, q1, q4, c))
-    ny, nx = ph.shape
+    cs = [np.array(x, dtype=np.float64) for x in (c if isinstance(c, (list, tuple)) else [c])]
+    f = [np.array(a, dtype=np.float64) for a in (phi, q1, q4)] + cs
+    ncomp = len(cs) + 1
+    ny, nx = f[0].shape
     Tp = pad(T)
     params = np.array([p["dx"], p["d"], p["v_m"], p["M_qmax"], p["H"], p["y_e"], p["beta"],
                        p["D_L"], p["D_S"], p["dt"]])
     c_params = np.array([p["L"], p["T_M"], p["S"], p["B"], p["W"], p["M"]])
     phases = tdb.phases
-    mod.ufunc_g_l = lambda arr: tdb.gibbs(phases[1], [arr[0], arr[1]], arr[2])
-    mod.ufunc_g_s = lambda arr: tdb.gibbs(phases[0], [arr[0], arr[1]], arr[2])
+    mod.ufunc_g_l = lambda arr: tdb.gibbs(phases[1], list(arr[:ncomp]), arr[ncomp])
+    mod.ufunc_g_s = lambda arr: tdb.gibbs(phases[0], list(arr[:ncomp]), arr[ncomp])
     for s in range(steps):
-        fields = np.stack([pad(ph), pad(a1), pad(a4), pad(cc)])
+        fields = np.stack([pad(a) for a in f])
         out = np.zeros_like(fields)
-        transfer = np.zeros((4,) + fields.shape[1:])
-        ufunc_array = np.zeros(fields.shape[1:] + (3,))
+        transfer = np.zeros((2 * ncomp,) + fields.shape[1:])
+        ufunc_array = np.zeros(fields.shape[1:] + (ncomp + 1,))
         nz = pad(noise_fields[s])
         _NC["queue"] = iter(nz.ravel().tolist())
         mod.NComponent_helper_kernel(fields, Tp, transfer, None, ufunc_array, params, c_params)
         _NC["queue"] = iter([0.0] * (ny * nx))
         mod.NComponent_kernel(fields, Tp, transfer, out, None, params, c_params)
-        ph, a1, a4, cc = (out[k, 1:-1, 1:-1].copy() for k in range(4))
+        f = [out[k, 1:-1, 1:-1].copy() for k in range(len(f))]
     _NC["queue"] = None
-    return ph, a1, a4, cc
+    return f

@@ -94,8 +94,9 @@ class PpfImplicitDiffusionParams(C.Structure):
 class PpfNcgpuParams(C.Structure):
     _fields_ = [(n, C.c_double) for n in ("dx", "dt", "v_m", "D_L", "D_S", "M_qmax", "H",
                                           "y_e", "beta", "ebar2", "noise_scale")] + [
-        ("W", C.c_double * 2), ("M", C.c_double * 2),
-        ("gibbs", (((C.c_double * 10) * 4) * 2) * 2), ("npieces", (C.c_int32 * 2) * 2)]
+        ("W", C.c_double * 3), ("M", C.c_double * 3),
+        ("gibbs", (((C.c_double * 10) * 4) * 3) * 2), ("npieces", (C.c_int32 * 3) * 2),
+        ("ncomp", C.c_int32), ("reserved", C.c_int32)]
 
 
 PPF_MODEL_WARREN1995 = 1

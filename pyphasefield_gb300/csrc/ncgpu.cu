@@ -1,5 +1,5 @@
 // NCGPU: the multi-component solidification engine with quaternion
-// orientation fields (pyphasefield Engines/NCGPU.py), binary systems.
+// orientation fields (pyphasefield Engines/NCGPU.py), 2 or 3 components.
 //
 //   ncgpu_thermo_kernel  (NComponent_helper_kernel, :248-303): per cell the
 //       molar Gibbs energies of the solid (first phase, sorted) and liquid,
@@ -23,15 +23,26 @@
 namespace ppf {
 namespace {
 
+constexpr int kMaxComp = 3;
+
 template <typename T>
 struct NcCoef {
   T idx, dt, v_m, D_L, D_S, M_qmax, H, y_e, beta, ebar2, eqbar2, noise;
-  T W0, W1, M0, M1;
+  T W[kMaxComp], M[kMaxComp];
 };
 
 struct NcGibbs {
-  double piece[2][2][4][10];  // [phase][component][piece] {lo, hi, 8 coefficients}
-  int npieces[2][2];
+  double piece[2][kMaxComp][4][10];  // [phase][component][piece] {lo, hi, 8 coefficients}
+  int npieces[2][kMaxComp];
+};
+
+// The concentration fields and the per-component thermodynamic terms.
+template <typename T>
+struct NcPtrs {
+  const T* c[kMaxComp - 1];
+  T* c_out[kMaxComp - 1];
+  T* Mc[kMaxComp - 1];
+  T* dF[kMaxComp - 1];
 };
 
 __device__ __forceinline__ double g_pure(const NcGibbs& g, int ph, int comp, double T,
@@ -48,14 +59,18 @@ __device__ __forceinline__ double g_pure(const NcGibbs& g, int ph, int comp, dou
   return 0.0;  // outside every range, as a piecewise TDB function gives
 }
 
-// Molar Gibbs energy of phase ph at (x0, x1) (x1 = 1 - x0 passed apart, as
-// the reference's perturbed argument is), pycalphad's ideal solution.
-__device__ __forceinline__ double gibbs(const NcGibbs& g, int ph, double x0, double x1,
-                                        double T, double lnT, double G0, double G1) {
-  double mix = 0.0;
-  if (x0 > 0) mix += x0 * log(x0);
-  if (x1 > 0) mix += x1 * log(x1);
-  return x0 * G0 + x1 * G1 + 8.3145 * T * mix;
+// Molar Gibbs energy of a phase at fractions x[0 .. N-1] (the last one passed
+// apart, as the reference's perturbed argument is), pycalphad's ideal
+// solution: sum x_i G_i + R T sum x_i ln x_i.
+template <int N>
+__device__ __forceinline__ double gibbs(const double (&x)[N], const double (&G)[N], double T) {
+  double g = 0.0, mix = 0.0;
+#pragma unroll
+  for (int i = 0; i < N; ++i) {
+    g += x[i] * G[i];
+    if (x[i] > 0) mix += x[i] * log(x[i]);
+  }
+  return g + 8.3145 * T * mix;
 }
 
 // N(0,1) of cell (row, col) at a step: Box-Muller on two uniforms from a
@@ -72,14 +87,14 @@ __device__ __forceinline__ T noise_normal(uint64_t seed, uint64_t step, int row,
   return (T)(sqrt(-2.0 * log(u1)) * cospi(2.0 * u2));
 }
 
-template <typename T>
+template <typename T, int NC>
 __global__ void __launch_bounds__(256)
     ncgpu_thermo_kernel(Geo g, NcCoef<T> k, NcGibbs gb, const T* __restrict__ phi,
-                        const T* __restrict__ c, const T* __restrict__ temp, T* __restrict__ dG,
-                        T* __restrict__ Mc, T* __restrict__ dF, uint64_t seed, uint64_t step,
-                        const uint64_t* step_base) {
+                        NcPtrs<T> cp, const T* __restrict__ temp, T* __restrict__ dG,
+                        uint64_t seed, uint64_t step, const uint64_t* step_base) {
   pdl_wait();
   pdl_launch_next();
+  constexpr int N = NC + 1;
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
   const int y = blockIdx.y;
   if (x >= g.n[1]) return;
@@ -87,18 +102,28 @@ __global__ void __launch_bounds__(256)
   const uint64_t st = step + (step_base ? *step_base : 0);
   const double t = (double)temp[i];
   const double lnT = log(t);
-  const double x0 = (double)c[i], x1 = 1.0 - x0;
-  double G[2][2];
+  double xs[N], xp[N], Gs[N], Gl[N];
+  double last = 1.0;
 #pragma unroll
-  for (int ph = 0; ph < 2; ++ph)
+  for (int l = 0; l < NC; ++l) {
+    xs[l] = (double)cp.c[l][i];
+    last -= xs[l];
+  }
+  xs[NC] = last;
 #pragma unroll
-    for (int cp = 0; cp < 2; ++cp) G[ph][cp] = g_pure(gb, ph, cp, t, lnT);
-  const double gs = gibbs(gb, 0, x0, x1, t, lnT, G[0][0], G[0][1]);
-  const double gl = gibbs(gb, 1, x0, x1, t, lnT, G[1][0], G[1][1]);
-  // the reference's forward difference (NCGPU.py:282-286)
-  const double xp1 = x1 - 0.0000001, xp0 = x0 + 0.0000001;
-  const double dgl = 10000000.0 * (gibbs(gb, 1, xp0, xp1, t, lnT, G[1][0], G[1][1]) - gl);
-  const double dgs = 10000000.0 * (gibbs(gb, 0, xp0, xp1, t, lnT, G[0][0], G[0][1]) - gs);
+  for (int l = 0; l < N; ++l) {
+    Gs[l] = g_pure(gb, 0, l, t, lnT);
+    Gl[l] = g_pure(gb, 1, l, t, lnT);
+    xp[l] = xs[l];
+  }
+  const double gs = gibbs<N>(xs, Gs, t);
+  const double gl = gibbs<N>(xs, Gl, t);
+  // the reference's forward difference (NCGPU.py:282-286): the last
+  // component down, the first up, one derivative for every component
+  xp[NC] -= 0.0000001;
+  xp[0] += 0.0000001;
+  const double dgl = 10000000.0 * (gibbs<N>(xp, Gl, t) - gl);
+  const double dgs = 10000000.0 * (gibbs<N>(xp, Gs, t) - gs);
   const T p = phi[i];
   const T gg = p * p * (T(1) - p) * (T(1) - p);
   const T h = p * p * p * (T(6) * p * p - T(15) * p + T(10));
@@ -107,8 +132,12 @@ __global__ void __launch_bounds__(256)
                    ? k.noise * sqrt(T(2) * T(8.314) * tt / k.v_m) * noise_normal<T>(seed, st, y, x)
                    : T(0);
   dG[i] = (T)(gs - gl);
-  Mc[i] = k.v_m * (T)x0 * (k.D_L + h * (k.D_S - k.D_L)) / (T(8.314) * tt);
-  dF[i] = (T)((dgl + (double)h * (dgs - dgl)) / (double)k.v_m) + (k.W0 - k.W1) * gg * tt + nz;
+  const T dfc = (T)((dgl + (double)h * (dgs - dgl)) / (double)k.v_m);
+#pragma unroll
+  for (int l = 0; l < NC; ++l) {
+    cp.Mc[l][i] = k.v_m * (T)xs[l] * (k.D_L + h * (k.D_S - k.D_L)) / (T(8.314) * tt);
+    cp.dF[l][i] = dfc + (k.W[l] - k.W[NC]) * gg * tt + nz;
+  }
 }
 
 template <typename T>
@@ -119,13 +148,12 @@ __device__ __forceinline__ T divagradb(T a, T axp, T axm, T ayp, T aym, T b, T b
           (a + aym) * (b - bym));
 }
 
-template <typename T>
+template <typename T, int NC>
 __global__ void __launch_bounds__(256)
     ncgpu_kernel(Geo g, Bc<T> bc, NcCoef<T> k, const T* __restrict__ phi,
-                 const T* __restrict__ q1, const T* __restrict__ q4, const T* __restrict__ c,
-                 const T* __restrict__ temp, const T* __restrict__ dG, const T* __restrict__ Mc,
-                 const T* __restrict__ dF, T* __restrict__ phi_o, T* __restrict__ q1_o,
-                 T* __restrict__ q4_o, T* __restrict__ c_o) {
+                 const T* __restrict__ q1, const T* __restrict__ q4, NcPtrs<T> cp,
+                 const T* __restrict__ temp, const T* __restrict__ dG, T* __restrict__ phi_o,
+                 T* __restrict__ q1_o, T* __restrict__ q4_o) {
   pdl_wait();
   pdl_launch_next();
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
@@ -204,9 +232,16 @@ __global__ void __launch_bounds__(256)
   ty += t * (uy * s4 * (T(4) * ux2 * ux * pxy + T(4) * ux * pxy * uy2 + T(4) * uy * pyy * ux2 +
                         T(4) * uy2 * uy * pyy));
   ty *= T(4) * k.y_e * k.ebar2;
-  const T ci = c[i];
-  const T cW = ci * k.W0 + (T(1) - ci) * k.W1;
-  const T M_phi = ci * k.M0 + (T(1) - ci) * k.M1;
+  T cW = T(0), M_phi = T(0), c_N = T(1);
+#pragma unroll
+  for (int l = 0; l < NC; ++l) {
+    const T cl = cp.c[l][i];
+    cW += cl * k.W[l];
+    M_phi += cl * k.M[l];
+    c_N -= cl;
+  }
+  cW += c_N * k.W[NC];
+  M_phi += c_N * k.M[NC];
   const T M_q = k.M_qmax + (T(1e-6) - k.M_qmax) * h;
   T dphidt = k.ebar2 * (T(1) - T(3) * k.y_e) * (t * lphi + dTx * dpx + dTy * dpy);
   dphidt += tx + ty;
@@ -214,15 +249,26 @@ __global__ void __launch_bounds__(256)
   dphidt -= gprime * t * cW;
   dphidt -= T(4) * k.H * t * ph * mgq;
   dphidt *= M_phi;
-  // c: div(M_c grad dF/dc) - div(M_c c grad dF/dc)
-  const T m0 = Mc[i], mxp = F(Mc, 0, 1), mxm = F(Mc, 0, -1), myp = F(Mc, 1, 0),
-          mym = F(Mc, -1, 0);
-  const T f0 = dF[i], fxp = F(dF, 0, 1), fxm = F(dF, 0, -1), fyp = F(dF, 1, 0),
-          fym = F(dF, -1, 0);
-  const T cxp = F(c, 0, 1), cxm = F(c, 0, -1), cyp = F(c, 1, 0), cym = F(c, -1, 0);
-  T dc = divagradb(m0, mxp, mxm, myp, mym, f0, fxp, fxm, fyp, fym, idx);
-  dc -= divagradb(m0 * ci, mxp * cxp, mxm * cxm, myp * cyp, mym * cym, f0, fxp, fxm, fyp, fym,
-                  idx);
+  // c_l: div(M_l grad dF_l) - sum_m div(M_l c_m grad dF_m)
+  T dc[NC];
+#pragma unroll
+  for (int l = 0; l < NC; ++l) {
+    const T* Mc = cp.Mc[l];
+    const T m0 = Mc[i], mxp = F(Mc, 0, 1), mxm = F(Mc, 0, -1), myp = F(Mc, 1, 0),
+            mym = F(Mc, -1, 0);
+    const T* dF = cp.dF[l];
+    T d = divagradb(m0, mxp, mxm, myp, mym, dF[i], F(dF, 0, 1), F(dF, 0, -1), F(dF, 1, 0),
+                    F(dF, -1, 0), idx);
+#pragma unroll
+    for (int mm = 0; mm < NC; ++mm) {
+      const T* c = cp.c[mm];
+      const T* dFm = cp.dF[mm];
+      d -= divagradb(m0 * c[i], mxp * F(c, 0, 1), mxm * F(c, 0, -1), myp * F(c, 1, 0),
+                     mym * F(c, -1, 0), dFm[i], F(dFm, 0, 1), F(dFm, 0, -1), F(dFm, 1, 0),
+                     F(dFm, -1, 0), idx);
+    }
+    dc[l] = d;
+  }
   // orientation
   const T Dq = T(2) * k.H * t * ph * ph;
   const T Dxp = T(2) * k.H * txp * pxp * pxp, Dxm = T(2) * k.H * txm * pxm * pxm;
@@ -246,7 +292,8 @@ __global__ void __launch_bounds__(256)
   phi_o[i] = pn;
   q1_o[i] = n1 / rn;
   q4_o[i] = n4 / rn;
-  c_o[i] = ci + k.dt * dc;
+#pragma unroll
+  for (int l = 0; l < NC; ++l) cp.c_out[l][i] = cp.c[l][i] + k.dt * dc[l];
 }
 
 template <typename T>
@@ -258,7 +305,11 @@ int32_t ncgpu_step(const PpfNcgpuParams* p, const PpfGrid* grid, const PpfBounda
   Geo g;
   int32_t rc = make_geo(grid, 2, 2, &g);
   if (rc) return rc;
-  for (int f = 0; f < 4; ++f)
+  const int ncomp = p->ncomp;
+  if (ncomp < 2 || ncomp > kMaxComp)
+    return fail(PPF_ERR_UNSUPPORTED, "NCGPU: 2 or 3 components (got %d)", ncomp);
+  const int nc = ncomp - 1;
+  for (int f = 0; f < 3 + nc; ++f)
     if (!in[f] || !out[f]) return fail(PPF_ERR_INVALID, "NULL field pointer");
   if (!temp || !transfer) return fail(PPF_ERR_INVALID, "NULL temperature or transfer buffer");
   if (g.n[0] > 65535) return fail(PPF_ERR_INVALID, "more than 65535 rows");
@@ -274,8 +325,8 @@ int32_t ncgpu_step(const PpfNcgpuParams* p, const PpfGrid* grid, const PpfBounda
         return fail(PPF_ERR_UNSUPPORTED, "NCGPU: Neumann boundaries with zero gradient only");
   }
   for (int ph = 0; ph < 2; ++ph)
-    for (int cp = 0; cp < 2; ++cp)
-      if (p->npieces[ph][cp] < 0 || p->npieces[ph][cp] > 4)
+    for (int c = 0; c < ncomp; ++c)
+      if (p->npieces[ph][c] < 0 || p->npieces[ph][c] > 4)
         return fail(PPF_ERR_INVALID, "npieces must be 0..4");
   NcCoef<T> k;
   k.idx = (T)(1.0 / p->dx);
@@ -290,25 +341,36 @@ int32_t ncgpu_step(const PpfNcgpuParams* p, const PpfGrid* grid, const PpfBounda
   k.ebar2 = (T)p->ebar2;
   k.eqbar2 = (T)(0.25 * p->ebar2);
   k.noise = (T)p->noise_scale;
-  k.W0 = (T)p->W[0];
-  k.W1 = (T)p->W[1];
-  k.M0 = (T)p->M[0];
-  k.M1 = (T)p->M[1];
+  for (int c = 0; c < kMaxComp; ++c) {
+    k.W[c] = (T)p->W[c];
+    k.M[c] = (T)p->M[c];
+  }
   NcGibbs gb;
   static_assert(sizeof(gb.piece) == sizeof(p->gibbs), "Gibbs table layout");
   memcpy(gb.piece, p->gibbs, sizeof(gb.piece));
   memcpy(gb.npieces, p->npieces, sizeof(gb.npieces));
   const int64_t fsz = (int64_t)g.n[0] * g.pitch;
+  NcPtrs<T> cp{};
+  for (int l = 0; l < nc; ++l) {
+    cp.c[l] = in[3 + l];
+    cp.c_out[l] = out[3 + l];
+    cp.Mc[l] = transfer + (1 + l) * fsz;
+    cp.dF[l] = transfer + (1 + nc + l) * fsz;
+  }
   T* dG = transfer;
-  T* Mc = transfer + fsz;
-  T* dF = transfer + 2 * fsz;
   cudaStream_t st = (cudaStream_t)stream;
   const dim3 grid2((g.n[1] + 255) / 256, g.n[0]);
-  PPF_TRY_CUDA(launch(ncgpu_thermo_kernel<T>, grid2, dim3(256), 0, st, true, g, k, gb, in[0],
-                      in[3], temp, dG, Mc, dF, seed, step, step_base));
-  PPF_TRY_CUDA(launch(ncgpu_kernel<T>, grid2, dim3(256), 0, st, true, g, bc, k, in[0], in[1],
-                      in[2], in[3], temp, (const T*)dG, (const T*)Mc, (const T*)dF, out[0],
-                      out[1], out[2], out[3]));
+  if (nc == 1) {
+    PPF_TRY_CUDA(launch(ncgpu_thermo_kernel<T, 1>, grid2, dim3(256), 0, st, true, g, k, gb,
+                        in[0], cp, temp, dG, seed, step, step_base));
+    PPF_TRY_CUDA(launch(ncgpu_kernel<T, 1>, grid2, dim3(256), 0, st, true, g, bc, k, in[0], in[1],
+                        in[2], cp, temp, (const T*)dG, out[0], out[1], out[2]));
+  } else {
+    PPF_TRY_CUDA(launch(ncgpu_thermo_kernel<T, 2>, grid2, dim3(256), 0, st, true, g, k, gb,
+                        in[0], cp, temp, dG, seed, step, step_base));
+    PPF_TRY_CUDA(launch(ncgpu_kernel<T, 2>, grid2, dim3(256), 0, st, true, g, bc, k, in[0], in[1],
+                        in[2], cp, temp, (const T*)dG, out[0], out[1], out[2]));
+  }
   return PPF_OK;
 }
 

@@ -1,10 +1,11 @@
 """NCGPUGB300: the reference's NCGPU engine (Engines/NCGPU.py:329-532) on the
-CUDA library: binary alloy solidification with a phase field, two quaternion
-orientation fields and the first component's fraction, thermodynamics from
-a TDB file (read by pyphasefield_gb300.tdb instead of pycalphad).
+CUDA library: alloy solidification (2 or 3 components) with a phase field,
+two quaternion orientation fields and the fractions of all but the last
+component, thermodynamics from a TDB file (read by pyphasefield_gb300.tdb
+instead of pycalphad).
 
-Fields, in the reference's order: phi (1 = solid), q1, q4, c_<first
-component>. user_data keys as the reference: d_ratio (4), sim_type ("seed"
+Fields, in the reference's order: phi (1 = solid), q1, q4, c_<component> for
+every component but the last (sorted). user_data keys as the reference: d_ratio (4), sim_type ("seed"
 places one seed at the centre; anything else leaves the melt), melt_angle,
 seed_angle, initial_concentration_array; added: seed (noise stream),
 noise_scale (1 = the reference's Langevin term on dF/dc, 0 = none).
@@ -36,8 +37,8 @@ def ncgpu_parameters(db: Database, dx: float, d_ratio: float = 4.0) -> dict:
     <COMP>_L / _TM / _S / _B functions, the derived W and M, and the scalar
     functions D_S, D_L, V_M, M_Q, H, Y_E."""
     comps = db.elements
-    if len(comps) != 2:
-        raise NotImplementedError(f"NCGPU: binary systems only (the TDB lists {comps})")
+    if len(comps) not in (2, 3):
+        raise NotImplementedError(f"NCGPU: 2 or 3 components (the TDB lists {comps})")
     d = dx * d_ratio
     ud = {"d": d, "R": 8.314}
     for key, fn in (("L", "_L"), ("T_M", "_TM"), ("S", "_S"), ("B", "_B")):
@@ -57,12 +58,12 @@ def ncgpu_parameters(db: Database, dx: float, d_ratio: float = 4.0) -> dict:
 
 
 def gibbs_table(db: Database):
-    """(gibbs[2][2][4][10], npieces[2][2]) for PpfNcgpuParams: phase 0 the
+    """(gibbs[2][3][4][10], npieces[2][3]) for PpfNcgpuParams: phase 0 the
     solid (first phase in sorted order), 1 the liquid; components sorted."""
     if len(db.phases) != 2:
         raise NotImplementedError(f"NCGPU: two phases expected (the TDB lists {db.phases})")
-    table = np.zeros((2, 2, 4, 10))
-    npieces = np.zeros((2, 2), dtype=np.int32)
+    table = np.zeros((2, 3, 4, 10))
+    npieces = np.zeros((2, 3), dtype=np.int32)
     for ph, phase in enumerate(db.phases):
         for cp, comp in enumerate(db.elements):
             pieces = db.params.get((phase, comp))
@@ -117,6 +118,8 @@ class _NcgpuMixin(GB300Engine):
                                                float(self.user_data["d_ratio"])))
         self._tdb_components = list(self._ppf_db.elements)
         self._tdb_phases = list(self._ppf_db.phases)
+        # phi, q1, q4 and all but the last component's fraction
+        self.NFIELDS = 2 + len(self._tdb_components)
         self.dt = self.user_data["dt"]  # set_time_step_length (:367)
 
     def init_fields(self):
@@ -137,8 +140,11 @@ class _NcgpuMixin(GB300Engine):
         self.add_field(q1, "q1")
         self.add_field(q4, "q4")
         c0 = ud.get("initial_concentration_array")
-        val = float(c0[0]) if c0 is not None else 1.0 / len(comps)
-        self.add_field(np.full(dim, val), "c_" + comps[0])
+        if c0 is not None and len(c0) + 1 != len(comps):
+            raise ValueError(f"initial_concentration_array needs {len(comps) - 1} values")
+        for j in range(len(comps) - 1):
+            val = float(c0[j]) if c0 is not None else 1.0 / len(comps)
+            self.add_field(np.full(dim, val), "c_" + comps[j])
 
     def _ppf_prepare(self):
         t = self._temperature_type
@@ -154,7 +160,8 @@ class _NcgpuMixin(GB300Engine):
         super()._ppf_setup()
         g = self._ppf_grid
         self._nc_temp = g.empty()
-        self._nc_transfer = torch.zeros((3,) + tuple(g.alloc_shape), dtype=g.dtype,
+        ncomp = len(self._tdb_components)
+        self._nc_transfer = torch.zeros((2 * ncomp - 1,) + tuple(g.alloc_shape), dtype=g.dtype,
                                         device=g.device)
         # the pinned staging copy must outlive the asynchronous upload
         self._nc_temp_staging = self._ppf_grid.upload(self._nc_temp, self.temperature.get_cells(),
@@ -167,20 +174,21 @@ class _NcgpuMixin(GB300Engine):
         p.dx = float(self.dx)
         p.ebar2 = float(ud["ebar"]) ** 2
         p.noise_scale = float(ud.get("noise_scale", 1.0))
-        for j in range(2):
+        p.ncomp = ncomp
+        for j in range(ncomp):
             p.W[j] = float(ud["W"][j])
             p.M[j] = float(ud["M"][j])
-        flat = table.reshape(-1)
-        for k in range(flat.size):
-            p.gibbs[k // 80][(k // 40) % 2][(k // 10) % 4][k % 10] = float(flat[k])
         for ph in range(2):
-            for cp in range(2):
+            for cp in range(3):
                 p.npieces[ph][cp] = int(npieces[ph, cp])
+                for k in range(4):
+                    for e in range(10):
+                        p.gibbs[ph][cp][k][e] = float(table[ph, cp, k, e])
         self._nc_params = p
 
     def _ppf_step(self, src, dst, depth, step, step_base, sp):
-        fin = (C.c_void_p * 4)(*[ptr(t) for t in src])
-        fout = (C.c_void_p * 4)(*[ptr(t) for t in dst])
+        fin = (C.c_void_p * len(src))(*[ptr(t) for t in src])
+        fout = (C.c_void_p * len(dst))(*[ptr(t) for t in dst])
         L.call(f"ppf_ncgpu_step_{_F[self._ppf_dtype]}", C.byref(self._nc_params),
                C.byref(self._ppf_grid.grid), C.byref(self._ppf_bc), fin, fout,
                ptr(self._nc_temp), ptr(self._nc_transfer), C.c_uint64(int(self.user_data["seed"])),

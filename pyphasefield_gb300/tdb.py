@@ -66,6 +66,11 @@ def _term(term: str, functions: dict) -> tuple[dict, tuple | None]:
             power += int(f[2:].strip("()"))
         elif re.fullmatch(_NUM, f):
             coef *= float(f)
+        elif "/" in f and all(re.fullmatch(_NUM, q) for q in f.split("/")):
+            q = f.split("/")
+            coef *= float(q[0])
+            for den in q[1:]:
+                coef /= float(den)
         else:
             raise TdbError(f"unsupported TDB term {term!r}")
     if has_ln:

@@ -175,6 +175,23 @@ def main():
         save(name, meta, phi0=phi0, q10=q10, q40=q40, c0=c0, phi=out[0], q1=out[1], q4=out[2],
              c=out[3])
 
+    # NCGPU with three components (the reference's tests/Ni-Cu-Al_Ideal.tdb)
+    tdb3_path = refshim.reference_root() / "pyphasefield" / "tests" / "Ni-Cu-Al_Ideal.tdb"
+    write_tdb(ncgpu_ref.Tdb(tdb3_path), HERE / "ncgpu_nicual.tdb")
+    tdb3 = ncgpu_ref.Tdb(HERE / "ncgpu_nicual.tdb")
+    shape = (18, 16)
+    p3 = ncgpu_ref.tdb_params(tdb3, 4.6e-6)
+    phi0, q10, q40, ca, cb = ncgpu_ref.seed_fields(shape, c0=[0.05, 0.4], ncomp=3)
+    ca = ca + nrng.uniform(-1e-3, 1e-3, shape)
+    cb = cb + nrng.uniform(-1e-3, 1e-3, shape)
+    T = np.full(shape, 1574.0)
+    noise = [ncgpu_ref.noise_normal(5, s, shape) for s in range(3)]
+    out = refshim.run_ncgpu(phi0, q10, q40, [ca, cb], T, 3, p3, tdb3, noise, "PERIODIC")
+    meta = dict(model="ncgpu", steps=3, bc="PERIODIC", seed=5, dx=4.6e-6, T=1574.0,
+                tdb="ncgpu_nicual.tdb")
+    save("ncgpu_ternary", meta, phi0=phi0, q10=q10, q40=q40, c0_0=ca, c0_1=cb, phi=out[0],
+         q1=out[1], q4=out[2], c_0=out[3], c_1=out[4])
+
     dx = 4.6e-8
     prm = dict(restate.WARREN_DEFAULTS)
     for name, shape, center, r, bc, steps, alpha, seed in [

@@ -22,11 +22,11 @@ TDB = GOLDEN / "ncgpu_nicu.tdb"
 TOL = {"fp64": 1e-8, "fp32": 1e-5}
 
 
-def params_struct(dx, noise_scale=1.0):
+def params_struct(dx, noise_scale=1.0, tdb=TDB):
     from pyphasefield_gb300 import _lib as L
     from pyphasefield_gb300.engines.ncgpu import gibbs_table, ncgpu_parameters
     from pyphasefield_gb300.tdb import Database
-    db = Database(TDB)
+    db = Database(tdb)
     ud = ncgpu_parameters(db, dx)
     table, npieces = gibbs_table(db)
     p = L.PpfNcgpuParams()
@@ -35,10 +35,11 @@ def params_struct(dx, noise_scale=1.0):
     p.dx = dx
     p.ebar2 = float(ud["ebar"]) ** 2
     p.noise_scale = noise_scale
-    for j in range(2):
+    p.ncomp = len(db.elements)
+    for j in range(p.ncomp):
         p.W[j], p.M[j] = ud["W"][j], ud["M"][j]
     for ph in range(2):
-        for cp in range(2):
+        for cp in range(3):
             p.npieces[ph][cp] = int(npieces[ph, cp])
             for k in range(4):
                 for e in range(10):
@@ -46,7 +47,7 @@ def params_struct(dx, noise_scale=1.0):
     return p
 
 
-def run_gpu(fields, T, steps, dx, seed, bc, precision, noise_scale=1.0):
+def run_gpu(fields, T, steps, dx, seed, bc, precision, noise_scale=1.0, tdb=TDB):
     import torch
     from pyphasefield_gb300 import _lib as L
     shape = fields[0].shape
@@ -55,13 +56,13 @@ def run_gpu(fields, T, steps, dx, seed, bc, precision, noise_scale=1.0):
     a = [to_dev(f, kshape, pitch, dtype, "cuda") for f in fields]
     o = [torch.zeros_like(t) for t in a]
     temp = to_dev(T, kshape, pitch, dtype, "cuda")
-    transfer = torch.zeros((3,) + tuple(a[0].shape), dtype=dtype, device="cuda")
-    p = params_struct(dx, noise_scale)
+    transfer = torch.zeros((2 * len(fields) - 5,) + tuple(a[0].shape), dtype=dtype, device="cuda")
+    p = params_struct(dx, noise_scale, tdb)
     sfx = "f64" if precision == "fp64" else "f32"
     s = C.c_void_p(torch.cuda.current_stream().cuda_stream)
     for k in range(steps):
-        fin = (C.c_void_p * 4)(*[t.data_ptr() for t in a])
-        fout = (C.c_void_p * 4)(*[t.data_ptr() for t in o])
+        fin = (C.c_void_p * len(a))(*[t.data_ptr() for t in a])
+        fout = (C.c_void_p * len(o))(*[t.data_ptr() for t in o])
         L.call(f"ppf_ncgpu_step_{sfx}", C.byref(p), C.byref(g), C.byref(b), fin, fout,
                C.c_void_p(temp.data_ptr()), C.c_void_p(transfer.data_ptr()), C.c_uint64(seed),
                C.c_uint64(k), None, s)
@@ -113,6 +114,18 @@ def test_gradient_run_against_oracle(cuda, gradient_case, precision, steps, tol)
     out = run_gpu(fields, T, steps, 4.6e-6, 5, "NEUMANN", precision)
     for got, r, key in zip(out, ref[steps], ("phi", "q1", "q4", "c")):
         assert rel_l2(got, r) < tol, (key, rel_l2(got, r))
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_ternary_reference_fixture(cuda, precision):
+    """Ni-Cu-Al (three components, two concentration fields)."""
+    z = np.load(GOLDEN / "ncgpu_ternary.npz")
+    m = json.loads(str(z["meta"]))
+    T = np.full(z["phi0"].shape, m["T"])
+    f = [z["phi0"], z["q10"], z["q40"], z["c0_0"], z["c0_1"]]
+    out = run_gpu(f, T, m["steps"], m["dx"], m["seed"], m["bc"], precision, tdb=GOLDEN / m["tdb"])
+    for got, key in zip(out, ("phi", "q1", "q4", "c_0", "c_1")):
+        assert rel_l2(got, z[key]) < TOL[precision], (key, rel_l2(got, z[key]))
 
 
 def test_noise_off_is_deterministic_and_noise_on_is_not(cuda):

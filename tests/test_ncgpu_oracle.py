@@ -45,7 +45,8 @@ def test_tdb_reader_matches_oracle_evaluation():
                     mine = g_eval(c, T)
             assert mine == pytest.approx(tdb.g_pure(ph, comp, T), rel=1e-13, abs=1e-9)
     table, npieces = gibbs_table(db)
-    assert table.shape == (2, 2, 4, 10) and (npieces == 2).all()
+    assert table.shape == (2, 3, 4, 10)
+    assert (npieces[:, :2] == 2).all() and (npieces[:, 2] == 0).all()
 
 
 def test_parameters_match_oracle():
@@ -73,3 +74,35 @@ def test_seed_matches_oracle(shape):
 def test_noise_is_standard_normal():
     z = N.noise_normal(3, 5, (300, 400))
     assert abs(z.mean()) < 0.01 and abs(z.std() - 1) < 0.01
+
+
+def test_ternary_oracle_matches_reference_kernels():
+    z = np.load(GOLDEN / "ncgpu_ternary.npz")
+    m = json.loads(str(z["meta"]))
+    tdb = N.Tdb(GOLDEN / m["tdb"])
+    p = N.tdb_params(tdb, m["dx"])
+    T = np.full(z["phi0"].shape, m["T"])
+    out = N.run([z["phi0"], z["q10"], z["q40"], z["c0_0"], z["c0_1"]], T, m["steps"], p, tdb,
+                seed=m["seed"], bc=m["bc"])
+    for got, key, tol in zip(out, ("phi", "q1", "q4", "c_0", "c_1"),
+                             (1e-10, 1e-12, 1e-12, 1e-8, 1e-8)):
+        ref = z[key]
+        assert np.abs(got - ref).max() <= tol * max(1.0, np.abs(ref).max()), key
+
+
+def test_ternary_tdb_reader():
+    path = GOLDEN / "ncgpu_nicual.tdb"
+    db, tdb = Database(path), N.Tdb(path)
+    assert db.elements == ["AL", "CU", "NI"]
+    assert db.scalar("M_Q") == pytest.approx(80000000 / 1574.0)
+    for (ph, comp), pieces in db.params.items():
+        for T in (500.0, 700.0, 800.0, 933.47, 1574.0):
+            mine = 0.0
+            for lo, hi, c in pieces:
+                if lo <= T < hi:
+                    mine = g_eval(c, T)
+            assert mine == pytest.approx(tdb.g_pure(ph, comp, T), rel=1e-13, abs=1e-9)
+    mine = ncgpu_parameters(db, 4.6e-6)
+    ref = N.tdb_params(tdb, 4.6e-6)
+    np.testing.assert_allclose(mine["W"], ref["W"], rtol=1e-14)
+    assert mine["ebar"] == pytest.approx(ref["ebar"], rel=1e-14)
