@@ -636,6 +636,7 @@ def profile_case(name: str):
                 3 steps: line solves along x and y
     acadi4096   semi-implicit ADI Allen-Cahn 2-D 4096^2, dt = 1, 3 steps: variable-diagonal
                 line solves along x and y
+    ncgpu1024   NCGPU Ni-Cu 1024^2 (precision from PPF_PRECISION, default fp64), 5 steps
     """
     import torch
     from pyphasefield_gb300 import CahnHilliardGB300, DiffusionGB300
@@ -683,6 +684,16 @@ def profile_case(name: str):
         sim.initialize_fields_and_imported_data()
         sim.fields[0].data[1:-1, 1:-1] = rng.random((4096, 4096))
         sim.simulate(3)
+    elif name == "ncgpu1024":
+        from pyphasefield_gb300 import NCGPUGB300
+        sim = NCGPUGB300(dimensions=[1024, 1024], dx=4.6e-6, tdb_path=str(NCGPU_TDB),
+                         temperature_type="ISOTHERMAL", initial_T=1574.0,
+                         boundary_conditions="PERIODIC",
+                         user_data={"use_graph": False, "sim_type": "seed",
+                                    "initial_concentration_array": [0.40831],
+                                    "precision": os.environ.get("PPF_PRECISION", "fp64")})
+        sim.initialize_fields_and_imported_data()
+        sim.simulate(5)
     elif name == "diff3d384":
         sim = DiffusionGB300(dimensions=[384, 384, 384], dx=1.0, dt=0.1,
                              boundary_conditions="PERIODIC", user_data={"D": 1.0, "use_graph": False})

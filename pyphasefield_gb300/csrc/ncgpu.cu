@@ -59,20 +59,6 @@ __device__ __forceinline__ double g_pure(const NcGibbs& g, int ph, int comp, dou
   return 0.0;  // outside every range, as a piecewise TDB function gives
 }
 
-// Molar Gibbs energy of a phase at fractions x[0 .. N-1] (the last one passed
-// apart, as the reference's perturbed argument is), pycalphad's ideal
-// solution: sum x_i G_i + R T sum x_i ln x_i.
-template <int N>
-__device__ __forceinline__ double gibbs(const double (&x)[N], const double (&G)[N], double T) {
-  double g = 0.0, mix = 0.0;
-#pragma unroll
-  for (int i = 0; i < N; ++i) {
-    g += x[i] * G[i];
-    if (x[i] > 0) mix += x[i] * log(x[i]);
-  }
-  return g + 8.3145 * T * mix;
-}
-
 // N(0,1) of cell (row, col) at a step: Box-Muller on two uniforms from a
 // Philox4x32-10 block (counter (col / 2, row, step), key seed ^ 0x5eed0000),
 // pair col % 2.
@@ -82,9 +68,10 @@ __device__ __forceinline__ T noise_normal(uint64_t seed, uint64_t step, int row,
                                 (uint32_t)(step >> 32)},
                              (uint32_t)seed ^ 0x5EED0000u, (uint32_t)(seed >> 32));
   const uint32_t a = (col & 1) ? w.z : w.x, b = (col & 1) ? w.w : w.y;
-  const double u1 = ((double)(a >> 8) + 0.5) * (1.0 / 16777216.0);
-  const double u2 = (double)(b >> 8) * (1.0 / 16777216.0);
-  return (T)(sqrt(-2.0 * log(u1)) * cospi(2.0 * u2));
+  // the uniforms are exact in either precision
+  const T u1 = ((T)(a >> 8) + T(0.5)) * (T(1) / T(16777216));
+  const T u2 = (T)(b >> 8) * (T(1) / T(16777216));
+  return sqrt(T(-2) * log(u1)) * cospi(T(2) * u2);
 }
 
 template <typename T, int NC>
@@ -116,14 +103,27 @@ __global__ void __launch_bounds__(256)
     Gl[l] = g_pure(gb, 1, l, t, lnT);
     xp[l] = xs[l];
   }
-  const double gs = gibbs<N>(xs, Gs, t);
-  const double gl = gibbs<N>(xs, Gl, t);
   // the reference's forward difference (NCGPU.py:282-286): the last
-  // component down, the first up, one derivative for every component
+  // component down, the first up, one derivative for every component, as the
+  // difference of the two molar Gibbs energies. The ideal mixing term is the
+  // same in both phases, so it is evaluated once at each composition.
   xp[NC] -= 0.0000001;
   xp[0] += 0.0000001;
-  const double dgl = 10000000.0 * (gibbs<N>(xp, Gl, t) - gl);
-  const double dgs = 10000000.0 * (gibbs<N>(xp, Gs, t) - gs);
+  double mix = 0.0, mixp = 0.0, lin_s = 0.0, lin_l = 0.0, linp_s = 0.0, linp_l = 0.0;
+#pragma unroll
+  for (int l = 0; l < N; ++l) {
+    if (xs[l] > 0) mix += xs[l] * log(xs[l]);
+    if (xp[l] > 0) mixp += xp[l] * log(xp[l]);
+    lin_s += xs[l] * Gs[l];
+    lin_l += xs[l] * Gl[l];
+    linp_s += xp[l] * Gs[l];
+    linp_l += xp[l] * Gl[l];
+  }
+  const double rt = 8.3145 * t;
+  const double gs = lin_s + rt * mix;
+  const double gl = lin_l + rt * mix;
+  const double dgl = 10000000.0 * ((linp_l + rt * mixp) - gl);
+  const double dgs = 10000000.0 * ((linp_s + rt * mixp) - gs);
   const T p = phi[i];
   const T gg = p * p * (T(1) - p) * (T(1) - p);
   const T h = p * p * p * (T(6) * p * p - T(15) * p + T(10));
@@ -273,10 +273,11 @@ __global__ void __launch_bounds__(256)
   const T Dq = T(2) * k.H * t * ph * ph;
   const T Dxp = T(2) * k.H * txp * pxp * pxp, Dxm = T(2) * k.H * txm * pxm * pxm;
   const T Dyp = T(2) * k.H * typ * pyp * pyp, Dym = T(2) * k.H * tym * pym * pym;
+  const T rxp = (Dq + Dxp) / gxp, rxm = (Dq + Dxm) / gxm;
+  const T ryp = (Dq + Dyp) / gyp, rym = (Dq + Dym) / gym;
   auto fori = [&](T q, T qxp, T qxm, T qyp, T qym) {
     return T(0.5) * idx * idx *
-           ((Dq + Dxp) * (qxp - q) / gxp - (Dq + Dxm) * (q - qxm) / gxm +
-            (Dq + Dyp) * (qyp - q) / gyp - (Dq + Dym) * (q - qym) / gym);
+           (rxp * (qxp - q) - rxm * (q - qxm) + ryp * (qyp - q) - rym * (q - qym));
   };
   const T f1 = fori(a1, q1xp, q1xm, q1yp, q1ym);
   const T f4 = fori(a4, q4xp, q4xm, q4yp, q4ym);
@@ -288,10 +289,10 @@ __global__ void __launch_bounds__(256)
   pn = pn < T(0.000001) ? T(0.000001) : pn;
   pn = pn > T(0.999999) ? T(0.999999) : pn;
   const T n1 = a1 + k.dt * dq1, n4 = a4 + k.dt * dq4;
-  const T rn = sqrt(n1 * n1 + n4 * n4);
+  const T irn = T(1) / sqrt(n1 * n1 + n4 * n4);
   phi_o[i] = pn;
-  q1_o[i] = n1 / rn;
-  q4_o[i] = n4 / rn;
+  q1_o[i] = n1 * irn;
+  q4_o[i] = n4 * irn;
 #pragma unroll
   for (int l = 0; l < NC; ++l) cp.c_out[l][i] = cp.c[l][i] + k.dt * dc[l];
 }
