@@ -5,7 +5,6 @@ host logic a multi-GPU run relies on."""
 import os
 import socket
 
-import pytest
 import torch
 import torch.distributed as dist
 import torch.multiprocessing as mp
