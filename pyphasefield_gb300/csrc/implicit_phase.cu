@@ -234,15 +234,8 @@ __global__ void __launch_bounds__(kPThreads)
 // w_first = v_last. Thomas with the Sherman-Morrison correction for the
 // corners (m >= 3), a direct solve for m <= 2. Writes sep_s to record slot 7
 // and uses slots 5-6 as scratch.
-template <typename T>
-__global__ void __launch_bounds__(kPThreads)
-    part_reduce(PLines L, T a, T* __restrict__ rec) {
-  pdl_wait();
-  pdl_launch_next();
-  const int line = blockIdx.x * blockDim.x + threadIdx.x;
-  if (line >= L.nlines) return;
-  const int m = L.nseg;
-  auto R = [&](int s) -> T* { return rec + ((int64_t)s * L.nlines + line) * kRec; };
+template <typename T, typename Rec>
+__device__ __forceinline__ void reduce_line(const Rec& R, int m, T a) {
   // coefficients of separator s (needs records s and s+1)
   auto coef = [&](int s, T& lo, T& di, T& up, T& rhs) {
     const T* r0 = R(s);
@@ -347,6 +340,45 @@ __global__ void __launch_bounds__(kPThreads)
     T* r = R(s);
     r[7] = r[6] - fac * r[7];
   }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kPThreads)
+    part_reduce(PLines L, T a, T* __restrict__ rec) {
+  pdl_wait();
+  pdl_launch_next();
+  const int line = blockIdx.x * blockDim.x + threadIdx.x;
+  if (line >= L.nlines) return;
+  reduce_line([&](int s) -> T* { return rec + ((int64_t)s * L.nlines + line) * kRec; },
+              L.nseg, a);
+}
+
+// The same with a warp's 32 lines staged in shared memory: the records are
+// read once, coalesced (each s: 32 consecutive lines), and the sequential
+// sweeps run on shared memory (records padded to 9 values: no bank
+// conflicts between the lanes). Used while m * 32 * 9 values fit.
+constexpr int kRecS = 9;
+
+template <typename T>
+__global__ void __launch_bounds__(32)
+    part_reduce_smem(PLines L, T a, T* __restrict__ rec) {
+  pdl_wait();
+  pdl_launch_next();
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* sm = reinterpret_cast<T*>(smem_raw);
+  const int lane = threadIdx.x;
+  const int line = blockIdx.x * 32 + lane;
+  if (line >= L.nlines) return;  // each lane works on its own records only
+  const int m = L.nseg;
+  for (int s = 0; s < m; ++s) {
+    const T* g = rec + ((int64_t)s * L.nlines + line) * kRec;
+    T* d = sm + ((int64_t)s * 32 + lane) * kRecS;
+#pragma unroll
+    for (int k = 0; k < 7; ++k) d[k] = g[k];
+  }
+  reduce_line([&](int s) -> T* { return sm + ((int64_t)s * 32 + lane) * kRecS; }, m, a);
+  for (int s = 0; s < m; ++s)
+    rec[((int64_t)s * L.nlines + line) * kRec + 7] = sm[((int64_t)s * 32 + lane) * kRecS + 7];
 }
 
 // Pass 3: the interior block with its true separators, then the line.
@@ -455,8 +487,19 @@ int32_t var_sweep(const Geo& g, int axis, double a, double dbase, double dc, con
   const dim3 grid((unsigned)((threads + kPThreads - 1) / kPThreads));
   PPF_TRY_CUDA(launch(part_sums<T>, grid, dim3(kPThreads), 0, st, true, L, k, in, rec));
   // one warp per block: the lines' sequential sweeps spread over every SM
-  PPF_TRY_CUDA(launch(part_reduce<T>, dim3((L.nlines + 31) / 32), dim3(32), 0, st, true, L,
-                      (T)a, rec));
+  const size_t sm_bytes = (size_t)L.nseg * 32 * kRecS * sizeof(T);
+  if (sm_bytes <= 200 * 1024) {
+    static bool attr_set[2] = {false, false};
+    if (!attr_set[sizeof(T) == 8]) {
+      PPF_TRY_CUDA(allow_smem(part_reduce_smem<T>, 200 * 1024));
+      attr_set[sizeof(T) == 8] = true;
+    }
+    PPF_TRY_CUDA(launch(part_reduce_smem<T>, dim3((L.nlines + 31) / 32), dim3(32), sm_bytes, st,
+                        true, L, (T)a, rec));
+  } else {
+    PPF_TRY_CUDA(launch(part_reduce<T>, dim3((L.nlines + 31) / 32), dim3(32), 0, st, true, L,
+                        (T)a, rec));
+  }
   PPF_TRY_CUDA(launch(part_solve<T>, grid, dim3(kPThreads), 0, st, true, L, k, in,
                       (const T*)rec, out));
   return PPF_OK;
