@@ -439,8 +439,10 @@ class _Warren1995Mixin(GB300Engine):
 
 
 def make_engines(base=Simulation) -> dict:
-    """Build the four engine classes on `base` (any class with the reference
-    Simulation interface). Returns {name: class}."""
+    """Build the engine classes on `base` (any class with the reference
+    Simulation interface): Diffusion, CahnAllen (= AllenCahn), CahnHilliard,
+    Warren1995 and NCGPU. Returns {name: class}."""
+    from .ncgpu import make_ncgpu
     out = {}
     for name, mix in (("DiffusionGB300", _DiffusionMixin), ("CahnAllenGB300", _CahnAllenMixin),
                       ("CahnHilliardGB300", _CahnHilliardMixin),
@@ -448,6 +450,7 @@ def make_engines(base=Simulation) -> dict:
         out[name] = type(name, (mix, base), {"__module__": __name__,
                                             "__doc__": mix.__doc__})
     out["AllenCahnGB300"] = out["CahnAllenGB300"]
+    out["NCGPUGB300"] = make_ncgpu(base)
     return out
 
 

@@ -79,6 +79,20 @@ def test_begun_simulation_runs_setup_once():
     assert Counting.calls == 1 and s.time_step_counter == 5
 
 
+def test_make_engines_builds_every_engine_on_a_given_base():
+    from pyphasefield_gb300 import Simulation, make_engines
+
+    class Host(Simulation):
+        pass
+
+    eng = make_engines(Host)
+    assert sorted(eng) == ["AllenCahnGB300", "CahnAllenGB300", "CahnHilliardGB300",
+                           "DiffusionGB300", "NCGPUGB300", "Warren1995GB300"]
+    assert eng["AllenCahnGB300"] is eng["CahnAllenGB300"]
+    for cls in eng.values():
+        assert issubclass(cls, Host)
+
+
 def test_boundary_struct_from_simulation():
     from pyphasefield_gb300 import DiffusionGB300
     from pyphasefield_gb300.device import DeviceGrid, boundary_struct
