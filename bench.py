@@ -393,6 +393,10 @@ SWEEP = {
     # default) and float32
     "ncgpu_2048": ("ncgpu", (2048, 2048), 1, 100, {"precision": "fp64"}),
     "ncgpu_2048_fp32": ("ncgpu", (2048, 2048), 1, 100, {"precision": "fp32"}),
+    # six components (Ni-Cu-Al and three pseudo-elements): five concentration fields
+    "ncgpu_6comp_2048": ("ncgpu", (2048, 2048), 1, 50,
+                         {"precision": "fp64", "tdb": "ncgpu_6comp.tdb",
+                          "c0": [0.05, 0.2, 0.3, 0.1, 0.15]}),
 }
 SWEEP_B_ALG = {"diffusion": 8, "allen_cahn": 8, "cahn_hilliard": 8, "warren1995": 16}
 NCGPU_TDB = ROOT / "tests" / "golden" / "ncgpu_nicu.tdb"
@@ -420,10 +424,12 @@ def sweep_engine(model, grid, depth, steps, rng, extra=None):
         init = [0.5 + rng.uniform(-0.05, 0.05, grid)]
     elif model == "ncgpu":
         from pyphasefield_gb300 import NCGPUGB300
-        sim = NCGPUGB300(dimensions=list(grid), dx=4.6e-6, tdb_path=str(NCGPU_TDB),
+        tdb = NCGPU_TDB.parent / ud.pop("tdb", NCGPU_TDB.name)
+        c0 = ud.pop("c0", [0.40831])
+        sim = NCGPUGB300(dimensions=list(grid), dx=4.6e-6, tdb_path=str(tdb),
                          temperature_type="ISOTHERMAL", initial_T=1574.0,
                          boundary_conditions="PERIODIC",
-                         user_data=dict(ud, sim_type="seed", initial_concentration_array=[0.40831],
+                         user_data=dict(ud, sim_type="seed", initial_concentration_array=c0,
                                         seed=SEED))
         sim.initialize_fields_and_imported_data()
         return sim
@@ -446,8 +452,9 @@ def sweep_bytes_per_cell(model, sim) -> int:
     right-hand side read, the new iterate written: 16 B in float)."""
     ud = sim.user_data
     if model == "ncgpu":
-        # phi, q1, q4, c read and written, the temperature read
-        return 9 * (8 if ud.get("precision", "fp64") == "fp64" else 4)
+        # phi, q1, q4 and every concentration field read and written, the
+        # temperature read
+        return (2 * len(sim.fields) + 1) * (8 if ud.get("precision", "fp64") == "fp64" else 4)
     if model in ("diffusion", "allen_cahn") and ud.get("solver", "explicit") != "explicit":
         if ud.get("adi") or len(sim.dimensions) == 1:
             return 8 * len(sim.dimensions)

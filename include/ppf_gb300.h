@@ -324,7 +324,7 @@ int32_t ppf_var_line_solve_f64(const PpfGrid* g, int32_t axis, double alpha, dou
 /* ---- NCGPU (multi-component solidification with orientation) ----------- */
 
 /* One step of the NCGPU engine (Engines/NCGPU.py:37-303, simulation_loop
- * :499-532), 2 or 3 components (ncomp), 2-D: fields phi, q1, q4 and the
+ * :499-532), 2 to PPF_NCGPU_MAX_COMP components (ncomp), 2-D: fields phi, q1, q4 and the
  * fractions c_1 .. c_{ncomp-1} of all but the last component (the last is
  * 1 - sum c), 3 + ncomp - 1 pointers in fields_in / fields_out. Parameters as
  * NCGPU.init_tdb_params derives them (:336-373): ebar2 = 6 sqrt(2) S[1] d /
@@ -332,7 +332,7 @@ int32_t ppf_var_line_solve_f64(const PpfGrid* g, int32_t axis, double alpha, dou
  * holds up to 4 temperature ranges of the pure element's Gibbs energy in
  * J/mol, {T_lo, T_hi, c_1, c_T, c_TlnT, c_T^2, c_T^3, c_T^7, c_1/T, c_T^-9}
  * (phase 0 = the solid, the first phase name in sorted order; 1 = liquid);
- * the molar Gibbs energy adds R T (x ln x + (1-x) ln(1-x)), R = 8.3145.
+ * the molar Gibbs energy adds R T sum_i x_i ln x_i, R = 8.3145.
  * noise_scale multiplies the Langevin term of dF/dc (1 = the reference);
  * its N(0,1) numbers come from Philox4x32-10 keyed by (seed, step
  * (+ *step_base), cell). temperature: a field of the grid's layout.
@@ -340,23 +340,36 @@ int32_t ppf_var_line_solve_f64(const PpfGrid* g, int32_t axis, double alpha, dou
  * Boundaries: periodic or zero-gradient Neumann. As the reference, dG/dc is
  * one forward difference per cell (the first component up, the last down)
  * shared by every component. */
+#define PPF_NCGPU_MAX_COMP 6
 typedef struct PpfNcgpuParams {
   double dx, dt, v_m, D_L, D_S, M_qmax, H, y_e, beta, ebar2, noise_scale;
-  double W[3], M[3];
-  double gibbs[2][3][4][10];
-  int32_t npieces[2][3];
+  double W[PPF_NCGPU_MAX_COMP], M[PPF_NCGPU_MAX_COMP];
+  double gibbs[2][PPF_NCGPU_MAX_COMP][4][10];
+  int32_t npieces[2][PPF_NCGPU_MAX_COMP];
   int32_t ncomp;
   int32_t reserved;
 } PpfNcgpuParams;
 
 int32_t ppf_ncgpu_step_f32(const PpfNcgpuParams* p, const PpfGrid* g, const PpfBoundary* bc,
                            const float* const* fields_in, float* const* fields_out,
-                           const float* temperature, float* transfer, uint64_t seed,
-                           uint64_t step, const uint64_t* step_base, void* stream);
+                           const float* temperature, const double* tables, float* transfer,
+                           uint64_t seed, uint64_t step, const uint64_t* step_base, void* stream);
 int32_t ppf_ncgpu_step_f64(const PpfNcgpuParams* p, const PpfGrid* g, const PpfBoundary* bc,
                            const double* const* fields_in, double* const* fields_out,
-                           const double* temperature, double* transfer, uint64_t seed,
-                           uint64_t step, const uint64_t* step_base, void* stream);
+                           const double* temperature, const double* tables, double* transfer,
+                           uint64_t seed, uint64_t step, const uint64_t* step_base, void* stream);
+
+/* The pure-element Gibbs energies of both phases at every cell's
+ * temperature, for a temperature field that stays fixed over many steps:
+ * tables = 2 ncomp planes of doubles in the grid's layout (rows x pitch
+ * each), plane l = G(solid, component l), plane ncomp + l = G(liquid, l).
+ * Passed as `tables` to ppf_ncgpu_step_*, the step reads them instead of
+ * evaluating the piecewise polynomials (NULL: evaluated every step, the
+ * same values). Recompute them whenever the temperature changes. */
+int32_t ppf_ncgpu_tables_f32(const PpfNcgpuParams* p, const PpfGrid* g, const float* temperature,
+                             double* tables, void* stream);
+int32_t ppf_ncgpu_tables_f64(const PpfNcgpuParams* p, const PpfGrid* g, const double* temperature,
+                             double* tables, void* stream);
 
 /* ---- batched ensemble ------------------------------------------------- */
 

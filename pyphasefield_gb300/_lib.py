@@ -91,11 +91,15 @@ class PpfImplicitDiffusionParams(C.Structure):
         ("solver", C.c_int32), ("adi", C.c_int32)]
 
 
+PPF_NCGPU_MAX_COMP = 6
+
+
 class PpfNcgpuParams(C.Structure):
     _fields_ = [(n, C.c_double) for n in ("dx", "dt", "v_m", "D_L", "D_S", "M_qmax", "H",
                                           "y_e", "beta", "ebar2", "noise_scale")] + [
-        ("W", C.c_double * 3), ("M", C.c_double * 3),
-        ("gibbs", (((C.c_double * 10) * 4) * 3) * 2), ("npieces", (C.c_int32 * 3) * 2),
+        ("W", C.c_double * PPF_NCGPU_MAX_COMP), ("M", C.c_double * PPF_NCGPU_MAX_COMP),
+        ("gibbs", (((C.c_double * 10) * 4) * PPF_NCGPU_MAX_COMP) * 2),
+        ("npieces", (C.c_int32 * PPF_NCGPU_MAX_COMP) * 2),
         ("ncomp", C.c_int32), ("reserved", C.c_int32)]
 
 
@@ -145,8 +149,10 @@ SIGNATURES: dict[str, list] = {
                                         SZ, C.POINTER(I32), P],
     "ppf_diffusion_implicit_step_f64": [C.POINTER(PpfImplicitDiffusionParams), PG, P, P, P, P,
                                         SZ, C.POINTER(I32), P],
-    "ppf_ncgpu_step_f32": [C.POINTER(PpfNcgpuParams), PG, PB, P, P, P, P, U64, U64, P, P],
-    "ppf_ncgpu_step_f64": [C.POINTER(PpfNcgpuParams), PG, PB, P, P, P, P, U64, U64, P, P],
+    "ppf_ncgpu_step_f32": [C.POINTER(PpfNcgpuParams), PG, PB, P, P, P, P, P, U64, U64, P, P],
+    "ppf_ncgpu_step_f64": [C.POINTER(PpfNcgpuParams), PG, PB, P, P, P, P, P, U64, U64, P, P],
+    "ppf_ncgpu_tables_f32": [C.POINTER(PpfNcgpuParams), PG, P, P, P],
+    "ppf_ncgpu_tables_f64": [C.POINTER(PpfNcgpuParams), PG, P, P, P],
     "ppf_phase_implicit_scratch_bytes": [PG, I32, C.POINTER(SZ)],
     "ppf_phase_implicit_step_f32": [C.POINTER(PpfImplicitPhaseParams), PG, P, P, P, P, SZ,
                                     C.POINTER(I32), P],

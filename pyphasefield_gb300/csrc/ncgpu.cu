@@ -1,5 +1,5 @@
 // NCGPU: the multi-component solidification engine with quaternion
-// orientation fields (pyphasefield Engines/NCGPU.py), 2 or 3 components.
+// orientation fields (pyphasefield Engines/NCGPU.py), 2 to 6 components.
 //
 //   ncgpu_thermo_kernel  (NComponent_helper_kernel, :248-303): per cell the
 //       molar Gibbs energies of the solid (first phase, sorted) and liquid,
@@ -23,7 +23,7 @@
 namespace ppf {
 namespace {
 
-constexpr int kMaxComp = 3;
+constexpr int kMaxComp = PPF_NCGPU_MAX_COMP;
 
 template <typename T>
 struct NcCoef {
@@ -74,11 +74,44 @@ __device__ __forceinline__ T noise_normal(uint64_t seed, uint64_t step, int row,
   return sqrt(T(-2) * log(u1)) * cospi(T(2) * u2);
 }
 
+// The pure-element Gibbs energies of both phases at a cell's temperature:
+// tab[l] = G_solid,l, tab[N + l] = G_liquid,l.
+template <int N>
+__device__ __forceinline__ void pure_energies(const NcGibbs& gb, double t, double* tab) {
+  const double lnT = log(t);
+#pragma unroll
+  for (int l = 0; l < N; ++l) {
+    tab[l] = g_pure(gb, 0, l, t, lnT);
+    tab[N + l] = g_pure(gb, 1, l, t, lnT);
+  }
+}
+
+// The per-cell table of pure-element energies (2 ncomp planes of doubles in
+// the grid's layout) for a temperature field that stays fixed over many
+// steps: the thermodynamics kernel then reads 2 ncomp values per cell
+// instead of evaluating 2 ncomp piecewise polynomials and a logarithm.
+template <typename T, int N>
+__global__ void __launch_bounds__(256)
+    ncgpu_table_kernel(Geo g, NcGibbs gb, const T* __restrict__ temp, double* __restrict__ tab) {
+  pdl_wait();
+  pdl_launch_next();
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y;
+  if (x >= g.n[1]) return;
+  const int64_t i = (int64_t)y * g.pitch + x;
+  const int64_t plane = (int64_t)g.n[0] * g.pitch;
+  double v[2 * N];
+  pure_energies<N>(gb, (double)temp[i], v);
+#pragma unroll
+  for (int l = 0; l < 2 * N; ++l) tab[l * plane + i] = v[l];
+}
+
 template <typename T, int NC>
 __global__ void __launch_bounds__(256)
     ncgpu_thermo_kernel(Geo g, NcCoef<T> k, NcGibbs gb, const T* __restrict__ phi,
-                        NcPtrs<T> cp, const T* __restrict__ temp, T* __restrict__ dG,
-                        uint64_t seed, uint64_t step, const uint64_t* step_base) {
+                        NcPtrs<T> cp, const T* __restrict__ temp, const double* __restrict__ tab,
+                        T* __restrict__ dG, uint64_t seed, uint64_t step,
+                        const uint64_t* step_base) {
   pdl_wait();
   pdl_launch_next();
   constexpr int N = NC + 1;
@@ -88,8 +121,7 @@ __global__ void __launch_bounds__(256)
   const int64_t i = (int64_t)y * g.pitch + x;
   const uint64_t st = step + (step_base ? *step_base : 0);
   const double t = (double)temp[i];
-  const double lnT = log(t);
-  double xs[N], xp[N], Gs[N], Gl[N];
+  double xs[N], xp[N], G[2 * N];
   double last = 1.0;
 #pragma unroll
   for (int l = 0; l < NC; ++l) {
@@ -97,12 +129,17 @@ __global__ void __launch_bounds__(256)
     last -= xs[l];
   }
   xs[NC] = last;
+  if (tab) {
+    const int64_t plane = (int64_t)g.n[0] * g.pitch;
 #pragma unroll
-  for (int l = 0; l < N; ++l) {
-    Gs[l] = g_pure(gb, 0, l, t, lnT);
-    Gl[l] = g_pure(gb, 1, l, t, lnT);
-    xp[l] = xs[l];
+    for (int l = 0; l < 2 * N; ++l) G[l] = __ldg(tab + l * plane + i);
+  } else {
+    pure_energies<N>(gb, t, G);
   }
+  const double* Gs = G;
+  const double* Gl = G + N;
+#pragma unroll
+  for (int l = 0; l < N; ++l) xp[l] = xs[l];
   // the reference's forward difference (NCGPU.py:282-286): the last
   // component down, the first up, one derivative for every component, as the
   // difference of the two molar Gibbs energies. The ideal mixing term is the
@@ -297,10 +334,67 @@ __global__ void __launch_bounds__(256)
   for (int l = 0; l < NC; ++l) cp.c_out[l][i] = cp.c[l][i] + k.dt * dc[l];
 }
 
+template <typename T, int NC>
+cudaError_t launch_ncgpu(dim3 grid2, cudaStream_t st, const Geo& g, const Bc<T>& bc,
+                         const NcCoef<T>& k, const NcGibbs& gb, const T* const* in,
+                         T* const* out, const NcPtrs<T>& cp, const T* temp, const double* tab,
+                         T* dG, uint64_t seed, uint64_t step, const uint64_t* step_base) {
+  cudaError_t e = launch(ncgpu_thermo_kernel<T, NC>, grid2, dim3(256), 0, st, true, g, k, gb,
+                         in[0], cp, temp, tab, dG, seed, step, step_base);
+  if (e != cudaSuccess) return e;
+  return launch(ncgpu_kernel<T, NC>, grid2, dim3(256), 0, st, true, g, bc, k, in[0], in[1], in[2],
+                cp, temp, (const T*)dG, out[0], out[1], out[2]);
+}
+
+int32_t make_gibbs(const PpfNcgpuParams* p, NcGibbs* gb) {
+  for (int ph = 0; ph < 2; ++ph)
+    for (int c = 0; c < p->ncomp; ++c)
+      if (p->npieces[ph][c] < 0 || p->npieces[ph][c] > 4)
+        return fail(PPF_ERR_INVALID, "npieces must be 0..4");
+  static_assert(sizeof(gb->piece) == sizeof(p->gibbs), "Gibbs table layout");
+  memcpy(gb->piece, p->gibbs, sizeof(gb->piece));
+  memcpy(gb->npieces, p->npieces, sizeof(gb->npieces));
+  return PPF_OK;
+}
+
+template <typename T>
+int32_t ncgpu_tables(const PpfNcgpuParams* p, const PpfGrid* grid, const T* temp, double* tables,
+                     void* stream) {
+  clear_error();
+  if (!p || !temp || !tables) return fail(PPF_ERR_INVALID, "NULL argument");
+  Geo g;
+  int32_t rc = make_geo(grid, 2, 2, &g);
+  if (rc) return rc;
+  if (p->ncomp < 2 || p->ncomp > kMaxComp)
+    return fail(PPF_ERR_UNSUPPORTED, "NCGPU: 2 to %d components (got %d)", kMaxComp, p->ncomp);
+  if (g.n[0] > 65535) return fail(PPF_ERR_INVALID, "more than 65535 rows");
+  NcGibbs gb;
+  if ((rc = make_gibbs(p, &gb))) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  const dim3 grid2((g.n[1] + 255) / 256, g.n[0]);
+  cudaError_t e;
+#define PPF_NC_CASE(n)                                                                        \
+  case n:                                                                                     \
+    e = launch(ncgpu_table_kernel<T, n>, grid2, dim3(256), 0, st, true, g, gb, temp, tables); \
+    break;
+  switch (p->ncomp) {
+    PPF_NC_CASE(2)
+    PPF_NC_CASE(3)
+    PPF_NC_CASE(4)
+    PPF_NC_CASE(5)
+    default:
+    PPF_NC_CASE(6)
+  }
+#undef PPF_NC_CASE
+  PPF_TRY_CUDA(e);
+  return PPF_OK;
+}
+
 template <typename T>
 int32_t ncgpu_step(const PpfNcgpuParams* p, const PpfGrid* grid, const PpfBoundary* bcin,
-                   const T* const* in, T* const* out, const T* temp, T* transfer, uint64_t seed,
-                   uint64_t step, const uint64_t* step_base, void* stream) {
+                   const T* const* in, T* const* out, const T* temp, const double* tables,
+                   T* transfer, uint64_t seed, uint64_t step, const uint64_t* step_base,
+                   void* stream) {
   clear_error();
   if (!p || !in || !out) return fail(PPF_ERR_INVALID, "NULL argument");
   Geo g;
@@ -308,7 +402,7 @@ int32_t ncgpu_step(const PpfNcgpuParams* p, const PpfGrid* grid, const PpfBounda
   if (rc) return rc;
   const int ncomp = p->ncomp;
   if (ncomp < 2 || ncomp > kMaxComp)
-    return fail(PPF_ERR_UNSUPPORTED, "NCGPU: 2 or 3 components (got %d)", ncomp);
+    return fail(PPF_ERR_UNSUPPORTED, "NCGPU: 2 to %d components (got %d)", kMaxComp, ncomp);
   const int nc = ncomp - 1;
   for (int f = 0; f < 3 + nc; ++f)
     if (!in[f] || !out[f]) return fail(PPF_ERR_INVALID, "NULL field pointer");
@@ -325,10 +419,6 @@ int32_t ncgpu_step(const PpfNcgpuParams* p, const PpfGrid* grid, const PpfBounda
       if (bcin && bcin->type[a] == PPF_BC_NEUMANN && bcin->value[0][a][s] != 0.0)
         return fail(PPF_ERR_UNSUPPORTED, "NCGPU: Neumann boundaries with zero gradient only");
   }
-  for (int ph = 0; ph < 2; ++ph)
-    for (int c = 0; c < ncomp; ++c)
-      if (p->npieces[ph][c] < 0 || p->npieces[ph][c] > 4)
-        return fail(PPF_ERR_INVALID, "npieces must be 0..4");
   NcCoef<T> k;
   k.idx = (T)(1.0 / p->dx);
   k.dt = (T)p->dt;
@@ -347,9 +437,7 @@ int32_t ncgpu_step(const PpfNcgpuParams* p, const PpfGrid* grid, const PpfBounda
     k.M[c] = (T)p->M[c];
   }
   NcGibbs gb;
-  static_assert(sizeof(gb.piece) == sizeof(p->gibbs), "Gibbs table layout");
-  memcpy(gb.piece, p->gibbs, sizeof(gb.piece));
-  memcpy(gb.npieces, p->npieces, sizeof(gb.npieces));
+  if ((rc = make_gibbs(p, &gb))) return rc;
   const int64_t fsz = (int64_t)g.n[0] * g.pitch;
   NcPtrs<T> cp{};
   for (int l = 0; l < nc; ++l) {
@@ -361,17 +449,23 @@ int32_t ncgpu_step(const PpfNcgpuParams* p, const PpfGrid* grid, const PpfBounda
   T* dG = transfer;
   cudaStream_t st = (cudaStream_t)stream;
   const dim3 grid2((g.n[1] + 255) / 256, g.n[0]);
-  if (nc == 1) {
-    PPF_TRY_CUDA(launch(ncgpu_thermo_kernel<T, 1>, grid2, dim3(256), 0, st, true, g, k, gb,
-                        in[0], cp, temp, dG, seed, step, step_base));
-    PPF_TRY_CUDA(launch(ncgpu_kernel<T, 1>, grid2, dim3(256), 0, st, true, g, bc, k, in[0], in[1],
-                        in[2], cp, temp, (const T*)dG, out[0], out[1], out[2]));
-  } else {
-    PPF_TRY_CUDA(launch(ncgpu_thermo_kernel<T, 2>, grid2, dim3(256), 0, st, true, g, k, gb,
-                        in[0], cp, temp, dG, seed, step, step_base));
-    PPF_TRY_CUDA(launch(ncgpu_kernel<T, 2>, grid2, dim3(256), 0, st, true, g, bc, k, in[0], in[1],
-                        in[2], cp, temp, (const T*)dG, out[0], out[1], out[2]));
+  static_assert(kMaxComp == 6, "one instantiation per concentration-field count");
+  cudaError_t e;
+#define PPF_NC_CASE(n)                                                                      \
+  case n:                                                                                   \
+    e = launch_ncgpu<T, n>(grid2, st, g, bc, k, gb, in, out, cp, temp, tables, dG, seed, step,  \
+                           step_base);                                                      \
+    break;
+  switch (nc) {
+    PPF_NC_CASE(1)
+    PPF_NC_CASE(2)
+    PPF_NC_CASE(3)
+    PPF_NC_CASE(4)
+    default:
+    PPF_NC_CASE(5)
   }
+#undef PPF_NC_CASE
+  PPF_TRY_CUDA(e);
   return PPF_OK;
 }
 
@@ -384,18 +478,30 @@ extern "C" {
 
 int32_t ppf_ncgpu_step_f32(const PpfNcgpuParams* p, const PpfGrid* g, const PpfBoundary* bc,
                            const float* const* fields_in, float* const* fields_out,
-                           const float* temperature, float* transfer, uint64_t seed,
-                           uint64_t step, const uint64_t* step_base, void* stream) {
-  return ncgpu_step<float>(p, g, bc, fields_in, fields_out, temperature, transfer, seed, step,
-                           step_base, stream);
+                           const float* temperature, const double* tables, float* transfer,
+                           uint64_t seed, uint64_t step, const uint64_t* step_base,
+                           void* stream) {
+  return ncgpu_step<float>(p, g, bc, fields_in, fields_out, temperature, tables, transfer, seed,
+                           step, step_base, stream);
 }
 
 int32_t ppf_ncgpu_step_f64(const PpfNcgpuParams* p, const PpfGrid* g, const PpfBoundary* bc,
                            const double* const* fields_in, double* const* fields_out,
-                           const double* temperature, double* transfer, uint64_t seed,
-                           uint64_t step, const uint64_t* step_base, void* stream) {
-  return ncgpu_step<double>(p, g, bc, fields_in, fields_out, temperature, transfer, seed, step,
-                            step_base, stream);
+                           const double* temperature, const double* tables, double* transfer,
+                           uint64_t seed, uint64_t step, const uint64_t* step_base,
+                           void* stream) {
+  return ncgpu_step<double>(p, g, bc, fields_in, fields_out, temperature, tables, transfer, seed,
+                            step, step_base, stream);
+}
+
+int32_t ppf_ncgpu_tables_f32(const PpfNcgpuParams* p, const PpfGrid* g, const float* temperature,
+                             double* tables, void* stream) {
+  return ncgpu_tables<float>(p, g, temperature, tables, stream);
+}
+
+int32_t ppf_ncgpu_tables_f64(const PpfNcgpuParams* p, const PpfGrid* g, const double* temperature,
+                             double* tables, void* stream) {
+  return ncgpu_tables<double>(p, g, temperature, tables, stream);
 }
 
 }  // extern "C"

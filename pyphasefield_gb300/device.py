@@ -64,9 +64,12 @@ class DeviceGrid:
     def upload(self, dst: torch.Tensor, host: np.ndarray, stream: torch.cuda.Stream):
         """H2D copy of a host interior array (any float dtype) into dst
         through pinned memory, ordered on `stream`. Returns the pinned
-        staging tensor (keep it alive until the stream passes the copy)."""
+        staging tensor (keep it alive until the stream passes the copy).
+        The copy is ordered after the work already queued on the current
+        stream (the zero fill of buffers allocated there)."""
         a = np.ascontiguousarray(np.asarray(host).astype(self.np_dtype).reshape(self.kshape))
         pinned = torch.from_numpy(a).pin_memory()
+        stream.wait_stream(torch.cuda.current_stream(dst.device))
         with torch.cuda.stream(stream):
             self.view(dst).copy_(pinned, non_blocking=True)
         return pinned

@@ -97,6 +97,8 @@ class GB300Engine:
         self._ppf_stream = torch.cuda.Stream(dev)
         self._ppf_bc = boundary_struct(self, self._ppf_grid, self.NFIELDS)
         self._ppf_stepctr = torch.zeros(1, dtype=torch.int64, device=dev)
+        # the buffers' zero fills ran on the current stream
+        self._ppf_stream.wait_stream(torch.cuda.current_stream(dev))
         self._ppf_graphs = {}
         self._ppf_staging = []
         self._uses_gpu = True

@@ -1,5 +1,5 @@
 """NCGPUGB300: the reference's NCGPU engine (Engines/NCGPU.py:329-532) on the
-CUDA library: alloy solidification (2 or 3 components) with a phase field,
+CUDA library: alloy solidification (2 to 6 components) with a phase field,
 two quaternion orientation fields and the fractions of all but the last
 component, thermodynamics from a TDB file (read by pyphasefield_gb300.tdb
 instead of pycalphad).
@@ -37,8 +37,9 @@ def ncgpu_parameters(db: Database, dx: float, d_ratio: float = 4.0) -> dict:
     <COMP>_L / _TM / _S / _B functions, the derived W and M, and the scalar
     functions D_S, D_L, V_M, M_Q, H, Y_E."""
     comps = db.elements
-    if len(comps) not in (2, 3):
-        raise NotImplementedError(f"NCGPU: 2 or 3 components (the TDB lists {comps})")
+    if not 2 <= len(comps) <= L.PPF_NCGPU_MAX_COMP:
+        raise NotImplementedError(f"NCGPU: 2 to {L.PPF_NCGPU_MAX_COMP} components "
+                                  f"(the TDB lists {comps})")
     d = dx * d_ratio
     ud = {"d": d, "R": 8.314}
     for key, fn in (("L", "_L"), ("T_M", "_TM"), ("S", "_S"), ("B", "_B")):
@@ -58,12 +59,13 @@ def ncgpu_parameters(db: Database, dx: float, d_ratio: float = 4.0) -> dict:
 
 
 def gibbs_table(db: Database):
-    """(gibbs[2][3][4][10], npieces[2][3]) for PpfNcgpuParams: phase 0 the
-    solid (first phase in sorted order), 1 the liquid; components sorted."""
+    """(gibbs[2][MAX_COMP][4][10], npieces[2][MAX_COMP]) for PpfNcgpuParams:
+    phase 0 the solid (first phase in sorted order), 1 the liquid; components
+    sorted."""
     if len(db.phases) != 2:
         raise NotImplementedError(f"NCGPU: two phases expected (the TDB lists {db.phases})")
-    table = np.zeros((2, 3, 4, 10))
-    npieces = np.zeros((2, 3), dtype=np.int32)
+    table = np.zeros((2, L.PPF_NCGPU_MAX_COMP, 4, 10))
+    npieces = np.zeros((2, L.PPF_NCGPU_MAX_COMP), dtype=np.int32)
     for ph, phase in enumerate(db.phases):
         for cp, comp in enumerate(db.elements):
             pieces = db.params.get((phase, comp))
@@ -76,6 +78,29 @@ def gibbs_table(db: Database):
                 table[ph, cp, k, 2:] = coefs
             npieces[ph, cp] = len(pieces)
     return table, npieces
+
+
+def params_struct(db: Database, ud: dict, dx: float, noise_scale: float = 1.0):
+    """PpfNcgpuParams from the derived parameters `ud` (ncgpu_parameters)
+    and the database's Gibbs-energy tables."""
+    table, npieces = gibbs_table(db)
+    p = L.PpfNcgpuParams()
+    for name in ("dt", "v_m", "D_L", "D_S", "M_qmax", "H", "y_e", "beta"):
+        setattr(p, name, float(ud[name]))
+    p.dx = float(dx)
+    p.ebar2 = float(ud["ebar"]) ** 2
+    p.noise_scale = float(noise_scale)
+    p.ncomp = len(db.elements)
+    for j in range(p.ncomp):
+        p.W[j] = float(ud["W"][j])
+        p.M[j] = float(ud["M"][j])
+    for ph in range(2):
+        for cp in range(L.PPF_NCGPU_MAX_COMP):
+            p.npieces[ph][cp] = int(npieces[ph, cp])
+            for k in range(4):
+                for e in range(10):
+                    p.gibbs[ph][cp][k][e] = float(table[ph, cp, k, e])
+    return p
 
 
 def make_seed(phi, q1, q4, x, y, angle, seed_radius):
@@ -166,32 +191,23 @@ class _NcgpuMixin(GB300Engine):
         # the pinned staging copy must outlive the asynchronous upload
         self._nc_temp_staging = self._ppf_grid.upload(self._nc_temp, self.temperature.get_cells(),
                                                       self._ppf_stream)
-        table, npieces = gibbs_table(self._ppf_db)
         ud = self.user_data
-        p = L.PpfNcgpuParams()
-        for name in ("dt", "v_m", "D_L", "D_S", "M_qmax", "H", "y_e", "beta"):
-            setattr(p, name, float(ud[name]))
-        p.dx = float(self.dx)
-        p.ebar2 = float(ud["ebar"]) ** 2
-        p.noise_scale = float(ud.get("noise_scale", 1.0))
-        p.ncomp = ncomp
-        for j in range(ncomp):
-            p.W[j] = float(ud["W"][j])
-            p.M[j] = float(ud["M"][j])
-        for ph in range(2):
-            for cp in range(3):
-                p.npieces[ph][cp] = int(npieces[ph, cp])
-                for k in range(4):
-                    for e in range(10):
-                        p.gibbs[ph][cp][k][e] = float(table[ph, cp, k, e])
-        self._nc_params = p
+        self._nc_params = params_struct(self._ppf_db, ud, self.dx, ud.get("noise_scale", 1.0))
+        # the temperature is fixed during a run: the pure-element energies of
+        # every cell are evaluated once, after the upload, on the same stream
+        self._nc_tables = torch.empty((2 * ncomp,) + tuple(g.alloc_shape), dtype=torch.float64,
+                                      device=g.device)
+        L.call(f"ppf_ncgpu_tables_{_F[self._ppf_dtype]}", C.byref(self._nc_params),
+               C.byref(g.grid), ptr(self._nc_temp), ptr(self._nc_tables),
+               C.c_void_p(self._ppf_stream.cuda_stream))
 
     def _ppf_step(self, src, dst, depth, step, step_base, sp):
         fin = (C.c_void_p * len(src))(*[ptr(t) for t in src])
         fout = (C.c_void_p * len(dst))(*[ptr(t) for t in dst])
         L.call(f"ppf_ncgpu_step_{_F[self._ppf_dtype]}", C.byref(self._nc_params),
                C.byref(self._ppf_grid.grid), C.byref(self._ppf_bc), fin, fout,
-               ptr(self._nc_temp), ptr(self._nc_transfer), C.c_uint64(int(self.user_data["seed"])),
+               ptr(self._nc_temp), ptr(self._nc_tables), ptr(self._nc_transfer),
+               C.c_uint64(int(self.user_data["seed"])),
                C.c_uint64(int(step)), ptr(step_base), sp)
 
 

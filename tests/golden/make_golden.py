@@ -40,7 +40,8 @@ def write_tdb(tdb, path):
     """The FUNCTION and PARAMETER records the NCGPU fixtures use, re-emitted
     from the parsed database (so the GPU machine, which has no reference
     checkout, reads the same thermodynamic data)."""
-    lines = ["$ Ni-Cu ideal solution records used by the NCGPU fixtures "
+    lines = ["$ " + ("Ni-Cu" if len(tdb.elements) == 2 else "-".join(tdb.elements))
+             + " ideal solution records used by the NCGPU fixtures "
              "(written by tests/golden/make_golden.py)"]
     for el in tdb.elements:
         lines.append(f"ELEMENT {el} FCC_A1 0 0 0 !")
@@ -191,6 +192,7 @@ def main():
                 tdb="ncgpu_nicual.tdb")
     save("ncgpu_ternary", meta, phi0=phi0, q10=q10, q40=q40, c0_0=ca, c0_1=cb, phi=out[0],
          q1=out[1], q4=out[2], c_0=out[3], c_1=out[4])
+    ncgpu_multicomponent()
 
     dx = 4.6e-8
     prm = dict(restate.WARREN_DEFAULTS)
@@ -212,5 +214,58 @@ def main():
         save(name, meta, phi0=phi0, c0=c0, phi=phi, c=c)
 
 
+def pseudo_element_tdb(tdb, names, path):
+    """A synthetic ideal database with more components: the ternary's records
+    plus pseudo-elements `names`, each a copy of Cu's records with its Gibbs
+    energies shifted by a few hundred J/mol and its melting point, surface
+    energy and kinetic coefficient scaled (no real element's data)."""
+    for j, name in enumerate(names):
+        shift = 300.0 * (j + 1)
+        for phase, fn in (("FCC_A1", "G_CU_FCC"), ("LIQUID", "G_CU_LIQUID")):
+            new = "G_" + name + fn[4:]
+            tdb.functions[new] = [(lo, hi, f"{expr}+{shift!r}-{0.05 * (j + 1)!r}*T")
+                                  for lo, hi, expr in tdb.functions[fn]]
+            tdb.params[(phase, name)] = [(298.15, 6000.0, new)]
+        for key, scale in (("_L", 1.0 + 0.1 * j), ("_TM", 1.0 - 0.03 * (j + 1)),
+                           ("_S", 1.0 + 0.05 * j), ("_B", 1.0 - 0.04 * j)):
+            lo, hi, expr = tdb.functions["CU" + key][0]
+            tdb.functions[name + key] = [(lo, hi, repr(float(expr) * scale))]
+        tdb.elements.append(name)
+    tdb.elements.sort()
+    write_tdb(tdb, path)
+
+
+def ncgpu_multicomponent():
+    """NCGPU with four and six components (three and five concentration
+    fields): the reference's kernels on pseudo-element extensions of
+    tests/Ni-Cu-Al_Ideal.tdb."""
+    from oracle import ncgpu_ref
+    base = refshim.reference_root() / "pyphasefield" / "tests" / "Ni-Cu-Al_Ideal.tdb"
+    nrng = np.random.default_rng(20240607)
+    for name, extra, shape, c0, seed in [
+            ("ncgpu_quaternary", ["XA"], (16, 18), [0.05, 0.3, 0.4], 9),
+            ("ncgpu_senary", ["XA", "XB", "XC"], (14, 16), [0.05, 0.2, 0.3, 0.1, 0.15], 13)]:
+        tdb_name = f"ncgpu_{len(extra) + 3}comp.tdb"
+        pseudo_element_tdb(ncgpu_ref.Tdb(base), extra, HERE / tdb_name)
+        tdb = ncgpu_ref.Tdb(HERE / tdb_name)
+        p = ncgpu_ref.tdb_params(tdb, 4.6e-6)
+        ncomp = len(tdb.elements)
+        init = ncgpu_ref.seed_fields(shape, c0=c0, ncomp=ncomp)
+        cs = [c + nrng.uniform(-1e-3, 1e-3, shape) for c in init[3:]]
+        T = np.full(shape, 1574.0)
+        noise = [ncgpu_ref.noise_normal(seed, s, shape) for s in range(3)]
+        out = refshim.run_ncgpu(*init[:3], cs, T, 3, p, tdb, noise, "PERIODIC")
+        meta = dict(model="ncgpu", steps=3, bc="PERIODIC", seed=seed, dx=4.6e-6, T=1574.0,
+                    tdb=tdb_name, ncomp=ncomp)
+        arrays = dict(phi0=init[0], q10=init[1], q40=init[2], phi=out[0], q1=out[1], q4=out[2])
+        for j, c in enumerate(cs):
+            arrays[f"c0_{j}"] = c
+            arrays[f"c_{j}"] = out[3 + j]
+        save(name, meta, **arrays)
+
+
 if __name__ == "__main__":
-    main()
+    if sys.argv[1:] == ["ncgpu_multicomponent"]:
+        ncgpu_multicomponent()
+    else:
+        main()

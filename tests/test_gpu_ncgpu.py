@@ -23,31 +23,15 @@ TOL = {"fp64": 1e-8, "fp32": 1e-5}
 
 
 def params_struct(dx, noise_scale=1.0, tdb=TDB):
-    from pyphasefield_gb300 import _lib as L
-    from pyphasefield_gb300.engines.ncgpu import gibbs_table, ncgpu_parameters
+    from pyphasefield_gb300.engines.ncgpu import ncgpu_parameters, params_struct as ps
     from pyphasefield_gb300.tdb import Database
     db = Database(tdb)
-    ud = ncgpu_parameters(db, dx)
-    table, npieces = gibbs_table(db)
-    p = L.PpfNcgpuParams()
-    for k in ("dt", "v_m", "D_L", "D_S", "M_qmax", "H", "y_e", "beta"):
-        setattr(p, k, float(ud[k]))
-    p.dx = dx
-    p.ebar2 = float(ud["ebar"]) ** 2
-    p.noise_scale = noise_scale
-    p.ncomp = len(db.elements)
-    for j in range(p.ncomp):
-        p.W[j], p.M[j] = ud["W"][j], ud["M"][j]
-    for ph in range(2):
-        for cp in range(3):
-            p.npieces[ph][cp] = int(npieces[ph, cp])
-            for k in range(4):
-                for e in range(10):
-                    p.gibbs[ph][cp][k][e] = float(table[ph, cp, k, e])
-    return p
+    return ps(db, ncgpu_parameters(db, dx), dx, noise_scale)
 
 
-def run_gpu(fields, T, steps, dx, seed, bc, precision, noise_scale=1.0, tdb=TDB):
+def run_gpu(fields, T, steps, dx, seed, bc, precision, noise_scale=1.0, tdb=TDB, tables=True):
+    """`steps` steps through ppf_ncgpu_step_*; tables: the pure-element
+    energies from ppf_ncgpu_tables_* (False: evaluated in every step)."""
     import torch
     from pyphasefield_gb300 import _lib as L
     shape = fields[0].shape
@@ -60,12 +44,17 @@ def run_gpu(fields, T, steps, dx, seed, bc, precision, noise_scale=1.0, tdb=TDB)
     p = params_struct(dx, noise_scale, tdb)
     sfx = "f64" if precision == "fp64" else "f32"
     s = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+    tab = None
+    if tables:
+        tab = torch.empty((2 * p.ncomp,) + tuple(a[0].shape), dtype=torch.float64, device="cuda")
+        L.call(f"ppf_ncgpu_tables_{sfx}", C.byref(p), C.byref(g), C.c_void_p(temp.data_ptr()),
+               C.c_void_p(tab.data_ptr()), s)
     for k in range(steps):
         fin = (C.c_void_p * len(a))(*[t.data_ptr() for t in a])
         fout = (C.c_void_p * len(o))(*[t.data_ptr() for t in o])
         L.call(f"ppf_ncgpu_step_{sfx}", C.byref(p), C.byref(g), C.byref(b), fin, fout,
-               C.c_void_p(temp.data_ptr()), C.c_void_p(transfer.data_ptr()), C.c_uint64(seed),
-               C.c_uint64(k), None, s)
+               C.c_void_p(temp.data_ptr()), C.c_void_p(None if tab is None else tab.data_ptr()),
+               C.c_void_p(transfer.data_ptr()), C.c_uint64(seed), C.c_uint64(k), None, s)
         a, o = o, a
     torch.cuda.synchronize()
     return [from_dev(t, kshape, shape) for t in a]
@@ -73,12 +62,13 @@ def run_gpu(fields, T, steps, dx, seed, bc, precision, noise_scale=1.0, tdb=TDB)
 
 @pytest.mark.parametrize("name", ["ncgpu_periodic", "ncgpu_neumann"])
 @pytest.mark.parametrize("precision", ["fp64", "fp32"])
-def test_reference_fixtures(cuda, name, precision):
+@pytest.mark.parametrize("tables", [True, False])
+def test_reference_fixtures(cuda, name, precision, tables):
     z = np.load(GOLDEN / f"{name}.npz")
     m = json.loads(str(z["meta"]))
     T = np.full(z["phi0"].shape, m["T"])
     out = run_gpu([z["phi0"], z["q10"], z["q40"], z["c0"]], T, m["steps"], m["dx"], m["seed"],
-                  m["bc"], precision)
+                  m["bc"], precision, tables=tables)
     for got, key in zip(out, ("phi", "q1", "q4", "c")):
         assert rel_l2(got, z[key]) < TOL[precision], (key, rel_l2(got, z[key]))
 
@@ -120,15 +110,33 @@ def test_gradient_run_against_oracle(cuda, gradient_case, precision, steps, tol)
         assert rel_l2(got, r) < t, (key, rel_l2(got, r))
 
 
+def test_tables_equal_the_per_step_evaluation(cuda, gradient_case):
+    """The pure-element energies read from ppf_ncgpu_tables_f64 (a
+    temperature that varies along x) give the same run as evaluating them
+    in every step."""
+    fields, T, _ = gradient_case
+    a = run_gpu(fields, T, 4, 4.6e-6, 5, "NEUMANN", "fp64", tables=True)
+    b = run_gpu(fields, T, 4, 4.6e-6, 5, "NEUMANN", "fp64", tables=False)
+    for x, y in zip(a, b):
+        assert rel_l2(x, y) < 1e-12
+
+
+MULTI = ["ncgpu_ternary", "ncgpu_quaternary", "ncgpu_senary"]
+
+
+@pytest.mark.parametrize("name", MULTI)
 @pytest.mark.parametrize("precision", ["fp64", "fp32"])
-def test_ternary_reference_fixture(cuda, precision):
-    """Ni-Cu-Al (three components, two concentration fields)."""
-    z = np.load(GOLDEN / "ncgpu_ternary.npz")
+def test_multicomponent_reference_fixture(cuda, name, precision):
+    """Three (Ni-Cu-Al), four and six components (Ni-Cu-Al plus pseudo
+    elements): two, three and five concentration fields."""
+    z = np.load(GOLDEN / f"{name}.npz")
     m = json.loads(str(z["meta"]))
+    nc = sum(1 for k in z.files if k.startswith("c0_"))
     T = np.full(z["phi0"].shape, m["T"])
-    f = [z["phi0"], z["q10"], z["q40"], z["c0_0"], z["c0_1"]]
+    f = [z["phi0"], z["q10"], z["q40"]] + [z[f"c0_{j}"] for j in range(nc)]
     out = run_gpu(f, T, m["steps"], m["dx"], m["seed"], m["bc"], precision, tdb=GOLDEN / m["tdb"])
-    for got, key in zip(out, ("phi", "q1", "q4", "c_0", "c_1")):
+    keys = ["phi", "q1", "q4"] + [f"c_{j}" for j in range(nc)]
+    for got, key in zip(out, keys):
         assert rel_l2(got, z[key]) < TOL[precision], (key, rel_l2(got, z[key]))
 
 
@@ -164,3 +172,28 @@ def test_engine_matches_oracle(cuda):
         assert rel_l2(f.get_cells(), r) < TOL["fp64"], f.name
     assert sim.time_step_counter == 5
     assert [f.name for f in sim.fields] == ["phi", "q1", "q4", "c_CU"]
+
+
+def test_engine_six_components_matches_oracle(cuda):
+    """The engine on the six-component database (five concentration fields,
+    the initial_concentration_array of the reference) against the oracle."""
+    from pyphasefield_gb300 import NCGPUGB300
+    path = GOLDEN / "ncgpu_6comp.tdb"
+    shape = (20, 18)
+    sim = NCGPUGB300(dimensions=list(shape), dx=4.6e-6, tdb_path=str(path),
+                     temperature_type="ISOTHERMAL", initial_T=1574.0,
+                     boundary_conditions="NEUMANN",
+                     user_data={"sim_type": "seed",
+                                "initial_concentration_array": [0.05, 0.2, 0.3, 0.1, 0.15],
+                                "seed": 4, "precision": "fp64", "graph_chunk": 2})
+    sim.initialize_fields_and_imported_data()
+    assert [f.name for f in sim.fields] == ["phi", "q1", "q4", "c_AL", "c_CU", "c_NI", "c_XA",
+                                            "c_XB"]
+    init = [f.get_cells().copy() for f in sim.fields]
+    sim.simulate(4)
+    sim.retrieve_fields_from_GPU()
+    tdb = N.Tdb(path)
+    ref = N.run(init, np.full(shape, 1574.0), 4, N.tdb_params(tdb, 4.6e-6), tdb, seed=4,
+                bc="NEUMANN")
+    for f, r in zip(sim.fields, ref):
+        assert rel_l2(f.get_cells(), r) < TOL["fp64"], f.name

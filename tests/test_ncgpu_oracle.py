@@ -9,7 +9,8 @@ import numpy as np
 import pytest
 
 from oracle import ncgpu_ref as N
-from pyphasefield_gb300.engines.ncgpu import gibbs_table, make_seed, ncgpu_parameters
+from pyphasefield_gb300.engines.ncgpu import (gibbs_table, make_seed, ncgpu_parameters,
+                                              params_struct)
 from pyphasefield_gb300.tdb import Database, g_eval
 
 GOLDEN = Path(__file__).resolve().parent / "golden"
@@ -45,8 +46,8 @@ def test_tdb_reader_matches_oracle_evaluation():
                     mine = g_eval(c, T)
             assert mine == pytest.approx(tdb.g_pure(ph, comp, T), rel=1e-13, abs=1e-9)
     table, npieces = gibbs_table(db)
-    assert table.shape == (2, 3, 4, 10)
-    assert (npieces[:, :2] == 2).all() and (npieces[:, 2] == 0).all()
+    assert table.shape == (2, 6, 4, 10)
+    assert (npieces[:, :2] == 2).all() and (npieces[:, 2:] == 0).all()
 
 
 def test_parameters_match_oracle():
@@ -76,18 +77,38 @@ def test_noise_is_standard_normal():
     assert abs(z.mean()) < 0.01 and abs(z.std() - 1) < 0.01
 
 
-def test_ternary_oracle_matches_reference_kernels():
-    z = np.load(GOLDEN / "ncgpu_ternary.npz")
+@pytest.mark.parametrize("name", ["ncgpu_ternary", "ncgpu_quaternary", "ncgpu_senary"])
+def test_multicomponent_oracle_matches_reference_kernels(name):
+    z = np.load(GOLDEN / f"{name}.npz")
     m = json.loads(str(z["meta"]))
+    nc = sum(1 for k in z.files if k.startswith("c0_"))
     tdb = N.Tdb(GOLDEN / m["tdb"])
+    assert len(tdb.elements) == nc + 1
     p = N.tdb_params(tdb, m["dx"])
     T = np.full(z["phi0"].shape, m["T"])
-    out = N.run([z["phi0"], z["q10"], z["q40"], z["c0_0"], z["c0_1"]], T, m["steps"], p, tdb,
-                seed=m["seed"], bc=m["bc"])
-    for got, key, tol in zip(out, ("phi", "q1", "q4", "c_0", "c_1"),
-                             (1e-10, 1e-12, 1e-12, 1e-8, 1e-8)):
+    out = N.run([z["phi0"], z["q10"], z["q40"]] + [z[f"c0_{j}"] for j in range(nc)], T,
+                m["steps"], p, tdb, seed=m["seed"], bc=m["bc"])
+    keys = ["phi", "q1", "q4"] + [f"c_{j}" for j in range(nc)]
+    for got, key, tol in zip(out, keys, [1e-10, 1e-12, 1e-12] + [1e-8] * nc):
         ref = z[key]
         assert np.abs(got - ref).max() <= tol * max(1.0, np.abs(ref).max()), key
+
+
+def test_pseudo_element_tdb_reader():
+    """The six-component database: every pure-element energy and the
+    derived per-component W and M agree between the package's reader and the
+    oracle's."""
+    path = GOLDEN / "ncgpu_6comp.tdb"
+    db, tdb = Database(path), N.Tdb(path)
+    assert db.elements == ["AL", "CU", "NI", "XA", "XB", "XC"]
+    for (ph, comp), pieces in db.params.items():
+        for T in (500.0, 1357.0, 1574.0):
+            mine = [g_eval(c, T) for lo, hi, c in pieces if lo <= T < hi]
+            assert mine[0] == pytest.approx(tdb.g_pure(ph, comp, T), rel=1e-13, abs=1e-9)
+    mine = ncgpu_parameters(db, 4.6e-6)
+    ref = N.tdb_params(tdb, 4.6e-6)
+    np.testing.assert_allclose(mine["W"], ref["W"], rtol=1e-14)
+    np.testing.assert_allclose(mine["M"], ref["M"], rtol=1e-14)
 
 
 def test_ternary_tdb_reader():
@@ -106,3 +127,28 @@ def test_ternary_tdb_reader():
     ref = N.tdb_params(tdb, 4.6e-6)
     np.testing.assert_allclose(mine["W"], ref["W"], rtol=1e-14)
     assert mine["ebar"] == pytest.approx(ref["ebar"], rel=1e-14)
+
+
+def test_more_components_than_the_tables_hold_are_rejected(tmp_path):
+    text = (GOLDEN / "ncgpu_6comp.tdb").read_text()
+    extra = [ln.replace("XC", "XD") for ln in text.splitlines() if "XC" in ln]
+    path = tmp_path / "seven.tdb"
+    path.write_text(text + "\n".join(extra) + "\n")
+    db = Database(path)
+    assert len(db.elements) == 7
+    with pytest.raises(NotImplementedError, match="2 to 6 components"):
+        ncgpu_parameters(db, 4.6e-6)
+
+
+def test_params_struct_fills_every_component():
+    db = Database(GOLDEN / "ncgpu_6comp.tdb")
+    ud = ncgpu_parameters(db, 4.6e-6)
+    p = params_struct(db, ud, 4.6e-6)
+    table, npieces = gibbs_table(db)
+    assert p.ncomp == 6
+    for j in range(6):
+        assert p.W[j] == ud["W"][j] and p.M[j] == ud["M"][j]
+        for ph in range(2):
+            assert p.npieces[ph][j] == npieces[ph, j] > 0
+            for k in range(4):
+                assert list(p.gibbs[ph][j][k]) == list(table[ph, j, k])
