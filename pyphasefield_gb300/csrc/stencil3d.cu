@@ -99,14 +99,41 @@ __device__ __forceinline__ void fixup_plane(const PlaneRing<T, NS>& ring, const 
   if (!xy_edge && !zfixed) return;
   T* dst = ring.plane(p);
   const int W = m.TX + 2 * m.H, Hh = m.TY + 2 * m.H;
-  for (int ly = threadIdx.y; ly < Hh; ly += kThreads / 32) {
-    const int gy = y0 - m.H + ly;
-    const bool yout = (unsigned)gy >= (unsigned)g.n[1];
-    for (int lx = threadIdx.x; lx < W; lx += 32) {
-      const int gx = x0 - m.H + lx;
-      if (zfixed || yout || (unsigned)gx >= (unsigned)g.n[2])
+  if (zfixed) {
+    for (int ly = threadIdx.y; ly < Hh; ly += kThreads / 32) {
+      const int gy = y0 - m.H + ly;
+      for (int lx = threadIdx.x; lx < W; lx += 32) {
+        const int gx = x0 - m.H + lx;
         dst[ly * m.BX + (gx - x0 + kXOff)] = fetch<T, 3>(in, g, bc, 0, p, gy, gx);
+      }
     }
+    return;
+  }
+  // Only the cells outside the grid: cl / cr columns on the left / right,
+  // rt / rb rows at the top / bottom of the W x Hh window, enumerated as the
+  // full rows first, then the outside columns of the remaining rows, one
+  // cell per thread.
+  const int cl = min(W, max(0, m.H - x0));
+  const int cr = min(W - cl, max(0, x0 - m.H + W - g.n[2]));
+  const int rt = min(Hh, max(0, m.H - y0));
+  const int rb = min(Hh - rt, max(0, y0 - m.H + Hh - g.n[1]));
+  const int nrow = (rt + rb) * W;
+  const int ncol = cl + cr;
+  const int count = nrow + (Hh - rt - rb) * ncol;
+  for (int e = threadIdx.x + 32 * threadIdx.y; e < count; e += kThreads) {
+    int ly, lx;
+    if (e < nrow) {
+      const int r = e / W;
+      ly = r < rt ? r : Hh - rb + (r - rt);
+      lx = e - r * W;
+    } else {
+      const int e2 = e - nrow;
+      const int r = e2 / ncol, c = e2 - r * ncol;
+      ly = rt + r;
+      lx = c < cl ? c : W - cr + (c - cl);
+    }
+    const int gy = y0 - m.H + ly, gx = x0 - m.H + lx;
+    dst[ly * m.BX + (gx - x0 + kXOff)] = fetch<T, 3>(in, g, bc, 0, p, gy, gx);
   }
 }
 
