@@ -171,7 +171,10 @@ __global__ void __launch_bounds__(kThreads)
   pdl_wait();
   pdl_launch_next();
   if (y0 >= ny) return;  // whole warp
-  const bool fast = vec_ok && x0 >= 1 && x0 + WW + 1 <= nx && y0 >= 1 && y0 + kRB + 1 <= ny;
+  // full strips whose rows y0 - 1 .. y0 + kRB lie inside the grid take the
+  // vector path; the left / right edge strips fetch their one ghost column
+  // through the boundary rule (lanes 0 / 31 only)
+  const bool fast = vec_ok && x0 + WW <= nx && y0 >= 1 && y0 + kRB + 1 <= ny;
   if (fast) {
     const T* base = in + (int64_t)(y0 - 1) * g.pitch + x0;
     VT r[kRB + 2];
@@ -182,8 +185,14 @@ __global__ void __launch_bounds__(kThreads)
 #pragma unroll
     for (int j = 0; j < kRB; ++j) {
       const T* row = base + (int64_t)(j + 1) * g.pitch;
-      wv[j] = lane == 0 ? __ldg(row - 1) : T(0);
-      ev[j] = lane == 31 ? __ldg(row + WW) : T(0);
+      if (lane == 0)
+        wv[j] = x0 >= 1 ? __ldg(row - 1) : fetch<T, 2>(in, g, bc, 0, y0 + j, x0 - 1);
+      else
+        wv[j] = T(0);
+      if (lane == 31)
+        ev[j] = x0 + WW + 1 <= nx ? __ldg(row + WW) : fetch<T, 2>(in, g, bc, 0, y0 + j, x0 + WW);
+      else
+        ev[j] = T(0);
     }
     T* obase = out + (int64_t)y0 * g.pitch + x0 + lane * V;
 #pragma unroll
