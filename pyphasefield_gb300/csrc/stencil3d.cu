@@ -88,9 +88,93 @@ __device__ __forceinline__ void issue_plane(const PlaneRing<T, NS>& ring, const 
   tma_load_3d(ring.plane(p), map, x0 - kXOff, y0 - m.H, pz, b);
 }
 
-// Rewrite the cells of plane p that the TMA box could not supply: columns or
-// rows outside the grid (edge tiles), or the whole of a ghost plane. Uses the
-// generic boundary rule.
+// The cells of a CTA's W x Hh window (W = TX + 2H, Hh = TY + 2H) that lie
+// outside the grid: cl / cr columns on the left / right, rt / rb rows at the
+// top / bottom, enumerated as the full rows first, then the outside columns
+// of the remaining rows.
+struct EdgeSet {
+  int W, Hh, cl, cr, rt, rb, nrow, ncol, count;
+};
+
+__device__ __forceinline__ EdgeSet edge_set(const MarchGeom& m, const Geo& g, int x0, int y0) {
+  EdgeSet E;
+  E.W = m.TX + 2 * m.H;
+  E.Hh = m.TY + 2 * m.H;
+  E.cl = min(E.W, max(0, m.H - x0));
+  E.cr = min(E.W - E.cl, max(0, x0 - m.H + E.W - g.n[2]));
+  E.rt = min(E.Hh, max(0, m.H - y0));
+  E.rb = min(E.Hh - E.rt, max(0, y0 - m.H + E.Hh - g.n[1]));
+  E.nrow = (E.rt + E.rb) * E.W;
+  E.ncol = E.cl + E.cr;
+  E.count = E.nrow + (E.Hh - E.rt - E.rb) * E.ncol;
+  return E;
+}
+
+// Window coordinates (ly, lx) of edge cell e < E.count.
+__device__ __forceinline__ void edge_cell(const EdgeSet& E, int e, int& ly, int& lx) {
+  if (e < E.nrow) {
+    const int r = e / E.W;
+    ly = r < E.rt ? r : E.Hh - E.rb + (r - E.rt);
+    lx = e - r * E.W;
+  } else {
+    const int e2 = e - E.nrow;
+    const int r = e2 / E.ncol, c = e2 - r * E.ncol;
+    ly = E.rt + r;
+    lx = c < E.cl ? c : E.W - E.cr + (c - E.cl);
+  }
+}
+
+// Edge cells per thread held in registers between the fetch of a plane's
+// edge values and their store into its slot.
+constexpr int kEdgeRegs = 2;
+
+// Fetch (boundary rule, global loads) the edge values of plane p into
+// registers: issued one plane ahead, the loads overlap the stencil of the
+// current plane.
+template <typename T>
+__device__ __forceinline__ void edge_load(const EdgeSet& E, const T* __restrict__ in,
+                                          const Geo& g, const Bc<T>& bc, const MarchGeom& m,
+                                          int x0, int y0, int p, T (&v)[kEdgeRegs]) {
+  const int tid = threadIdx.x + 32 * threadIdx.y;
+#pragma unroll
+  for (int k = 0; k < kEdgeRegs; ++k) {
+    const int e = tid + k * kThreads;
+    if (e < E.count) {
+      int ly, lx;
+      edge_cell(E, e, ly, lx);
+      v[k] = fetch<T, 3>(in, g, bc, 0, p, y0 - m.H + ly, x0 - m.H + lx);
+    }
+  }
+}
+
+// Store the edge values of plane p (after its TMA load landed); cells
+// beyond kEdgeRegs per thread are fetched here.
+template <typename T, int NS>
+__device__ __forceinline__ void edge_store(const EdgeSet& E, const PlaneRing<T, NS>& ring,
+                                           const T* __restrict__ in, const Geo& g,
+                                           const Bc<T>& bc, const MarchGeom& m, int x0, int y0,
+                                           int p, const T (&v)[kEdgeRegs]) {
+  T* dst = ring.plane(p) + (kXOff - m.H);
+  const int tid = threadIdx.x + 32 * threadIdx.y;
+#pragma unroll
+  for (int k = 0; k < kEdgeRegs; ++k) {
+    const int e = tid + k * kThreads;
+    if (e < E.count) {
+      int ly, lx;
+      edge_cell(E, e, ly, lx);
+      dst[ly * m.BX + lx] = v[k];
+    }
+  }
+  for (int e = tid + kEdgeRegs * kThreads; e < E.count; e += kThreads) {
+    int ly, lx;
+    edge_cell(E, e, ly, lx);
+    dst[ly * m.BX + lx] = fetch<T, 3>(in, g, bc, 0, p, y0 - m.H + ly, x0 - m.H + lx);
+  }
+}
+
+// Rewrite the cells of plane p that the TMA box could not supply: the edge
+// cells of an edge tile, or the whole of a ghost plane, by the generic
+// boundary rule.
 template <typename T, int NS>
 __device__ __forceinline__ void fixup_plane(const PlaneRing<T, NS>& ring, const T* __restrict__ in,
                                             const Geo& g, const Bc<T>& bc, const MarchGeom& m,
@@ -109,31 +193,12 @@ __device__ __forceinline__ void fixup_plane(const PlaneRing<T, NS>& ring, const 
     }
     return;
   }
-  // Only the cells outside the grid: cl / cr columns on the left / right,
-  // rt / rb rows at the top / bottom of the W x Hh window, enumerated as the
-  // full rows first, then the outside columns of the remaining rows, one
-  // cell per thread.
-  const int cl = min(W, max(0, m.H - x0));
-  const int cr = min(W - cl, max(0, x0 - m.H + W - g.n[2]));
-  const int rt = min(Hh, max(0, m.H - y0));
-  const int rb = min(Hh - rt, max(0, y0 - m.H + Hh - g.n[1]));
-  const int nrow = (rt + rb) * W;
-  const int ncol = cl + cr;
-  const int count = nrow + (Hh - rt - rb) * ncol;
-  for (int e = threadIdx.x + 32 * threadIdx.y; e < count; e += kThreads) {
+  const EdgeSet E = edge_set(m, g, x0, y0);
+  for (int e = threadIdx.x + 32 * threadIdx.y; e < E.count; e += kThreads) {
     int ly, lx;
-    if (e < nrow) {
-      const int r = e / W;
-      ly = r < rt ? r : Hh - rb + (r - rt);
-      lx = e - r * W;
-    } else {
-      const int e2 = e - nrow;
-      const int r = e2 / ncol, c = e2 - r * ncol;
-      ly = rt + r;
-      lx = c < cl ? c : W - cr + (c - cl);
-    }
-    const int gy = y0 - m.H + ly, gx = x0 - m.H + lx;
-    dst[ly * m.BX + (gx - x0 + kXOff)] = fetch<T, 3>(in, g, bc, 0, p, gy, gx);
+    edge_cell(E, e, ly, lx);
+    dst[ly * m.BX + lx + (kXOff - m.H)] =
+        fetch<T, 3>(in, g, bc, 0, p, y0 - m.H + ly, x0 - m.H + lx);
   }
 }
 
@@ -319,6 +384,8 @@ __global__ void __launch_bounds__(kThreads)
       drain(ring, z + 1, min(z + kNSL - 2, last));
       return;
     }
+    // (no register prefetch of the edge values here: its registers cost
+    // this kernel more occupancy than the hidden loads gain)
     if (xy_edge || ghost_plane(g, bc, z + 1)) {
       fixup_plane(ring, in, g, bc, m, x0, y0, z + 1, xy_edge);
       __syncthreads();
@@ -500,6 +567,13 @@ __global__ void __launch_bounds__(kThreads)
   long long acc_q = 0;
   double acc = 0.0;
   T vmax = T(0), vsum = T(0);
+  // edge tiles: the boundary-rule values of plane z + 2 are fetched into
+  // registers during iteration z - 1
+  const EdgeSet E = edge_set(m, g, x0, y0);
+  const bool has_edge = xy_edge && E.count > 0;
+  T pre[kEdgeRegs];
+  if (has_edge && z0 + 2 <= last && !ghost_plane(g, bc, z0 + 2))
+    edge_load(E, in, g, bc, m, x0, y0, z0 + 2, pre);
   for (int z = z0; z < z1; ++z) {
     // plane z + kNSC - 2 reuses the slot of plane z - 2, last read in
     // iteration z - 2 (c plane p is read in iterations p - 2 .. p), before
@@ -510,10 +584,15 @@ __global__ void __launch_bounds__(kThreads)
       drain(ring, z + 2, min(z + kNSC - 2, last));
       return;
     }
-    if (xy_edge || ghost_plane(g, bc, z + 2)) {
+    if (ghost_plane(g, bc, z + 2)) {
       fixup_plane(ring, in, g, bc, m, x0, y0, z + 2, xy_edge);
       __syncthreads();
+    } else if (has_edge) {
+      edge_store(E, ring, in, g, bc, m, x0, y0, z + 2, pre);
+      __syncthreads();
     }
+    if (has_edge && z + 3 <= last && !ghost_plane(g, bc, z + 3))
+      edge_load(E, in, g, bc, m, x0, y0, z + 3, pre);
     const T* P0 = ring.plane(z);
     const T* P1 = ring.plane(z + 1);
     const T* P2 = ring.plane(z + 2);
