@@ -437,13 +437,15 @@ __device__ __forceinline__ T ch_flux(const ChCoef<T>& k, T mn, T mc) {
   return k.a * (mn - mc);
 }
 
-constexpr int kNSC = 8;  // c planes z..z+2 read, z+3 .. z+6 in flight
+constexpr int kNSC = 7;  // c planes z..z+2 read, z+3 .. z+5 in flight
+constexpr int kMuSlots = 3;  // mu planes z - 1, z, z + 1
 // Cahn-Hilliard tile: 32 x 32 cells, 256 threads; thread (tx, ty) owns the
 // kCQ = 4 xy-columns (ty + 8q, tx) and keeps, per column, c(z), c(z+1),
 // mu(z) and the flux through the face below plane z in registers while
 // marching along z (the flux through a face is computed once: the cell
 // above takes it negated, bit for bit). mu of the tile plus a one-cell ring
-// lives in a two-plane shared ring for the xy fluxes; the kRingN ring
+// lives in a three-plane shared ring for the xy fluxes (one block barrier
+// per plane: the one that publishes mu(z + 1)); the kRingN ring
 // positions are computed by threads 0..kRingN-1. Every shared index is a
 // compile-time offset from a per-thread base.
 constexpr int kCTX = 32;
@@ -491,8 +493,10 @@ __global__ void __launch_bounds__(kThreads)
   const bool xy_edge = x0 - kXOff < 0 || y0 - 2 < 0 || x0 + kCTX + kXOff > nx ||
                        y0 + kCTY + 2 > ny;
   PlaneRing<T, kNSC> ring{align128<T>(smem_raw), bars, kCSlot, z0 - 2};
-  T* const mring = ring.slots + kNSC * kCSlot;  // 2 mu planes
-  auto mslot = [&](int z) { return mring + ((z - z0) & 1) * kMN; };
+  // kMuSlots mu planes: in iteration z a thread writes mu(z + 1) while
+  // others may still read mu(z - 1) (nothing but the one barrier per plane
+  // orders the iterations), so mu(z - 1), mu(z), mu(z + 1) need three slots
+  T* const mring = ring.slots + kNSC * kCSlot;
   const bool leader = tid == 0;
   (void)slot_elems;
 
@@ -539,7 +543,7 @@ __global__ void __launch_bounds__(kThreads)
     const T* Pm1 = ring.plane(z0 - 1);
     const T* P0 = ring.plane(z0);
     const T* P1 = ring.plane(z0 + 1);
-    T* M0 = mslot(z0);
+    T* M0 = mring;
 #pragma unroll
     for (int q = 0; q < kCQ; ++q) {
       const int i = ci + q * 8 * kCW;
@@ -554,6 +558,9 @@ __global__ void __launch_bounds__(kThreads)
     }
     if (has_ring) M0[rmi] = mu_at(Pm1, P0, P1, rci);
   }
+  // the first iteration's load goes into the slot of plane z0 - 2, read
+  // just above
+  __syncthreads();
 
   T* optr = out + (int64_t)z0 * g.plane + (int64_t)(y0 + ty) * g.pitch + x0 + tx;
   const int64_t qstride = (int64_t)8 * g.pitch;
@@ -567,6 +574,7 @@ __global__ void __launch_bounds__(kThreads)
   long long acc_q = 0;
   double acc = 0.0;
   T vmax = T(0), vsum = T(0);
+  int m0i = 0;  // mu slot of plane z
   // edge tiles: the boundary-rule values of plane z + 2 are fetched into
   // registers during iteration z - 1
   const EdgeSet E = edge_set(m, g, x0, y0);
@@ -579,11 +587,9 @@ __global__ void __launch_bounds__(kThreads)
     // iteration z - 2 (c plane p is read in iterations p - 2 .. p), before
     // the barriers of iteration z - 1
     if (leader && z + kNSC - 2 <= last) issue_plane(ring, &map, g, bc, m, x0, y0, z + kNSC - 2);
-    if (!wait_all(ring.bar(z + 2), ring.parity(z + 2), &abort_flag)) {
-      report_timeout<T>(lib_status);
-      drain(ring, z + 2, min(z + kNSC - 2, last));
-      return;
-    }
+    // every thread waits for plane z + 2 itself; a timeout is acted on, by
+    // all threads alike, after the barrier below
+    if (!mbar_wait(ring.bar(z + 2), ring.parity(z + 2))) abort_flag = 1;
     if (ghost_plane(g, bc, z + 2)) {
       fixup_plane(ring, in, g, bc, m, x0, y0, z + 2, xy_edge);
       __syncthreads();
@@ -596,7 +602,8 @@ __global__ void __launch_bounds__(kThreads)
     const T* P0 = ring.plane(z);
     const T* P1 = ring.plane(z + 1);
     const T* P2 = ring.plane(z + 2);
-    T* M1 = mslot(z + 1);
+    const int m1i = m0i == kMuSlots - 1 ? 0 : m0i + 1;
+    T* M1 = mring + m1i * kMN;
     T c2[kCQ], mup[kCQ];
 #pragma unroll
     for (int q = 0; q < kCQ; ++q) {
@@ -607,7 +614,13 @@ __global__ void __launch_bounds__(kThreads)
     }
     if (has_ring) M1[rmi] = mu_at(P0, P1, P2, rci);
     __syncthreads();
-    const T* M0 = mslot(z);
+    if (abort_flag) {
+      report_timeout<T>(lib_status);
+      drain(ring, z + 2, min(z + kNSC - 2, last));
+      return;
+    }
+    const T* M0 = mring + m0i * kMN;
+    m0i = m1i;
     int32_t quanta = 0;
 #pragma unroll
     for (int q = 0; q < kCQ; ++q) {
@@ -804,7 +817,7 @@ int32_t cahn_hilliard(const PpfCahnHilliardParams* p, const PpfGrid* grid_in,
   ct.depth = tiling ? tiling->depth : 0;
   ct.tile_x = kCTX;
   ct.tile_y = kCTY;
-  if ((rc = plan3d<T>(&ct, g, 2, kNSC, 2, &m, &slot_elems, &smem))) return rc;
+  if ((rc = plan3d<T>(&ct, g, 2, kNSC, kMuSlots, &m, &slot_elems, &smem))) return rc;
   if (slot_elems != kCSlot || m.BX != kCW || m.BY != kCH)
     return fail(PPF_ERR_INVALID, "Cahn-Hilliard plane slot mismatch");
   ChCoef<T> k;
