@@ -38,8 +38,8 @@ def save(name, meta, **arrays):
 
 def write_tdb(tdb, path):
     """The FUNCTION and PARAMETER records the NCGPU fixtures use, re-emitted
-    from the parsed database (so the GPU machine, which has no reference
-    checkout, reads the same thermodynamic data)."""
+    from the parsed database (so that a machine without the reference
+    checkout reads the same thermodynamic data)."""
     lines = ["$ " + ("Ni-Cu" if len(tdb.elements) == 2 else "-".join(tdb.elements))
              + " ideal solution records used by the NCGPU fixtures "
              "(written by tests/golden/make_golden.py)"]
