@@ -222,15 +222,24 @@ __global__ void __launch_bounds__(256)
   const T q4xp = F(q4, 0, 1), q4xm = F(q4, 0, -1), q4yp = F(q4, 1, 0), q4ym = F(q4, -1, 0);
   const T dq1x = T(0.5) * idx * (q1xp - q1xm), dq1y = T(0.5) * idx * (q1yp - q1ym);
   const T dq4x = T(0.5) * idx * (q4xp - q4xm), dq4y = T(0.5) * idx * (q4yp - q4ym);
-  T gxp = idx * sqrt((q1xp - a1) * (q1xp - a1) + (q4xp - a4) * (q4xp - a4));
-  T gxm = idx * sqrt((q1xm - a1) * (q1xm - a1) + (q4xm - a4) * (q4xm - a4));
-  T gyp = idx * sqrt((q1yp - a1) * (q1yp - a1) + (q4yp - a4) * (q4yp - a4));
-  T gym = idx * sqrt((q1ym - a1) * (q1ym - a1) + (q4ym - a4) * (q4ym - a4));
+  // |grad q| across each face, g = idx sqrt(s), and the reciprocal of its
+  // value clamped below at beta, from one reciprocal square root per face
+  // (s = 0, a uniform orientation, takes 1 / beta)
+  T gxp, gxm, gyp, gym, igxp, igxm, igyp, igym;
+  {
+    const T dx_ = T(1) / idx, ibeta = T(1) / k.beta;
+    auto face = [&](T dq1, T dq4, T& gf, T& igf) {
+      const T sq = dq1 * dq1 + dq4 * dq4;
+      const T r = sq > T(0) ? rsqrt(sq) : T(0);
+      gf = idx * (sq * r);
+      igf = gf < k.beta ? ibeta : dx_ * r;
+    };
+    face(q1xp - a1, q4xp - a4, gxp, igxp);
+    face(q1xm - a1, q4xm - a4, gxm, igxm);
+    face(q1yp - a1, q4yp - a4, gyp, igyp);
+    face(q1ym - a1, q4ym - a4, gym, igym);
+  }
   const T mgq = T(0.5) * (gxp + gxm + gyp + gym);
-  gxp = gxp < k.beta ? k.beta : gxp;
-  gxm = gxm < k.beta ? k.beta : gxm;
-  gyp = gyp < k.beta ? k.beta : gyp;
-  gym = gym < k.beta ? k.beta : gym;
   // psi: the phi gradient rotated by the orientation. The anisotropy terms
   // divide powers of psi by powers of |grad phi|^2 (up to the 8th); they are
   // evaluated here on the unit vectors u = grad phi / m, s = psi / m
@@ -238,7 +247,7 @@ __global__ void __launch_bounds__(256)
   // the same expressions, without the float overflow of |grad phi|^8 at
   // centimetre cell sizes
   const T q2q2 = a1 * a1 - a4 * a4, qq2 = T(2) * a1 * a4;
-  const T m = sqrt(mg2), im = T(1) / m;
+  const T im = rsqrt(mg2), m = mg2 * im;
   const T ux = dpx * im, uy = dpy * im;
   const T sx = (q2q2 * dpx - qq2 * dpy) * im, sy = (qq2 * dpx + q2q2 * dpy) * im;
   const T sx2 = sx * sx, sy2 = sy * sy;
@@ -310,8 +319,8 @@ __global__ void __launch_bounds__(256)
   const T Dq = T(2) * k.H * t * ph * ph;
   const T Dxp = T(2) * k.H * txp * pxp * pxp, Dxm = T(2) * k.H * txm * pxm * pxm;
   const T Dyp = T(2) * k.H * typ * pyp * pyp, Dym = T(2) * k.H * tym * pym * pym;
-  const T rxp = (Dq + Dxp) / gxp, rxm = (Dq + Dxm) / gxm;
-  const T ryp = (Dq + Dyp) / gyp, rym = (Dq + Dym) / gym;
+  const T rxp = (Dq + Dxp) * igxp, rxm = (Dq + Dxm) * igxm;
+  const T ryp = (Dq + Dyp) * igyp, rym = (Dq + Dym) * igym;
   auto fori = [&](T q, T qxp, T qxm, T qyp, T qym) {
     return T(0.5) * idx * idx *
            (rxp * (qxp - q) - rxm * (q - qxm) + ryp * (qyp - q) - rym * (q - qym));
@@ -326,7 +335,7 @@ __global__ void __launch_bounds__(256)
   pn = pn < T(0.000001) ? T(0.000001) : pn;
   pn = pn > T(0.999999) ? T(0.999999) : pn;
   const T n1 = a1 + k.dt * dq1, n4 = a4 + k.dt * dq4;
-  const T irn = T(1) / sqrt(n1 * n1 + n4 * n4);
+  const T irn = rsqrt(n1 * n1 + n4 * n4);
   phi_o[i] = pn;
   q1_o[i] = n1 * irn;
   q4_o[i] = n4 * irn;
