@@ -167,6 +167,28 @@ def test_cahn_hilliard_vs_oracle(cuda, shape, bc):
     assert rel_l2(out, ref) < F64_TOL
 
 
+@pytest.mark.parametrize("shape,bc", [((30, 37, 45), "PERIODIC"), ((24, 100, 100), "PERIODIC"),
+                                      ((26, 41, 35), "NEUMANN"),
+                                      ((25, 70, 99), ["PERIODIC", "NEUMANN", "PERIODIC"])])
+def test_cahn_hilliard_edge_and_interior_tiles(cuda, shape, bc):
+    """Grids with partial 32 x 32 tiles, interior tiles beside edge tiles
+    (whose cells outside the grid are fetched a plane ahead) and several
+    z chunks: fp64 against the oracle, and the quantised float path within
+    the float tolerance with its sum exactly constant."""
+    q = 2.0 ** -24
+    rng = np.random.default_rng(18)
+    c0 = 0.5 + rng.uniform(-0.05, 0.05, shape)
+    c0 = 0.5 + np.rint((c0 - 0.5) / q) * q
+    ref = restate.run_single("cahn_hilliard", c0, 12, bc, 1.0, 0.01, M=1.0, epsilon=1.0)
+    out = run_single_gpu("cahn_hilliard", c0, 12, bc, 1.0, 0.01, precision="fp64", M=1.0,
+                         epsilon=1.0)
+    assert rel_l2(out, ref) < F64_TOL
+    out = run_single_gpu("cahn_hilliard", c0, 12, bc, 1.0, 0.01, precision="fp32", quantum=q,
+                         centered=1, M=1.0, epsilon=1.0)
+    assert rel_l2(out, ref) < F32_TOL
+    assert (out - 0.5).sum() == (c0 - 0.5).sum()
+
+
 def test_cahn_hilliard_quantised_conserves_mass_exactly(cuda):
     """Centered storage + 2^-24 face-flux quantum: the float field's sum is
     exactly constant, and the field stays within 1e-5 of FP64."""
