@@ -23,6 +23,9 @@ _POWER = {0: "1", 1: "T", 2: "T2", 3: "T3", 7: "T7", -1: "TM1", -9: "TM9"}
 R_GAS = 8.3145  # pycalphad's gas constant, used in the ideal mixing energy
 
 _NUM = r"[+-]?(?:\d+\.?\d*|\.\d+)(?:[eE][+-]?\d+)?"
+# a number's mantissa and its exponent letter (1.5E, .5e), not a name that
+# ends in E (GHSERFE): the sign that follows belongs to the exponent
+_EXP_MANTISSA = re.compile(r"(?:^|[^A-Za-z_0-9.])(?:\d+\.?\d*|\.\d+)[eE]$")
 
 
 class TdbError(ValueError):
@@ -38,7 +41,7 @@ def _split_terms(expr: str) -> list[str]:
             depth += 1
         elif ch == ")":
             depth -= 1
-        if ch in "+-" and depth == 0 and cur.strip() and not re.search(r"[eE]$", cur.strip()) \
+        if ch in "+-" and depth == 0 and cur.strip() and not _EXP_MANTISSA.search(cur.strip()) \
                 and not cur.rstrip().endswith("*"):
             terms.append(cur)
             cur = ch

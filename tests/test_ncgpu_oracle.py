@@ -152,3 +152,59 @@ def test_params_struct_fills_every_component():
             assert p.npieces[ph][j] == npieces[ph, j] > 0
             for k in range(4):
                 assert list(p.gibbs[ph][j][k]) == list(table[ph, j, k])
+
+
+def _write(tmp_path, text):
+    path = tmp_path / "db.tdb"
+    path.write_text(text)
+    return path
+
+
+def test_tdb_reader_abbreviations_exponents_and_nested_functions(tmp_path):
+    """Abbreviated keywords, `$` comments, exponents written 1.5E-003 and
+    T**(-1), a FUNCTION whose name ends in E followed by a sign (GBASE+...),
+    and a FUNCTION that refers to another across a range boundary (the
+    pieces split where either expression changes)."""
+    path = _write(tmp_path, """
+$ comment line
+ELEM AA FCC_A1 0 0 0 !
+ELEM BB FCC_A1 0 0 0 !
+FUNCT GBASE 300 +100.0-2.5E+000*T+1.5E-003*T**2; 1000 Y
+   -50.0+3*T*LN(T); 3000 N !
+FUNCT GSHIFT 300 GBASE+1000*T**(-1)+2*T**(-1); 3000 N !
+PHASE FCC_A1 % 1 1 !
+PHASE LIQUID % 1 1 !
+PARA G(FCC_A1,AA;0) 300 GSHIFT; 3000 N !
+PARA G(FCC_A1,BB;0) 300 -GBASE; 3000 N !
+PARA G(LIQUID,AA;0) 300 +GBASE-10*T; 3000 N !
+PARA G(LIQUID,BB;0) 300 1.0E+029*T**(-9); 3000 N !
+""")
+    db = Database(path)
+    assert db.elements == ["AA", "BB"] and db.phases == ["FCC_A1", "LIQUID"]
+
+    def g(ph, comp, T):
+        return [g_eval(c, T) for lo, hi, c in db.params[(ph, comp)] if lo <= T < hi][0]
+
+    import math
+    for T in (400.0, 999.0, 1000.0, 2500.0):
+        base = 100.0 - 2.5 * T + 1.5e-3 * T * T if T < 1000 else -50.0 + 3 * T * math.log(T)
+        assert g("FCC_A1", "AA", T) == pytest.approx(base + 1000 / T + 2 / T, rel=1e-13)
+        assert g("FCC_A1", "BB", T) == pytest.approx(-base, rel=1e-13)
+        assert g("LIQUID", "AA", T) == pytest.approx(base - 10 * T, rel=1e-13)
+        assert g("LIQUID", "BB", T) == pytest.approx(1e29 * T ** -9, rel=1e-13)
+    assert [(lo, hi) for lo, hi, _ in db.params[("FCC_A1", "AA")]] == [(300.0, 1000.0),
+                                                                       (1000.0, 3000.0)]
+
+
+@pytest.mark.parametrize("record", [
+    "PARAMETER L(LIQUID,AA,BB;0) 300 -1000; 3000 N !",   # excess (interaction) parameter
+    "PARAMETER G(FCC_A1,AA:VA;0) 300 100; 3000 N !",     # two sublattices
+    "PARAMETER G(FCC_A1,AA;1) 300 100; 3000 N !",        # order 1
+    "PARAMETER G(FCC_A1,AA;0) 300 100*SIN(T); 3000 N !",  # a term outside the basis
+])
+def test_tdb_reader_rejects_what_the_kernel_cannot_evaluate(tmp_path, record):
+    from pyphasefield_gb300.tdb import TdbError
+    path = _write(tmp_path, "ELEM AA FCC_A1 0 0 0 !\nELEM BB FCC_A1 0 0 0 !\n"
+                            "PHASE FCC_A1 % 1 1 !\nPHASE LIQUID % 1 1 !\n" + record + "\n")
+    with pytest.raises(TdbError):
+        Database(path)
