@@ -332,7 +332,8 @@ int32_t ppf_var_line_solve_f64(const PpfGrid* g, int32_t axis, double alpha, dou
  * holds up to 4 temperature ranges of the pure element's Gibbs energy in
  * J/mol, {T_lo, T_hi, c_1, c_T, c_TlnT, c_T^2, c_T^3, c_T^7, c_1/T, c_T^-9}
  * (phase 0 = the solid, the first phase name in sorted order; 1 = liquid);
- * the molar Gibbs energy adds R T sum_i x_i ln x_i, R = 8.3145.
+ * the molar Gibbs energy adds R T sum_i x_i ln x_i, R = 8.3145, and the
+ * binary Redlich-Kister terms of `excess`.
  * noise_scale multiplies the Langevin term of dF/dc (1 = the reference);
  * its N(0,1) numbers come from Philox4x32-10 keyed by (seed, step
  * (+ *step_base), cell). temperature: a field of the grid's layout.
@@ -341,13 +342,25 @@ int32_t ppf_var_line_solve_f64(const PpfGrid* g, int32_t axis, double alpha, dou
  * one forward difference per cell (the first component up, the last down)
  * shared by every component. */
 #define PPF_NCGPU_MAX_COMP 6
+#define PPF_NCGPU_MAX_EXCESS 16
+/* One binary Redlich-Kister term of a phase: x_a x_b L(T) (x_a - x_b)^order
+ * added to its molar Gibbs energy, L piecewise in T as the gibbs ranges. */
+typedef struct PpfNcgpuExcess {
+  int32_t phase;      /* 0 the solid, 1 the liquid */
+  int32_t a, b;       /* component indices (sorted order), a != b */
+  int32_t order;      /* k >= 0 */
+  int32_t npieces;    /* temperature ranges in piece, 0..4 */
+  int32_t reserved;
+  double piece[4][10];
+} PpfNcgpuExcess;
 typedef struct PpfNcgpuParams {
   double dx, dt, v_m, D_L, D_S, M_qmax, H, y_e, beta, ebar2, noise_scale;
   double W[PPF_NCGPU_MAX_COMP], M[PPF_NCGPU_MAX_COMP];
   double gibbs[2][PPF_NCGPU_MAX_COMP][4][10];
   int32_t npieces[2][PPF_NCGPU_MAX_COMP];
   int32_t ncomp;
-  int32_t reserved;
+  int32_t nexcess;    /* 0..PPF_NCGPU_MAX_EXCESS terms in excess */
+  PpfNcgpuExcess excess[PPF_NCGPU_MAX_EXCESS];
 } PpfNcgpuParams;
 
 int32_t ppf_ncgpu_step_f32(const PpfNcgpuParams* p, const PpfGrid* g, const PpfBoundary* bc,
@@ -359,10 +372,11 @@ int32_t ppf_ncgpu_step_f64(const PpfNcgpuParams* p, const PpfGrid* g, const PpfB
                            const double* temperature, const double* tables, double* transfer,
                            uint64_t seed, uint64_t step, const uint64_t* step_base, void* stream);
 
-/* The pure-element Gibbs energies of both phases at every cell's
- * temperature, for a temperature field that stays fixed over many steps:
- * tables = 2 ncomp planes of doubles in the grid's layout (rows x pitch
- * each), plane l = G(solid, component l), plane ncomp + l = G(liquid, l).
+/* The pure-element Gibbs energies of both phases and the interaction
+ * parameters at every cell's temperature, for a temperature field that
+ * stays fixed over many steps: tables = 2 ncomp + nexcess planes of doubles
+ * in the grid's layout (rows x pitch each), plane l = G(solid, component l),
+ * plane ncomp + l = G(liquid, l), plane 2 ncomp + e = L of excess[e].
  * Passed as `tables` to ppf_ncgpu_step_*, the step reads them instead of
  * evaluating the piecewise polynomials (NULL: evaluated every step, the
  * same values). Recompute them whenever the temperature changes. */

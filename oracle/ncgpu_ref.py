@@ -10,8 +10,8 @@ Reference: Engines/NCGPU.py
 
 The Gibbs energies are what pyphasefield builds with pycalphad
 (simulation.py:179-243 / ppf_utils.TDBContainer): for each phase the
-Redlich-Kister sum of the TDB's G parameters (here only pure-element terms)
-plus pycalphad's ideal mixing energy R T sum x ln x, R = 8.3145 (pycalphad's
+Redlich-Kister sum of the TDB's G and binary L parameters plus pycalphad's
+ideal mixing energy R T sum x ln x, R = 8.3145 (pycalphad's
 gas constant), evaluated at (x_1 .. x_N, T) with components and phases in
 sorted order. pycalphad is not installed here; this module parses the TDB
 FUNCTION / PARAMETER records it needs itself (`Tdb`). The reference kernel
@@ -20,8 +20,10 @@ module); tests/golden/make_golden.py pins `step` below to it.
 
 Restatement notes:
   * dG/dc: the reference takes a forward difference with step 1e-7 in
-    float64 (:283-286); here the same difference is taken (the GPU uses the
-    exact derivative; the two differ by ~1e-7 relative).
+    float64 (:283-286); here (and on the GPU) the same difference is taken.
+  * excess energies: binary Redlich-Kister L parameters are added in the
+    CALPHAD convention (constituents in the order the record writes them);
+    pycalphad, absent here, is the reference's evaluator of these terms.
   * noise: the reference draws N(0,1) per cell from numba's xoroshiro128p
     streams indexed by the x thread index only (:290); here a normal per
     (cell, step) from Philox4x32-10 by Box-Muller (`noise_normal`), the same
@@ -56,6 +58,8 @@ class Tdb:
         records = " ".join(lines).split("!")
         self.functions: dict[str, list] = {}
         self.params: dict[tuple, str] = {}
+        # binary Redlich-Kister terms: (phase, A, B, order k, pieces)
+        self.excess: list[tuple] = []
         self.elements: list[str] = []
         self.phases: list[str] = []
         for rec in records:
@@ -79,6 +83,13 @@ class Tdb:
                     comp = m.group(2).strip().upper()
                     body = self._pieces(m.group(3))
                     self.params[(phase, comp)] = body
+                    continue
+                m = re.match(r"\s*PARAMETER\s+L\s*\(\s*([^,]+?)\s*,\s*([^,;:]+?)\s*,"
+                             r"\s*([^,;:]+?)\s*;\s*(\d+)\s*\)\s*(.*)", rec, re.IGNORECASE)
+                if m:
+                    self.excess.append((m.group(1).upper(), m.group(2).upper(),
+                                        m.group(3).upper(), int(m.group(4)),
+                                        self._pieces(m.group(5))))
         self.elements.sort()
         self.phases.sort()
 
@@ -111,7 +122,7 @@ class Tdb:
     def _eval(self, expr: str, T: float, depth: int) -> float:
         if depth > 8:
             raise ValueError("TDB function nesting too deep")
-        e = re.sub(r"LN\(", "log(", expr, flags=re.IGNORECASE)
+        e = re.sub(r"LN\(", "log(", expr.replace("#", ""), flags=re.IGNORECASE)
         e = e.replace("e+0", "e+").replace("e-0", "e-")
         names = {"T": T, "log": math.log}
         for sym in set(re.findall(r"[A-Za-z_][A-Za-z_0-9]*", e)):
@@ -127,14 +138,29 @@ class Tdb:
                 return self._eval(expr, T, 0)
         return 0.0
 
+    def excess_value(self, pieces, T: float) -> float:
+        for lo, hi, expr in pieces:
+            if lo <= T < hi:
+                return self._eval(expr, T, 0)
+        return 0.0
+
     def gibbs(self, phase: str, x, T: float) -> float:
         """Molar Gibbs energy of `phase` at site fractions x (components in
-        sorted order): sum x_i G_i + R T sum x_i ln x_i."""
+        sorted order): sum x_i G_i + R T sum x_i ln x_i + the binary
+        Redlich-Kister terms x_A x_B L_k(T) (x_A - x_B)^k, A and B in the
+        order the PARAMETER record writes them (the CALPHAD convention for
+        odd k)."""
         g = 0.0
         for comp, xi in zip(self.elements, x):
             g += xi * self.g_pure(phase, comp, T)
         mix = sum(xi * math.log(xi) for xi in x if xi > 0)
-        return g + R_PYCALPHAD * T * mix
+        g = g + R_PYCALPHAD * T * mix
+        for ph, a, b, k, pieces in self.excess:
+            if ph != phase.upper():
+                continue
+            xa, xb = x[self.elements.index(a)], x[self.elements.index(b)]
+            g += xa * xb * self.excess_value(pieces, T) * (xa - xb) ** k
+        return g
 
     def scalar(self, name: str) -> float:
         """A constant FUNCTION (CU_L, V_M, ...) evaluated as npvalue does

@@ -92,6 +92,12 @@ class PpfImplicitDiffusionParams(C.Structure):
 
 
 PPF_NCGPU_MAX_COMP = 6
+PPF_NCGPU_MAX_EXCESS = 16
+
+
+class PpfNcgpuExcess(C.Structure):
+    _fields_ = [(n, C.c_int32) for n in ("phase", "a", "b", "order", "npieces", "reserved")] + [
+        ("piece", (C.c_double * 10) * 4)]
 
 
 class PpfNcgpuParams(C.Structure):
@@ -100,7 +106,8 @@ class PpfNcgpuParams(C.Structure):
         ("W", C.c_double * PPF_NCGPU_MAX_COMP), ("M", C.c_double * PPF_NCGPU_MAX_COMP),
         ("gibbs", (((C.c_double * 10) * 4) * PPF_NCGPU_MAX_COMP) * 2),
         ("npieces", (C.c_int32 * PPF_NCGPU_MAX_COMP) * 2),
-        ("ncomp", C.c_int32), ("reserved", C.c_int32)]
+        ("ncomp", C.c_int32), ("nexcess", C.c_int32),
+        ("excess", PpfNcgpuExcess * PPF_NCGPU_MAX_EXCESS)]
 
 
 PPF_MODEL_WARREN1995 = 1

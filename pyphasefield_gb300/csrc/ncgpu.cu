@@ -31,9 +31,14 @@ struct NcCoef {
   T W[kMaxComp], M[kMaxComp];
 };
 
+constexpr int kMaxExcess = PPF_NCGPU_MAX_EXCESS;
+
 struct NcGibbs {
   double piece[2][kMaxComp][4][10];  // [phase][component][piece] {lo, hi, 8 coefficients}
   int npieces[2][kMaxComp];
+  int nex;                            // binary Redlich-Kister terms
+  int ex_meta[kMaxExcess][5];         // phase, a, b, order, npieces
+  double ex_piece[kMaxExcess][4][10];
 };
 
 // The concentration fields and the per-component thermodynamic terms.
@@ -45,10 +50,12 @@ struct NcPtrs {
   T* dF[kMaxComp - 1];
 };
 
-__device__ __forceinline__ double g_pure(const NcGibbs& g, int ph, int comp, double T,
-                                         double lnT) {
-  for (int k = 0; k < g.npieces[ph][comp]; ++k) {
-    const double* c = g.piece[ph][comp][k];
+// A function piecewise in T over the basis 1, T, T ln T, T^2, T^3, T^7,
+// 1/T, T^-9: pieces[k] = {T_lo, T_hi, 8 coefficients}.
+__device__ __forceinline__ double piecewise(const double (*pieces)[10], int np, double T,
+                                           double lnT) {
+  for (int k = 0; k < np; ++k) {
+    const double* c = pieces[k];
     if (T >= c[0] && T < c[1]) {
       const double T2 = T * T, T3 = T2 * T, T7 = T3 * T3 * T, iT = 1.0 / T;
       const double iT3 = iT * iT * iT, iT9 = iT3 * iT3 * iT3;
@@ -57,6 +64,15 @@ __device__ __forceinline__ double g_pure(const NcGibbs& g, int ph, int comp, dou
     }
   }
   return 0.0;  // outside every range, as a piecewise TDB function gives
+}
+
+__device__ __forceinline__ double g_pure(const NcGibbs& g, int ph, int comp, double T,
+                                         double lnT) {
+  return piecewise(g.piece[ph][comp], g.npieces[ph][comp], T, lnT);
+}
+
+__device__ __forceinline__ double l_excess(const NcGibbs& g, int e, double T, double lnT) {
+  return piecewise(g.ex_piece[e], g.ex_meta[e][4], T, lnT);
 }
 
 // N(0,1) of cell (row, col) at a step: Box-Muller on two uniforms from a
@@ -77,8 +93,8 @@ __device__ __forceinline__ T noise_normal(uint64_t seed, uint64_t step, int row,
 // The pure-element Gibbs energies of both phases at a cell's temperature:
 // tab[l] = G_solid,l, tab[N + l] = G_liquid,l.
 template <int N>
-__device__ __forceinline__ void pure_energies(const NcGibbs& gb, double t, double* tab) {
-  const double lnT = log(t);
+__device__ __forceinline__ void pure_energies(const NcGibbs& gb, double t, double lnT,
+                                              double* tab) {
 #pragma unroll
   for (int l = 0; l < N; ++l) {
     tab[l] = g_pure(gb, 0, l, t, lnT);
@@ -86,13 +102,15 @@ __device__ __forceinline__ void pure_energies(const NcGibbs& gb, double t, doubl
   }
 }
 
-// The per-cell table of pure-element energies (2 ncomp planes of doubles in
-// the grid's layout) for a temperature field that stays fixed over many
-// steps: the thermodynamics kernel then reads 2 ncomp values per cell
-// instead of evaluating 2 ncomp piecewise polynomials and a logarithm.
+// The per-cell table of pure-element energies and interaction parameters
+// (2 ncomp + nex planes of doubles in the grid's layout) for a temperature
+// field that stays fixed over many steps: the thermodynamics kernel then
+// reads them instead of evaluating the piecewise polynomials and a
+// logarithm.
 template <typename T, int N>
 __global__ void __launch_bounds__(256)
-    ncgpu_table_kernel(Geo g, NcGibbs gb, const T* __restrict__ temp, double* __restrict__ tab) {
+    ncgpu_table_kernel(Geo g, const __grid_constant__ NcGibbs gb, const T* __restrict__ temp,
+                       double* __restrict__ tab) {
   pdl_wait();
   pdl_launch_next();
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
@@ -100,15 +118,18 @@ __global__ void __launch_bounds__(256)
   if (x >= g.n[1]) return;
   const int64_t i = (int64_t)y * g.pitch + x;
   const int64_t plane = (int64_t)g.n[0] * g.pitch;
+  const double t = (double)temp[i], lnT = log(t);
   double v[2 * N];
-  pure_energies<N>(gb, (double)temp[i], v);
+  pure_energies<N>(gb, t, lnT, v);
 #pragma unroll
   for (int l = 0; l < 2 * N; ++l) tab[l * plane + i] = v[l];
+  for (int e = 0; e < gb.nex; ++e) tab[(2 * N + e) * plane + i] = l_excess(gb, e, t, lnT);
 }
 
 template <typename T, int NC>
 __global__ void __launch_bounds__(256)
-    ncgpu_thermo_kernel(Geo g, NcCoef<T> k, NcGibbs gb, const T* __restrict__ phi,
+    ncgpu_thermo_kernel(Geo g, NcCoef<T> k, const __grid_constant__ NcGibbs gb,
+                        const T* __restrict__ phi,
                         NcPtrs<T> cp, const T* __restrict__ temp, const double* __restrict__ tab,
                         T* __restrict__ dG, uint64_t seed, uint64_t step,
                         const uint64_t* step_base) {
@@ -129,12 +150,13 @@ __global__ void __launch_bounds__(256)
     last -= xs[l];
   }
   xs[NC] = last;
+  const int64_t plane = (int64_t)g.n[0] * g.pitch;
+  const double lnT = tab ? 0.0 : log(t);
   if (tab) {
-    const int64_t plane = (int64_t)g.n[0] * g.pitch;
 #pragma unroll
     for (int l = 0; l < 2 * N; ++l) G[l] = __ldg(tab + l * plane + i);
   } else {
-    pure_energies<N>(gb, t, G);
+    pure_energies<N>(gb, t, lnT, G);
   }
   const double* Gs = G;
   const double* Gl = G + N;
@@ -156,11 +178,38 @@ __global__ void __launch_bounds__(256)
     linp_s += xp[l] * Gs[l];
     linp_l += xp[l] * Gl[l];
   }
+  // binary Redlich-Kister terms x_a x_b L (x_a - x_b)^k of each phase, at
+  // both compositions
+  double ex_s = 0.0, ex_l = 0.0, exp_s = 0.0, exp_l = 0.0;
+  for (int e = 0; e < gb.nex; ++e) {
+    const int a = gb.ex_meta[e][1], b = gb.ex_meta[e][2], ord = gb.ex_meta[e][3];
+    const double L = tab ? __ldg(tab + (2 * N + e) * plane + i) : l_excess(gb, e, t, lnT);
+    double xa = 0.0, xb = 0.0, pa = 0.0, pb = 0.0;
+#pragma unroll
+    for (int l = 0; l < N; ++l) {
+      xa = l == a ? xs[l] : xa;
+      xb = l == b ? xs[l] : xb;
+      pa = l == a ? xp[l] : pa;
+      pb = l == b ? xp[l] : pb;
+    }
+    double ts = xa * xb * L, tp = pa * pb * L;
+    for (int j = 0; j < ord; ++j) {
+      ts *= xa - xb;
+      tp *= pa - pb;
+    }
+    if (gb.ex_meta[e][0] == 0) {
+      ex_s += ts;
+      exp_s += tp;
+    } else {
+      ex_l += ts;
+      exp_l += tp;
+    }
+  }
   const double rt = 8.3145 * t;
-  const double gs = lin_s + rt * mix;
-  const double gl = lin_l + rt * mix;
-  const double dgl = 10000000.0 * ((linp_l + rt * mixp) - gl);
-  const double dgs = 10000000.0 * ((linp_s + rt * mixp) - gs);
+  const double gs = lin_s + rt * mix + ex_s;
+  const double gl = lin_l + rt * mix + ex_l;
+  const double dgl = 10000000.0 * ((linp_l + rt * mixp + exp_l) - gl);
+  const double dgs = 10000000.0 * ((linp_s + rt * mixp + exp_s) - gs);
   const T p = phi[i];
   const T gg = p * p * (T(1) - p) * (T(1) - p);
   const T h = p * p * p * (T(6) * p * p - T(15) * p + T(10));
@@ -363,6 +412,26 @@ int32_t make_gibbs(const PpfNcgpuParams* p, NcGibbs* gb) {
   static_assert(sizeof(gb->piece) == sizeof(p->gibbs), "Gibbs table layout");
   memcpy(gb->piece, p->gibbs, sizeof(gb->piece));
   memcpy(gb->npieces, p->npieces, sizeof(gb->npieces));
+  if (p->nexcess < 0 || p->nexcess > kMaxExcess)
+    return fail(PPF_ERR_INVALID, "nexcess must be 0..%d", kMaxExcess);
+  gb->nex = p->nexcess;
+  memset(gb->ex_meta, 0, sizeof(gb->ex_meta));
+  memset(gb->ex_piece, 0, sizeof(gb->ex_piece));
+  for (int e = 0; e < p->nexcess; ++e) {
+    const PpfNcgpuExcess& x = p->excess[e];
+    if (x.phase < 0 || x.phase > 1 || x.a < 0 || x.a >= p->ncomp || x.b < 0 ||
+        x.b >= p->ncomp || x.a == x.b || x.order < 0 || x.order > 16 || x.npieces < 0 ||
+        x.npieces > 4)
+      return fail(PPF_ERR_INVALID, "excess term %d: phase 0..1, components a != b below ncomp, "
+                  "order 0..16, npieces 0..4", e);
+    gb->ex_meta[e][0] = x.phase;
+    gb->ex_meta[e][1] = x.a;
+    gb->ex_meta[e][2] = x.b;
+    gb->ex_meta[e][3] = x.order;
+    gb->ex_meta[e][4] = x.npieces;
+    static_assert(sizeof(gb->ex_piece[0]) == sizeof(x.piece), "excess table layout");
+    memcpy(gb->ex_piece[e], x.piece, sizeof(x.piece));
+  }
   return PPF_OK;
 }
 

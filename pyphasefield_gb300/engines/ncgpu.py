@@ -2,7 +2,8 @@
 CUDA library: alloy solidification (2 to 6 components) with a phase field,
 two quaternion orientation fields and the fractions of all but the last
 component, thermodynamics from a TDB file (read by pyphasefield_gb300.tdb
-instead of pycalphad).
+instead of pycalphad: pure-element energies, ideal mixing and binary
+Redlich-Kister excess terms).
 
 Fields, in the reference's order: phi (1 = solid), q1, q4, c_<component> for
 every component but the last (sorted). user_data keys as the reference: d_ratio (4), sim_type ("seed"
@@ -100,7 +101,33 @@ def params_struct(db: Database, ud: dict, dx: float, noise_scale: float = 1.0):
             for k in range(4):
                 for e in range(10):
                     p.gibbs[ph][cp][k][e] = float(table[ph, cp, k, e])
+    terms = excess_terms(db)
+    p.nexcess = len(terms)
+    for j, (phase, a, b, order, pieces) in enumerate(terms):
+        x = p.excess[j]
+        x.phase, x.a, x.b, x.order, x.npieces = phase, a, b, order, len(pieces)
+        for k, (lo, hi, coefs) in enumerate(pieces):
+            x.piece[k][0], x.piece[k][1] = lo, hi
+            for e, v in enumerate(coefs):
+                x.piece[k][2 + e] = float(v)
     return p
+
+
+def excess_terms(db: Database) -> list:
+    """The database's binary Redlich-Kister terms as (phase index (0 the
+    solid, 1 the liquid), component index a, b, order, pieces)."""
+    out = []
+    for phase, a, b, order, pieces in db.excess:
+        if phase not in db.phases:
+            raise ValueError(f"L({phase},{a},{b};{order}): phase not listed")
+        if len(pieces) > 4:
+            raise NotImplementedError("more than 4 temperature ranges")
+        out.append((db.phases.index(phase), db.elements.index(a), db.elements.index(b), order,
+                    pieces))
+    if len(out) > L.PPF_NCGPU_MAX_EXCESS:
+        raise NotImplementedError(f"NCGPU: at most {L.PPF_NCGPU_MAX_EXCESS} interaction terms "
+                                  f"(the TDB has {len(out)})")
+    return out
 
 
 def make_seed(phi, q1, q4, x, y, angle, seed_radius):
@@ -195,7 +222,8 @@ class _NcgpuMixin(GB300Engine):
         self._nc_params = params_struct(self._ppf_db, ud, self.dx, ud.get("noise_scale", 1.0))
         # the temperature is fixed during a run: the pure-element energies of
         # every cell are evaluated once, after the upload, on the same stream
-        self._nc_tables = torch.empty((2 * ncomp,) + tuple(g.alloc_shape), dtype=torch.float64,
+        nplanes = 2 * ncomp + int(self._nc_params.nexcess)
+        self._nc_tables = torch.empty((nplanes,) + tuple(g.alloc_shape), dtype=torch.float64,
                                       device=g.device)
         L.call(f"ppf_ncgpu_tables_{_F[self._ppf_dtype]}", C.byref(self._nc_params),
                C.byref(g.grid), ptr(self._nc_temp), ptr(self._nc_tables),

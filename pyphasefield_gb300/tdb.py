@@ -4,14 +4,17 @@ pyphasefield builds its Gibbs energies with pycalphad (simulation.py:179-243,
 ppf_utils.TDBContainer): per phase, the Redlich-Kister sum of the TDB's G
 parameters plus the ideal mixing energy R T sum x ln x, components and phases
 in sorted order. pycalphad is not a dependency here: this reader handles the
-records such databases use for ideal solutions (ELEMENT, PHASE, FUNCTION,
-PARAMETER G(phase, component; 0)) and turns every temperature range of a pure
-element's Gibbs energy into coefficients of the basis
+records such databases use (ELEMENT, PHASE, FUNCTION, PARAMETER G(phase,
+component; 0) and the binary Redlich-Kister PARAMETER L(phase, A, B; k)) and
+turns every temperature range of a pure element's Gibbs energy or of an
+interaction parameter into coefficients of the basis
 
     1, T, T ln T, T^2, T^3, T^7, T^-1, T^-9
 
-which the CUDA kernel evaluates per cell. Excess (L) parameters and
-sublattices are not read: a database that has them is rejected.
+which the CUDA kernel evaluates per cell. An L parameter adds
+x_A x_B L_k(T) (x_A - x_B)^k to its phase, A and B in the order the record
+writes them (the CALPHAD convention for odd k). Sublattices and ternary
+interactions are not read: a database that has them is rejected.
 """
 from __future__ import annotations
 
@@ -94,6 +97,7 @@ class Database:
         records = [r.strip() for r in " ".join(lines).split("!")]
         self.functions: dict[str, list] = {}
         raw_params: dict[tuple, list] = {}
+        raw_excess: list[tuple] = []
         self.elements: list[str] = []
         self.phases: list[str] = []
         for rec in records:
@@ -115,13 +119,25 @@ class Database:
                 if not m:
                     raise TdbError(f"unreadable PARAMETER record {rec[:60]!r}")
                 kind, phase, comp, order, body = m.groups()
-                if kind.upper() != "G" or int(order) != 0 or ":" in comp or "," in comp:
-                    raise TdbError("only pure-element G parameters of one-sublattice phases are "
-                                   f"supported (got {rec[:60]!r})")
-                raw_params[(phase.upper(), comp.upper())] = self._ranges(body)
+                comps = [c.strip().upper() for c in comp.split(",")]
+                if ":" in comp or any(not c for c in comps):
+                    raise TdbError(f"sublattice parameters are not supported (got {rec[:60]!r})")
+                if kind.upper() == "G" and int(order) == 0 and len(comps) == 1:
+                    raw_params[(phase.upper(), comps[0])] = self._ranges(body)
+                elif kind.upper() == "L" and len(comps) == 2:
+                    raw_excess.append((phase.upper(), comps[0], comps[1], int(order),
+                                       self._ranges(body)))
+                else:
+                    raise TdbError("only pure-element G and binary L parameters are supported "
+                                   f"(got {rec[:60]!r})")
         self.elements.sort()
         self.phases.sort()
         self.params = {k: self._resolve(v) for k, v in raw_params.items()}
+        # binary Redlich-Kister terms: (phase, A, B, order k, pieces)
+        self.excess = [(ph, a, b, k, self._resolve(v)) for ph, a, b, k, v in raw_excess]
+        for ph, a, b, k, _ in self.excess:
+            if a not in self.elements or b not in self.elements or a == b:
+                raise TdbError(f"L({ph},{a},{b};{k}): components must be two listed elements")
 
     @staticmethod
     def _ranges(body: str) -> list:
@@ -144,7 +160,8 @@ class Database:
         if depth > 8:
             raise TdbError("FUNCTION references nest too deep")
         pieces = [(lo, hi, {})]
-        for term in _split_terms(expr):
+        # '#' marks a FUNCTION reference in some databases (GHSERNI#)
+        for term in _split_terms(expr.replace("#", "")):
             coefs, ref = _term(term, self.functions)
             if ref is None:
                 for _, _, acc in pieces:

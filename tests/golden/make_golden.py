@@ -40,8 +40,7 @@ def write_tdb(tdb, path):
     """The FUNCTION and PARAMETER records the NCGPU fixtures use, re-emitted
     from the parsed database (so that a machine without the reference
     checkout reads the same thermodynamic data)."""
-    lines = ["$ " + ("Ni-Cu" if len(tdb.elements) == 2 else "-".join(tdb.elements))
-             + " ideal solution records used by the NCGPU fixtures "
+    lines = ["$ " + "-".join(tdb.elements) + " records used by the NCGPU fixtures "
              "(written by tests/golden/make_golden.py)"]
     for el in tdb.elements:
         lines.append(f"ELEMENT {el} FCC_A1 0 0 0 !")
@@ -51,12 +50,21 @@ def write_tdb(tdb, path):
             more = k + 1 < len(pieces)
             body += f"; {hi!r} " + (f"Y {pieces[k + 1][2]}" if more else "N")
         lines.append(f"FUNCTION {name} {body} !")
+    def ranges(pieces):
+        body = f"{pieces[0][0]!r} {pieces[0][2].replace('#', '')}"
+        for k, (lo, hi, expr) in enumerate(pieces):
+            more = k + 1 < len(pieces)
+            body += f"; {hi!r} " + (f"Y {pieces[k + 1][2].replace('#', '')}" if more else "N")
+        return body
+
     for ph in tdb.phases:
         lines.append(f"PHASE {ph} % 1 1 !")
         for (pph, comp), pieces in tdb.params.items():
             if pph == ph:
-                lo, hi, expr = pieces[0]
-                lines.append(f"PARAMETER G({ph},{comp};0) {lo!r} {expr}; {hi!r} N !")
+                lines.append(f"PARAMETER G({ph},{comp};0) {ranges(pieces)} !")
+        for pph, a, b, k, pieces in getattr(tdb, "excess", []):
+            if pph == ph:
+                lines.append(f"PARAMETER L({ph},{a},{b};{k}) {ranges(pieces)} !")
     Path(path).write_text("\n".join(lines) + "\n")
 
 
@@ -193,6 +201,7 @@ def main():
     save("ncgpu_ternary", meta, phi0=phi0, q10=q10, q40=q40, c0_0=ca, c0_1=cb, phi=out[0],
          q1=out[1], q4=out[2], c_0=out[3], c_1=out[4])
     ncgpu_multicomponent()
+    ncgpu_excess()
 
     dx = 4.6e-8
     prm = dict(restate.WARREN_DEFAULTS)
@@ -264,8 +273,33 @@ def ncgpu_multicomponent():
         save(name, meta, **arrays)
 
 
+def ncgpu_excess():
+    """NCGPU on the reference's non-ideal Ni-Nb database
+    (tests/Ni-Nb_Simplified.tdb: binary Redlich-Kister L parameters of
+    orders 0-2 in both phases), re-emitted as tests/golden/ncgpu_ninb.tdb."""
+    from oracle import ncgpu_ref
+    src = refshim.reference_root() / "pyphasefield" / "tests" / "Ni-Nb_Simplified.tdb"
+    write_tdb(ncgpu_ref.Tdb(src), HERE / "ncgpu_ninb.tdb")
+    tdb = ncgpu_ref.Tdb(HERE / "ncgpu_ninb.tdb")
+    assert len(tdb.excess) == 5
+    nrng = np.random.default_rng(20240611)
+    shape, steps, seed, T0 = (20, 18), 3, 21, 1600.0
+    p = ncgpu_ref.tdb_params(tdb, 4.6e-6)
+    phi0, q10, q40, c0 = ncgpu_ref.seed_fields(shape, c0=0.10)
+    c0 = c0 + nrng.uniform(-1e-3, 1e-3, shape)
+    T = np.full(shape, T0)
+    noise = [ncgpu_ref.noise_normal(seed, s, shape) for s in range(steps)]
+    out = refshim.run_ncgpu(phi0, q10, q40, c0, T, steps, p, tdb, noise, "PERIODIC")
+    meta = dict(model="ncgpu", steps=steps, bc="PERIODIC", seed=seed, dx=4.6e-6, T=T0,
+                tdb="ncgpu_ninb.tdb")
+    save("ncgpu_ninb", meta, phi0=phi0, q10=q10, q40=q40, c0=c0, phi=out[0], q1=out[1],
+         q4=out[2], c=out[3])
+
+
 if __name__ == "__main__":
     if sys.argv[1:] == ["ncgpu_multicomponent"]:
         ncgpu_multicomponent()
+    elif sys.argv[1:] == ["ncgpu_excess"]:
+        ncgpu_excess()
     else:
         main()

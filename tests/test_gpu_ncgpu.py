@@ -46,7 +46,8 @@ def run_gpu(fields, T, steps, dx, seed, bc, precision, noise_scale=1.0, tdb=TDB,
     s = C.c_void_p(torch.cuda.current_stream().cuda_stream)
     tab = None
     if tables:
-        tab = torch.empty((2 * p.ncomp,) + tuple(a[0].shape), dtype=torch.float64, device="cuda")
+        tab = torch.empty((2 * p.ncomp + p.nexcess,) + tuple(a[0].shape), dtype=torch.float64,
+                          device="cuda")
         L.call(f"ppf_ncgpu_tables_{sfx}", C.byref(p), C.byref(g), C.c_void_p(temp.data_ptr()),
                C.c_void_p(tab.data_ptr()), s)
     for k in range(steps):
@@ -60,15 +61,17 @@ def run_gpu(fields, T, steps, dx, seed, bc, precision, noise_scale=1.0, tdb=TDB,
     return [from_dev(t, kshape, shape) for t in a]
 
 
-@pytest.mark.parametrize("name", ["ncgpu_periodic", "ncgpu_neumann"])
+@pytest.mark.parametrize("name", ["ncgpu_periodic", "ncgpu_neumann", "ncgpu_ninb"])
 @pytest.mark.parametrize("precision", ["fp64", "fp32"])
 @pytest.mark.parametrize("tables", [True, False])
 def test_reference_fixtures(cuda, name, precision, tables):
+    """Ni-Cu (ideal) and Ni-Nb (binary Redlich-Kister terms of orders 0-2)
+    against the reference's kernels."""
     z = np.load(GOLDEN / f"{name}.npz")
     m = json.loads(str(z["meta"]))
     T = np.full(z["phi0"].shape, m["T"])
     out = run_gpu([z["phi0"], z["q10"], z["q40"], z["c0"]], T, m["steps"], m["dx"], m["seed"],
-                  m["bc"], precision, tables=tables)
+                  m["bc"], precision, tables=tables, tdb=GOLDEN / m["tdb"])
     for got, key in zip(out, ("phi", "q1", "q4", "c")):
         assert rel_l2(got, z[key]) < TOL[precision], (key, rel_l2(got, z[key]))
 

@@ -17,7 +17,7 @@ GOLDEN = Path(__file__).resolve().parent / "golden"
 TDB = GOLDEN / "ncgpu_nicu.tdb"
 
 
-@pytest.mark.parametrize("name", ["ncgpu_periodic", "ncgpu_neumann"])
+@pytest.mark.parametrize("name", ["ncgpu_periodic", "ncgpu_neumann", "ncgpu_ninb"])
 def test_oracle_matches_reference_kernels(name):
     z = np.load(GOLDEN / f"{name}.npz")
     m = json.loads(str(z["meta"]))
@@ -197,7 +197,7 @@ PARA G(LIQUID,BB;0) 300 1.0E+029*T**(-9); 3000 N !
 
 
 @pytest.mark.parametrize("record", [
-    "PARAMETER L(LIQUID,AA,BB;0) 300 -1000; 3000 N !",   # excess (interaction) parameter
+    "PARAMETER L(LIQUID,AA,DD;0) 300 -1000; 3000 N !",   # interaction with no element DD
     "PARAMETER G(FCC_A1,AA:VA;0) 300 100; 3000 N !",     # two sublattices
     "PARAMETER G(FCC_A1,AA;1) 300 100; 3000 N !",        # order 1
     "PARAMETER G(FCC_A1,AA;0) 300 100*SIN(T); 3000 N !",  # a term outside the basis
@@ -206,5 +206,46 @@ def test_tdb_reader_rejects_what_the_kernel_cannot_evaluate(tmp_path, record):
     from pyphasefield_gb300.tdb import TdbError
     path = _write(tmp_path, "ELEM AA FCC_A1 0 0 0 !\nELEM BB FCC_A1 0 0 0 !\n"
                             "PHASE FCC_A1 % 1 1 !\nPHASE LIQUID % 1 1 !\n" + record + "\n")
+    with pytest.raises(TdbError):
+        Database(path)
+
+
+def test_redlich_kister_terms_reader_oracle_and_struct():
+    """The non-ideal Ni-Nb database (binary L parameters of orders 0-2 in
+    both phases): the package's reader, the oracle and the C struct agree,
+    and the molar Gibbs energy carries x_A x_B L_k (x_A - x_B)^k with A, B
+    in the order the records write them."""
+    import math
+    path = GOLDEN / "ncgpu_ninb.tdb"
+    db, tdb = Database(path), N.Tdb(path)
+    assert db.elements == ["NB", "NI"] and len(db.excess) == 5
+    T, x = 1600.0, [0.2, 0.8]
+    for ph in db.phases:
+        pure = sum(xi * tdb.g_pure(ph, c, T) for c, xi in zip(db.elements, x))
+        ideal = pure + 8.3145 * T * sum(xi * math.log(xi) for xi in x)
+        ex = 0.0
+        for eph, a, b, k, pieces in db.excess:
+            if eph == ph:
+                xa, xb = x[db.elements.index(a)], x[db.elements.index(b)]
+                L = [g_eval(c, T) for lo, hi, c in pieces if lo <= T < hi][0]
+                ex += xa * xb * L * (xa - xb) ** k
+        assert ex != 0.0
+        assert tdb.gibbs(ph, x, T) == pytest.approx(ideal + ex, rel=1e-13)
+    p = params_struct(db, ncgpu_parameters(db, 4.6e-6), 4.6e-6)
+    assert p.nexcess == 5
+    got = sorted((p.excess[j].phase, p.excess[j].a, p.excess[j].b, p.excess[j].order)
+                 for j in range(5))
+    # NI is component 1, NB component 0; FCC_A1 (the solid) is phase 0
+    assert got == [(0, 1, 0, 0), (0, 1, 0, 1), (1, 1, 0, 0), (1, 1, 0, 1), (1, 1, 0, 2)]
+    j = [p.excess[j].phase == 0 and p.excess[j].order == 1 for j in range(5)].index(True)
+    assert p.excess[j].npieces == 1 and p.excess[j].piece[0][2] == 94812.0
+
+
+def test_ternary_interactions_are_rejected(tmp_path):
+    from pyphasefield_gb300.tdb import TdbError
+    path = tmp_path / "t.tdb"
+    path.write_text("ELEM AA FCC_A1 0 0 0 !\nELEM BB FCC_A1 0 0 0 !\nELEM CC FCC_A1 0 0 0 !\n"
+                    "PHASE LIQUID % 1 1 !\n"
+                    "PARAMETER L(LIQUID,AA,BB,CC;0) 300 100; 3000 N !\n")
     with pytest.raises(TdbError):
         Database(path)
