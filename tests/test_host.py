@@ -171,3 +171,33 @@ def test_library_rejects_bad_arguments_without_gpu(built_lib):
     assert "pitch" in L.last_error()
     with pytest.raises(L.PpfError):
         L.call("ppf_diffusion_step_f32", None, C.byref(g), C.byref(b), None, None, None, None)
+
+
+def test_ncgpu_entry_points_validate_without_gpu(built_lib):
+    """NCGPU parameter checks run on the host before any launch: component
+    count, interaction-term count and indices, NULL buffers."""
+    from pyphasefield_gb300 import _lib as L
+    lib = L.load()
+    g = L.PpfGrid()
+    g.ndim = 2
+    g.shape[0], g.shape[1] = 8, 8
+    g.pitch = 8
+    p = L.PpfNcgpuParams()
+    p.dx = 1e-4
+    dummy = C.c_void_p(16)  # never dereferenced: every call fails validation first
+    p.ncomp = 7
+    assert lib.ppf_ncgpu_tables_f64(C.byref(p), C.byref(g), dummy, dummy, None) == \
+        L.PPF_ERR_UNSUPPORTED
+    assert "components" in L.last_error()
+    p.ncomp = 2
+    p.nexcess = L.PPF_NCGPU_MAX_EXCESS + 1
+    assert lib.ppf_ncgpu_tables_f64(C.byref(p), C.byref(g), dummy, dummy, None) == \
+        L.PPF_ERR_INVALID
+    assert "nexcess" in L.last_error()
+    p.nexcess = 1
+    p.excess[0].a, p.excess[0].b = 0, 2  # b beyond ncomp
+    assert lib.ppf_ncgpu_tables_f64(C.byref(p), C.byref(g), dummy, dummy, None) == \
+        L.PPF_ERR_INVALID
+    assert "excess term 0" in L.last_error()
+    assert lib.ppf_ncgpu_tables_f64(C.byref(p), C.byref(g), None, dummy, None) == \
+        L.PPF_ERR_INVALID
