@@ -249,3 +249,29 @@ def test_ternary_interactions_are_rejected(tmp_path):
                     "PARAMETER L(LIQUID,AA,BB,CC;0) 300 100; 3000 N !\n")
     with pytest.raises(TdbError):
         Database(path)
+
+
+@pytest.mark.parametrize("tdb_name,c0", [("ncgpu_ninb.tdb", [0.1]),
+                                         ("ncgpu_6comp.tdb", [0.05, 0.2, 0.3, 0.1, 0.15])])
+def test_engine_initialisation_without_gpu(tdb_name, c0):
+    """NCGPUGB300 reads the database, derives the reference's parameters and
+    lays out its fields before any device work."""
+    from pyphasefield_gb300 import NCGPUGB300
+    path = GOLDEN / tdb_name
+    sim = NCGPUGB300(dimensions=[16, 20], dx=4.6e-6, tdb_path=str(path),
+                     temperature_type="ISOTHERMAL", initial_T=1600.0,
+                     boundary_conditions="PERIODIC",
+                     user_data={"sim_type": "seed", "initial_concentration_array": c0})
+    sim.initialize_fields_and_imported_data()
+    tdb = N.Tdb(path)
+    ref = N.tdb_params(tdb, 4.6e-6)
+    assert [f.name for f in sim.fields] == ["phi", "q1", "q4"] + [
+        "c_" + e for e in tdb.elements[:-1]]
+    assert sim.dt == pytest.approx(ref["dt"], rel=1e-14)
+    np.testing.assert_allclose(sim.user_data["W"], ref["W"], rtol=1e-14)
+    np.testing.assert_allclose(sim.user_data["M"], ref["M"], rtol=1e-14)
+    phi0, q10, q40, *cs = N.seed_fields((16, 20), c0=c0, ncomp=len(tdb.elements))
+    np.testing.assert_array_equal(sim.fields[0].get_cells(), phi0)
+    np.testing.assert_allclose(sim.fields[1].get_cells(), q10, rtol=1e-15)
+    for f, c in zip(sim.fields[3:], cs):
+        np.testing.assert_array_equal(f.get_cells(), c)
