@@ -168,8 +168,10 @@ class Tdb:
         return self.value(name, 1000.0)
 
 
-def tdb_params(tdb: Tdb, dx: float, d_ratio: float = 4.0) -> dict:
-    """NCGPU.init_tdb_params (:336-373)."""
+def tdb_params(tdb: Tdb, dx: float, d_ratio: float = 4.0, variant: str = "NCGPU") -> dict:
+    """NCGPU.init_tdb_params (:336-373); variant "NCGPU_new" as
+    NCGPU_new.init_tdb_params (NCGPU_new.py:350-386): eqbar = 0.1 ebar and
+    the noise amplitudes noise_phi / noise_c / noise_q (1 by default)."""
     comps = tdb.elements
     d = dx * d_ratio
     p = {"d": d, "R": 8.314}
@@ -186,7 +188,9 @@ def tdb_params(tdb: Tdb, dx: float, d_ratio: float = 4.0) -> dict:
     p["H"] = tdb.scalar("H")
     p["y_e"] = tdb.scalar("Y_E")
     p["ebar"] = np.sqrt(6 * np.sqrt(2) * p["S"][1] * d / p["T_M"][1])
-    p["eqbar"] = 0.5 * p["ebar"]
+    p["eqbar"] = (0.1 if variant == "NCGPU_new" else 0.5) * p["ebar"]
+    if variant == "NCGPU_new":
+        p.update(noise_phi=1.0, noise_c=1.0, noise_q=1.0)
     p["dt"] = dx ** 2 / 5.0 / p["D_L"] / 8
     p["beta"] = 1.5
     p["dx"] = dx
@@ -219,11 +223,13 @@ def seed_fields(shape, melt_angle=0.0, seed_angle=np.pi / 4, radius=5, c0=None, 
     return (phi, q1, q4) + tuple(np.full(shape, v) for v in vals)
 
 
-def noise_normal(seed: int, step: int, shape) -> np.ndarray:
+def noise_normal(seed: int, step: int, shape, stream: int = 0) -> np.ndarray:
     """N(0,1) per cell: Box-Muller on two uniforms made from words 2k and
     2k+1 of the Philox4x32-10 block with counter (col / 2, row, step low,
-    step high) and key (seed low ^ 0x5eed0000, seed high); cell (row, col)
-    takes pair k = col % 2. u1 = (top 24 bits + 1/2) 2^-24 (never 0),
+    step high) and key (seed low ^ (0x5eed0000 + stream), seed high); cell
+    (row, col) takes pair k = col % 2. Streams (NCGPU_new): 0 .. N - 2 the
+    concentration noise of each component (NCGPU draws stream 0 only),
+    NOISE_PHI, NOISE_Q1, NOISE_Q4 the phase and orientation noise. u1 = (top 24 bits + 1/2) 2^-24 (never 0),
     u2 = top 24 bits 2^-24; z = sqrt(-2 ln u1) cos(2 pi u2). The library
     draws the same numbers."""
     ny, nx = shape
@@ -232,7 +238,7 @@ def noise_normal(seed: int, step: int, shape) -> np.ndarray:
     r = np.repeat(np.arange(ny, dtype=np.uint64), ng)
     step, seed = int(step), int(seed)
     w = philox4x32_10((g, r, step & 0xFFFFFFFF, step >> 32),
-                      ((seed & 0xFFFFFFFF) ^ 0x5EED0000, seed >> 32))
+                      ((seed & 0xFFFFFFFF) ^ (0x5EED0000 + stream), seed >> 32))
     w = [(x >> np.uint64(8)).astype(np.float64) for x in w]
     z = []
     for k in range(2):
@@ -243,18 +249,41 @@ def noise_normal(seed: int, step: int, shape) -> np.ndarray:
     return out
 
 
+NOISE_PHI, NOISE_Q1, NOISE_Q4 = 8, 9, 10
+
+
+def noise_new(seed: int, step: int, shape, nc: int) -> dict:
+    """The N(0,1) fields NCGPU_new draws in one step: one per concentration
+    field, and for phi, q1 and q4."""
+    return {"c": [noise_normal(seed, step, shape, l) for l in range(nc)],
+            "phi": noise_normal(seed, step, shape, NOISE_PHI),
+            "q1": noise_normal(seed, step, shape, NOISE_Q1),
+            "q4": noise_normal(seed, step, shape, NOISE_Q4)}
+
+
 def _pad(a, bc):
     mode = "wrap" if bc == "PERIODIC" else "symmetric"
     return np.pad(a, 1, mode=mode)
 
 
-def step(fields, T, p: dict, tdb: Tdb, noise, bc: str = "PERIODIC", noise_scale: float = 1.0):
+def step(fields, T, p: dict, tdb: Tdb, noise, bc: str = "PERIODIC", noise_scale: float = 1.0,
+         variant: str = "NCGPU"):
     """One NCGPU step (helper kernel, then main kernel) on interior arrays
     (phi, q1, q4, c_1 .. c_{N-1}); the last component's fraction is 1 - sum
     c. T an interior array. `bc`: PERIODIC or NEUMANN (zero gradient),
     applied to every field as ghost cells. As the reference, dG/dc is taken
     once per cell (first component up, last one down, :282-286) and used for
-    every component."""
+    every component; `noise` is the interior N(0,1) field.
+
+    variant "NCGPU_new" (Engines/NCGPU_new.py): dG/dc_l per component (the
+    last component down once, then component l up and back, in place, as
+    :298-313 mutate their input array), a noise draw per component scaled by
+    noise_c, the phase noise sqrt(2 R T M_phi / v_m) noise_phi added after
+    the mobility (:186-189), orientation noise sqrt(1e-10 R T / v_m)
+    noise_q inside the quaternion brackets (:225-231), eqbar = 0.1 ebar,
+    ebar^2 and eqbar^2 as products of the square roots (:78-79), phi clamped
+    to [1e-4, 0.9999]; `noise` is noise_new()'s dict."""
+    new = variant == "NCGPU_new"
     phi, q1, q4 = fields[:3]
     cs = list(fields[3:])
     nc = len(cs)
@@ -278,16 +307,28 @@ def step(fields, T, p: dict, tdb: Tdb, noise, bc: str = "PERIODIC", noise_scale:
             xs.append(1.0 - sum(xs))
             gl = tdb.gibbs(phases[1], xs, t)
             gs = tdb.gibbs(phases[0], xs, t)
+            ph = phi[i, j]
+            g = ph * ph * (1 - ph) ** 2
+            h = ph ** 3 * (6 * ph * ph - 15 * ph + 10)
+            GL[i, j], GS[i, j] = gl, gs
+            if new:
+                x = list(xs)
+                x[nc] -= 1e-7
+                for l in range(nc):
+                    x[l] += 1e-7
+                    dgl = 1e7 * (tdb.gibbs(phases[1], x, t) - gl)
+                    dgs = 1e7 * (tdb.gibbs(phases[0], x, t) - gs)
+                    Mcs[l][i, j] = v_m * xs[l] * (D_L + h * (D_S - D_L)) / (R_KERNEL * t)
+                    nz = p["noise_c"] * math.sqrt(2.0 * R_KERNEL * t / v_m) * noise["c"][l][i, j]
+                    dFs[l][i, j] = (dgl + h * (dgs - dgl)) / v_m + (W[l] - W[nc]) * g * t + nz
+                    x[l] -= 1e-7
+                continue
             xp = list(xs)
             xp[nc] -= 1e-7
             xp[0] += 1e-7
             dgl = 1e7 * (tdb.gibbs(phases[1], xp, t) - gl)
             dgs = 1e7 * (tdb.gibbs(phases[0], xp, t) - gs)
-            ph = phi[i, j]
-            g = ph * ph * (1 - ph) ** 2
-            h = ph ** 3 * (6 * ph * ph - 15 * ph + 10)
             nz = noise_scale * math.sqrt(2.0 * R_KERNEL * t / v_m) * noise[i, j]
-            GL[i, j], GS[i, j] = gl, gs
             for l in range(nc):
                 Mcs[l][i, j] = v_m * xs[l] * (D_L + h * (D_S - D_L)) / (R_KERNEL * t)
                 dFs[l][i, j] = (dgl + h * (dgs - dgl)) / v_m + (W[l] - W[nc]) * g * t + nz
@@ -295,11 +336,17 @@ def step(fields, T, p: dict, tdb: Tdb, noise, bc: str = "PERIODIC", noise_scale:
     CC = [_pad(a, bc) for a in cs]
     MC = [_pad(a, bc) for a in Mcs]
     DF = [_pad(a, bc) for a in dFs]
+    if new:
+        ebar2, eqbar2 = p["ebar"] * p["ebar"], p["eqbar"] * p["eqbar"]
+        return _update(P, Q1, Q4, CC, TT, GL, GS, MC, DF, p, ebar2, eqbar2, idx, noise=noise,
+                       clamp=(0.0001, 0.9999))
     return _update(P, Q1, Q4, CC, TT, GL, GS, MC, DF, p, ebar2, eqbar2, idx)
 
 
-def _update(P, Q1, Q4, CC, TT, GL, GS, MC, DF, p, ebar2, eqbar2, idx):
-    """NComponent_kernel (:37-242) on padded arrays."""
+def _update(P, Q1, Q4, CC, TT, GL, GS, MC, DF, p, ebar2, eqbar2, idx, noise=None,
+            clamp=(0.000001, 0.999999)):
+    """NComponent_kernel (:37-242) on padded arrays; with `noise` (a
+    noise_new() dict) the NCGPU_new kernel's phase and orientation noise."""
     v_m, W, M = p["v_m"], p["W"], p["M"]
     y_e, H, beta, M_qmax, dt = p["y_e"], p["H"], p["beta"], p["M_qmax"], p["dt"]
     nc = len(CC)
@@ -382,6 +429,13 @@ def _update(P, Q1, Q4, CC, TT, GL, GS, MC, DF, p, ebar2, eqbar2, idx):
             dphidt -= gprime * t * cW
             dphidt -= 4 * H * t * ph * mgq
             dphidt *= M_phi
+            nq1 = nq4 = 0.0
+            if noise is not None:
+                dphidt += (math.sqrt(2.0 * R_KERNEL * t * M_phi / v_m) * noise["phi"][i - 1, j - 1]
+                           * p["noise_phi"])
+                qa = p["noise_q"] * math.sqrt(0.0000000001 * R_KERNEL * t / v_m)
+                nq1 = qa * noise["q1"][i - 1, j - 1]
+                nq4 = qa * noise["q4"][i - 1, j - 1]
 
             def divagradb(a, axp, axm, ayp, aym, b, bxp, bxm, byp, bym):
                 return 0.5 * idx * idx * ((axp + a) * (bxp - b) - (a + axm) * (b - bxm)
@@ -413,9 +467,15 @@ def _update(P, Q1, Q4, CC, TT, GL, GS, MC, DF, p, ebar2, eqbar2, idx):
             f4 = fori(a4, Q4[i, j + 1], Q4[i, j - 1], Q4[i + 1, j], Q4[i - 1, j])
             lq1 = (Q1[i, j + 1] + Q1[i, j - 1] + Q1[i + 1, j] + Q1[i - 1, j] - 4 * a1) * idx * idx
             lq4 = (Q4[i, j + 1] + Q4[i, j - 1] + Q4[i + 1, j] + Q4[i - 1, j] - 4 * a4) * idx * idx
-            dq1 = M_q * ((1 - a1 * a1) * (f1 + lq1 * eqbar2) - a1 * a4 * (f4 + lq4 * eqbar2))
-            dq4 = M_q * ((1 - a4 * a4) * (f4 + lq4 * eqbar2) - a1 * a4 * (f1 + lq1 * eqbar2))
-            pn = min(max(ph + dt * dphidt, 0.000001), 0.999999)
+            if noise is None:
+                dq1 = M_q * ((1 - a1 * a1) * (f1 + lq1 * eqbar2) - a1 * a4 * (f4 + lq4 * eqbar2))
+                dq4 = M_q * ((1 - a4 * a4) * (f4 + lq4 * eqbar2) - a1 * a4 * (f1 + lq1 * eqbar2))
+            else:
+                b1 = f1 + lq1 * eqbar2 - 0.0 + nq1
+                b4 = f4 + lq4 * eqbar2 - 0.0 + nq4
+                dq1 = M_q * ((1 - a1 * a1) * b1 - a1 * a4 * b4)
+                dq4 = M_q * ((1 - a4 * a4) * b4 - a1 * a4 * b1)
+            pn = min(max(ph + dt * dphidt, clamp[0]), clamp[1])
             n1, n4 = a1 + dt * dq1, a4 + dt * dq4
             rn = math.sqrt(n1 * n1 + n4 * n4)
             out[0][i - 1, j - 1] = pn
@@ -426,9 +486,13 @@ def _update(P, Q1, Q4, CC, TT, GL, GS, MC, DF, p, ebar2, eqbar2, idx):
     return out
 
 
-def run(fields, T, steps, p, tdb, seed=0, bc="PERIODIC", noise_scale=1.0, step0=0):
+def run(fields, T, steps, p, tdb, seed=0, bc="PERIODIC", noise_scale=1.0, step0=0,
+        variant="NCGPU"):
     f = [np.array(a, dtype=np.float64) for a in fields]
     for s in range(steps):
-        nz = noise_normal(seed, step0 + s, f[0].shape) if noise_scale else np.zeros(f[0].shape)
-        f = step(f, T, p, tdb, nz, bc, noise_scale)
+        if variant == "NCGPU_new":
+            nz = noise_new(seed, step0 + s, f[0].shape, len(f) - 3)
+        else:
+            nz = noise_normal(seed, step0 + s, f[0].shape) if noise_scale else np.zeros(f[0].shape)
+        f = step(f, T, p, tdb, nz, bc, noise_scale, variant)
     return f

@@ -292,9 +292,11 @@ def _install_numba_standin(normal_source):
 _NC = {"queue": None}
 
 
-def ncgpu_module():
-    """Import Engines/NCGPU.py with the numba stand-in (test use only)."""
-    mod = sys.modules.get("pyphasefield.Engines.NCGPU")
+def ncgpu_module(name: str = "NCGPU"):
+    """Import Engines/NCGPU.py (or NCGPU_new.py) with the numba stand-in
+    (test use only)."""
+    full = "pyphasefield.Engines." + name
+    mod = sys.modules.get(full)
     if mod is not None and getattr(mod, "_ppf_standin", False):
         return mod
 
@@ -307,8 +309,8 @@ def ncgpu_module():
     _install_numba_standin(normal)
     try:
         import importlib
-        sys.modules.pop("pyphasefield.Engines.NCGPU", None)
-        mod = importlib.import_module("pyphasefield.Engines.NCGPU")
+        sys.modules.pop(full, None)
+        mod = importlib.import_module(full)
         mod._ppf_standin = True
     finally:
         for k, v in saved.items():
@@ -349,6 +351,43 @@ def run_ncgpu(phi, q1, q4, c, T, steps: int, p: dict, tdb, noise_fields, bc="PER
         _NC["queue"] = iter(nz.ravel().tolist())
         mod.NComponent_helper_kernel(fields, Tp, transfer, None, ufunc_array, params, c_params)
         _NC["queue"] = iter([0.0] * (ny * nx))
+        mod.NComponent_kernel(fields, Tp, transfer, out, None, params, c_params)
+        f = [out[k, 1:-1, 1:-1].copy() for k in range(len(f))]
+    _NC["queue"] = None
+    return f
+
+
+def run_ncgpu_new(phi, q1, q4, c, T, steps: int, p: dict, tdb, noise, bc="PERIODIC"):
+    """Drive NCGPU_new's helper and main kernels (Engines/NCGPU_new.py:38-314)
+    for `steps` steps. noise[s] is oracle.ncgpu_ref.noise_new's dict for step
+    s: the helper draws one normal per concentration field and cell (ghost
+    cells take the draw of the cell the boundary rule maps them to), the
+    main kernel three per interior cell (phase, q1, q4) in its own loop order
+    (columns outer, rows inner)."""
+    mod = ncgpu_module("NCGPU_new")
+    mode = "wrap" if bc == "PERIODIC" else "symmetric"
+    pad = lambda a: np.pad(np.asarray(a, dtype=np.float64), 1, mode=mode)  # noqa: E731
+    cs = [np.array(x, dtype=np.float64) for x in (c if isinstance(c, (list, tuple)) else [c])]
+    f = [np.array(a, dtype=np.float64) for a in (phi, q1, q4)] + cs
+    ncomp = len(cs) + 1
+    Tp = pad(T)
+    params = np.array([p["dx"], p["d"], p["v_m"], p["M_qmax"], p["H"], p["y_e"], p["beta"],
+                       p["D_L"], p["D_S"], p["dt"], p["ebar"], p["eqbar"], p["noise_phi"],
+                       p["noise_c"], p["noise_q"]])
+    c_params = np.array([p["L"], p["T_M"], p["S"], p["B"], p["W"], p["M"]])
+    phases = tdb.phases
+    mod.ufunc_g_l = lambda arr: tdb.gibbs(phases[1], list(arr[:ncomp]), arr[ncomp])
+    mod.ufunc_g_s = lambda arr: tdb.gibbs(phases[0], list(arr[:ncomp]), arr[ncomp])
+    for s in range(steps):
+        fields = np.stack([pad(a) for a in f])
+        out = np.zeros_like(fields)
+        transfer = np.zeros((2 * ncomp,) + fields.shape[1:])
+        ufunc_array = np.zeros(fields.shape[1:] + (ncomp + 1,))
+        nzc = np.stack([pad(a) for a in noise[s]["c"]], axis=-1)  # (rows, cols, component)
+        _NC["queue"] = iter(nzc.ravel().tolist())
+        mod.NComponent_helper_kernel(fields, Tp, transfer, None, ufunc_array, params, c_params)
+        nzm = np.stack([noise[s][k] for k in ("phi", "q1", "q4")], axis=-1)  # interior
+        _NC["queue"] = iter(np.transpose(nzm, (1, 0, 2)).ravel().tolist())
         mod.NComponent_kernel(fields, Tp, transfer, out, None, params, c_params)
         f = [out[k, 1:-1, 1:-1].copy() for k in range(len(f))]
     _NC["queue"] = None

@@ -202,6 +202,7 @@ def main():
          q1=out[1], q4=out[2], c_0=out[3], c_1=out[4])
     ncgpu_multicomponent()
     ncgpu_excess()
+    ncgpu_new()
 
     dx = 4.6e-8
     prm = dict(restate.WARREN_DEFAULTS)
@@ -296,10 +297,38 @@ def ncgpu_excess():
          q4=out[2], c=out[3])
 
 
+def ncgpu_new():
+    """NCGPU_new (Engines/NCGPU_new.py): its kernels run serially under the
+    numba stand-in with the oracle's noise streams (per component, phase and
+    orientation), binary Ni-Cu periodic and ternary Ni-Cu-Al zero-gradient."""
+    from oracle import ncgpu_ref
+    nrng = np.random.default_rng(20240613)
+    cases = [("ncgpu_new_periodic", "ncgpu_nicu.tdb", (18, 16), "PERIODIC", [0.40831], 4, 31),
+             ("ncgpu_new_ternary", "ncgpu_nicual.tdb", (16, 18), "NEUMANN", [0.05, 0.4], 3, 37)]
+    for name, tdb_name, shape, bc, c0, steps, seed in cases:
+        tdb = ncgpu_ref.Tdb(HERE / tdb_name)
+        p = ncgpu_ref.tdb_params(tdb, 4.6e-6, variant="NCGPU_new")
+        init = ncgpu_ref.seed_fields(shape, melt_angle=0.1, seed_angle=0.5, c0=c0,
+                                     ncomp=len(tdb.elements))
+        cs = [c + nrng.uniform(-1e-3, 1e-3, shape) for c in init[3:]]
+        T = np.full(shape, 1574.0)
+        noise = [ncgpu_ref.noise_new(seed, s, shape, len(cs)) for s in range(steps)]
+        out = refshim.run_ncgpu_new(*init[:3], cs, T, steps, p, tdb, noise, bc)
+        meta = dict(model="ncgpu_new", steps=steps, bc=bc, seed=seed, dx=4.6e-6, T=1574.0,
+                    tdb=tdb_name)
+        arrays = dict(phi0=init[0], q10=init[1], q40=init[2], phi=out[0], q1=out[1], q4=out[2])
+        for j, c in enumerate(cs):
+            arrays[f"c0_{j}"] = c
+            arrays[f"c_{j}"] = out[3 + j]
+        save(name, meta, **arrays)
+
+
 if __name__ == "__main__":
     if sys.argv[1:] == ["ncgpu_multicomponent"]:
         ncgpu_multicomponent()
     elif sys.argv[1:] == ["ncgpu_excess"]:
         ncgpu_excess()
+    elif sys.argv[1:] == ["ncgpu_new"]:
+        ncgpu_new()
     else:
         main()

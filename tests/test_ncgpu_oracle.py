@@ -275,3 +275,34 @@ def test_engine_initialisation_without_gpu(tdb_name, c0):
     np.testing.assert_allclose(sim.fields[1].get_cells(), q10, rtol=1e-15)
     for f, c in zip(sim.fields[3:], cs):
         np.testing.assert_array_equal(f.get_cells(), c)
+
+
+@pytest.mark.parametrize("name", ["ncgpu_new_periodic", "ncgpu_new_ternary"])
+def test_ncgpu_new_oracle_matches_reference_kernels(name):
+    """The NCGPU_new variant (per-component dG/dc and noise, phase and
+    orientation noise, eqbar = 0.1 ebar, phi in [1e-4, 0.9999]) against
+    Engines/NCGPU_new.py's own kernels run serially."""
+    z = np.load(GOLDEN / f"{name}.npz")
+    m = json.loads(str(z["meta"]))
+    nc = sum(1 for k in z.files if k.startswith("c0_"))
+    tdb = N.Tdb(GOLDEN / m["tdb"])
+    p = N.tdb_params(tdb, m["dx"], variant="NCGPU_new")
+    assert p["eqbar"] == pytest.approx(0.1 * p["ebar"], rel=1e-15)
+    T = np.full(z["phi0"].shape, m["T"])
+    out = N.run([z["phi0"], z["q10"], z["q40"]] + [z[f"c0_{j}"] for j in range(nc)], T,
+                m["steps"], p, tdb, seed=m["seed"], bc=m["bc"], variant="NCGPU_new")
+    keys = ["phi", "q1", "q4"] + [f"c_{j}" for j in range(nc)]
+    for got, key, tol in zip(out, keys, [1e-10, 1e-12, 1e-12] + [1e-8] * nc):
+        ref = z[key]
+        assert np.abs(got - ref).max() <= tol * max(1.0, np.abs(ref).max()), key
+
+
+def test_noise_streams_are_distinct_and_stream_zero_is_the_ncgpu_stream():
+    a = N.noise_normal(5, 2, (9, 11))
+    np.testing.assert_array_equal(a, N.noise_normal(5, 2, (9, 11), stream=0))
+    d = N.noise_new(5, 2, (9, 11), 2)
+    np.testing.assert_array_equal(d["c"][0], a)
+    fields = d["c"] + [d["phi"], d["q1"], d["q4"]]
+    for i in range(len(fields)):
+        for j in range(i + 1, len(fields)):
+            assert np.abs(fields[i] - fields[j]).max() > 0.1
