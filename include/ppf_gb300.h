@@ -342,6 +342,12 @@ int32_t ppf_var_line_solve_f64(const PpfGrid* g, int32_t axis, double alpha, dou
  * one forward difference per cell (the first component up, the last down)
  * shared by every component. */
 #define PPF_NCGPU_MAX_COMP 6
+/* Engines/NCGPU.py, and Engines/NCGPU_new.py (per-component dG/dc and
+ * concentration noise, phase noise sqrt(2 R T M_phi / v_m) noise_phi added
+ * after the mobility, orientation noise sqrt(1e-10 R T / v_m) noise_q in the
+ * quaternion brackets, phi clamped to [1e-4, 0.9999]) */
+#define PPF_NCGPU_VARIANT_NCGPU 0
+#define PPF_NCGPU_VARIANT_NEW 1
 #define PPF_NCGPU_MAX_EXCESS 16
 /* One binary Redlich-Kister term of a phase: x_a x_b L(T) (x_a - x_b)^order
  * added to its molar Gibbs energy, L piecewise in T as the gibbs ranges. */
@@ -361,6 +367,12 @@ typedef struct PpfNcgpuParams {
   int32_t ncomp;
   int32_t nexcess;    /* 0..PPF_NCGPU_MAX_EXCESS terms in excess */
   PpfNcgpuExcess excess[PPF_NCGPU_MAX_EXCESS];
+  int32_t variant;    /* PPF_NCGPU_VARIANT_NCGPU or PPF_NCGPU_VARIANT_NEW */
+  int32_t reserved;
+  /* PPF_NCGPU_VARIANT_NEW only: eqbar^2 (the orientation gradient energy;
+   * NCGPU uses ebar2 / 4) and the phase and orientation noise amplitudes
+   * (noise_scale is the concentration noise's) */
+  double eqbar2, noise_phi, noise_q;
 } PpfNcgpuParams;
 
 int32_t ppf_ncgpu_step_f32(const PpfNcgpuParams* p, const PpfGrid* g, const PpfBoundary* bc,

@@ -14,8 +14,10 @@ The compute path is libppf_gb300.so (CUDA, built by
 from .field import Field
 from .simulation import Simulation
 from .engines import (AllenCahnGB300, CahnAllenGB300, CahnHilliardGB300, DiffusionGB300,
-                      NCGPUGB300, Warren1995GB300, make_engines, make_ncgpu)
+                      NCGPUGB300, NCGPU_newGB300, Warren1995GB300, make_engines,
+                      make_ncgpu, make_ncgpu_new)
 
 __version__ = "0.1.0"
 __all__ = ["Field", "Simulation", "DiffusionGB300", "CahnAllenGB300", "AllenCahnGB300",
-           "CahnHilliardGB300", "Warren1995GB300", "NCGPUGB300", "make_engines", "make_ncgpu"]
+           "CahnHilliardGB300", "Warren1995GB300", "NCGPUGB300", "NCGPU_newGB300", "make_engines",
+           "make_ncgpu", "make_ncgpu_new"]

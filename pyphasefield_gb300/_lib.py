@@ -93,6 +93,8 @@ class PpfImplicitDiffusionParams(C.Structure):
 
 PPF_NCGPU_MAX_COMP = 6
 PPF_NCGPU_MAX_EXCESS = 16
+PPF_NCGPU_VARIANT_NCGPU = 0
+PPF_NCGPU_VARIANT_NEW = 1
 
 
 class PpfNcgpuExcess(C.Structure):
@@ -107,7 +109,9 @@ class PpfNcgpuParams(C.Structure):
         ("gibbs", (((C.c_double * 10) * 4) * PPF_NCGPU_MAX_COMP) * 2),
         ("npieces", (C.c_int32 * PPF_NCGPU_MAX_COMP) * 2),
         ("ncomp", C.c_int32), ("nexcess", C.c_int32),
-        ("excess", PpfNcgpuExcess * PPF_NCGPU_MAX_EXCESS)]
+        ("excess", PpfNcgpuExcess * PPF_NCGPU_MAX_EXCESS),
+        ("variant", C.c_int32), ("reserved", C.c_int32),
+        ("eqbar2", C.c_double), ("noise_phi", C.c_double), ("noise_q", C.c_double)]
 
 
 PPF_MODEL_WARREN1995 = 1

@@ -28,8 +28,16 @@ constexpr int kMaxComp = PPF_NCGPU_MAX_COMP;
 template <typename T>
 struct NcCoef {
   T idx, dt, v_m, D_L, D_S, M_qmax, H, y_e, beta, ebar2, eqbar2, noise;
+  T noise_phi, noise_q;  // NCGPU_new only
+  T phi_lo, phi_hi;      // the phi clamp
+  int variant;           // PPF_NCGPU_VARIANT_*
   T W[kMaxComp], M[kMaxComp];
 };
+
+// Noise streams: 0 .. ncomp - 2 the concentration noise of each component
+// (NCGPU draws stream 0 only), then the phase and the orientation noise of
+// NCGPU_new.
+constexpr int kStreamPhi = 8, kStreamQ1 = 9, kStreamQ4 = 10;
 
 constexpr int kMaxExcess = PPF_NCGPU_MAX_EXCESS;
 
@@ -76,13 +84,15 @@ __device__ __forceinline__ double l_excess(const NcGibbs& g, int e, double T, do
 }
 
 // N(0,1) of cell (row, col) at a step: Box-Muller on two uniforms from a
-// Philox4x32-10 block (counter (col / 2, row, step), key seed ^ 0x5eed0000),
-// pair col % 2.
+// Philox4x32-10 block (counter (col / 2, row, step), key seed ^ (0x5eed0000 +
+// stream)), pair col % 2.
 template <typename T>
-__device__ __forceinline__ T noise_normal(uint64_t seed, uint64_t step, int row, int col) {
+__device__ __forceinline__ T noise_normal(uint64_t seed, uint64_t step, int row, int col,
+                                          int stream) {
   const U4 w = philox4x32_10(U4{(uint32_t)(col >> 1), (uint32_t)row, (uint32_t)step,
                                 (uint32_t)(step >> 32)},
-                             (uint32_t)seed ^ 0x5EED0000u, (uint32_t)(seed >> 32));
+                             (uint32_t)seed ^ (0x5EED0000u + (uint32_t)stream),
+                             (uint32_t)(seed >> 32));
   const uint32_t a = (col & 1) ? w.z : w.x, b = (col & 1) ? w.w : w.y;
   // the uniforms are exact in either precision
   const T u1 = ((T)(a >> 8) + T(0.5)) * (T(1) / T(16777216));
@@ -160,69 +170,85 @@ __global__ void __launch_bounds__(256)
   }
   const double* Gs = G;
   const double* Gl = G + N;
-#pragma unroll
-  for (int l = 0; l < N; ++l) xp[l] = xs[l];
-  // the reference's forward difference (NCGPU.py:282-286): the last
-  // component down, the first up, one derivative for every component, as the
-  // difference of the two molar Gibbs energies. The ideal mixing term is the
-  // same in both phases, so it is evaluated once at each composition.
-  xp[NC] -= 0.0000001;
-  xp[0] += 0.0000001;
-  double mix = 0.0, mixp = 0.0, lin_s = 0.0, lin_l = 0.0, linp_s = 0.0, linp_l = 0.0;
-#pragma unroll
-  for (int l = 0; l < N; ++l) {
-    if (xs[l] > 0) mix += xs[l] * log(xs[l]);
-    if (xp[l] > 0) mixp += xp[l] * log(xp[l]);
-    lin_s += xs[l] * Gs[l];
-    lin_l += xs[l] * Gl[l];
-    linp_s += xp[l] * Gs[l];
-    linp_l += xp[l] * Gl[l];
-  }
-  // binary Redlich-Kister terms x_a x_b L (x_a - x_b)^k of each phase, at
-  // both compositions
-  double ex_s = 0.0, ex_l = 0.0, exp_s = 0.0, exp_l = 0.0;
-  for (int e = 0; e < gb.nex; ++e) {
-    const int a = gb.ex_meta[e][1], b = gb.ex_meta[e][2], ord = gb.ex_meta[e][3];
-    const double L = tab ? __ldg(tab + (2 * N + e) * plane + i) : l_excess(gb, e, t, lnT);
-    double xa = 0.0, xb = 0.0, pa = 0.0, pb = 0.0;
+  // the ideal part (sum x G and sum x ln x) and the binary Redlich-Kister
+  // terms x_a x_b L (x_a - x_b)^k of both phases at a composition xv
+  auto energies = [&](const double* xv, double& mixv, double& ls, double& ll, double& es,
+                      double& el) {
+    mixv = ls = ll = es = el = 0.0;
 #pragma unroll
     for (int l = 0; l < N; ++l) {
-      xa = l == a ? xs[l] : xa;
-      xb = l == b ? xs[l] : xb;
-      pa = l == a ? xp[l] : pa;
-      pb = l == b ? xp[l] : pb;
+      if (xv[l] > 0) mixv += xv[l] * log(xv[l]);
+      ls += xv[l] * Gs[l];
+      ll += xv[l] * Gl[l];
     }
-    double ts = xa * xb * L, tp = pa * pb * L;
-    for (int j = 0; j < ord; ++j) {
-      ts *= xa - xb;
-      tp *= pa - pb;
+    for (int e = 0; e < gb.nex; ++e) {
+      const int a = gb.ex_meta[e][1], b = gb.ex_meta[e][2], ord = gb.ex_meta[e][3];
+      const double L = tab ? __ldg(tab + (2 * N + e) * plane + i) : l_excess(gb, e, t, lnT);
+      double xa = 0.0, xb = 0.0;
+#pragma unroll
+      for (int l = 0; l < N; ++l) {
+        xa = l == a ? xv[l] : xa;
+        xb = l == b ? xv[l] : xb;
+      }
+      double term = xa * xb * L;
+      for (int j = 0; j < ord; ++j) term *= xa - xb;
+      if (gb.ex_meta[e][0] == 0)
+        es += term;
+      else
+        el += term;
     }
-    if (gb.ex_meta[e][0] == 0) {
-      ex_s += ts;
-      exp_s += tp;
-    } else {
-      ex_l += ts;
-      exp_l += tp;
-    }
-  }
+  };
   const double rt = 8.3145 * t;
+  double mix, lin_s, lin_l, ex_s, ex_l;
+  energies(xs, mix, lin_s, lin_l, ex_s, ex_l);
   const double gs = lin_s + rt * mix + ex_s;
   const double gl = lin_l + rt * mix + ex_l;
-  const double dgl = 10000000.0 * ((linp_l + rt * mixp + exp_l) - gl);
-  const double dgs = 10000000.0 * ((linp_s + rt * mixp + exp_s) - gs);
   const T p = phi[i];
   const T gg = p * p * (T(1) - p) * (T(1) - p);
   const T h = p * p * p * (T(6) * p * p - T(15) * p + T(10));
   const T tt = (T)t;
-  const T nz = k.noise > T(0)
-                   ? k.noise * sqrt(T(2) * T(8.314) * tt / k.v_m) * noise_normal<T>(seed, st, y, x)
-                   : T(0);
+  const T namp = k.noise * sqrt(T(2) * T(8.314) * tt / k.v_m);
   dG[i] = (T)(gs - gl);
-  const T dfc = (T)((dgl + (double)h * (dgs - dgl)) / (double)k.v_m);
+  if (k.variant == 0) {
+    // the reference's forward difference (NCGPU.py:282-286): the last
+    // component down, the first up, one derivative for every component, as
+    // the difference of the two molar Gibbs energies; one noise draw
+    // shared by every component
 #pragma unroll
-  for (int l = 0; l < NC; ++l) {
-    cp.Mc[l][i] = k.v_m * (T)xs[l] * (k.D_L + h * (k.D_S - k.D_L)) / (T(8.314) * tt);
-    cp.dF[l][i] = dfc + (k.W[l] - k.W[NC]) * gg * tt + nz;
+    for (int l = 0; l < N; ++l) xp[l] = xs[l];
+    xp[NC] -= 0.0000001;
+    xp[0] += 0.0000001;
+    double mixp, linp_s, linp_l, exp_s, exp_l;
+    energies(xp, mixp, linp_s, linp_l, exp_s, exp_l);
+    const double dgl = 10000000.0 * ((linp_l + rt * mixp + exp_l) - gl);
+    const double dgs = 10000000.0 * ((linp_s + rt * mixp + exp_s) - gs);
+    const T nz = k.noise > T(0) ? namp * noise_normal<T>(seed, st, y, x, 0) : T(0);
+    const T dfc = (T)((dgl + (double)h * (dgs - dgl)) / (double)k.v_m);
+#pragma unroll
+    for (int l = 0; l < NC; ++l) {
+      cp.Mc[l][i] = k.v_m * (T)xs[l] * (k.D_L + h * (k.D_S - k.D_L)) / (T(8.314) * tt);
+      cp.dF[l][i] = dfc + (k.W[l] - k.W[NC]) * gg * tt + nz;
+    }
+  } else {
+    // NCGPU_new (NCGPU_new.py:298-313): the last component down once, then
+    // each component up and back in place, one derivative and one noise
+    // draw (stream l) per component
+#pragma unroll
+    for (int l = 0; l < N; ++l) xp[l] = xs[l];
+    xp[NC] -= 0.0000001;
+#pragma unroll
+    for (int l = 0; l < NC; ++l) {
+      xp[l] += 0.0000001;
+      double mixp, linp_s, linp_l, exp_s, exp_l;
+      energies(xp, mixp, linp_s, linp_l, exp_s, exp_l);
+      const double dgl = 10000000.0 * ((linp_l + rt * mixp + exp_l) - gl);
+      const double dgs = 10000000.0 * ((linp_s + rt * mixp + exp_s) - gs);
+      const T nz = k.noise > T(0) ? namp * noise_normal<T>(seed, st, y, x, l) : T(0);
+      cp.Mc[l][i] = k.v_m * (T)xs[l] * (k.D_L + h * (k.D_S - k.D_L)) / (T(8.314) * tt);
+      cp.dF[l][i] = (T)((dgl + (double)h * (dgs - dgl)) / (double)k.v_m) +
+                    (k.W[l] - k.W[NC]) * gg * tt + nz;
+      xp[l] -= 0.0000001;
+    }
   }
 }
 
@@ -239,7 +265,8 @@ __global__ void __launch_bounds__(256)
     ncgpu_kernel(Geo g, Bc<T> bc, NcCoef<T> k, const T* __restrict__ phi,
                  const T* __restrict__ q1, const T* __restrict__ q4, NcPtrs<T> cp,
                  const T* __restrict__ temp, const T* __restrict__ dG, T* __restrict__ phi_o,
-                 T* __restrict__ q1_o, T* __restrict__ q4_o) {
+                 T* __restrict__ q1_o, T* __restrict__ q4_o, uint64_t seed, uint64_t step,
+                 const uint64_t* step_base) {
   pdl_wait();
   pdl_launch_next();
   const int x = blockIdx.x * blockDim.x + threadIdx.x;
@@ -344,6 +371,12 @@ __global__ void __launch_bounds__(256)
   dphidt -= gprime * t * cW;
   dphidt -= T(4) * k.H * t * ph * mgq;
   dphidt *= M_phi;
+  if (k.variant != 0) {
+    // NCGPU_new's phase noise, after the mobility (NCGPU_new.py:186-189)
+    const uint64_t st = step + (step_base ? *step_base : 0);
+    dphidt += sqrt(T(2) * T(8.314) * t * M_phi / k.v_m) *
+              noise_normal<T>(seed, st, y, x, kStreamPhi) * k.noise_phi;
+  }
   // c_l: div(M_l grad dF_l) - sum_m div(M_l c_m grad dF_m)
   T dc[NC];
 #pragma unroll
@@ -378,11 +411,21 @@ __global__ void __launch_bounds__(256)
   const T f4 = fori(a4, q4xp, q4xm, q4yp, q4ym);
   const T lq1 = (q1xp + q1xm + q1yp + q1ym - T(4) * a1) * idx * idx;
   const T lq4 = (q4xp + q4xm + q4yp + q4ym - T(4) * a4) * idx * idx;
-  const T dq1 = M_q * ((T(1) - a1 * a1) * (f1 + lq1 * k.eqbar2) - a1 * a4 * (f4 + lq4 * k.eqbar2));
-  const T dq4 = M_q * ((T(1) - a4 * a4) * (f4 + lq4 * k.eqbar2) - a1 * a4 * (f1 + lq1 * k.eqbar2));
+  // NCGPU_new's orientation noise enters the brackets (NCGPU_new.py:225-231);
+  // NCGPU adds nothing (x + 0 = x)
+  T nq1 = T(0), nq4 = T(0);
+  if (k.variant != 0) {
+    const uint64_t st = step + (step_base ? *step_base : 0);
+    const T qa = k.noise_q * sqrt(T(0.0000000001) * T(8.314) * t / k.v_m);
+    nq1 = qa * noise_normal<T>(seed, st, y, x, kStreamQ1);
+    nq4 = qa * noise_normal<T>(seed, st, y, x, kStreamQ4);
+  }
+  const T b1 = f1 + lq1 * k.eqbar2 + nq1, b4 = f4 + lq4 * k.eqbar2 + nq4;
+  const T dq1 = M_q * ((T(1) - a1 * a1) * b1 - a1 * a4 * b4);
+  const T dq4 = M_q * ((T(1) - a4 * a4) * b4 - a1 * a4 * b1);
   T pn = ph + k.dt * dphidt;
-  pn = pn < T(0.000001) ? T(0.000001) : pn;
-  pn = pn > T(0.999999) ? T(0.999999) : pn;
+  pn = pn < k.phi_lo ? k.phi_lo : pn;
+  pn = pn > k.phi_hi ? k.phi_hi : pn;
   const T n1 = a1 + k.dt * dq1, n4 = a4 + k.dt * dq4;
   const T irn = rsqrt(n1 * n1 + n4 * n4);
   phi_o[i] = pn;
@@ -401,7 +444,7 @@ cudaError_t launch_ncgpu(dim3 grid2, cudaStream_t st, const Geo& g, const Bc<T>&
                          in[0], cp, temp, tab, dG, seed, step, step_base);
   if (e != cudaSuccess) return e;
   return launch(ncgpu_kernel<T, NC>, grid2, dim3(256), 0, st, true, g, bc, k, in[0], in[1], in[2],
-                cp, temp, (const T*)dG, out[0], out[1], out[2]);
+                cp, temp, (const T*)dG, out[0], out[1], out[2], seed, step, step_base);
 }
 
 int32_t make_gibbs(const PpfNcgpuParams* p, NcGibbs* gb) {
@@ -508,8 +551,16 @@ int32_t ncgpu_step(const PpfNcgpuParams* p, const PpfGrid* grid, const PpfBounda
   k.y_e = (T)p->y_e;
   k.beta = (T)p->beta;
   k.ebar2 = (T)p->ebar2;
-  k.eqbar2 = (T)(0.25 * p->ebar2);
+  if (p->variant != PPF_NCGPU_VARIANT_NCGPU && p->variant != PPF_NCGPU_VARIANT_NEW)
+    return fail(PPF_ERR_INVALID, "variant must be PPF_NCGPU_VARIANT_NCGPU or _NEW");
+  k.variant = p->variant;
+  const bool nv = p->variant == PPF_NCGPU_VARIANT_NEW;
+  k.eqbar2 = (T)(nv ? p->eqbar2 : 0.25 * p->ebar2);
   k.noise = (T)p->noise_scale;
+  k.noise_phi = (T)(nv ? p->noise_phi : 0.0);
+  k.noise_q = (T)(nv ? p->noise_q : 0.0);
+  k.phi_lo = (T)(nv ? 0.0001 : 0.000001);
+  k.phi_hi = (T)(nv ? 0.9999 : 0.999999);
   for (int c = 0; c < kMaxComp; ++c) {
     k.W[c] = (T)p->W[c];
     k.M[c] = (T)p->M[c];

@@ -441,8 +441,8 @@ class _Warren1995Mixin(GB300Engine):
 def make_engines(base=Simulation) -> dict:
     """Build the engine classes on `base` (any class with the reference
     Simulation interface): Diffusion, CahnAllen (= AllenCahn), CahnHilliard,
-    Warren1995 and NCGPU. Returns {name: class}."""
-    from .ncgpu import make_ncgpu
+    Warren1995, NCGPU and NCGPU_new. Returns {name: class}."""
+    from .ncgpu import make_ncgpu, make_ncgpu_new
     out = {}
     for name, mix in (("DiffusionGB300", _DiffusionMixin), ("CahnAllenGB300", _CahnAllenMixin),
                       ("CahnHilliardGB300", _CahnHilliardMixin),
@@ -451,6 +451,7 @@ def make_engines(base=Simulation) -> dict:
                                             "__doc__": mix.__doc__})
     out["AllenCahnGB300"] = out["CahnAllenGB300"]
     out["NCGPUGB300"] = make_ncgpu(base)
+    out["NCGPU_newGB300"] = make_ncgpu_new(base)
     return out
 
 

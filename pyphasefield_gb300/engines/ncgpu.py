@@ -81,15 +81,23 @@ def gibbs_table(db: Database):
     return table, npieces
 
 
-def params_struct(db: Database, ud: dict, dx: float, noise_scale: float = 1.0):
+def params_struct(db: Database, ud: dict, dx: float, noise_scale: float = 1.0,
+                  variant: int = L.PPF_NCGPU_VARIANT_NCGPU):
     """PpfNcgpuParams from the derived parameters `ud` (ncgpu_parameters)
-    and the database's Gibbs-energy tables."""
+    and the database's Gibbs-energy tables. variant PPF_NCGPU_VARIANT_NEW
+    (NCGPU_new) takes eqbar, noise_phi and noise_q from `ud`; noise_scale is
+    the concentration noise's amplitude."""
     table, npieces = gibbs_table(db)
     p = L.PpfNcgpuParams()
+    p.variant = int(variant)
+    if variant == L.PPF_NCGPU_VARIANT_NEW:
+        p.eqbar2 = float(ud["eqbar"]) * float(ud["eqbar"])
+        p.noise_phi = float(ud["noise_phi"])
+        p.noise_q = float(ud["noise_q"])
     for name in ("dt", "v_m", "D_L", "D_S", "M_qmax", "H", "y_e", "beta"):
         setattr(p, name, float(ud[name]))
     p.dx = float(dx)
-    p.ebar2 = float(ud["ebar"]) ** 2
+    p.ebar2 = float(ud["ebar"]) * float(ud["ebar"])
     p.noise_scale = float(noise_scale)
     p.ncomp = len(db.elements)
     for j in range(p.ncomp):
@@ -148,6 +156,7 @@ def make_seed(phi, q1, q4, x, y, angle, seed_radius):
 
 class _NcgpuMixin(GB300Engine):
     NFIELDS = 4
+    VARIANT = L.PPF_NCGPU_VARIANT_NCGPU
 
     def __init__(self, **kwargs):
         super().__init__(**kwargs)
@@ -191,9 +200,16 @@ class _NcgpuMixin(GB300Engine):
         self.add_field(phi, "phi")
         self.add_field(q1, "q1")
         self.add_field(q4, "q4")
-        c0 = ud.get("initial_concentration_array")
+        self._add_concentrations()
+
+    def _add_concentrations(self):
+        """c_<component> for all but the last component: the
+        initial_concentration_array, or 1 / N each when it is missing or has
+        the wrong length (the reference's fallback, NCGPU.py:404-415)."""
+        dim, comps = self.dimensions, self._tdb_components
+        c0 = self.user_data.get("initial_concentration_array")
         if c0 is not None and len(c0) + 1 != len(comps):
-            raise ValueError(f"initial_concentration_array needs {len(comps) - 1} values")
+            c0 = None
         for j in range(len(comps) - 1):
             val = float(c0[j]) if c0 is not None else 1.0 / len(comps)
             self.add_field(np.full(dim, val), "c_" + comps[j])
@@ -219,7 +235,8 @@ class _NcgpuMixin(GB300Engine):
         self._nc_temp_staging = self._ppf_grid.upload(self._nc_temp, self.temperature.get_cells(),
                                                       self._ppf_stream)
         ud = self.user_data
-        self._nc_params = params_struct(self._ppf_db, ud, self.dx, ud.get("noise_scale", 1.0))
+        noise = ud.get("noise_c", 1.0) if self.VARIANT else ud.get("noise_scale", 1.0)
+        self._nc_params = params_struct(self._ppf_db, ud, self.dx, noise, self.VARIANT)
         # the temperature is fixed during a run: the pure-element energies of
         # every cell are evaluated once, after the upload, on the same stream
         nplanes = 2 * ncomp + int(self._nc_params.nexcess)
@@ -239,9 +256,61 @@ class _NcgpuMixin(GB300Engine):
                C.c_uint64(int(step)), ptr(step_base), sp)
 
 
+class _NcgpuNewMixin(_NcgpuMixin):
+    """NCGPU_new (Engines/NCGPU_new.py:340-553): the same fields and
+    database, with a derivative dF/dc and a noise draw per component, phase
+    noise sqrt(2 R T M_phi / v_m) scaled by user_data noise_phi, orientation
+    noise sqrt(1e-10 R T / v_m) scaled by noise_q, concentration noise
+    scaled by noise_c (all 1 by default), eqbar = 0.1 ebar and phi clamped
+    to [1e-4, 0.9999]. The orientation starts at melt_angle for every
+    sim_type; "seeds" places number_of_seeds seeds (default one per 10,000
+    cells) at positions and angles from the engine's seeded generator
+    (the reference draws them from numpy's global one)."""
+    VARIANT = L.PPF_NCGPU_VARIANT_NEW
+
+    def __init__(self, **kwargs):
+        super().__init__(**kwargs)
+        for key in ("noise_phi", "noise_c", "noise_q"):
+            self.user_data.setdefault(key, 1.0)
+
+    def init_tdb_params(self):
+        super().init_tdb_params()
+        self.user_data["eqbar"] = 0.1 * self.user_data["ebar"]  # NCGPU_new.py:385
+
+    def init_fields(self):
+        dim = self.dimensions
+        if len(dim) != 2:
+            raise NotImplementedError("NCGPU_new runs 2-D grids")
+        ud = self.user_data
+        melt = float(ud.get("melt_angle", 0.0))
+        phi = np.zeros(dim)
+        q1 = np.full(dim, np.cos(0.5 * melt))
+        q4 = np.full(dim, np.sin(0.5 * melt))
+        if ud.get("sim_type") == "seed":
+            seed_angle = float(ud.get("seed_angle", np.pi / 4))
+            phi, q1, q4 = make_seed(phi, q1, q4, dim[1] / 2, dim[0] / 2, seed_angle, 5)
+        elif ud.get("sim_type") == "seeds":
+            rng = np.random.default_rng(int(ud["seed"]))
+            for _ in range(int(ud.get("number_of_seeds", int(np.prod(dim)) // 10000))):
+                angle = (rng.random() - 0.5) * np.pi / 2 + melt
+                x = int(rng.random() * dim[1])
+                y = int(rng.random() * dim[0])
+                phi, q1, q4 = make_seed(phi, q1, q4, x, y, angle, 5)
+        self.add_field(phi, "phi")
+        self.add_field(q1, "q1")
+        self.add_field(q4, "q4")
+        self._add_concentrations()
+
+
 def make_ncgpu(base=Simulation):
     return type("NCGPUGB300", (_NcgpuMixin, base), {"__module__": __name__,
                                                    "__doc__": __doc__})
 
 
+def make_ncgpu_new(base=Simulation):
+    return type("NCGPU_newGB300", (_NcgpuNewMixin, base),
+                {"__module__": __name__, "__doc__": _NcgpuNewMixin.__doc__})
+
+
 NCGPUGB300 = make_ncgpu(Simulation)
+NCGPU_newGB300 = make_ncgpu_new(Simulation)

@@ -22,14 +22,18 @@ TDB = GOLDEN / "ncgpu_nicu.tdb"
 TOL = {"fp64": 1e-8, "fp32": 1e-5}
 
 
-def params_struct(dx, noise_scale=1.0, tdb=TDB):
+def params_struct(dx, noise_scale=1.0, tdb=TDB, variant=0):
     from pyphasefield_gb300.engines.ncgpu import ncgpu_parameters, params_struct as ps
     from pyphasefield_gb300.tdb import Database
     db = Database(tdb)
-    return ps(db, ncgpu_parameters(db, dx), dx, noise_scale)
+    ud = ncgpu_parameters(db, dx)
+    if variant:
+        ud.update(eqbar=0.1 * ud["ebar"], noise_phi=1.0, noise_q=1.0)
+    return ps(db, ud, dx, noise_scale, variant)
 
 
-def run_gpu(fields, T, steps, dx, seed, bc, precision, noise_scale=1.0, tdb=TDB, tables=True):
+def run_gpu(fields, T, steps, dx, seed, bc, precision, noise_scale=1.0, tdb=TDB, tables=True,
+            variant=0):
     """`steps` steps through ppf_ncgpu_step_*; tables: the pure-element
     energies from ppf_ncgpu_tables_* (False: evaluated in every step)."""
     import torch
@@ -41,7 +45,7 @@ def run_gpu(fields, T, steps, dx, seed, bc, precision, noise_scale=1.0, tdb=TDB,
     o = [torch.zeros_like(t) for t in a]
     temp = to_dev(T, kshape, pitch, dtype, "cuda")
     transfer = torch.zeros((2 * len(fields) - 5,) + tuple(a[0].shape), dtype=dtype, device="cuda")
-    p = params_struct(dx, noise_scale, tdb)
+    p = params_struct(dx, noise_scale, tdb, variant)
     sfx = "f64" if precision == "fp64" else "f32"
     s = C.c_void_p(torch.cuda.current_stream().cuda_stream)
     tab = None
@@ -198,5 +202,48 @@ def test_engine_six_components_matches_oracle(cuda):
     tdb = N.Tdb(path)
     ref = N.run(init, np.full(shape, 1574.0), 4, N.tdb_params(tdb, 4.6e-6), tdb, seed=4,
                 bc="NEUMANN")
+    for f, r in zip(sim.fields, ref):
+        assert rel_l2(f.get_cells(), r) < TOL["fp64"], f.name
+
+
+@pytest.mark.parametrize("name", ["ncgpu_new_periodic", "ncgpu_new_ternary"])
+@pytest.mark.parametrize("precision", ["fp64"])
+def test_ncgpu_new_reference_fixtures(cuda, name, precision):
+    """PPF_NCGPU_VARIANT_NEW against Engines/NCGPU_new.py's own kernels:
+    per-component dG/dc and noise, phase and orientation noise. float64
+    only: in float32 the binary periodic case parts by 1.3e-4 (relative L2)
+    in q4 after 4 steps, over the 1e-5 float tolerance; float64 is the
+    engine's default."""
+    z = np.load(GOLDEN / f"{name}.npz")
+    m = json.loads(str(z["meta"]))
+    nc = sum(1 for k in z.files if k.startswith("c0_"))
+    T = np.full(z["phi0"].shape, m["T"])
+    f = [z["phi0"], z["q10"], z["q40"]] + [z[f"c0_{j}"] for j in range(nc)]
+    out = run_gpu(f, T, m["steps"], m["dx"], m["seed"], m["bc"], precision, tdb=GOLDEN / m["tdb"],
+                  variant=1)
+    keys = ["phi", "q1", "q4"] + [f"c_{j}" for j in range(nc)]
+    for got, key in zip(out, keys):
+        assert rel_l2(got, z[key]) < TOL[precision], (key, rel_l2(got, z[key]))
+
+
+def test_ncgpu_new_engine_matches_oracle(cuda):
+    """NCGPU_newGB300 (sim_type seeds, melt angle) through captured graphs
+    against the oracle's NCGPU_new variant."""
+    from pyphasefield_gb300 import NCGPU_newGB300
+    path = GOLDEN / "ncgpu_nicual.tdb"
+    shape = (22, 24)
+    sim = NCGPU_newGB300(dimensions=list(shape), dx=4.6e-6, tdb_path=str(path),
+                         temperature_type="ISOTHERMAL", initial_T=1574.0,
+                         boundary_conditions="NEUMANN",
+                         user_data={"sim_type": "seeds", "number_of_seeds": 2, "melt_angle": 0.2,
+                                    "initial_concentration_array": [0.05, 0.4], "seed": 6,
+                                    "precision": "fp64", "graph_chunk": 2})
+    sim.initialize_fields_and_imported_data()
+    init = [f.get_cells().copy() for f in sim.fields]
+    sim.simulate(4)
+    sim.retrieve_fields_from_GPU()
+    tdb = N.Tdb(path)
+    ref = N.run(init, np.full(shape, 1574.0), 4, N.tdb_params(tdb, 4.6e-6, variant="NCGPU_new"),
+                tdb, seed=6, bc="NEUMANN", variant="NCGPU_new")
     for f, r in zip(sim.fields, ref):
         assert rel_l2(f.get_cells(), r) < TOL["fp64"], f.name

@@ -87,7 +87,7 @@ def test_make_engines_builds_every_engine_on_a_given_base():
 
     eng = make_engines(Host)
     assert sorted(eng) == ["AllenCahnGB300", "CahnAllenGB300", "CahnHilliardGB300",
-                           "DiffusionGB300", "NCGPUGB300", "Warren1995GB300"]
+                           "DiffusionGB300", "NCGPUGB300", "NCGPU_newGB300", "Warren1995GB300"]
     assert eng["AllenCahnGB300"] is eng["CahnAllenGB300"]
     for cls in eng.values():
         assert issubclass(cls, Host)

@@ -306,3 +306,34 @@ def test_noise_streams_are_distinct_and_stream_zero_is_the_ncgpu_stream():
     for i in range(len(fields)):
         for j in range(i + 1, len(fields)):
             assert np.abs(fields[i] - fields[j]).max() > 0.1
+
+
+def test_ncgpu_new_engine_initialisation_without_gpu():
+    """NCGPU_newGB300: eqbar = 0.1 ebar, noise amplitudes default to 1, the
+    orientation starts at melt_angle, "seeds" places the requested number
+    of seeds from the engine's seeded generator (reproducible), and a wrong
+    initial_concentration_array falls back to 1 / N as in the reference."""
+    from pyphasefield_gb300 import NCGPU_newGB300
+    path = GOLDEN / "ncgpu_nicual.tdb"
+
+    def make(**ud):
+        sim = NCGPU_newGB300(dimensions=[40, 44], dx=4.6e-6, tdb_path=str(path),
+                             temperature_type="ISOTHERMAL", initial_T=1574.0,
+                             user_data=dict(ud, seed=3))
+        sim.initialize_fields_and_imported_data()
+        return sim
+
+    a = make(sim_type="seeds", number_of_seeds=3, melt_angle=0.3,
+             initial_concentration_array=[0.1])
+    assert a.user_data["eqbar"] == pytest.approx(0.1 * a.user_data["ebar"], rel=1e-15)
+    assert (a.user_data["noise_phi"], a.user_data["noise_c"], a.user_data["noise_q"]) == \
+        (1.0, 1.0, 1.0)
+    phi, q1 = a.fields[0].get_cells(), a.fields[1].get_cells()
+    assert phi.sum() > 0 and np.isclose(q1[phi == 0], np.cos(0.15)).mean() > 0.5
+    for f in a.fields[3:]:
+        np.testing.assert_array_equal(f.get_cells(), 1.0 / 3)  # wrong length: 1 / N
+    b = make(sim_type="seeds", number_of_seeds=3, melt_angle=0.3)
+    np.testing.assert_array_equal(b.fields[0].get_cells(), phi)
+    melt = make(melt_angle=0.3)
+    assert melt.fields[0].get_cells().sum() == 0
+    np.testing.assert_allclose(melt.fields[1].get_cells(), np.cos(0.15), rtol=1e-15)
