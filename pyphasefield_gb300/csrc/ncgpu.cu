@@ -1,17 +1,25 @@
 // NCGPU: the multi-component solidification engine with quaternion
-// orientation fields (pyphasefield Engines/NCGPU.py), 2 to 6 components.
+// orientation fields (pyphasefield Engines/NCGPU.py, and its variant
+// Engines/NCGPU_new.py), 2 to 6 components.
 //
-//   ncgpu_thermo_kernel  (NComponent_helper_kernel, :248-303): per cell the
-//       molar Gibbs energies of the solid (first phase, sorted) and liquid,
-//       from the pure-element energies of the TDB (piecewise in T, basis
-//       1, T, T ln T, T^2, T^3, T^7, 1/T, T^-9) plus R T sum x ln x, in
-//       double; dG/dc by the reference's forward difference (step 1e-7);
-//       stores G_S - G_L, the mobility M_c and dF/dc (with the Langevin
-//       noise) for the update.
-//   ncgpu_kernel (NComponent_kernel, :37-242): phi (anisotropic through the
-//       quaternion-rotated gradient psi), q1 and q4 (orientation diffusion
-//       normalised to unit length), c (div M_c grad dF/dc minus the
-//       c-weighted term), phi clamped to [1e-6, 1 - 1e-6].
+//   ncgpu_table_kernel: the pure-element energies and interaction
+//       parameters at every cell's temperature, once per run (the
+//       temperature is fixed while the engine steps).
+//   ncgpu_thermo_kernel  (NComponent_helper_kernel, NCGPU.py:248-303,
+//       NCGPU_new.py:256-314): per cell the molar Gibbs energies of the
+//       solid (first phase, sorted) and liquid, from the pure-element
+//       energies of the TDB (piecewise in T, basis 1, T, T ln T, T^2, T^3,
+//       T^7, 1/T, T^-9) plus R T sum x ln x and the binary Redlich-Kister
+//       terms, in double; dG/dc by the reference's forward difference (step
+//       1e-7; one for every component in NCGPU, one per component in
+//       NCGPU_new); stores G_S - G_L, the mobility M_c and dF/dc (with the
+//       Langevin noise) for the update.
+//   ncgpu_kernel (NComponent_kernel, NCGPU.py:37-242, NCGPU_new.py:38-252):
+//       phi (anisotropic through the quaternion-rotated gradient psi; plus
+//       the phase noise in NCGPU_new), q1 and q4 (orientation diffusion,
+//       plus the orientation noise in NCGPU_new, normalised to unit
+//       length), c (div M_c grad dF/dc minus the c-weighted term), phi
+//       clamped to [1e-6, 1 - 1e-6] ([1e-4, 0.9999] in NCGPU_new).
 // Ghost cells follow the boundary rule while the tiles are read (periodic
 // or zero-gradient), for the fields, the temperature and the per-cell
 // thermodynamic terms alike.
