@@ -207,13 +207,16 @@ def test_engine_six_components_matches_oracle(cuda):
 
 
 @pytest.mark.parametrize("name", ["ncgpu_new_periodic", "ncgpu_new_ternary"])
-@pytest.mark.parametrize("precision", ["fp64"])
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
 def test_ncgpu_new_reference_fixtures(cuda, name, precision):
     """PPF_NCGPU_VARIANT_NEW against Engines/NCGPU_new.py's own kernels:
-    per-component dG/dc and noise, phase and orientation noise. float64
-    only: in float32 the binary periodic case parts by 1.3e-4 (relative L2)
-    in q4 after 4 steps, over the 1e-5 float tolerance; float64 is the
-    engine's default."""
+    per-component dG/dc and noise, phase and orientation noise. In float32
+    the binary periodic case parts by 1.3e-4 (relative L2) in q4: at step 2
+    one interface cell's |grad q| falls on the other side of the beta clamp
+    than in float64 and the jump spreads to ~30 cells (a float32 emulation
+    of the kernel on the CPU gives 1.28e-4, the GPU 1.31e-4); that case is
+    held to 1e-3, the others to the float tolerance."""
+    tol = 1e-3 if (precision, name) == ("fp32", "ncgpu_new_periodic") else TOL[precision]
     z = np.load(GOLDEN / f"{name}.npz")
     m = json.loads(str(z["meta"]))
     nc = sum(1 for k in z.files if k.startswith("c0_"))
@@ -223,7 +226,7 @@ def test_ncgpu_new_reference_fixtures(cuda, name, precision):
                   variant=1)
     keys = ["phi", "q1", "q4"] + [f"c_{j}" for j in range(nc)]
     for got, key in zip(out, keys):
-        assert rel_l2(got, z[key]) < TOL[precision], (key, rel_l2(got, z[key]))
+        assert rel_l2(got, z[key]) < tol, (key, rel_l2(got, z[key]))
 
 
 def test_ncgpu_new_engine_matches_oracle(cuda):
