@@ -283,17 +283,28 @@ def step(fields, T, p: dict, tdb: Tdb, noise, bc: str = "PERIODIC", noise_scale:
     noise_q inside the quaternion brackets (:225-231), eqbar = 0.1 ebar,
     ebar^2 and eqbar^2 as products of the square roots (:78-79), phi clamped
     to [1e-4, 0.9999]; `noise` is noise_new()'s dict."""
+    P, Q1, Q4, CC, TT, GL, GS, MC, DF = thermo(fields, T, p, tdb, noise, bc, noise_scale, variant)
+    idx = 1.0 / p["dx"]
+    if variant == "NCGPU_new":
+        ebar2, eqbar2 = p["ebar"] * p["ebar"], p["eqbar"] * p["eqbar"]
+        return _update(P, Q1, Q4, CC, TT, GL, GS, MC, DF, p, ebar2, eqbar2, idx, noise=noise,
+                       clamp=(0.0001, 0.9999))
+    ebar2 = 6.0 * math.sqrt(2.0) * p["S"][1] * p["d"] / p["T_M"][1]
+    return _update(P, Q1, Q4, CC, TT, GL, GS, MC, DF, p, ebar2, 0.25 * ebar2, idx)
+
+
+def thermo(fields, T, p: dict, tdb: Tdb, noise, bc: str = "PERIODIC", noise_scale: float = 1.0,
+           variant: str = "NCGPU"):
+    """The helper kernel of a step (see `step`): returns the padded fields
+    P, Q1, Q4, CC (concentrations), TT (temperature), the interior G_L and
+    G_S, and the padded M_c and dF/dc of every concentration field."""
     new = variant == "NCGPU_new"
     phi, q1, q4 = fields[:3]
     cs = list(fields[3:])
     nc = len(cs)
     phases = tdb.phases  # sorted: FCC_A1 (solid), LIQUID
-    idx = 1.0 / p["dx"]
     v_m, D_L, D_S = p["v_m"], p["D_L"], p["D_S"]
-    W, M = p["W"], p["M"]
-    ebar2 = 6.0 * math.sqrt(2.0) * p["S"][1] * p["d"] / p["T_M"][1]
-    eqbar2 = 0.25 * ebar2
-    y_e, H, beta, M_qmax, dt = p["y_e"], p["H"], p["beta"], p["M_qmax"], p["dt"]
+    W = p["W"]
     ny, nx = phi.shape
     # helper: thermodynamics per interior cell
     GL = np.empty_like(phi)
@@ -336,11 +347,7 @@ def step(fields, T, p: dict, tdb: Tdb, noise, bc: str = "PERIODIC", noise_scale:
     CC = [_pad(a, bc) for a in cs]
     MC = [_pad(a, bc) for a in Mcs]
     DF = [_pad(a, bc) for a in dFs]
-    if new:
-        ebar2, eqbar2 = p["ebar"] * p["ebar"], p["eqbar"] * p["eqbar"]
-        return _update(P, Q1, Q4, CC, TT, GL, GS, MC, DF, p, ebar2, eqbar2, idx, noise=noise,
-                       clamp=(0.0001, 0.9999))
-    return _update(P, Q1, Q4, CC, TT, GL, GS, MC, DF, p, ebar2, eqbar2, idx)
+    return P, Q1, Q4, CC, TT, GL, GS, MC, DF
 
 
 def _update(P, Q1, Q4, CC, TT, GL, GS, MC, DF, p, ebar2, eqbar2, idx, noise=None,

@@ -337,3 +337,32 @@ def test_ncgpu_new_engine_initialisation_without_gpu():
     melt = make(melt_angle=0.3)
     assert melt.fields[0].get_cells().sum() == 0
     np.testing.assert_allclose(melt.fields[1].get_cells(), np.cos(0.15), rtol=1e-15)
+
+
+@pytest.mark.parametrize("name,variant", [("ncgpu_periodic", "NCGPU"),
+                                          ("ncgpu_new_periodic", "NCGPU_new"),
+                                          ("ncgpu_new_ternary", "NCGPU_new")])
+def test_float32_emulation_sets_the_float_tolerances(name, variant):
+    """The kernel's float32 arithmetic repeated on the CPU (oracle/ncgpu_f32)
+    against the reference's kernels: within the GPU tests' float tolerance
+    (1e-5), except q4 of the binary NCGPU_new case, where one interface
+    cell's |grad q| falls on the other side of the beta clamp at step 2
+    (~1.3e-4, the GPU measured the same): the GPU test holds that case to
+    1e-3."""
+    from oracle import ncgpu_f32 as E
+    z = np.load(GOLDEN / f"{name}.npz")
+    m = json.loads(str(z["meta"]))
+    tdb = N.Tdb(GOLDEN / m["tdb"])
+    p = N.tdb_params(tdb, m["dx"], variant=variant)
+    cks = sorted(k for k in z.files if k.startswith("c0_"))
+    c0 = [z["c0"]] if "c0" in z.files else [z[k] for k in cks]
+    keys = ["phi", "q1", "q4"] + (["c"] if "c" in z.files else [k.replace("c0_", "c_") for k in cks])
+    with np.errstate(all="ignore"):
+        out = E.run([z["phi0"], z["q10"], z["q40"]] + c0, np.full(z["phi0"].shape, m["T"]),
+                    m["steps"], p, tdb, m["seed"], m["bc"], variant)
+    for got, key in zip(out, keys):
+        err = np.linalg.norm(got - z[key]) / np.linalg.norm(z[key])
+        if (name, key) == ("ncgpu_new_periodic", "q4"):
+            assert 5e-5 < err < 1e-3, err
+        else:
+            assert err < 1e-5, (key, err)
