@@ -397,6 +397,11 @@ SWEEP = {
     "ncgpu_6comp_2048": ("ncgpu", (2048, 2048), 1, 50,
                          {"precision": "fp64", "tdb": "ncgpu_6comp.tdb",
                           "c0": [0.05, 0.2, 0.3, 0.1, 0.15]}),
+    # Ni-Nb with binary Redlich-Kister terms (the reference's non-ideal database), and the
+    # NCGPU_new variant (per-component derivatives and noise, phase and orientation noise)
+    "ncgpu_ninb_2048": ("ncgpu", (2048, 2048), 1, 50,
+                        {"precision": "fp64", "tdb": "ncgpu_ninb.tdb", "c0": [0.1]}),
+    "ncgpu_new_2048": ("ncgpu_new", (2048, 2048), 1, 50, {"precision": "fp64"}),
 }
 SWEEP_B_ALG = {"diffusion": 8, "allen_cahn": 8, "cahn_hilliard": 8, "warren1995": 16}
 NCGPU_TDB = ROOT / "tests" / "golden" / "ncgpu_nicu.tdb"
@@ -422,11 +427,12 @@ def sweep_engine(model, grid, depth, steps, rng, extra=None):
                                 boundary_conditions="PERIODIC",
                                 user_data=dict(ud, M=1.0, epsilon=1.0))
         init = [0.5 + rng.uniform(-0.05, 0.05, grid)]
-    elif model == "ncgpu":
-        from pyphasefield_gb300 import NCGPUGB300
+    elif model in ("ncgpu", "ncgpu_new"):
+        from pyphasefield_gb300 import NCGPU_newGB300, NCGPUGB300
         tdb = NCGPU_TDB.parent / ud.pop("tdb", NCGPU_TDB.name)
         c0 = ud.pop("c0", [0.40831])
-        sim = NCGPUGB300(dimensions=list(grid), dx=4.6e-6, tdb_path=str(tdb),
+        cls = NCGPUGB300 if model == "ncgpu" else NCGPU_newGB300
+        sim = cls(dimensions=list(grid), dx=4.6e-6, tdb_path=str(tdb),
                          temperature_type="ISOTHERMAL", initial_T=1574.0,
                          boundary_conditions="PERIODIC",
                          user_data=dict(ud, sim_type="seed", initial_concentration_array=c0,
@@ -451,7 +457,7 @@ def sweep_bytes_per_cell(model, sim) -> int:
     axis) or per Chebyshev iteration (iterate, previous iterate and the
     right-hand side read, the new iterate written: 16 B in float)."""
     ud = sim.user_data
-    if model == "ncgpu":
+    if model in ("ncgpu", "ncgpu_new"):
         # phi, q1, q4 and every concentration field read and written, the
         # temperature read
         return (2 * len(sim.fields) + 1) * (8 if ud.get("precision", "fp64") == "fp64" else 4)
