@@ -366,3 +366,31 @@ def test_float32_emulation_sets_the_float_tolerances(name, variant):
             assert 5e-5 < err < 1e-3, err
         else:
             assert err < 1e-5, (key, err)
+
+
+@pytest.mark.parametrize("tdb_name", ["ncgpu_nicu.tdb", "ncgpu_nicual.tdb", "ncgpu_4comp.tdb",
+                                      "ncgpu_6comp.tdb", "ncgpu_ninb.tdb"])
+def test_fixture_databases_survive_re_emission(tmp_path, tdb_name):
+    """The fixture script re-emits parsed databases (every temperature range
+    of every G and L parameter): written again, a database evaluates the
+    same."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("make_golden", GOLDEN / "make_golden.py")
+    mg = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mg)
+    src = GOLDEN / tdb_name
+    out = tmp_path / tdb_name
+    mg.write_tdb(N.Tdb(src), out)
+    a, b = Database(src), Database(out)
+    assert a.elements == b.elements and a.phases == b.phases
+    assert sorted(a.params) == sorted(b.params)
+    assert [e[:4] for e in a.excess] == [e[:4] for e in b.excess]
+    for T in (400.0, 1200.0, 1574.0, 1800.0, 2800.0):
+        for key in a.params:
+            va = [g_eval(c, T) for lo, hi, c in a.params[key] if lo <= T < hi]
+            vb = [g_eval(c, T) for lo, hi, c in b.params[key] if lo <= T < hi]
+            assert va == pytest.approx(vb, rel=1e-14), (key, T)
+        for ea, eb in zip(a.excess, b.excess):
+            va = [g_eval(c, T) for lo, hi, c in ea[4] if lo <= T < hi]
+            vb = [g_eval(c, T) for lo, hi, c in eb[4] if lo <= T < hi]
+            assert va == pytest.approx(vb, rel=1e-14)
