@@ -394,3 +394,20 @@ def test_fixture_databases_survive_re_emission(tmp_path, tdb_name):
             va = [g_eval(c, T) for lo, hi, c in ea[4] if lo <= T < hi]
             vb = [g_eval(c, T) for lo, hi, c in eb[4] if lo <= T < hi]
             assert va == pytest.approx(vb, rel=1e-14)
+
+
+@pytest.mark.parametrize("dims", [[10, 10], [5, 5], [20, 1]])
+def test_reference_ncomponent_shapes_initialise(dims):
+    """The reference's NComponent tests (tests/test_NComponent.py: 10 x 10,
+    a 5 x 5 grid smaller than the seed, a 20 x 1 strip) on the Ni-Cu
+    database: the seed wraps around the grid as make_seed does, the fields
+    and parameters are laid out without a GPU."""
+    from pyphasefield_gb300 import NCGPUGB300
+    sim = NCGPUGB300(dimensions=dims, dx=4.6e-6, tdb_path=str(TDB),
+                     temperature_type="ISOTHERMAL", initial_T=1574.0,
+                     user_data={"sim_type": "seed", "initial_concentration_array": [0.40831]})
+    sim.initialize_fields_and_imported_data()
+    phi0, q10, q40, c0 = N.seed_fields(tuple(dims), c0=0.40831)
+    np.testing.assert_array_equal(sim.fields[0].get_cells(), phi0)
+    np.testing.assert_allclose(sim.fields[2].get_cells(), q40, rtol=1e-15, atol=0)
+    assert [f.name for f in sim.fields] == ["phi", "q1", "q4", "c_CU"]
