@@ -72,7 +72,7 @@ class Tdb:
                 if el not in ("/-", "VA"):
                     self.elements.append(el)
             elif kw == "PHASE":
-                self.phases.append(toks[1].upper())
+                self.phases.append(toks[1].upper().split(":")[0])  # LIQUID:L -> LIQUID
             elif kw == "FUNCTION":
                 self.functions[toks[1].upper()] = self._pieces(" ".join(toks[2:]))
             elif kw == "PARAMETER":

@@ -110,7 +110,8 @@ class Database:
                 if el not in ("/-", "VA"):
                     self.elements.append(el)
             elif kw == "PHASE":
-                self.phases.append(toks[1].upper())
+                # a phase name may carry a type suffix (LIQUID:L)
+                self.phases.append(toks[1].upper().split(":")[0])
             elif kw in ("FUNCTION", "FUNCT", "FUNC"):
                 self.functions[toks[1].upper()] = self._ranges(" ".join(toks[2:]))
             elif kw in ("PARAMETER", "PARAM", "PARA"):

@@ -161,8 +161,9 @@ def _write(tmp_path, text):
 
 
 def test_tdb_reader_abbreviations_exponents_and_nested_functions(tmp_path):
-    """Abbreviated keywords, `$` comments, exponents written 1.5E-003 and
-    T**(-1), a FUNCTION whose name ends in E followed by a sign (GBASE+...),
+    """Abbreviated keywords, `$` comments, a phase type suffix (LIQUID:L),
+    exponents written 1.5E-003 and T**(-1), a FUNCTION whose name ends in E
+    followed by a sign (GBASE+...),
     and a FUNCTION that refers to another across a range boundary (the
     pieces split where either expression changes)."""
     path = _write(tmp_path, """
@@ -173,7 +174,7 @@ FUNCT GBASE 300 +100.0-2.5E+000*T+1.5E-003*T**2; 1000 Y
    -50.0+3*T*LN(T); 3000 N !
 FUNCT GSHIFT 300 GBASE+1000*T**(-1)+2*T**(-1); 3000 N !
 PHASE FCC_A1 % 1 1 !
-PHASE LIQUID % 1 1 !
+PHASE LIQUID:L % 1 1 !
 PARA G(FCC_A1,AA;0) 300 GSHIFT; 3000 N !
 PARA G(FCC_A1,BB;0) 300 -GBASE; 3000 N !
 PARA G(LIQUID,AA;0) 300 +GBASE-10*T; 3000 N !
