@@ -5,9 +5,13 @@ Run in a checkout that has the reference (see oracle/refshim.py):
 Each fixture stores the initial interior field(s), the run parameters, and
 the interior after `steps` steps computed by the reference's numpy engine
 (engine_ExplicitDiffusion, engine_CahnAllenExplicit,
-engine_CahnHilliardExplicit, engine_Warren1995, and the implicit /
-Crank-Nicolson diffusion engines) driven by oracle.refshim.
-The inputs are seeded synthetic fields (numpy default_rng).
+engine_CahnHilliardExplicit, engine_Warren1995, the implicit /
+Crank-Nicolson / IMEX engines) driven by oracle.refshim, or by the
+reference's NCGPU and NCGPU_new numba kernels run serially under a stand-in
+numba module (ncgpu_* fixtures, with the databases they read re-emitted
+beside them). The inputs are seeded synthetic fields (numpy default_rng).
+Parts can be regenerated alone: `python tests/golden/make_golden.py
+ncgpu_multicomponent | ncgpu_excess | ncgpu_new`.
 """
 from __future__ import annotations
 
