@@ -502,10 +502,11 @@ def run_sweep(args):
         torch.cuda.synchronize()
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        advance(steps)
-        e1.record(stream)
-        e1.synchronize()
+        with ClockSampler(torch.cuda.current_device()) as clk:
+            e0.record(stream)
+            advance(steps)
+            e1.record(stream)
+            e1.synchronize()
         sec = e0.elapsed_time(e1) / 1e3
         line = {"sweep": name, "model": model, "grid": list(grid) if grid else "config ensemble",
                 "temporal_depth": depth, "steps": steps, "cells": cells, "options": extra or {},
@@ -514,6 +515,9 @@ def run_sweep(args):
                 "achieved_gbs": bytes_per_step * steps / sec / 1e9, "peak_gbs": peak,
                 "peak_source": peak_kind}
         line["frac"] = line["achieved_gbs"] / peak
+        # SM clocks sampled every 200 ms during the timed steps (null when
+        # the case ends before the first sample)
+        line["clocks"] = clk.summary()
         if model == "cahn_hilliard":
             m = sim.collect_mass_history()
             line["mass_rel_drift"] = float(abs(m[-1] - m[0]) / abs(m[0]))
