@@ -201,3 +201,37 @@ def test_ncgpu_entry_points_validate_without_gpu(built_lib):
     assert "excess term 0" in L.last_error()
     assert lib.ppf_ncgpu_tables_f64(C.byref(p), C.byref(g), None, dummy, None) == \
         L.PPF_ERR_INVALID
+
+
+def test_ctypes_structs_match_the_c_header(tmp_path):
+    """Every struct of include/ppf_gb300.h has the same size and field
+    offsets in the ctypes binding as gcc lays it out (a layout mismatch
+    would pass garbage across the ABI without an error)."""
+    import shutil
+    import subprocess
+    from pyphasefield_gb300 import _lib as L
+    if shutil.which("gcc") is None:
+        pytest.skip("gcc not available")
+    structs = [n for n in dir(L) if n.startswith("Ppf") and isinstance(getattr(L, n), type)
+               and issubclass(getattr(L, n), C.Structure)]
+    assert len(structs) >= 14
+    lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "ppf_gb300.h"',
+             "int main(void) {"]
+    for n in structs:
+        lines.append(f'  printf("{n} size %zu\\n", sizeof({n}));')
+        for fname, _ in getattr(L, n)._fields_:
+            lines.append(f'  printf("{n} {fname} %zu\\n", offsetof({n}, {fname}));')
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-I", str(ROOT / "include"), str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout
+    seen = 0
+    for line in out.splitlines():
+        n, field, value = line.split()
+        cls = getattr(L, n)
+        expect = C.sizeof(cls) if field == "size" else getattr(cls, field).offset
+        assert int(value) == expect, (n, field, int(value), expect)
+        seen += 1
+    assert seen > len(structs)
