@@ -235,3 +235,17 @@ def test_ctypes_structs_match_the_c_header(tmp_path):
         assert int(value) == expect, (n, field, int(value), expect)
         seen += 1
     assert seen > len(structs)
+
+
+def test_ctypes_signatures_match_the_header_argument_counts():
+    """Each entry point's ctypes argtypes has as many arguments as its C
+    prototype in include/ppf_gb300.h."""
+    from pyphasefield_gb300 import _lib as L
+    text = (ROOT / "include" / "ppf_gb300.h").read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    protos = dict(re.findall(r"int32_t\s+(ppf_\w+)\s*\(([^)]*)\)\s*;", text))
+    assert sorted(protos) == sorted(L.SIGNATURES)
+    for name, args in protos.items():
+        args = args.strip()
+        n = 0 if args in ("", "void") else args.count(",") + 1
+        assert len(L.SIGNATURES[name]) == n, (name, n, len(L.SIGNATURES[name]))
