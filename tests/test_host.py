@@ -249,3 +249,15 @@ def test_ctypes_signatures_match_the_header_argument_counts():
         args = args.strip()
         n = 0 if args in ("", "void") else args.count(",") + 1
         assert len(L.SIGNATURES[name]) == n, (name, n, len(L.SIGNATURES[name]))
+
+
+def test_header_constants_match_the_binding():
+    """Every #define of include/ppf_gb300.h that the ctypes binding also
+    names has the same value there."""
+    from pyphasefield_gb300 import _lib as L
+    text = (ROOT / "include" / "ppf_gb300.h").read_text()
+    defines = dict(re.findall(r"^#define\s+(PPF_\w+)\s+\(?(-?\d+)\)?", text, re.M))
+    shared = [n for n in defines if hasattr(L, n)]
+    assert len(shared) >= 10
+    for n in shared:
+        assert getattr(L, n) == int(defines[n]), n
