@@ -29,7 +29,7 @@
 extern "C" {
 #endif
 
-#define PPF_ABI_VERSION 1
+#define PPF_ABI_VERSION 2
 
 #define PPF_OK 0
 #define PPF_ERR_INVALID (-1)     /* bad argument (shape, pitch, pointer, depth) */

@@ -11,6 +11,7 @@ from pathlib import Path
 
 LIB_PATH = Path(__file__).resolve().parent / "libppf_gb300.so"
 
+PPF_ABI_VERSION = 2  # the struct layouts and signatures below
 PPF_OK = 0
 PPF_ERR_INVALID = -1
 PPF_ERR_CUDA = -2
@@ -232,6 +233,12 @@ def load(path: str | Path | None = None):
                 fn = getattr(lib, name)
                 fn.argtypes = argtypes
                 fn.restype = C.c_int32
+            abi = I32()
+            buf = C.create_string_buffer(128)
+            lib.ppf_version(C.byref(abi), buf, len(buf))
+            if abi.value != PPF_ABI_VERSION:
+                raise OSError(f"{p} has ABI {abi.value}, this binding {PPF_ABI_VERSION}: "
+                              "rebuild it with `python -m pyphasefield_gb300.build`")
             _lib = lib
     return _lib
 
