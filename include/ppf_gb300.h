@@ -29,7 +29,7 @@
 extern "C" {
 #endif
 
-#define PPF_ABI_VERSION 2
+#define PPF_ABI_VERSION 3
 
 #define PPF_OK 0
 #define PPF_ERR_INVALID (-1)     /* bad argument (shape, pitch, pointer, depth) */
@@ -523,8 +523,10 @@ int32_t ppf_reduce_sum_f64(const double* x, const PpfGrid* g, double* out,
  * 8 KiB device array inside the library (1024 doubles, one per first-pass
  * CTA; grids needing more are rejected with PPF_ERR_INVALID, which the
  * current split never does). The first call on each device looks up that
- * array's device address (cudaGetSymbolAddress) with the device current;
- * make that first call before any stream capture. Every call shares the
+ * array's device address (cudaGetSymbolAddress) with the device current
+ * (again after a context reset; concurrent host threads may make the first
+ * call safely); make that first call before any stream capture. Every call
+ * shares the
  * array, so calls that overlap on the GPU (different streams, or different
  * host threads, with no ordering between them) race and give wrong sums.
  * No counterpart in the reference. */
@@ -542,15 +544,23 @@ int32_t ppf_free_energy_f64(const double* x, const PpfGrid* g,
                             const PpfBoundary* bc, double dx, double w,
                             double kappa, double* out, void* scratch,
                             size_t scratch_bytes, void* stream);
-/* Writes PPF_STATUS_NONFINITE into *status if any interior cell is not
- * finite (the host checks it every window). */
+/* ORs PPF_STATUS_NONFINITE into *status (device memory) if any interior
+ * cell is not finite: the NaN/Inf sentinel the engines run after every
+ * chunk of steps. No counterpart in the reference (its engines never check). */
 int32_t ppf_check_finite_f32(const float* x, const PpfGrid* g, int32_t* status,
+                             void* stream);
+int32_t ppf_check_finite_f64(const double* x, const PpfGrid* g, int32_t* status,
                              void* stream);
 
 /* Reads and clears the library's device status word (PPF_STATUS_* bits
  * or'ed in by kernels: a bounded wait that gave up, a non-finite value).
  * Synchronous. */
 int32_t ppf_status_take(int32_t* status);
+/* Stream-ordered, graph-capturable form: moves the library's status bits
+ * into *dst (device memory; *dst |= bits) and clears the library word, so
+ * that an engine can keep its own sticky status word and copy it to the
+ * host asynchronously. No counterpart in the reference. */
+int32_t ppf_status_collect(int32_t* dst, void* stream);
 /* Launches a kernel whose barrier wait can never complete, with a poll
  * limit, so that it gives up and reports PPF_STATUS_TIMEOUT (test of the
  * bounded-wait path; nothing is left in flight). */

@@ -11,7 +11,7 @@ from pathlib import Path
 
 LIB_PATH = Path(__file__).resolve().parent / "libppf_gb300.so"
 
-PPF_ABI_VERSION = 2  # the struct layouts and signatures below
+PPF_ABI_VERSION = 3  # the struct layouts and signatures below
 PPF_OK = 0
 PPF_ERR_INVALID = -1
 PPF_ERR_CUDA = -2
@@ -205,7 +205,9 @@ SIGNATURES: dict[str, list] = {
     "ppf_free_energy_f32": [P, PG, PB, C.c_double, C.c_double, C.c_double, P, P, SZ, P],
     "ppf_free_energy_f64": [P, PG, PB, C.c_double, C.c_double, C.c_double, P, P, SZ, P],
     "ppf_check_finite_f32": [P, PG, P, P],
+    "ppf_check_finite_f64": [P, PG, P, P],
     "ppf_status_take": [C.POINTER(I32)],
+    "ppf_status_collect": [P, P],
     "ppf_selftest_wait_timeout": [I32, P],
     "ppf_counter_add_u64": [P, U64, P],
     "ppf_graph_begin": [P],
@@ -229,16 +231,23 @@ def load(path: str | Path | None = None):
                     f"{p} not found: build it with `python -m pyphasefield_gb300.build` "
                     "(the CUDA library is the only compute path)")
             lib = C.CDLL(str(p))
-            for name, argtypes in SIGNATURES.items():
-                fn = getattr(lib, name)
-                fn.argtypes = argtypes
-                fn.restype = C.c_int32
+            # the ABI first: a library of another ABI may lack symbols bound below
+            lib.ppf_version.argtypes = [C.POINTER(I32), C.c_char_p, SZ]
+            lib.ppf_version.restype = C.c_int32
             abi = I32()
             buf = C.create_string_buffer(128)
             lib.ppf_version(C.byref(abi), buf, len(buf))
             if abi.value != PPF_ABI_VERSION:
                 raise OSError(f"{p} has ABI {abi.value}, this binding {PPF_ABI_VERSION}: "
                               "rebuild it with `python -m pyphasefield_gb300.build`")
+            for name, argtypes in SIGNATURES.items():
+                try:
+                    fn = getattr(lib, name)
+                except AttributeError:
+                    raise OSError(f"{p} lacks {name}: rebuild it with "
+                                  "`python -m pyphasefield_gb300.build`") from None
+                fn.argtypes = argtypes
+                fn.restype = C.c_int32
             _lib = lib
     return _lib
 

@@ -6,6 +6,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <mutex>
+
 #include "ppf_gb300.h"
 
 namespace ppf {
@@ -47,6 +49,47 @@ struct Bc {
 // current device; kernels that wait on barriers or check values OR
 // their findings into it.
 int* status_ptr();
+
+// Identifier of the CUDA context current on this thread (cuCtxGetId: unique
+// for the life of the process, so a primary context that was reset and
+// re-created gets a new one); 0 when the driver cannot tell.
+unsigned long long current_context_id();
+
+// Per-device cache of the device address of one __device__ array. On the
+// host a __device__ array's name stands for a host-side stand-in, not for
+// device memory, so host code looks the address up (cudaGetSymbolAddress)
+// with the device current and hands it to kernels. Entries are keyed by
+// device and by context id, so a context reset leads to a fresh lookup;
+// the mutex makes concurrent host threads safe.
+struct SymbolCache {
+  static constexpr int kMaxDevices = 64;
+  std::mutex m;
+  void* addr[kMaxDevices] = {};
+  unsigned long long ctx[kMaxDevices] = {};
+};
+
+// Looks up `sym` through `cache` for the current device; the lookup is
+// compiled into the translation unit that names the symbol.
+template <typename S>
+inline int32_t symbol_address(const S& sym, SymbolCache& cache, void** out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return fail(PPF_ERR_CUDA, "cudaGetDevice: %s", cudaGetErrorString(e));
+  if (dev < 0 || dev >= SymbolCache::kMaxDevices)
+    return fail(PPF_ERR_UNSUPPORTED, "device %d out of range", dev);
+  const unsigned long long ctx = current_context_id();
+  std::lock_guard<std::mutex> lock(cache.m);
+  if (!cache.addr[dev] || cache.ctx[dev] != ctx) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, sym);
+    if (e != cudaSuccess)
+      return fail(PPF_ERR_CUDA, "cudaGetSymbolAddress: %s", cudaGetErrorString(e));
+    cache.addr[dev] = p;
+    cache.ctx[dev] = ctx;
+  }
+  *out = cache.addr[dev];
+  return PPF_OK;
+}
 
 // Validates a PpfGrid and fills a Geo. Returns PPF_OK or an error code.
 int32_t make_geo(const PpfGrid* g, int want_ndim_min, int want_ndim_max,

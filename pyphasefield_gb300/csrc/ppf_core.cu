@@ -104,16 +104,43 @@ __global__ void counter_add_kernel(uint64_t* c, uint64_t inc) {
 // ------------------------------------------------------------ status word
 __device__ int g_status;
 
-int* status_ptr() {
-  static int* cached[64] = {};
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
-  if (!cached[dev]) {
+unsigned long long current_context_id() {
+  using GetCurrent = CUresult (*)(CUcontext*);
+  using GetId = CUresult (*)(CUcontext, unsigned long long*);
+  static GetCurrent get_current = nullptr;
+  static GetId get_id = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
     void* p = nullptr;
-    if (cudaGetSymbolAddress(&p, g_status) != cudaSuccess) return nullptr;
-    cached[dev] = (int*)p;
-  }
-  return cached[dev];
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess && q == cudaDriverEntryPointSuccess)
+      get_current = (GetCurrent)p;
+    p = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess && q == cudaDriverEntryPointSuccess)
+      get_id = (GetId)p;
+  });
+  if (!get_current || !get_id) return 0;
+  CUcontext ctx = nullptr;
+  if (get_current(&ctx) != CUDA_SUCCESS || !ctx) return 0;
+  unsigned long long id = 0;
+  return get_id(ctx, &id) == CUDA_SUCCESS ? id : 0;
+}
+
+int* status_ptr() {
+  static SymbolCache cache;
+  void* p = nullptr;
+  if (symbol_address(g_status, cache, &p) != PPF_OK) return nullptr;
+  return (int*)p;
+}
+
+// Moves the library's status bits into the caller's word: *dst |= bits,
+// library word cleared (stream-ordered, so it can sit in a captured graph).
+__global__ void status_collect_kernel(int* lib, int* dst) {
+  pdl_wait();
+  const int v = atomicExch(lib, 0);
+  if (v) atomicOr(dst, v);
 }
 
 // Waits on an mbarrier that nothing completes, with a small poll limit, to
@@ -268,6 +295,16 @@ int32_t ppf_status_take(int32_t* status) {
   PPF_TRY_CUDA(cudaMemcpy(&v, p, sizeof(int), cudaMemcpyDeviceToHost));
   PPF_TRY_CUDA(cudaMemset(p, 0, sizeof(int)));
   *status = v;
+  return PPF_OK;
+}
+
+int32_t ppf_status_collect(int32_t* dst, void* stream) {
+  clear_error();
+  if (!dst) return fail(PPF_ERR_INVALID, "dst is NULL");
+  int* p = status_ptr();
+  if (!p) return fail(PPF_ERR_CUDA, "status word unavailable");
+  status_collect_kernel<<<1, 1, 0, (cudaStream_t)stream>>>(p, (int*)dst);
+  PPF_TRY_CUDA(cudaGetLastError());
   return PPF_OK;
 }
 

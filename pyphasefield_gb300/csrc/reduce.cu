@@ -171,22 +171,28 @@ static __device__ __align__(256) double g_noalloc_partials[kNoAllocPartials];
 
 // Device address of g_noalloc_partials on the current device. Host code must
 // not pass the symbol itself to a kernel (on the host it names a stand-in,
-// not device memory), so the address is looked up once per device, with that
-// device current, and cached.
+// not device memory), so the address is looked up with the device current,
+// here in the file that defines the array, and cached per device and
+// context (SymbolCache: safe for concurrent host threads, looked up afresh
+// after a context reset).
 static int32_t noalloc_partials(double** out) {
-  static double* cached[64] = {};
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return fail(PPF_ERR_CUDA, "cudaGetDevice: %s", cudaGetErrorString(e));
-  if (dev < 0 || dev >= 64) return fail(PPF_ERR_UNSUPPORTED, "device %d out of range", dev);
-  if (!cached[dev]) {
-    void* p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_noalloc_partials);
-    if (e != cudaSuccess)
-      return fail(PPF_ERR_CUDA, "cudaGetSymbolAddress: %s", cudaGetErrorString(e));
-    cached[dev] = static_cast<double*>(p);
-  }
-  *out = cached[dev];
+  static SymbolCache cache;
+  void* p = nullptr;
+  const int32_t rc = symbol_address(g_noalloc_partials, cache, &p);
+  if (rc) return rc;
+  *out = static_cast<double*>(p);
+  return PPF_OK;
+}
+
+template <typename T>
+int32_t check_finite(const T* x, const PpfGrid* grid, int32_t* status, void* stream) {
+  clear_error();
+  Geo g;
+  int32_t rc = make_geo(grid, 2, 3, &g);
+  if (rc) return rc;
+  if (!x || !status) return fail(PPF_ERR_INVALID, "NULL pointer");
+  finite_kernel<T><<<152 * 4, kRedThreads, 0, (cudaStream_t)stream>>>(x, g, (int*)status);
+  PPF_TRY_CUDA(cudaGetLastError());
   return PPF_OK;
 }
 
@@ -268,14 +274,11 @@ int32_t ppf_free_energy_f64(const double* x, const PpfGrid* g,
 
 int32_t ppf_check_finite_f32(const float* x, const PpfGrid* grid, int32_t* status,
                              void* stream) {
-  clear_error();
-  Geo g;
-  int32_t rc = make_geo(grid, 2, 3, &g);
-  if (rc) return rc;
-  if (!x || !status) return fail(PPF_ERR_INVALID, "NULL pointer");
-  finite_kernel<float><<<152 * 4, kRedThreads, 0, (cudaStream_t)stream>>>(x, g, (int*)status);
-  PPF_TRY_CUDA(cudaGetLastError());
-  return PPF_OK;
+  return check_finite<float>(x, grid, status, stream);
+}
+int32_t ppf_check_finite_f64(const double* x, const PpfGrid* grid, int32_t* status,
+                             void* stream) {
+  return check_finite<double>(x, grid, status, stream);
 }
 
 }  // extern "C"

@@ -609,13 +609,16 @@ __global__ void splitk_reduce_kernel(const float* __restrict__ part, int nz, lon
   }
 }
 
+// Device address of g_splitk on the current device (per device and
+// context, see SymbolCache); nullptr if the lookup failed.
 float* splitk_buffer() {
-  static float* p = nullptr;
-  if (!p && cudaGetSymbolAddress((void**)&p, g_splitk) != cudaSuccess) {
+  static SymbolCache cache;
+  void* p = nullptr;
+  if (symbol_address(g_splitk, cache, &p) != PPF_OK) {
     cudaGetLastError();
-    p = nullptr;
+    return nullptr;
   }
-  return p;
+  return (float*)p;
 }
 
 // y[M x N] += A B with k = tokens (about 256 per split).

@@ -19,12 +19,27 @@ retrieve_fields_from_GPU / apply_boundary_conditions, ppf_gpu_utils.py:
 
 User-data keys added to the reference's: precision ("fp32" | "fp64"),
 temporal_depth (steps per HBM pass, 2-D Diffusion/Allen-Cahn), tile
-((tile_x, tile_y) or None), pdl (bool), use_graph (bool), graph_chunk (int).
+((tile_x, tile_y) or None), pdl (bool), use_graph (bool), graph_chunk (int),
+check_status (bool, default True).
+
+Failure detection: after every chunk of steps (inside the captured graph)
+the engine runs the NaN/Inf sentinel over its fields (ppf_check_finite_*),
+moves the library's status bits (a bounded barrier wait that gave up, a
+Cahn-Hilliard range overflow) into its own sticky status word
+(ppf_status_collect) and copies that word to pinned host memory. The host
+reads the copy at the next chunk boundary (waiting for the chunk before the
+last, so the device stays a chunk ahead), at every autosave and in
+retrieve_fields_from_GPU, and raises EngineFault on any set bit: a run never
+carries on from a state a kernel reported as corrupt. The library's word is
+shared by every engine on a device; whichever engine collects it first
+reports the fault.
 """
 from __future__ import annotations
 
+import collections
 import ctypes as C
 import gc
+import hashlib
 
 import numpy as np
 import torch
@@ -34,7 +49,23 @@ from ..device import DeviceGrid, boundary_struct, ptr, require_cuda, tiling_stru
 from ..simulation import fill_ghosts_host
 
 COMMON_DEFAULTS = dict(precision="fp32", temporal_depth=1, tile=None, pdl=True,
-                       use_graph=True, graph_chunk=64)
+                       use_graph=True, graph_chunk=64, check_status=True)
+
+#: captured graphs kept per engine (one per distinct parameter set)
+MAX_GRAPHS = 8
+
+_STATUS_NAMES = ((L.PPF_STATUS_TIMEOUT, "a bounded barrier wait timed out (tile not written)"),
+                 (L.PPF_STATUS_NONFINITE, "a field holds NaN or Inf"),
+                 (L.PPF_STATUS_RANGE, "a value left the kernel's representable range"))
+
+
+class EngineFault(RuntimeError):
+    """A kernel reported a fault through the device status word."""
+
+    def __init__(self, bits: int, where: str):
+        self.bits = bits
+        names = [n for b, n in _STATUS_NAMES if bits & b] or [f"status bits {bits:#x}"]
+        super().__init__(f"{where}: " + "; ".join(names))
 
 
 class GB300Engine:
@@ -99,14 +130,70 @@ class GB300Engine:
         self._ppf_stepctr = torch.zeros(1, dtype=torch.int64, device=dev)
         # the buffers' zero fills ran on the current stream
         self._ppf_stream.wait_stream(torch.cuda.current_stream(dev))
-        self._ppf_graphs = {}
+        self._ppf_graphs = collections.OrderedDict()
         self._ppf_staging = []
+        self._ppf_status = torch.zeros(1, dtype=torch.int32, device=dev)
+        self._ppf_status_host = torch.zeros(1, dtype=torch.int32, pin_memory=True)
+        self._ppf_status_events = collections.deque()
         self._uses_gpu = True
 
     def _ppf_release_graphs(self):
         for g in getattr(self, "_ppf_graphs", {}).values():
             L.call("ppf_graph_destroy", g)
-        self._ppf_graphs = {}
+        self._ppf_graphs = collections.OrderedDict()
+
+    # ------------------------------------------------------------ status
+    def _ppf_watch(self, stream):
+        """Launches issued after a chunk of steps (captured with it): the
+        NaN/Inf sentinel on the current fields, the library status bits
+        moved into the engine's word, and the word copied to pinned host
+        memory."""
+        if not self.user_data.get("check_status", True):
+            return
+        sp = C.c_void_p(stream.cuda_stream)
+        f = "f32" if self._ppf_dtype == torch.float32 else "f64"
+        st = ptr(self._ppf_status)
+        for t in self._ppf_bufs[self._ppf_cur]:
+            L.call(f"ppf_check_finite_{f}", ptr(t), C.byref(self._ppf_grid.grid), st, sp)
+        L.call("ppf_status_collect", st, sp)
+        with torch.cuda.stream(stream):
+            self._ppf_status_host.copy_(self._ppf_status, non_blocking=True)
+
+    def _ppf_watch_launches(self) -> int:
+        """Kernels _ppf_watch launches (the copy is not a kernel)."""
+        return self.NFIELDS + 1 if self.user_data.get("check_status", True) else 0
+
+    def _ppf_mark(self):
+        """Records the point after a chunk's status copy (host side)."""
+        if self.user_data.get("check_status", True):
+            ev = torch.cuda.Event()
+            ev.record(self._ppf_stream)
+            self._ppf_status_events.append(ev)
+
+    def _ppf_check_status(self, block: bool, where: str = "simulate"):
+        """Raises EngineFault if a chunk reported a fault. block=False waits
+        only for chunks two or more behind the newest, so the device keeps
+        one chunk queued; block=True waits for everything issued."""
+        if not self._ppf_ready():
+            return
+        evs = self._ppf_status_events
+        if block:
+            if evs:
+                evs[-1].synchronize()
+                evs.clear()
+        else:
+            while len(evs) > 1:
+                evs.popleft().synchronize()
+        bits = int(self._ppf_status_host.item())
+        if bits:
+            self.synchronize()
+            bits = int(self._ppf_status_host.item())
+            with torch.cuda.stream(self._ppf_stream):
+                self._ppf_status.zero_()
+            self._ppf_stream.synchronize()
+            self._ppf_status_host.zero_()
+            raise EngineFault(bits, f"{type(self).__name__} {where} (step "
+                                    f"{self.time_step_counter})")
 
     def __del__(self):
         try:
@@ -190,6 +277,7 @@ class GB300Engine:
     def retrieve_fields_from_GPU(self):
         if not self._ppf_ready():
             return
+        self._ppf_check_status(True, "retrieve_fields_from_GPU")
         s = self._ppf_stream
         for j, f in enumerate(self.fields):
             f.data[f._slice] = self._ppf_decode(
@@ -235,11 +323,17 @@ class GB300Engine:
                 chunk = min(chunk, rate - self.time_step_counter % rate)
             # the reference increments the counter before each engine call;
             # the step index keyed into the noise is the counter before it
-            self._ppf_advance(chunk, self.time_step_counter)
+            try:
+                self._ppf_advance(chunk, self.time_step_counter)
+            except EngineFault:
+                # the counter covers the steps launched before the fault
+                self.time_step_counter += self._ppf_done
+                raise
             self.time_step_counter += chunk
             self._ppf_advance_temperature(chunk)
             n -= chunk
             if rate and self.time_step_counter % rate == 0:
+                self._ppf_check_status(True, "autosave")
                 self._ppf_checkpoint()
         self._ppf_checkpoint_wait()
 
@@ -312,11 +406,32 @@ class GB300Engine:
         self._ppf_step(src, dst, depth, step, step_base, C.c_void_p(self._ppf_stream.cuda_stream))
         self._ppf_cur ^= 1
 
+    def _ppf_state_key(self):
+        """What a captured graph bakes in besides the buffers: every
+        user_data value (parameters, tiling, seed, ...), dt, dx and the
+        boundary struct. A graph is reused only while all of it is unchanged,
+        so editing user_data between simulate() calls never replays stale
+        constants."""
+        items = []
+        for k, v in sorted(self.user_data.items(), key=lambda kv: str(kv[0])):
+            if isinstance(v, np.ndarray):
+                v = (v.shape, v.dtype.str,
+                     hashlib.sha1(np.ascontiguousarray(v).tobytes()).hexdigest())
+            elif isinstance(v, torch.Tensor):
+                v = ("tensor", v.data_ptr(), tuple(v.shape), v._version)
+            else:
+                v = repr(v)
+            items.append((str(k), v))
+        return (tuple(items), repr(self.dt), repr(self.dx), bytes(self._ppf_bc))
+
     def _ppf_graph(self, depths: tuple[int, ...]):
-        key = (self._ppf_cur, depths)
+        key = (self._ppf_cur, depths, self._ppf_state_key())
         g = self._ppf_graphs.get(key)
         if g is not None:
+            self._ppf_graphs.move_to_end(key)
             return g
+        while len(self._ppf_graphs) >= MAX_GRAPHS:
+            L.call("ppf_graph_destroy", self._ppf_graphs.popitem(last=False)[1])
         s = self._ppf_stream
         sp = C.c_void_p(s.cuda_stream)
         cur0 = self._ppf_cur
@@ -336,6 +451,7 @@ class GB300Engine:
                     self._ppf_launch_pass(d, off, self._ppf_stepctr)
                     off += d
                 L.call("ppf_counter_add_u64", ptr(self._ppf_stepctr), C.c_uint64(total), sp)
+                self._ppf_watch(s)
         finally:
             try:
                 L.call("ppf_graph_end", sp, C.byref(exec_))
@@ -350,6 +466,7 @@ class GB300Engine:
         """Advance nsteps from absolute step index step0 (noise key)."""
         if nsteps <= 0:
             return
+        self._ppf_done = 0
         passes = self._ppf_passes(nsteps)
         ud = self.user_data
         chunk = max(2, int(ud.get("graph_chunk", 64)) // 2 * 2)
@@ -365,17 +482,23 @@ class GB300Engine:
                 with torch.cuda.stream(s):
                     self._ppf_stepctr.fill_(step)
                 while len(passes) - i >= chunk:
+                    self._ppf_check_status(False)
                     L.call("ppf_graph_launch", g, sp)
+                    self._ppf_mark()
                     self._ppf_segment_end(span, s)
                     i += chunk
                     step += span
+                    self._ppf_done += span
         if i < len(passes):
+            self._ppf_check_status(False)
             rest = passes[i:]
             with torch.cuda.stream(s):
                 self._ppf_segment_begin(sum(rest), s)
                 for d in rest:
                     self._ppf_launch_pass(d, step, None)
                     step += d
+                self._ppf_watch(s)
+            self._ppf_mark()
             self._ppf_segment_end(sum(rest), s)
 
     # ------------------------------------------------------------ access

@@ -311,7 +311,6 @@ class _CahnHilliardMixin(_ImplicitPhase, GB300Engine):
         chunk = max(2, int(self.user_data.get("graph_chunk", 64)))
         self._ch_mass = torch.zeros(max(chunk, 1024), dtype=torch.float64,
                                     device=self._ppf_grid.device)
-        self._ch_status = torch.zeros(1, dtype=torch.int32, device=self._ppf_grid.device)
 
     def _ppf_encode(self, j, x):
         if self._ppf_phase_solver is not None:
@@ -361,7 +360,7 @@ class _CahnHilliardMixin(_ImplicitPhase, GB300Engine):
         self._ch_k += 1
         L.call(f"ppf_cahn_hilliard_step_{_F[self._ppf_dtype]}", C.byref(p),
                C.byref(self._ppf_grid.grid), C.byref(self._ppf_bc), ptr(src[0]), ptr(dst[0]),
-               ptr(mass), ptr(self._ch_status), C.byref(self._ppf_tiling(depth)), sp)
+               ptr(mass), ptr(self._ppf_status), C.byref(self._ppf_tiling(depth)), sp)
 
     def collect_mass_history(self) -> np.ndarray:
         """FP64 total mass sum(c) after every step run so far (host sync)."""
@@ -374,8 +373,10 @@ class _CahnHilliardMixin(_ImplicitPhase, GB300Engine):
         return np.asarray(self.mass_history)
 
     def status_flags(self) -> int:
+        """The engine's sticky status word (PPF_STATUS_* bits seen so far
+        and not yet raised as EngineFault; host sync)."""
         self.synchronize()
-        return int(self._ch_status.item())
+        return int(self._ppf_status.item())
 
 
 class _Warren1995Mixin(GB300Engine):

@@ -150,9 +150,15 @@ class Ensemble:
             m.ac = s._ppf_params()
         return m
 
+    def _members_key(self) -> bytes:
+        """Every member's parameter struct as bytes: the plan (and so every
+        captured graph) bakes these in."""
+        return b"".join(bytes(self._member(s)) for s in self.sims)
+
     def _build(self):
         n = len(self.sims)
         self.members = (L.PpfMember * n)(*[self._member(s) for s in self.sims])
+        self._key = b"".join(bytes(m) for m in self.members)
         nbytes = C.c_size_t()
         L.call("ppf_ensemble_plan_bytes", self.members, n, C.byref(self.tiling), C.byref(nbytes))
         self.table = torch.empty(max(16, nbytes.value), dtype=torch.uint8,
@@ -191,9 +197,17 @@ class Ensemble:
         return exec_
 
     def simulate(self, n: int, use_graph: bool = True):
-        """Advance every member n steps."""
+        """Advance every member n steps. A member whose parameters changed
+        since the last call (user_data edited) gets a new plan: no captured
+        graph replays old constants."""
         n = int(n)
         sp = C.c_void_p(self.stream.cuda_stream)
+        if self._members_key() != self._key:
+            self.synchronize()
+            for g in self.graphs.values():
+                L.call("ppf_graph_destroy", g)
+            self.graphs = {}
+            self._build()
         if use_graph and n >= self.graph_chunk:
             g = self._graph()
             with torch.cuda.stream(self.stream):

@@ -158,7 +158,7 @@ def test_library_rejects_bad_arguments_without_gpu(built_lib):
     from pyphasefield_gb300 import _lib as L
     L.load()
     abi, text = L.version()
-    assert abi == L.PPF_ABI_VERSION == 2 and "sm_103a" in text
+    assert abi == L.PPF_ABI_VERSION == 3 and "sm_103a" in text
     g = L.PpfGrid()
     g.ndim = 2
     g.shape[0], g.shape[1] = 8, 8

@@ -132,3 +132,27 @@ def test_allen_cahn_flat_interface_is_stationary():
     out = restate.run_single("allen_cahn", phi0, 500, ["PERIODIC", "NEUMANN"], 1.0, 0.002,
                              M=M, epsilon=eps, W=W)
     assert np.abs(out - phi0).max() < 2e-3
+
+
+@pytest.mark.parametrize("shape,bc,alpha,steps", [
+    ((40, 52), "NEUMANN", 0.0, 30),
+    ((33, 47), ["PERIODIC", "NEUMANN"], 0.3, 40),
+    ((64, 64), "PERIODIC", 0.3, 60),
+    ((21, 30), ["NEUMANN", "DIRCHLET"], 0.3, 12),
+])
+def test_c_restatement_equals_numpy_restatement(shape, bc, alpha, steps):
+    """oracle/warren_c.c (the checker for the full-size Warren1995 runs) against
+    the numpy restatement: equal up to the last bits of atan2/cos/sin."""
+    from oracle import coracle
+    rng = np.random.default_rng(11)
+    phi0 = np.ones(shape)
+    yy, xx = np.mgrid[0:shape[0], 0:shape[1]]
+    phi0[(yy - shape[0] // 2) ** 2 + (xx - shape[1] // 2) ** 2 < 25] = 0.0
+    c0 = 0.40783 + rng.uniform(-1e-3, 1e-3, shape)
+    p = dict(restate.WARREN_DEFAULTS, alpha=alpha)
+    vals = [[[0.0, 0.0], [0.9, 1.0]], [[0.0, 0.0], [0.41, 0.40]]] if "DIRCHLET" in bc else None
+    a = restate.run_warren(phi0, c0, steps, bc, 4.6e-8, p, seed=5, step0=3, values=vals)
+    b = coracle.run_warren(phi0, c0, steps, bc, 4.6e-8, p, seed=5, step0=3, values=vals)
+    for x, y in zip(a, b):
+        assert rel_l2(y, x) < 1e-14
+        assert np.abs(x - y).max() < 1e-13

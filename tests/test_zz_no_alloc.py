@@ -4,9 +4,11 @@ It exists for callers that cannot allocate device memory (their memory
 manager owns the GPU, or allocation is not allowed where they need the
 mass): it takes no scratch and keeps its partial sums in a fixed array inside
 the library. This test calls it through the C ABI twice in a row and checks
-both results against ppf_reduce_sum_f32 (which takes caller scratch) at the
-tolerance the other reduction tests use (1e-12 relative). The file is named
-to run last, and it works alone in a fresh process as well.
+both results against ppf_reduce_sum_f32 (which takes caller scratch) and,
+independently of the library's kernels, against numpy's float64 sum of the
+same float32 values, at the tolerance the other reduction tests use (1e-12
+relative). The file is named to run last, and it works alone in a fresh
+process as well.
 """
 import ctypes as C
 
@@ -48,6 +50,8 @@ def test_noalloc_sum_matches_scratch_sum_twice(cuda, shape):
                C.c_void_p(out.data_ptr()), s)
         torch.cuda.synchronize()
         assert abs(out.item() - want) <= 1e-12 * abs(want), (call, out.item(), want)
+        exact = x.astype(np.float32).astype(np.float64).sum()
+        assert abs(out.item() - exact) <= 1e-12 * abs(exact), (call, out.item(), exact)
 
 
 def test_noalloc_sum_rejects_bad_arguments(cuda):
