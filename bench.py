@@ -15,6 +15,15 @@ Metric: cell-updates/s (one cell advanced one time step, both fields).
   roofline  the Warren1995 step kernel: 16 algorithmic bytes per
          cell-update (read and write phi and c once) x cells per launch /
          average launch-to-launch time, against the measured HBM copy peak.
+         The 16 MiB state stays in L2, so this is an effective figure and
+         the kernel is bound by FP32 instruction issue and latency:
+         issue_frac = warp instructions per launch (the committed ncu
+         capture named in `capture`) / (SMs x 4 schedulers x sampled SM
+         clock x launch time); traffic = that capture's DRAM bytes.
+  fp64   the same workload in float64, device timed (one bench step).
+  sweep  three cases beyond L2 (Diffusion 2-D 16384^2, Cahn-Hilliard 3-D
+         256^3, Warren1995 4096^2), 100 steps each, CUDA events: the
+         HBM-bound kernels' fraction of the copy peak.
   cpu_baseline  the FP64 numpy oracle (oracle/restate.py, a restatement of
          Engines/Warren1995.py:50-92) on a bounded sample of the same
          workload on one host core.
@@ -76,12 +85,15 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def committed_traffic():
-    """DRAM bytes per Warren1995 launch from the committed ncu summary."""
-    p = ROOT / "profiles" / "warren1995_1024_traffic.json"
+def committed_capture():
+    """The ncu capture of one Warren1995 launch on the benchmark grid
+    (profiles/warren1995_1024_ncu.json: DRAM bytes and warp instructions per
+    launch, with the command that made it). Counters cannot be read without
+    a profiler, so the bench line quotes the capture and names it."""
+    p = ROOT / "profiles" / "warren1995_1024_ncu.json"
     if p.exists():
-        return json.loads(p.read_text()).get("dram_bytes_per_launch")
-    return None
+        return json.loads(p.read_text())
+    return {}
 
 
 class ClockSampler:
@@ -206,10 +218,11 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
-def make_sim(phi, c, graph_chunk):
+def make_sim(phi, c, graph_chunk, precision="fp32"):
     from pyphasefield_gb300 import Warren1995GB300
     sim = Warren1995GB300(dimensions=list(SHAPE), dx=DX, boundary_conditions="NEUMANN",
-                          user_data={"seed": SEED, "alpha": 0.3, "graph_chunk": graph_chunk})
+                          user_data={"seed": SEED, "alpha": 0.3, "graph_chunk": graph_chunk,
+                                     "precision": precision})
     sim.initialize_fields_and_imported_data()
     sim.fields[0].data[1:-1, 1:-1] = phi
     sim.fields[1].data[1:-1, 1:-1] = c
@@ -307,11 +320,54 @@ def run_gb300(args):
     e2e_s = max_over_ranks(float(np.mean(e2e_times)))
     e2e_value = world * cells * args.sim_steps / e2e_s
 
+    # the same workload in float64 (the precision of the reference), device
+    # timed: one warm-up and one timed bench step
+    fp64 = None
+    if not args.no_fp64:
+        sim64 = make_sim(phi0, c0, chunk, precision="fp64")
+        sim64._begun_simulation = True
+        sim64.just_before_simulating()
+        s64 = sim64._ppf_stream
+        with torch.cuda.stream(s64):
+            init64 = [t.clone() for t in sim64._ppf_bufs[sim64._ppf_cur]]
+        sims64 = []
+        for k in range(2):
+            with torch.cuda.stream(s64):
+                for t, i in zip(sim64._ppf_bufs[sim64._ppf_cur], init64):
+                    t.copy_(i)
+                flush.fill_(1.0)
+            sim64.time_step_counter = 0
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(s64)
+            sim64.simulate(args.sim_steps)
+            b.record(s64)
+            b.synchronize()
+            sims64.append(a.elapsed_time(b) / 1e3)
+        sec64 = max_over_ranks(sims64[-1])
+        fp64 = {"value": world * cells * args.sim_steps / sec64, "unit": METRIC,
+                "ms_per_step": 1e3 * sec64, "dtype": "f64",
+                "kernel": "warren1995_kernel<double>",
+                "per_launch_us": sec64 / args.sim_steps * 1e6}
+        del sim64, init64
+
+    sweep = None
+    if not args.no_sweep:
+        sweep = {}
+        for name, steps in (("diffusion_16384", 100), ("cahn_hilliard_256", 100),
+                            ("warren1995_4096", 100)):
+            sweep[name] = time_sweep_case(name, steps)
+            torch.cuda.empty_cache()
+
     if rank == 0:
         peak, peak_kind = peaks()
         achieved = B_ALG * cells / step_launch_s / 1e9
-        traffic = committed_traffic()
-        launches = args.steps * (args.sim_steps + -(-args.sim_steps // chunk))
+        cap = committed_capture()
+        # per graph chunk: the steps, the step counter, and the status watch
+        # (NaN/Inf sentinel per field and the status collect)
+        n_chunks = -(-args.sim_steps // chunk)
+        launches = args.steps * (args.sim_steps + n_chunks * (1 + sim._ppf_watch_launches()))
+        sm_count = torch.cuda.get_device_properties(local).multi_processor_count
         line = {
             "metric": METRIC, "value": value, "unit": "cell-updates/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup,
@@ -325,10 +381,11 @@ def run_gb300(args):
                        "graph_chunk": chunk},
             "e2e": {"value": e2e_value, "unit": "cell-updates/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": traffic,
+            "roofline": {"bound": "L2-resident state; FP32 issue/latency",
+                         "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": cap.get("dram_bytes_per_launch"),
                          "peak_source": peak_kind,
-                         "kernel": "warren1995_kernel<float>",
+                         "kernel": "warren1995_kernel<float, 2>",
                          "per_launch_us": step_launch_s * 1e6},
             "gpu_launches": launches,
             "wall_s": wall,
@@ -336,6 +393,17 @@ def run_gb300(args):
         clocks = clk.summary()
         if clocks:
             line["clocks"] = clocks
+        if cap.get("warp_instructions_per_launch"):
+            # warp instructions issued per launch (ncu) over the issue slots of
+            # the average launch: SMs x 4 schedulers x SM clock x launch time
+            mhz = (clocks or {}).get("sm_mhz") or cap.get("sm_mhz")
+            slots = sm_count * 4 * mhz * 1e6 * step_launch_s
+            line["roofline"]["issue_frac"] = cap["warp_instructions_per_launch"] / slots
+            line["roofline"]["capture"] = cap.get("source")
+        if fp64:
+            line["fp64"] = fp64
+        if sweep:
+            line["sweep"] = sweep
         if not args.no_cpu_baseline and world == 1:  # the CPU baseline is an N = 1 figure
             line["cpu_baseline"] = cpu_baseline(budget_s=args.cpu_budget)
         print(json.dumps(line), flush=True)
@@ -475,59 +543,68 @@ def run_sweep(args):
     import __graft_entry__
     if not (ROOT / "pyphasefield_gb300" / "libppf_gb300.so").exists():
         __graft_entry__.build()
-    peak, peak_kind = peaks()
     names = list(SWEEP) if args.sweep == "all" else args.sweep.split(",")
     for name in names:
-        model, grid, depth, steps = SWEEP[name][:4]
-        extra = SWEEP[name][4] if len(SWEEP[name]) > 4 else None
-        rng = np.random.default_rng(0)
-        if model == "ensemble":
-            from pyphasefield_gb300.ensemble import Ensemble, make_config_ensemble
-            sims = make_config_ensemble(n=64, seed=0)
-            runner = Ensemble(sims, graph_chunk=100)
-            cells = runner.cells
-            bytes_per_step = sum(s._ppf_grid.cells * (16 if len(s.fields) == 2 else 8)
-                                 for s in sims)
-            stream = runner.stream
-            advance = runner.simulate
-        else:
-            sim = sweep_engine(model, grid, depth, steps, rng, extra)
-            cells = int(np.prod(grid))
-            advance = sim.simulate
-        advance(min(steps, 100))  # set-up, upload, graph capture, warm-up
-        if model != "ensemble":
-            bytes_per_step = sweep_bytes_per_cell(model, sim) * cells
-        if model != "ensemble":
-            stream = sim._ppf_stream
-        torch.cuda.synchronize()
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        with ClockSampler(torch.cuda.current_device()) as clk:
-            e0.record(stream)
-            advance(steps)
-            e1.record(stream)
-            e1.synchronize()
-        sec = e0.elapsed_time(e1) / 1e3
-        line = {"sweep": name, "model": model, "grid": list(grid) if grid else "config ensemble",
-                "temporal_depth": depth, "steps": steps, "cells": cells, "options": extra or {},
-                "cell_updates_per_s": cells * steps / sec, "ms_per_step": 1e3 * sec / steps,
-                "algorithmic_bytes_per_step": bytes_per_step,
-                "achieved_gbs": bytes_per_step * steps / sec / 1e9, "peak_gbs": peak,
-                "peak_source": peak_kind}
-        line["frac"] = line["achieved_gbs"] / peak
-        # SM clocks sampled every 200 ms during the timed steps (null when
-        # the case ends before the first sample)
-        line["clocks"] = clk.summary()
-        if model == "cahn_hilliard":
-            m = sim.collect_mass_history()
-            line["mass_rel_drift"] = float(abs(m[-1] - m[0]) / abs(m[0]))
-        print(json.dumps(line), flush=True)
-        del advance, stream
-        if model == "ensemble":
-            del runner, sims
-        else:
-            del sim
+        print(json.dumps(time_sweep_case(name)), flush=True)
         torch.cuda.empty_cache()
+
+
+def time_sweep_case(name, steps=None):
+    """One sweep case: set-up, upload and warm-up (with graph capture), then
+    `steps` steps (default: the case's own) timed with CUDA events on the
+    engine's stream. Returns the case's JSON record."""
+    import torch
+    peak, peak_kind = peaks()
+    model, grid, depth, case_steps = SWEEP[name][:4]
+    steps = steps or case_steps
+    extra = SWEEP[name][4] if len(SWEEP[name]) > 4 else None
+    rng = np.random.default_rng(0)
+    if model == "ensemble":
+        from pyphasefield_gb300.ensemble import Ensemble, make_config_ensemble
+        sims = make_config_ensemble(n=64, seed=0)
+        runner = Ensemble(sims, graph_chunk=100)
+        cells = runner.cells
+        bytes_per_step = sum(s._ppf_grid.cells * (16 if len(s.fields) == 2 else 8)
+                             for s in sims)
+        stream = runner.stream
+        advance = runner.simulate
+    else:
+        sim = sweep_engine(model, grid, depth, steps, rng, extra)
+        cells = int(np.prod(grid))
+        advance = sim.simulate
+    advance(min(steps, 100))  # set-up, upload, graph capture, warm-up
+    if model != "ensemble":
+        bytes_per_step = sweep_bytes_per_cell(model, sim) * cells
+    if model != "ensemble":
+        stream = sim._ppf_stream
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(torch.cuda.current_device()) as clk:
+        e0.record(stream)
+        advance(steps)
+        e1.record(stream)
+        e1.synchronize()
+    sec = e0.elapsed_time(e1) / 1e3
+    line = {"sweep": name, "model": model, "grid": list(grid) if grid else "config ensemble",
+            "temporal_depth": depth, "steps": steps, "cells": cells, "options": extra or {},
+            "cell_updates_per_s": cells * steps / sec, "ms_per_step": 1e3 * sec / steps,
+            "algorithmic_bytes_per_step": bytes_per_step,
+            "achieved_gbs": bytes_per_step * steps / sec / 1e9, "peak_gbs": peak,
+            "peak_source": peak_kind}
+    line["frac"] = line["achieved_gbs"] / peak
+    # SM clocks sampled every 200 ms during the timed steps (null when
+    # the case ends before the first sample)
+    line["clocks"] = clk.summary()
+    if model == "cahn_hilliard":
+        m = sim.collect_mass_history()
+        line["mass_rel_drift"] = float(abs(m[-1] - m[0]) / abs(m[0]))
+    del advance, stream
+    if model == "ensemble":
+        del runner, sims
+    else:
+        del sim
+    return line
 
 
 def _errors(a, b):
@@ -736,6 +813,10 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true",
+                    help="skip the float64 rate of the same workload")
+    ap.add_argument("--no-sweep", action="store_true",
+                    help="skip the three beyond-L2 cases added to the bench line")
     ap.add_argument("--sweep", default=None,
                     help="roofline sweep instead of the benchmark: 'all' or a comma list of "
                          + ", ".join(SWEEP))

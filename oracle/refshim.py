@@ -19,8 +19,9 @@ functions with a duck-typed simulation object:
   * The implicit / Crank-Nicolson engines (Diffusion.py:210-633) run on an
     interior-only field (run_implicit).
 
-Available only where the reference checkout exists (PPF_REFERENCE_ROOT or the
-default below); callers skip otherwise. Nothing here is used at run time.
+Available only where the environment variable PPF_REFERENCE_ROOT names a
+reference checkout (the directory holding the pyphasefield package); callers
+skip otherwise. Nothing here is used at run time.
 """
 from __future__ import annotations
 
@@ -33,11 +34,11 @@ import numpy as np
 
 from . import restate
 
-DEFAULT_ROOT = "/root/reference/pyphasefield"
-
-
 def reference_root() -> Path | None:
-    root = Path(os.environ.get("PPF_REFERENCE_ROOT", DEFAULT_ROOT))
+    env = os.environ.get("PPF_REFERENCE_ROOT")
+    if not env:
+        return None
+    root = Path(env)
     return root if (root / "pyphasefield" / "Engines" / "Warren1995.py").exists() else None
 
 

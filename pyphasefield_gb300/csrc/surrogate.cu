@@ -365,9 +365,10 @@ bool tc_enabled() { return g_tc_enabled != 0; }
 // convolutions and the output head. One CTA (4 warps) owns a 128 x 128
 // output tile whose FP32 accumulator lives in tensor memory (128 lanes x
 // 128 columns, allocated by warp 0); k advances in 64-wide tiles staged in
-// shared memory in the canonical K-major no-swizzle layout (8 x 16-byte core
-// matrices: element (row, k) at (row / 8) * 1024 + (k / 8) * 128 +
-// (row % 8) * 16 + (k % 8) * 2 bytes). Two stages: the tile for kt + 1 is
+// shared memory in the K-major 128-byte-swizzled layout (8-row x 128-byte
+// atoms, 1024 bytes apart along the rows: row r's 16-byte chunk j of k at
+// (r / 8) * 1024 + (r % 8) * 128 + ((j ^ (r % 8)) * 16), see tc_desc and
+// tc_load_tile). Two stages: the tile for kt + 1 is
 // loaded while the tensor core works on kt. One thread issues
 // tcgen05.mma (kind::f16, BF16 x BF16 -> F32, M = 128, N = 128, K = 16 per
 // instruction) and tcgen05.commit arrives on the stage's mbarrier; the

@@ -37,9 +37,12 @@ reports the fault.
 from __future__ import annotations
 
 import collections
+import contextlib
 import ctypes as C
 import gc
 import hashlib
+import inspect
+from pathlib import Path
 
 import numpy as np
 import torch
@@ -57,6 +60,37 @@ MAX_GRAPHS = 8
 _STATUS_NAMES = ((L.PPF_STATUS_TIMEOUT, "a bounded barrier wait timed out (tile not written)"),
                  (L.PPF_STATUS_NONFINITE, "a field holds NaN or Inf"),
                  (L.PPF_STATUS_RANGE, "a value left the kernel's representable range"))
+
+
+try:
+    from torch.cuda import nvtx as _nvtx
+except Exception:  # pragma: no cover - torch without NVTX
+    _nvtx = None
+
+
+@contextlib.contextmanager
+def nvtx_range(name: str):
+    """NVTX range on the host timeline (shown by Nsight Systems / ncu
+    --nvtx): simulate calls, graph replays, eager passes, transfers."""
+    if _nvtx is None:
+        yield
+        return
+    _nvtx.range_push(name)
+    try:
+        yield
+    finally:
+        _nvtx.range_pop()
+
+
+def _save_npz(sim, step: int) -> None:
+    """The reference's checkpoint format: np.savez of every field's interior
+    keyed by field name, to <save_path>/step_<step>.npz."""
+    if not sim._save_path:
+        print("self._save_path not defined, aborting save!")
+        return
+    loc = Path(sim._save_path)
+    loc.mkdir(parents=True, exist_ok=True)
+    np.savez(str(loc) + "/step_" + str(int(step)), **{f.name: f.get_cells() for f in sim.fields})
 
 
 class EngineFault(RuntimeError):
@@ -269,6 +303,10 @@ class GB300Engine:
         if not self._ppf_ready():
             self._ppf_setup()
         s = self._ppf_stream
+        with nvtx_range("ppf.send_fields_to_GPU"):
+            self._ppf_send(s)
+
+    def _ppf_send(self, s):
         self._ppf_staging = [
             self._ppf_grid.upload(self._ppf_bufs[self._ppf_cur][j],
                                   self._ppf_encode(j, f.get_cells()), s)
@@ -279,9 +317,10 @@ class GB300Engine:
             return
         self._ppf_check_status(True, "retrieve_fields_from_GPU")
         s = self._ppf_stream
-        for j, f in enumerate(self.fields):
-            f.data[f._slice] = self._ppf_decode(
-                j, self._ppf_grid.download(self._ppf_bufs[self._ppf_cur][j], s))
+        with nvtx_range("ppf.retrieve_fields_from_GPU"):
+            for j, f in enumerate(self.fields):
+                f.data[f._slice] = self._ppf_decode(
+                    j, self._ppf_grid.download(self._ppf_bufs[self._ppf_cur][j], s))
         self._ppf_staging = []
         fill_ghosts_host(self)
 
@@ -312,6 +351,10 @@ class GB300Engine:
         self._ppf_advance(1, self.time_step_counter)
 
     def simulate(self, number_of_timesteps):
+        with nvtx_range(f"ppf.simulate {type(self).__name__} n={int(number_of_timesteps)}"):
+            self._ppf_simulate(number_of_timesteps)
+
+    def _ppf_simulate(self, number_of_timesteps):
         if not self._begun_simulation or not self._ppf_ready():
             self._begun_simulation = True
             self.just_before_simulating()
@@ -346,6 +389,10 @@ class GB300Engine:
         the next steps run. simulate() returns after every write finished,
         with Field.data holding the last autosaved state, as in the
         reference."""
+        with nvtx_range(f"ppf.autosave step {self.time_step_counter}"):
+            self._ppf_checkpoint_issue()
+
+    def _ppf_checkpoint_issue(self):
         import concurrent.futures as cf
         ck = getattr(self, "_ppf_ckpt", None)
         g = self._ppf_grid
@@ -382,7 +429,13 @@ class GB300Engine:
             host = slot["host"][j][..., : g.kshape[-1]].numpy().astype(np.float64)
             f.data[f._slice] = self._ppf_decode(j, host.reshape(g.user_shape))
         fill_ghosts_host(self)
-        self.save_simulation(step=step)
+        if "step" in inspect.signature(self.save_simulation).parameters:
+            self.save_simulation(step=step)
+        else:
+            # the reference's save_simulation (simulation.py:399-420) names the
+            # file by the live counter, which has moved on by now: write the
+            # same file under the step that was snapshotted
+            _save_npz(self, step)
 
     def _ppf_checkpoint_wait(self):
         ck = getattr(self, "_ppf_ckpt", None)
@@ -483,7 +536,8 @@ class GB300Engine:
                     self._ppf_stepctr.fill_(step)
                 while len(passes) - i >= chunk:
                     self._ppf_check_status(False)
-                    L.call("ppf_graph_launch", g, sp)
+                    with nvtx_range(f"ppf.graph {span} steps from {step}"):
+                        L.call("ppf_graph_launch", g, sp)
                     self._ppf_mark()
                     self._ppf_segment_end(span, s)
                     i += chunk
@@ -492,7 +546,7 @@ class GB300Engine:
         if i < len(passes):
             self._ppf_check_status(False)
             rest = passes[i:]
-            with torch.cuda.stream(s):
+            with torch.cuda.stream(s), nvtx_range(f"ppf.eager {sum(rest)} steps from {step}"):
                 self._ppf_segment_begin(sum(rest), s)
                 for d in rest:
                     self._ppf_launch_pass(d, step, None)

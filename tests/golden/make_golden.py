@@ -16,6 +16,7 @@ ncgpu_multicomponent | ncgpu_excess | ncgpu_new`.
 from __future__ import annotations
 
 import json
+import os
 import sys
 from pathlib import Path
 
@@ -83,8 +84,10 @@ def single(name, model, c0, steps, bc, dx, dt, values=None, **params):
 
 
 def main():
+    # this script reads the reference checkout; PPF_REFERENCE_ROOT names it
+    os.environ.setdefault("PPF_REFERENCE_ROOT", "/root/reference/pyphasefield")
     if not refshim.available():
-        raise SystemExit("reference checkout not found")
+        raise SystemExit("reference checkout not found (set PPF_REFERENCE_ROOT)")
     rng = np.random.default_rng(20240601)
     single("diffusion_2d_periodic", "diffusion", 0.5 + 0.01 * rng.standard_normal((24, 20)),
            10, "PERIODIC", 1.0, 0.2, D=1.0)
