@@ -48,6 +48,7 @@ extern "C" {
 #define PPF_STATUS_NONFINITE 1
 #define PPF_STATUS_TIMEOUT 2
 #define PPF_STATUS_RANGE 4
+#define PPF_STATUS_NOT_CONVERGED 8 /* an iterative solve hit its iteration cap */
 
 typedef struct PpfGrid {
   int32_t ndim;     /* 2 or 3 */
@@ -421,10 +422,12 @@ typedef struct PpfEnsemblePlan {
   const void* device_table; /* caller device memory holding the member table */
   int64_t n_items;          /* warp bands over all members */
   int32_t n_members;
-  int32_t rows; /* rows per warp band (tiling->tile_y: 2, 4 or 8) */
+  int32_t rows;    /* rows per warp band (tiling->tile_y: 2, 4 or 8) */
+  int64_t n_units; /* four-band units (one CTA pass each) */
 } PpfEnsemblePlan;
 
-/* Device bytes of the member table for these members. */
+/* Device bytes of the member table (members and unit map) for these
+ * members. */
 int32_t ppf_ensemble_plan_bytes(const PpfMember* members, int32_t n,
                                 const PpfTiling* tiling, size_t* bytes);
 /* Validates the members, folds their parameters and copies the table into
@@ -432,11 +435,23 @@ int32_t ppf_ensemble_plan_bytes(const PpfMember* members, int32_t n,
 int32_t ppf_ensemble_build(const PpfMember* members, int32_t n,
                            const PpfTiling* tiling, void* device_table,
                            size_t bytes, PpfEnsemblePlan* plan, void* stream);
-/* One time step of every member in one persistent launch; Warren1995 noise
- * keyed by (member seed, step + *step_base). */
+/* One time step of every member in one launch; Warren1995 noise keyed by
+ * (member seed, step + *step_base). Replaces the per-instance
+ * Simulation.simulate loop (simulation.py:245-271) over the reference's
+ * engine_Warren1995 / engine_CahnAllenExplicit. */
 int32_t ppf_ensemble_step_f32(const PpfEnsemblePlan* plan, int32_t parity,
                               uint64_t step, const uint64_t* step_base,
                               const PpfTiling* tiling, void* stream);
+/* nsteps time steps of every member in ONE persistent cooperative launch:
+ * the CTAs meet at a grid barrier between steps (waits bounded; a timeout
+ * sets PPF_STATUS_TIMEOUT in the status word and ends the launch early).
+ * `sync` is caller device memory of 8 bytes, zeroed once before its first
+ * use and used by one launch at a time; after a timeout zero it again. The
+ * member buffers swap by step parity, starting from `parity`. */
+int32_t ppf_ensemble_run_f32(const PpfEnsemblePlan* plan, int32_t parity,
+                             uint64_t step, const uint64_t* step_base,
+                             int32_t nsteps, void* sync, const PpfTiling* tiling,
+                             void* stream);
 
 /* ---- learned surrogate (no counterpart in the reference) --------------- *
  * A convolutional encoder-decoder that advances a Warren1995 (phi, c) state

@@ -26,6 +26,7 @@ PPF_BC_DIRCHLET = 2
 PPF_STATUS_NONFINITE = 1
 PPF_STATUS_TIMEOUT = 2
 PPF_STATUS_RANGE = 4
+PPF_STATUS_NOT_CONVERGED = 8
 
 
 class PpfError(RuntimeError):
@@ -128,7 +129,7 @@ class PpfMember(C.Structure):
 
 class PpfEnsemblePlan(C.Structure):
     _fields_ = [("device_table", C.c_void_p), ("n_items", C.c_int64),
-                ("n_members", C.c_int32), ("rows", C.c_int32)]
+                ("n_members", C.c_int32), ("rows", C.c_int32), ("n_units", C.c_int64)]
 
 
 class PpfSgShape(C.Structure):
@@ -183,6 +184,7 @@ SIGNATURES: dict[str, list] = {
     "ppf_ensemble_plan_bytes": [C.POINTER(PpfMember), I32, PT, C.POINTER(SZ)],
     "ppf_ensemble_build": [C.POINTER(PpfMember), I32, PT, P, SZ, C.POINTER(PpfEnsemblePlan), P],
     "ppf_ensemble_step_f32": [C.POINTER(PpfEnsemblePlan), I32, U64, P, PT, P],
+    "ppf_ensemble_run_f32": [C.POINTER(PpfEnsemblePlan), I32, U64, P, I32, P, PT, P],
     "ppf_sg_gemm": [P, C.c_longlong, C.c_longlong, P, C.c_longlong, C.c_longlong, P,
                     C.c_longlong, P, I32, C.c_longlong, C.c_longlong, C.c_longlong, I32, P],
     "ppf_sg_patch_fwd": [C.POINTER(PpfSgShape), P, P, P, P, P, P],

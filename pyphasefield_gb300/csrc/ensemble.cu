@@ -1,15 +1,18 @@
 // Batched ensemble: many Warren1995 and Allen-Cahn instances with uneven 2-D
-// grids and per-instance parameters advanced one step by ONE persistent
-// launch.
+// grids and per-instance parameters, advanced together by one cooperative,
+// persistent launch per chunk of steps.
 //
-// Work items are warp bands (a 30-column strip x ROWS rows of one member);
-// member m owns items [item_begin[m], item_begin[m+1]). A persistent grid of
-// warps walks the items round-robin (every warp gets the same count, +-1),
-// finds each item's member by binary search over item_begin, and runs that
-// member's band update (w95_core.cuh for Warren1995, the Allen-Cahn band
-// below). Each member has its own ping-pong buffers; `parity` selects the
-// direction, so a captured graph of an even number of steps replays
-// unchanged.
+// Work: a member's grid is cut into warp bands (a 30-column strip x ROWS
+// rows), and its bands are grouped four at a time into units, one per CTA
+// pass; a member's units are padded so that no unit spans two members. A
+// unit table maps every unit to its member, so a CTA finds its member with
+// one load and stages the member's folded constants in shared memory for its
+// four warps. The launch is cooperative (every CTA resident) and persistent:
+// each CTA walks the units grid-stride, then all CTAs meet at a grid barrier
+// before the next step (each member's ping-pong buffers swap by step
+// parity). The barrier's waits are bounded: a CTA that waits too long sets
+// PPF_STATUS_TIMEOUT and the launch ends early. Reads of the fields use
+// plain (coherent) loads, since other CTAs of the same launch wrote them.
 //
 // Reference: engine_Warren1995 (Engines/Warren1995.py:50-92) and
 // engine_CahnAllenExplicit (Engines/CahnAllen.py:128-135), one instance per
@@ -19,6 +22,7 @@
 #include <vector>
 
 #include "ppf_common.cuh"
+#include "ppf_grid.cuh"
 #include "w95_core.cuh"
 
 namespace ppf {
@@ -30,7 +34,9 @@ constexpr int kCtaThreads = 32 * kWarpsPerCta;
 struct MemberDev {
   int model;
   int strips;
-  long long item_begin;
+  long long item_begin;  // first band (items of a member are [begin, begin + items))
+  long long items;
+  long long unit_begin;  // first unit
   Geo g;
   Bc<float> bc;
   float* phi[2];
@@ -39,6 +45,9 @@ struct MemberDev {
   w95::Coef<float> w;
   float ac_a, ac_b;  // dt M eps^2 / dx^2, dt M 16 W
 };
+
+// Device table layout: MemberDev[n_members], then int unit_member[n_units].
+inline size_t units_offset(int n) { return ((size_t)n * sizeof(MemberDev) + 15) / 16 * 16; }
 
 // Allen-Cahn band in the warp-strip layout: phi + a lap - b (4phi^3 - 6phi^2
 // + 2phi), neighbour sum grouped ((w + e) + (n + s)) as in the single-grid
@@ -50,14 +59,14 @@ __device__ __forceinline__ void ac_band(float a, float b, const Geo& g, const Bc
   const int lane = threadIdx.x;
   const int ny = g.n[0], nx = g.n[1];
   const int x = xs + lane;
-  const bool x_in = xs >= 0 && xs + 31 < nx;
+  const bool x_in = (unsigned)x < (unsigned)nx;
   const bool owner = lane >= 1 && lane <= w95::kStrip && x < nx;
   float v[ROWS + 2];
 #pragma unroll
   for (int j = 0; j < ROWS + 2; ++j) {
     const int row = y0 - 1 + j;
-    v[j] = (x_in && (unsigned)row < (unsigned)ny) ? __ldg(in + (int64_t)row * g.pitch + x)
-                                                   : fetch<float, 2>(in, g, bc, 0, row, x);
+    v[j] = (x_in && (unsigned)row < (unsigned)ny) ? in[(int64_t)row * g.pitch + x]
+                                                   : fetch<float, 2, true>(in, g, bc, 0, row, x);
   }
 #pragma unroll
   for (int r = 0; r < ROWS; ++r) {
@@ -71,43 +80,52 @@ __device__ __forceinline__ void ac_band(float a, float b, const Geo& g, const Bc
 }
 
 template <int ROWS>
-__global__ void __launch_bounds__(kCtaThreads, 8)
-    ensemble_kernel(const MemberDev* __restrict__ members, int n_members, long long n_items,
-                    int parity, uint64_t step, const uint64_t* __restrict__ step_base) {
-  const long long nwarps = (long long)gridDim.x * kWarpsPerCta;
-  long long it = (long long)blockIdx.x * kWarpsPerCta + threadIdx.y;
-  if (it >= n_items) return;  // whole warp
+__device__ __forceinline__ void run_unit(const MemberDev& m, long long unit, int parity,
+                                         uint64_t step) {
+  const long long local = (unit - m.unit_begin) * kWarpsPerCta + threadIdx.y;
+  if (local >= m.items) return;  // padding warp (whole warp)
+  const int xs = (int)(local % m.strips) * w95::kStrip - 1;
+  const int y0 = (int)(local / m.strips) * ROWS;
+  if (m.model == PPF_MODEL_WARREN1995)
+    w95::band<float, ROWS, true>(m.w, m.g, m.bc, m.phi[parity], m.c[parity], m.phi[1 - parity],
+                                 m.c[1 - parity], m.seed, step, xs, y0);
+  else
+    ac_band<ROWS>(m.ac_a, m.ac_b, m.g, m.bc, m.phi[parity], m.phi[1 - parity], xs, y0);
+}
+
+template <int ROWS>
+__global__ void __launch_bounds__(kCtaThreads, 7)
+    ensemble_kernel(const MemberDev* __restrict__ members, const int* __restrict__ unit_member,
+                    long long n_units, int parity, uint64_t step,
+                    const uint64_t* __restrict__ step_base, int nsteps, unsigned* sync,
+                    int* status) {
+  __shared__ MemberDev sm;
+  __shared__ int flag;
+  const int tid = threadIdx.x + 32 * threadIdx.y;
+  if (tid == 0) flag = 0;
   pdl_wait();
   pdl_launch_next();
   if (step_base) step += *step_base;
-  for (; it < n_items; it += nwarps) {
-    int lo = 0, hi = n_members - 1;
-    while (lo < hi) {
-      const int mid = (lo + hi + 1) >> 1;
-      if (members[mid].item_begin <= it) lo = mid;
-      else hi = mid - 1;
+  for (int s = 0; s < nsteps; ++s) {
+    const int par = (parity + s) & 1;
+    for (long long u = blockIdx.x; u < n_units; u += gridDim.x) {
+      const int mi = unit_member[u];
+      __syncthreads();  // the previous unit is done with sm
+      {
+        const int* src = reinterpret_cast<const int*>(members + mi);
+        int* dst = reinterpret_cast<int*>(&sm);
+        for (int i = tid; i < (int)(sizeof(MemberDev) / 4); i += kCtaThreads) dst[i] = src[i];
+      }
+      __syncthreads();
+      run_unit<ROWS>(sm, u, par, step + s);
     }
-    const MemberDev& m = members[lo];
-    const int local = (int)(it - m.item_begin);
-    const int xs = (local % m.strips) * w95::kStrip - 1;
-    const int y0 = (local / m.strips) * ROWS;
-    // the member's constants are copied to registers once per item: the
-    // band reads them many times, and from global memory each read would be
-    // a dependent load
-    const Geo g = m.g;
-    const Bc<float> bc = m.bc;
-    if (m.model == PPF_MODEL_WARREN1995) {
-      const w95::Coef<float> k = m.w;
-      w95::band<float, ROWS>(k, g, bc, m.phi[parity], m.c[parity], m.phi[1 - parity],
-                             m.c[1 - parity], m.seed, step, xs, y0);
-    } else {
-      ac_band<ROWS>(m.ac_a, m.ac_b, g, bc, m.phi[parity], m.phi[1 - parity], xs, y0);
-    }
+    if (s + 1 < nsteps && !grid_barrier(sync, gridDim.x, status, &flag)) return;
   }
 }
 
 int32_t build_table(const PpfMember* members, int32_t n, const PpfTiling* tiling,
-                    std::vector<MemberDev>* out, long long* n_items, int* rows) {
+                    std::vector<MemberDev>* out, std::vector<int>* units, long long* n_items,
+                    int* rows) {
   if (!members || n < 1 || n > (1 << 20))
     return fail(PPF_ERR_INVALID, "ensemble needs 1..2^20 members (got %d)", n);
   *rows = tiling && tiling->tile_y ? tiling->tile_y : 2;
@@ -117,6 +135,7 @@ int32_t build_table(const PpfMember* members, int32_t n, const PpfTiling* tiling
     return fail(PPF_ERR_UNSUPPORTED, "ensemble steps advance one step per pass");
   const bool bulk = !(tiling && (tiling->flags & PPF_TILING_FULL_EVAL));
   out->resize(n);
+  units->clear();
   long long items = 0;
   for (int i = 0; i < n; ++i) {
     const PpfMember& s = members[i];
@@ -155,33 +174,95 @@ int32_t build_table(const PpfMember* members, int32_t n, const PpfTiling* tiling
     }
     d.strips = (int)((s.nx + w95::kStrip - 1) / w95::kStrip);
     d.item_begin = items;
-    items += (long long)d.strips * ((s.ny + *rows - 1) / *rows);
+    d.items = (long long)d.strips * ((s.ny + *rows - 1) / *rows);
+    d.unit_begin = (long long)units->size();
+    const long long nu = (d.items + kWarpsPerCta - 1) / kWarpsPerCta;
+    if ((long long)units->size() + nu > (1LL << 31) - 1)
+      return fail(PPF_ERR_INVALID, "ensemble too large");
+    units->insert(units->end(), (size_t)nu, i);
+    items += d.items;
   }
   *n_items = items;
   return PPF_OK;
 }
 
+struct Occupancy {
+  int sms = 0, per_sm = 0;
+};
+
 template <int ROWS>
 cudaError_t launch_ensemble(const PpfEnsemblePlan* p, int parity, uint64_t step,
-                            const uint64_t* step_base, bool pdl, cudaStream_t s) {
+                            const uint64_t* step_base, int nsteps, unsigned* sync, int* status,
+                            bool pdl, cudaStream_t s) {
   auto kern = ensemble_kernel<ROWS>;
-  static int sms = 0, per_sm = 0;
-  if (!sms) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kCtaThreads, 0) !=
-            cudaSuccess || per_sm < 1)
-      per_sm = 1;
+  static Occupancy occ[SymbolCache::kMaxDevices];
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= SymbolCache::kMaxDevices) return cudaErrorInvalidDevice;
+  Occupancy& o = occ[dev];
+  if (!o.sms) {
+    int sms = 0, per_sm = 0;
+    if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess)
+      return e;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kCtaThreads, 0)) !=
+        cudaSuccess)
+      return e;
+    o.per_sm = per_sm < 1 ? 1 : per_sm;
+    o.sms = sms;
   }
-  // fewest warps that still give every warp the same item count (+-1)
-  const long long resident = (long long)sms * per_sm * kWarpsPerCta;
-  const long long rounds = (p->n_items + resident - 1) / resident;
-  const long long warps = (p->n_items + rounds - 1) / rounds;
-  const long long ctas = (warps + kWarpsPerCta - 1) / kWarpsPerCta;
-  return launch(kern, dim3((unsigned)ctas), dim3(32, kWarpsPerCta), 0, s, pdl,
-                (const MemberDev*)p->device_table, p->n_members, (long long)p->n_items, parity,
-                step, step_base);
+  const char* base = reinterpret_cast<const char*>(p->device_table);
+  const MemberDev* members = reinterpret_cast<const MemberDev*>(base);
+  const int* units = reinterpret_cast<const int*>(base + units_offset(p->n_members));
+  // every CTA resident (cooperative), each walking the same number of
+  // units (+-1)
+  const long long resident = (long long)o.sms * o.per_sm;
+  const long long rounds = (p->n_units + resident - 1) / resident;
+  const long long ctas = (p->n_units + rounds - 1) / rounds;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)ctas);
+  cfg.blockDim = dim3(32, kWarpsPerCta);
+  cfg.stream = s;
+  cudaLaunchAttribute attr[2];
+  int na = 0;
+  if (nsteps > 1) {
+    attr[na].id = cudaLaunchAttributeCooperative;
+    attr[na].val.cooperative = 1;
+    ++na;
+  } else if (pdl) {
+    attr[na].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[na].val.programmaticStreamSerializationAllowed = 1;
+    ++na;
+  }
+  cfg.attrs = attr;
+  cfg.numAttrs = na;
+  return cudaLaunchKernelEx(&cfg, kern, members, units, (long long)p->n_units, parity, step,
+                            step_base, nsteps, sync, status);
+}
+
+int32_t run(const PpfEnsemblePlan* plan, int32_t parity, uint64_t step,
+            const uint64_t* step_base, int32_t nsteps, void* sync, const PpfTiling* tiling,
+            void* stream) {
+  if (!plan || !plan->device_table) return fail(PPF_ERR_INVALID, "plan is NULL");
+  if (parity != 0 && parity != 1) return fail(PPF_ERR_INVALID, "parity must be 0 or 1");
+  if (plan->n_items < 1 || plan->n_units < 1) return fail(PPF_ERR_INVALID, "empty plan");
+  if (nsteps < 1) return fail(PPF_ERR_INVALID, "nsteps must be >= 1");
+  if (nsteps > 1 && (!sync || ((uintptr_t)sync) % 8))
+    return fail(PPF_ERR_INVALID, "several steps per launch need an 8-byte aligned sync buffer");
+  int* status = status_ptr();
+  if (!status) return fail(PPF_ERR_CUDA, "status word unavailable");
+  const bool pdl = tiling && tiling->pdl;
+  cudaStream_t s = (cudaStream_t)stream;
+  unsigned* sy = (unsigned*)sync;
+  cudaError_t e;
+  switch (plan->rows) {
+    case 2: e = launch_ensemble<2>(plan, parity, step, step_base, nsteps, sy, status, pdl, s); break;
+    case 4: e = launch_ensemble<4>(plan, parity, step, step_base, nsteps, sy, status, pdl, s); break;
+    case 8: e = launch_ensemble<8>(plan, parity, step, step_base, nsteps, sy, status, pdl, s); break;
+    default: return fail(PPF_ERR_INVALID, "plan rows %d invalid", plan->rows);
+  }
+  if (e != cudaSuccess) return fail(PPF_ERR_CUDA, "ensemble launch: %s", cudaGetErrorString(e));
+  return PPF_OK;
 }
 
 }  // namespace
@@ -196,11 +277,12 @@ int32_t ppf_ensemble_plan_bytes(const PpfMember* members, int32_t n, const PpfTi
   clear_error();
   if (!bytes) return fail(PPF_ERR_INVALID, "bytes is NULL");
   std::vector<MemberDev> t;
+  std::vector<int> units;
   long long items;
   int rows;
-  int32_t rc = build_table(members, n, tiling, &t, &items, &rows);
+  int32_t rc = build_table(members, n, tiling, &t, &units, &items, &rows);
   if (rc) return rc;
-  *bytes = t.size() * sizeof(MemberDev);
+  *bytes = units_offset(n) + units.size() * sizeof(int);
   return PPF_OK;
 }
 
@@ -210,43 +292,40 @@ int32_t ppf_ensemble_build(const PpfMember* members, int32_t n, const PpfTiling*
   clear_error();
   if (!device_table || !plan) return fail(PPF_ERR_INVALID, "NULL table or plan");
   std::vector<MemberDev> t;
+  std::vector<int> units;
   long long items;
   int rows;
-  int32_t rc = build_table(members, n, tiling, &t, &items, &rows);
+  int32_t rc = build_table(members, n, tiling, &t, &units, &items, &rows);
   if (rc) return rc;
-  if (bytes < t.size() * sizeof(MemberDev))
-    return fail(PPF_ERR_INVALID, "table needs %zu bytes, got %zu", t.size() * sizeof(MemberDev),
-                bytes);
+  const size_t need = units_offset(n) + units.size() * sizeof(int);
+  if (bytes < need) return fail(PPF_ERR_INVALID, "table needs %zu bytes, got %zu", need, bytes);
   if (((uintptr_t)device_table) % 16) return fail(PPF_ERR_INVALID, "table not 16-byte aligned");
   if (items > (1LL << 40)) return fail(PPF_ERR_INVALID, "ensemble too large");
+  std::vector<unsigned char> host(need, 0);
+  memcpy(host.data(), t.data(), t.size() * sizeof(MemberDev));
+  memcpy(host.data() + units_offset(n), units.data(), units.size() * sizeof(int));
   cudaStream_t s = (cudaStream_t)stream;
-  PPF_TRY_CUDA(cudaMemcpyAsync(device_table, t.data(), t.size() * sizeof(MemberDev),
-                               cudaMemcpyHostToDevice, s));
+  PPF_TRY_CUDA(cudaMemcpyAsync(device_table, host.data(), need, cudaMemcpyHostToDevice, s));
   PPF_TRY_CUDA(cudaStreamSynchronize(s));  // the host table dies with this call
   plan->device_table = device_table;
   plan->n_items = items;
   plan->n_members = n;
   plan->rows = rows;
+  plan->n_units = (int64_t)units.size();
   return PPF_OK;
 }
 
 int32_t ppf_ensemble_step_f32(const PpfEnsemblePlan* plan, int32_t parity, uint64_t step,
                               const uint64_t* step_base, const PpfTiling* tiling, void* stream) {
   clear_error();
-  if (!plan || !plan->device_table) return fail(PPF_ERR_INVALID, "plan is NULL");
-  if (parity != 0 && parity != 1) return fail(PPF_ERR_INVALID, "parity must be 0 or 1");
-  if (plan->n_items < 1) return fail(PPF_ERR_INVALID, "empty plan");
-  const bool pdl = tiling && tiling->pdl;
-  cudaStream_t s = (cudaStream_t)stream;
-  cudaError_t e;
-  switch (plan->rows) {
-    case 2: e = launch_ensemble<2>(plan, parity, step, step_base, pdl, s); break;
-    case 4: e = launch_ensemble<4>(plan, parity, step, step_base, pdl, s); break;
-    case 8: e = launch_ensemble<8>(plan, parity, step, step_base, pdl, s); break;
-    default: return fail(PPF_ERR_INVALID, "plan rows %d invalid", plan->rows);
-  }
-  if (e != cudaSuccess) return fail(PPF_ERR_CUDA, "ensemble launch: %s", cudaGetErrorString(e));
-  return PPF_OK;
+  return run(plan, parity, step, step_base, 1, nullptr, tiling, stream);
+}
+
+int32_t ppf_ensemble_run_f32(const PpfEnsemblePlan* plan, int32_t parity, uint64_t step,
+                             const uint64_t* step_base, int32_t nsteps, void* sync,
+                             const PpfTiling* tiling, void* stream) {
+  clear_error();
+  return run(plan, parity, step, step_base, nsteps, sync, tiling, stream);
 }
 
 }  // extern "C"

@@ -25,6 +25,7 @@
 #include <math.h>
 
 #include "ppf_common.cuh"
+#include "ppf_grid.cuh"
 
 namespace ppf {
 namespace {
@@ -709,8 +710,257 @@ int32_t jacobi_solve(const Geo& g, double a, double dbase, double dc, double tol
   return PPF_OK;
 }
 
-// ---------------------------------------------------------------- dispatch
+// ---------------------------------------------------------------- MINRES
+// The same full 2-D system where the Chebyshev bound fails (16 W M dt >= 4:
+// the diagonal 1 + 4a + c g(phi) can fall below the off-diagonal sum and
+// the symmetric matrix may be indefinite; the reference's GMRES still
+// returns a step). MINRES (Paige & Saunders 1975, in the Lanczos form of
+// Elman, Silvester & Wathen, Algorithm 2.4) solves symmetric indefinite
+// systems with short recurrences: one matrix-vector product and two inner
+// products per iteration. It runs as ONE persistent cooperative kernel:
+// every CTA resident, the iterations separated by grid barriers (three per
+// iteration: after the product and its inner product, after the Lanczos
+// vector and its norm, after the solution update), the inner products
+// accumulated in double from per-CTA partial sums that every CTA adds up in
+// the same order (so every CTA takes the same scalars and the same stopping
+// decision). The loop ends on the device when the residual norm (|eta|,
+// exact in exact arithmetic) reaches tol ||b|| or after max_iter
+// iterations, which sets PPF_STATUS_NOT_CONVERGED. Initial guess: b (the
+// field before the step).
+constexpr int kMinresThreads = 256;
+constexpr int kMinresMaxCtas = 2048;
+constexpr int kMinresMaxIter = 20000;
+
+struct MinresBufs {
+  void* v0;  // Lanczos vector v_{j-1}
+  void* v1;  // v_j
+  void* t;   // A v_j, then the next Lanczos vector before its scaling
+  void* w0;  // w_{j-2}
+  void* w1;  // w_{j-1}
+  double* part_a;  // per-CTA partial sums (two arrays: consecutive reductions)
+  double* part_b;
+  unsigned* sync;  // grid barrier words
+  int* info;       // [0] iterations run, [1] converged
+};
+
+__device__ __forceinline__ double block_sum_d(double v, double* red) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  __syncthreads();
+  if (lane == 0) red[warp] = v;
+  __syncthreads();
+  double r = 0.0;
+  if (threadIdx.x < 32) {
+    r = threadIdx.x < kMinresThreads / 32 ? red[threadIdx.x] : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) r += __shfl_down_sync(0xffffffffu, r, o);
+    if (threadIdx.x == 0) red[0] = r;
+  }
+  __syncthreads();
+  r = red[0];
+  __syncthreads();
+  return r;
+}
+
+// Sum of the n partials, in the same order in every CTA.
+__device__ __forceinline__ double total(const double* part, int n, double* red) {
+  double v = 0.0;
+  for (int i = threadIdx.x; i < n; i += kMinresThreads) v += part[i];
+  return block_sum_d(v, red);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kMinresThreads)
+    minres_kernel(Geo g, T dbase, T dc, T a, double tol, int max_iter, const T* __restrict__ b,
+                  T* __restrict__ x, MinresBufs bufs, int* status) {
+  __shared__ double red[kMinresThreads / 32];
+  __shared__ int flag;
+  if (threadIdx.x == 0) flag = 0;
+  const int nx = g.n[1], ny = g.n[0];
+  const int nb = gridDim.x;
+  T* V0 = (T*)bufs.v0;
+  T* V1 = (T*)bufs.v1;
+  T* Tv = (T*)bufs.t;
+  T* W0 = (T*)bufs.w0;
+  T* W1 = (T*)bufs.w1;
+  // (A y)_i = d_i y_i - a (sum of the four periodic neighbours),
+  // d_i = dbase + dc g(b_i): the reference's matrix (CahnAllen.py:170-176)
+  auto apply = [&](const T* y, int row, int col) -> T {
+    const int64_t yb = (int64_t)row * g.pitch;
+    const int64_t ym = (int64_t)(row == 0 ? ny - 1 : row - 1) * g.pitch;
+    const int64_t yp = (int64_t)(row == ny - 1 ? 0 : row + 1) * g.pitch;
+    const int xm = col == 0 ? nx - 1 : col - 1, xp = col == nx - 1 ? 0 : col + 1;
+    const T bv = b[yb + col];
+    const T d = dbase + dc * ((T(4) * bv - T(6)) * bv + T(2));
+    const T sy = (y[yb + xm] + y[yb + xp]) + (y[ym + col] + y[yp + col]);
+    return d * y[yb + col] - a * sy;
+  };
+#define PPF_CELLS                                                   \
+  for (int row = blockIdx.x; row < ny; row += nb)                   \
+    for (int col = threadIdx.x; col < nx; col += kMinresThreads)
+#define PPF_SYNC \
+  if (!grid_barrier(bufs.sync, nb, status, &flag)) return
+
+  // r0 = b - A b into V1, x = b, w = 0; ||r0||^2 and ||b||^2
+  double pr = 0.0, pb = 0.0;
+  PPF_CELLS {
+    const int64_t i = (int64_t)row * g.pitch + col;
+    const T bv = b[i];
+    const T r = bv - apply(b, row, col);
+    V1[i] = r;
+    x[i] = bv;
+    V0[i] = T(0);
+    W0[i] = T(0);
+    W1[i] = T(0);
+    pr += (double)r * (double)r;
+    pb += (double)bv * (double)bv;
+  }
+  pr = block_sum_d(pr, red);
+  pb = block_sum_d(pb, red);
+  if (threadIdx.x == 0) {
+    bufs.part_a[blockIdx.x] = pr;
+    bufs.part_b[blockIdx.x] = pb;
+  }
+  PPF_SYNC;
+  const double beta1 = sqrt(total(bufs.part_a, nb, red));
+  const double bnorm = sqrt(total(bufs.part_b, nb, red));
+  const double goal = tol * bnorm;
+  int it = 0;
+  bool converged = beta1 <= goal;
+  if (!converged) {
+    const T inv = (T)(1.0 / beta1);
+    PPF_CELLS {
+      const int64_t i = (int64_t)row * g.pitch + col;
+      V1[i] *= inv;
+    }
+    PPF_SYNC;
+    double beta = beta1, eta = beta1;
+    double c_prev = 1.0, c = 1.0, s_prev = 0.0, sg = 0.0;
+    for (it = 1; it <= max_iter; ++it) {
+      // t = A v_j; alpha = v_j . A v_j
+      double pa = 0.0;
+      PPF_CELLS {
+        const int64_t i = (int64_t)row * g.pitch + col;
+        const T av = apply(V1, row, col);
+        Tv[i] = av;
+        pa += (double)V1[i] * (double)av;
+      }
+      pa = block_sum_d(pa, red);
+      if (threadIdx.x == 0) bufs.part_a[blockIdx.x] = pa;
+      PPF_SYNC;
+      const double alpha = total(bufs.part_a, nb, red);
+      // t = A v_j - alpha v_j - beta v_{j-1}; its norm
+      double pn = 0.0;
+      PPF_CELLS {
+        const int64_t i = (int64_t)row * g.pitch + col;
+        const T tv = Tv[i] - (T)alpha * V1[i] - (T)beta * V0[i];
+        Tv[i] = tv;
+        pn += (double)tv * (double)tv;
+      }
+      pn = block_sum_d(pn, red);
+      if (threadIdx.x == 0) bufs.part_b[blockIdx.x] = pn;
+      PPF_SYNC;
+      const double beta_n = sqrt(total(bufs.part_b, nb, red));
+      // Givens rotations of the tridiagonal's QR factorisation
+      const double a0 = c * alpha - c_prev * sg * beta;
+      const double a1 = sqrt(a0 * a0 + beta_n * beta_n);
+      const double a2 = sg * alpha + c_prev * c * beta;
+      const double a3 = s_prev * beta;
+      const double c_n = a0 / a1, s_n = beta_n / a1;
+      const double step = c_n * eta;
+      const T inv_b = beta_n > 0 ? (T)(1.0 / beta_n) : T(0);
+      // v_{j+1} = t / beta_n into V0; w_j = (v_j - a3 w_{j-2} - a2 w_{j-1}) / a1
+      // into W0; x += c_n eta w_j
+      PPF_CELLS {
+        const int64_t i = (int64_t)row * g.pitch + col;
+        const T w = (V1[i] - (T)a3 * W0[i] - (T)a2 * W1[i]) / (T)a1;
+        W0[i] = w;
+        x[i] += (T)step * w;
+        V0[i] = Tv[i] * inv_b;
+      }
+      eta = -s_n * eta;
+      c_prev = c;
+      c = c_n;
+      s_prev = sg;
+      sg = s_n;
+      beta = beta_n;
+      T* tmp = V0;
+      V0 = V1;
+      V1 = tmp;  // v_j becomes v_{j-1}, v_{j+1} becomes v_j
+      tmp = W0;
+      W0 = W1;
+      W1 = tmp;  // w_j is now the newest
+      if (fabs(eta) <= goal || beta_n == 0.0) {
+        converged = true;
+        break;
+      }
+      PPF_SYNC;
+    }
+  }
+#undef PPF_CELLS
+#undef PPF_SYNC
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    bufs.info[0] = it;
+    bufs.info[1] = converged ? 1 : 0;
+    if (!converged) atomicOr(status, PPF_STATUS_NOT_CONVERGED);
+  }
+}
+
 size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+size_t minres_scratch_bytes(const Geo& g, int eb) {
+  const size_t vec = align256((size_t)g.n[0] * g.pitch * eb);
+  return 5 * vec + 2 * align256(kMinresMaxCtas * sizeof(double)) + 256;
+}
+
+template <typename T>
+int32_t minres_solve(const Geo& g, double a, double dbase, double dc, double tol, int max_iter,
+                     const T* in, T* out, void* scratch, size_t bytes, int32_t* iterations,
+                     cudaStream_t st) {
+  if (bytes < minres_scratch_bytes(g, sizeof(T)))
+    return fail(PPF_ERR_INVALID, "the MINRES solve needs %zu bytes of scratch",
+                minres_scratch_bytes(g, sizeof(T)));
+  int* status = status_ptr();
+  if (!status) return fail(PPF_ERR_CUDA, "status word unavailable");
+  char* p = static_cast<char*>(scratch);
+  const size_t vec = align256((size_t)g.n[0] * g.pitch * sizeof(T));
+  MinresBufs bb;
+  bb.v0 = p;
+  bb.v1 = p + vec;
+  bb.t = p + 2 * vec;
+  bb.w0 = p + 3 * vec;
+  bb.w1 = p + 4 * vec;
+  bb.part_a = reinterpret_cast<double*>(p + 5 * vec);
+  bb.part_b = reinterpret_cast<double*>(p + 5 * vec + align256(kMinresMaxCtas * sizeof(double)));
+  char* tail = p + 5 * vec + 2 * align256(kMinresMaxCtas * sizeof(double));
+  bb.sync = reinterpret_cast<unsigned*>(tail);
+  bb.info = reinterpret_cast<int*>(tail + 16);
+  PPF_TRY_CUDA(cudaMemsetAsync(tail, 0, 256, st));
+  auto kern = minres_kernel<T>;
+  int dev = 0, sms = 0, per_sm = 0;
+  PPF_TRY_CUDA(cudaGetDevice(&dev));
+  PPF_TRY_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  PPF_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kMinresThreads, 0));
+  long long ctas = (long long)sms * (per_sm < 1 ? 1 : per_sm);
+  if (ctas > kMinresMaxCtas) ctas = kMinresMaxCtas;
+  if (ctas > g.n[0]) ctas = g.n[0];
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)ctas);
+  cfg.blockDim = dim3(kMinresThreads);
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  PPF_TRY_CUDA(cudaLaunchKernelEx(&cfg, kern, g, (T)dbase, (T)dc, (T)a, tol, max_iter, in, out,
+                                  bb, status));
+  if (iterations) *iterations = -max_iter;  // run on the device: at most max_iter
+  return PPF_OK;
+}
+
+// ---------------------------------------------------------------- dispatch
 
 size_t phase_scratch_bytes(const Geo& g, int eb) {
   size_t m = 0;
@@ -721,7 +971,11 @@ size_t phase_scratch_bytes(const Geo& g, int eb) {
   const bool oned = g.ndim == 2 && g.n[0] == 1;
   const size_t dv = (size_t)(g.n[0] + g.n[1] + g.n[2]) * eb;
   const size_t penta = oned ? (size_t)10 * g.n[1] * eb : 0;
-  return align256(m) + align256(dv) + align256(penta);
+  const size_t base = align256(m) + align256(dv) + align256(penta);
+  // the full 2-D solve beyond the Chebyshev bound (MINRES) reuses the same
+  // scratch from its start
+  const size_t mr = (g.ndim == 2 && !oned) ? minres_scratch_bytes(g, eb) : 0;
+  return base > mr ? base : mr;
 }
 
 template <typename T>
@@ -819,8 +1073,15 @@ int32_t phase_step(const PpfImplicitPhaseParams* p, const PpfGrid* grid, const T
                                      scratch, bytes, st);
   if (dims == 2) {
     if (p->gmres && !p->adi) {
+      const double dbase = 1 + 4 * a, dc = 16 * wm;
+      const double dmin = dbase - 0.25 * dc;
+      if (dc >= 0 && dmin > 0 && 4.0 * a / dmin < 1) {
+        const double tol = p->tol > 0 ? p->tol : (sizeof(T) == 4 ? 1e-7 : 1e-14);
+        return jacobi_solve<T>(g, a, dbase, dc, tol, in, out, tmp, iterations, st);
+      }
       const double tol = p->tol > 0 ? p->tol : (sizeof(T) == 4 ? 1e-7 : 1e-14);
-      return jacobi_solve<T>(g, a, 1 + 4 * a, 16 * wm, tol, in, out, tmp, iterations, st);
+      return minres_solve<T>(g, a, dbase, dc, tol, kMinresMaxIter, in, out, scratch, bytes,
+                             iterations, st);
     }
     rc = var_sweep<T>(g, 1, a, 1 + 2 * a, 8 * wm, nullptr, 0, 0.0, in, out, scratch, bytes, st);
     if (rc) return rc;

@@ -119,7 +119,19 @@ __host__ __device__ __forceinline__ int mirror_index(int i, int n) {
 //   PERIODIC  ghost = cell wrapped to the other side
 //   NEUMANN   ghost = mirrored edge cell -/+ dx*b
 //   DIRCHLET  ghost = value
-template <typename T, int ND>
+// Field load: through the read-only (non-coherent) path by default, which
+// is valid when the field was written by an earlier kernel; COHERENT = true
+// for kernels that read what other CTAs of the same launch wrote before a
+// grid barrier (plain ld.global, ordered by the barrier's acquire).
+template <bool COHERENT, typename T>
+__device__ __forceinline__ T ldf(const T* p) {
+  if constexpr (COHERENT)
+    return *p;
+  else
+    return __ldg(p);
+}
+
+template <typename T, int ND, bool COHERENT = false>
 __device__ __forceinline__ T fetch(const T* __restrict__ f, const Geo& g,
                                    const Bc<T>& bc, int fld, int i0, int i1,
                                    int i2 = 0) {
@@ -150,7 +162,7 @@ __device__ __forceinline__ T fetch(const T* __restrict__ f, const Geo& g,
     off = (int64_t)idx[0] * g.pitch + idx[1];
   else
     off = (int64_t)idx[0] * g.plane + (int64_t)idx[1] * g.pitch + idx[2];
-  return __ldg(f + off) + extra;
+  return ldf<COHERENT>(f + off) + extra;
 }
 
 // True when the cell lies outside the grid along a DIRCHLET axis: such a

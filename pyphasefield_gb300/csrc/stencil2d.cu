@@ -1,15 +1,18 @@
-// 2-D Diffusion and Allen-Cahn explicit steps with temporal blocking.
+// 2-D Diffusion and Allen-Cahn explicit steps, one or several per pass.
 //
-// One CTA owns a TY x TX output tile. It stages the tile plus a halo of
-// `depth` cells (ghost rule applied at load time) in shared memory with
-// 16-byte vector loads, advances `depth` time steps in shared memory (the
-// valid region shrinks by one cell per step) and writes only the centre back:
-// HBM sees one read and one write per cell per `depth` steps.
+// Kernels: stencil2d_lean_kernel (one step, warp strips of 16-byte
+// vectors, the default), stencil2d_march_kernel (depth 2..8 steps per HBM
+// pass: warps march down column windows fed by TMA, a pipeline of one
+// register stage per step) and stencil2d_tb_kernel (depth steps on a
+// TY x TX shared-memory tile with a halo of `depth` cells, used when a tile
+// shape is asked for). Every kernel reads each cell once and writes it once
+// per pass, applying the ghost rule at load time.
 //
 // Reference: engine_ExplicitDiffusion (Engines/Diffusion.py:198-208) and
 // engine_CahnAllenExplicit (Engines/CahnAllen.py:128-135), with Field.laplacian
 // (field.py:60-67) as the 5-point stencil.
 #include "ppf_common.cuh"
+#include "ppf_tma.cuh"
 
 namespace ppf {
 namespace {
@@ -231,6 +234,206 @@ __global__ void __launch_bounds__(kThreads)
   }
 }
 
+// ------------------------------------------------------------ marching
+// Temporal blocking by marching (depth K = 2..8 steps per HBM pass). A warp
+// owns a window of 32 V columns (V cells of one 16-byte vector per lane) and
+// a segment of `seg` output rows. It reads the segment's rows plus K halo
+// rows above and below once, top to bottom, and pushes each row through a
+// pipeline of K stages held in registers: stage k keeps two rows of step
+// k-1 and, when the next row of step k-1 arrives, emits one row of step k
+// (west / east neighbours by shuffles). Only stage K's rows go back to
+// memory, so HBM sees one read and one write per cell per K steps, plus the
+// 2K halo rows per segment. The window's outer KA = K rounded up to V
+// columns per side are halo (lost one column per step); lanes KA/V ..
+// 31 - KA/V own the output columns, so neighbouring windows overlap by 2 KA.
+//
+// Rows arrive through a per-warp ring of kMSlots shared-memory slots of
+// kMRows rows each, filled by TMA tensor loads (cp.async.bulk.tensor.2d,
+// one lane, completion on the slot's mbarrier; every wait bounded) while
+// earlier slots are consumed. Blocks of rows that reach outside the grid
+// (the grid's first and last rows, windows over the left or right edge) are
+// filled by the warp itself with the boundary rule instead; the ghost cells
+// they hold then evolve with the stencil like the cells they copy (periodic
+// wrap, no-flux mirror: the neighbour sum ((w + e) + (n + s)) is symmetric,
+// so a mirrored cell stays bit-identical to its image), and Dirichlet
+// ghosts keep their value at every step.
+constexpr int kMWarps = 4;
+constexpr int kMRows = 4;
+constexpr int kMSlots = 4;
+
+// A block of kMRows rows of a window filled by the warp itself with the
+// boundary rule (edges of the grid); kept out of line, off the hot path.
+template <typename T, int V>
+__device__ __noinline__ void march_fill(T* dst, const T* __restrict__ in, const Geo* g,
+                                        const Bc<T>* bc, int r0, int xl, int lane) {
+  for (int r = 0; r < kMRows; ++r)
+    for (int e = 0; e < V; ++e)
+      dst[r * 32 * V + lane * V + e] = fetch<T, 2>(in, *g, *bc, 0, r0 + r, xl + e);
+  __syncwarp();
+}
+
+// Resident CTAs per SM asked of the register allocator: the pipeline holds
+// 2 K V values per lane, so deeper pipelines get fewer CTAs (shared memory
+// allows seven).
+template <typename T, int K>
+struct MarchMinBlocks {
+  static constexpr int regs = 8 * K + 64;  // pipeline (2 K vectors of 16 bytes) + the rest
+  static constexpr int fit = 65536 / (32 * kMWarps * regs);
+  static constexpr int value = fit > 7 ? 7 : fit;
+};
+
+template <typename T, typename Op, int K>
+__global__ void __launch_bounds__(32 * kMWarps, (MarchMinBlocks<T, K>::value))
+    stencil2d_march_kernel(const __grid_constant__ CUtensorMap map, Op op,
+                           const __grid_constant__ Geo g, const __grid_constant__ Bc<T> bc,
+                           const T* __restrict__ in, T* __restrict__ out, int ow, int seg,
+                           int nstrips, int* __restrict__ status) {
+  constexpr int V = Vec16<T>::n;
+  using VT = typename Vec16<T>::type;
+  constexpr int WW = 32 * V;                    // window columns
+  constexpr int KA = (K + V - 1) / V * V;       // halo columns per side
+  constexpr int SLOT = kMRows * WW;             // elements per slot
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  __shared__ __align__(8) uint64_t bars[kMWarps][kMSlots];
+  const int lane = threadIdx.x, wid = threadIdx.y;
+  T* ring = reinterpret_cast<T*>(smem_raw) + (size_t)wid * kMSlots * SLOT;
+  uint64_t* bar = bars[wid];
+  if (lane == 0) {
+    for (int i = 0; i < kMSlots; ++i) mbar_init(&bar[i], 1);
+    mbar_init_fence();
+  }
+  __syncwarp();
+  pdl_wait();
+  pdl_launch_next();
+  const int strip = blockIdx.x * kMWarps + wid;
+  if (strip >= nstrips) return;  // whole warp; no block-wide barrier follows
+  const int ny = g.n[0], nx = g.n[1];
+  const int xs = strip * ow - KA;
+  const int y0 = blockIdx.y * seg;
+  const int y1 = min(y0 + seg, ny);
+  const int ylo = y0 - K, yhi = y1 - 1 + K;  // rows read
+  const int nb = (yhi - ylo + kMRows) / kMRows;
+  const bool xin = xs >= 0 && xs + WW <= nx;
+  const int xl = xs + lane * V;  // this lane's first column
+
+  // Dirichlet ghosts along x (edge windows only): those columns never change
+  uint32_t fix_x = 0;
+#pragma unroll
+  for (int e = 0; e < V; ++e)
+    if (bc.type[1] == PPF_BC_DIRCHLET && (unsigned)(xl + e) >= (unsigned)nx) fix_x |= 1u << e;
+  const bool fix_y = bc.type[0] == PPF_BC_DIRCHLET;
+
+  auto tma_block = [&](int b) {
+    const int r0 = ylo + b * kMRows;
+    return xin && r0 >= 0 && r0 + kMRows <= ny;
+  };
+  auto issue = [&](int b) {
+    const int slot = b % kMSlots;
+    T* dst = ring + slot * SLOT;
+    const int r0 = ylo + b * kMRows;
+    if (tma_block(b)) {
+      if (lane == 0) {
+        fence_proxy_async();
+        mbar_expect_tx(&bar[slot], SLOT * (uint32_t)sizeof(T));
+        tma_load_2d(dst, &map, xs, r0, &bar[slot]);
+      }
+    } else {
+      march_fill<T, V>(dst, in, &g, &bc, r0, xl, lane);
+    }
+  };
+
+  // pipeline state: stage k keeps rows (r - 1, r) of step k - 1
+  T wa[K][V], wb[K][V];
+#pragma unroll
+  for (int k = 0; k < K; ++k)
+#pragma unroll
+    for (int e = 0; e < V; ++e) wa[k][e] = wb[k][e] = T(0);
+  const bool owner = lane >= KA / V && lane <= 31 - KA / V;
+
+  for (int b = 0; b < min(kMSlots, nb); ++b) issue(b);
+  uint32_t phase = 0;
+  for (int b = 0; b < nb; ++b) {
+    const int slot = b % kMSlots;
+    if (tma_block(b)) {
+      if (!mbar_wait(&bar[slot], (phase >> slot) & 1u)) {
+        if (lane == 0) {
+          atomicOr(status, PPF_STATUS_TIMEOUT);
+          // let every load still in flight land before the warp leaves
+          // (blocks b .. b + kMSlots - 1 occupy distinct slots, none consumed)
+          for (int q = b; q < min(b + kMSlots, nb); ++q)
+            if (tma_block(q)) mbar_wait(&bar[q % kMSlots], (phase >> (q % kMSlots)) & 1u);
+        }
+        __syncwarp();
+        return;
+      }
+      phase ^= 1u << slot;
+    }
+    const T* src = ring + slot * SLOT;
+#pragma unroll 1
+    for (int r = 0; r < kMRows; ++r) {
+      const int y = ylo + b * kMRows + r;  // row of step 0 entering the pipeline
+      // (rows past yhi only feed outputs below the segment, never stored)
+      T cur[V];
+      {
+        const VT v = *reinterpret_cast<const VT*>(src + r * WW + lane * V);
+        const T* pv = reinterpret_cast<const T*>(&v);
+#pragma unroll
+        for (int e = 0; e < V; ++e) cur[e] = pv[e];
+      }
+#pragma unroll
+      for (int k = 0; k < K; ++k) {
+        // stage k + 1: rows y - k - 2 (wa), y - k - 1 (wb), y - k (cur) of
+        // step k give row y - k - 1 of step k + 1
+        const int row = y - k - 1;
+        T nxt[V];
+        const T wl = __shfl_up_sync(0xffffffffu, wb[k][V - 1], 1);
+        const T er = __shfl_down_sync(0xffffffffu, wb[k][0], 1);
+#pragma unroll
+        for (int e = 0; e < V; ++e) {
+          const T w = e == 0 ? wl : wb[k][e - 1];
+          const T ea = e == V - 1 ? er : wb[k][e + 1];
+          nxt[e] = op(wb[k][e], w, ea, wa[k][e], cur[e]);
+        }
+        if (fix_x) {
+#pragma unroll
+          for (int e = 0; e < V; ++e)
+            if (fix_x & (1u << e)) nxt[e] = wb[k][e];
+        }
+        if (fix_y && (unsigned)row >= (unsigned)ny) {
+#pragma unroll
+          for (int e = 0; e < V; ++e) nxt[e] = wb[k][e];
+        }
+#pragma unroll
+        for (int e = 0; e < V; ++e) {
+          wa[k][e] = wb[k][e];
+          wb[k][e] = cur[e];
+          cur[e] = nxt[e];
+        }
+      }
+      // cur: row y - K of step K
+      const int row = y - K;
+      if (owner && row >= y0 && row < y1) {
+        T* o = out + (int64_t)row * g.pitch + xl;
+        if (xl + V <= nx) {
+          VT v;
+          T* pv = reinterpret_cast<T*>(&v);
+#pragma unroll
+          for (int e = 0; e < V; ++e) pv[e] = cur[e];
+          *reinterpret_cast<VT*>(o) = v;
+        } else {
+#pragma unroll
+          for (int e = 0; e < V; ++e)
+            if (xl + e < nx) o[e] = cur[e];
+        }
+      }
+    }
+    // every lane's reads of the slot are ordered before the TMA that refills it
+    fence_proxy_async();
+    __syncwarp();
+    if (b + kMSlots < nb) issue(b + kMSlots);
+  }
+}
+
 struct Tile2d {
   int tx, ty, k, ka;
   size_t smem;
@@ -258,6 +461,63 @@ int32_t plan_tile2d(const PpfTiling* t, Tile2d* out) {
   return PPF_OK;
 }
 
+// Segment rows per warp: enough warps to fill the GPU (about 28 resident
+// per SM) while the 2K halo rows re-read per segment stay a small share.
+inline int march_segment(int ny, int nstrips, int K) {
+  long want = ((long)ny * nstrips + 4095) / 4096;
+  long seg = want < 8L * K ? 8L * K : (want > 512 ? 512 : want);
+  seg = (seg + kMRows - 1) / kMRows * kMRows;
+  return (int)(seg < ny ? seg : (ny + kMRows - 1) / kMRows * kMRows);
+}
+
+template <typename T, typename Op, int K>
+int32_t launch_march(const CUtensorMap& map, Op op, const Geo& g, const Bc<T>& bc, const T* in,
+                     T* out, int ow, int seg, int nstrips, int* st, bool pdl, cudaStream_t s) {
+  constexpr int WW = 32 * Vec16<T>::n;
+  const size_t smem = (size_t)kMWarps * kMSlots * kMRows * WW * sizeof(T);
+  auto kern = stencil2d_march_kernel<T, Op, K>;
+  PPF_TRY_CUDA(allow_smem(kern, smem));
+  const long gy = (g.n[0] + seg - 1) / seg;
+  if (gy > 65535) return fail(PPF_ERR_INVALID, "too many row segments");
+  dim3 grid_dim((nstrips + kMWarps - 1) / kMWarps, (unsigned)gy);
+  PPF_TRY_CUDA(launch(kern, grid_dim, dim3(32, kMWarps), smem, s, pdl, map, op, g, bc, in, out,
+                      ow, seg, nstrips, st));
+  return PPF_OK;
+}
+
+template <typename T, typename Op>
+int32_t run_march(Op op, const Geo& g, const Bc<T>& bc, const T* in, T* out, int K, int seg_req,
+                  bool pdl, cudaStream_t s) {
+  constexpr int V = Vec16<T>::n;
+  constexpr int WW = 32 * V;
+  if (((uintptr_t)in) % 16 || ((uintptr_t)out) % 16 || (g.pitch * sizeof(T)) % 16)
+    return fail(PPF_ERR_INVALID, "temporal blocking needs 16-byte aligned rows");
+  const int KA = (K + V - 1) / V * V;
+  const int ow = WW - 2 * KA;
+  const int nstrips = (g.n[1] + ow - 1) / ow;
+  int seg = seg_req > 0 ? (seg_req + kMRows - 1) / kMRows * kMRows
+                        : march_segment(g.n[0], nstrips, K);
+  if (seg < kMRows) seg = kMRows;
+  CUtensorMap map;
+  const uint64_t dims[2] = {(uint64_t)g.n[1], (uint64_t)g.n[0]};
+  const uint64_t strides[1] = {(uint64_t)g.pitch * sizeof(T)};
+  const uint32_t box[2] = {(uint32_t)WW, (uint32_t)kMRows};
+  int32_t rc = tensor_map(&map, in, (int)sizeof(T), 2, dims, strides, box);
+  if (rc) return rc;
+  int* st = status_ptr();
+  if (!st) return fail(PPF_ERR_CUDA, "status word unavailable");
+  switch (K) {
+    case 2: return launch_march<T, Op, 2>(map, op, g, bc, in, out, ow, seg, nstrips, st, pdl, s);
+    case 3: return launch_march<T, Op, 3>(map, op, g, bc, in, out, ow, seg, nstrips, st, pdl, s);
+    case 4: return launch_march<T, Op, 4>(map, op, g, bc, in, out, ow, seg, nstrips, st, pdl, s);
+    case 5: return launch_march<T, Op, 5>(map, op, g, bc, in, out, ow, seg, nstrips, st, pdl, s);
+    case 6: return launch_march<T, Op, 6>(map, op, g, bc, in, out, ow, seg, nstrips, st, pdl, s);
+    case 7: return launch_march<T, Op, 7>(map, op, g, bc, in, out, ow, seg, nstrips, st, pdl, s);
+    case 8: return launch_march<T, Op, 8>(map, op, g, bc, in, out, ow, seg, nstrips, st, pdl, s);
+    default: return fail(PPF_ERR_INVALID, "depth=%d not in [2, 8]", K);
+  }
+}
+
 template <typename T, typename Op>
 int32_t run2d(Op op, double dx, const PpfGrid* grid, const PpfBoundary* b,
               const T* in, T* out, const PpfTiling* tiling, void* stream) {
@@ -273,7 +533,7 @@ int32_t run2d(Op op, double dx, const PpfGrid* grid, const PpfBoundary* b,
   const int vec_ok = (((uintptr_t)in) % 16 == 0) && (((uintptr_t)out) % 16 == 0) &&
                      ((g.pitch * sizeof(T)) % 16 == 0);
   const bool pdl = tiling && tiling->pdl;
-  if (t.k == 1 && !(tiling && (tiling->tile_x || tiling->tile_y))) {
+  if (t.k == 1 && !(tiling && tiling->tile_x)) {
     constexpr int WW = 32 * Vec16<T>::n;
     dim3 grid_dim((g.n[1] + WW - 1) / WW,
                   (g.n[0] + kRB * (kThreads / 32) - 1) / (kRB * (kThreads / 32)));
@@ -282,6 +542,9 @@ int32_t run2d(Op op, double dx, const PpfGrid* grid, const PpfBoundary* b,
                         (cudaStream_t)stream, pdl, op, g, bc, in, out, vec_ok));
     return PPF_OK;
   }
+  if (!(tiling && tiling->tile_x)) return run_march<T, Op>(op, g, bc, in, out, t.k,
+                                                          tiling ? tiling->tile_y : 0, pdl,
+                                                          (cudaStream_t)stream);
   auto kern = stencil2d_tb_kernel<T, Op>;
   PPF_TRY_CUDA(allow_smem(kern, t.smem));
   dim3 grid_dim((g.n[1] + t.tx - 1) / t.tx, (g.n[0] + t.ty - 1) / t.ty);

@@ -85,17 +85,19 @@ __device__ __forceinline__ float tiny_r2<float>() { return 1e-30f; }
 template <>
 __device__ __forceinline__ double tiny_r2<double>() { return 0.0; }
 
-template <typename T>
+// One cell of phi and c; cells outside the grid through the boundary rule.
+// COHERENT: see ldf (ppf_common.cuh).
+template <typename T, bool COHERENT = false>
 __device__ __forceinline__ void load_cell(const T* __restrict__ phi, const T* __restrict__ c,
                                           const Geo& g, const Bc<T>& bc, int row, int x,
                                           bool x_in, T& p, T& cc) {
   if (x_in && (unsigned)row < (unsigned)g.n[0]) {
     const int64_t o = (int64_t)row * g.pitch + x;
-    p = __ldg(phi + o);
-    cc = __ldg(c + o);
+    p = ldf<COHERENT>(phi + o);
+    cc = ldf<COHERENT>(c + o);
   } else {
-    p = fetch<T, 2>(phi, g, bc, 0, row, x);
-    cc = fetch<T, 2>(c, g, bc, 1, row, x);
+    p = fetch<T, 2, COHERENT>(phi, g, bc, 0, row, x);
+    cc = fetch<T, 2, COHERENT>(c, g, bc, 1, row, x);
   }
 }
 
@@ -160,17 +162,19 @@ __device__ __forceinline__ T shfl_e(T v) { return __shfl_down_sync(0xffffffffu, 
 namespace ppf {
 namespace w95 {
 
-// Loads of one band (rows y0 - 1 .. y0 + ROWS, this lane's column).
-template <typename T, int ROWS>
+// Loads of one band (rows y0 - 1 .. y0 + ROWS, this lane's column). Only
+// the lanes whose column lies outside the grid (the edge strips' halo
+// lanes) take the boundary rule.
+template <typename T, int ROWS, bool COHERENT = false>
 __device__ __forceinline__ void band_load(const Geo& g, const Bc<T>& bc,
                                           const T* __restrict__ phi_in,
                                           const T* __restrict__ c_in, int xs, int y0,
                                           T (&bp)[ROWS + 2], T (&bcv)[ROWS + 2]) {
   const int x = xs + (int)threadIdx.x;
-  const bool x_in = xs >= 0 && xs + 31 < g.n[1];
+  const bool x_in = (unsigned)x < (unsigned)g.n[1];
 #pragma unroll
   for (int j = 0; j < ROWS + 2; ++j)
-    load_cell(phi_in, c_in, g, bc, y0 - 1 + j, x, x_in, bp[j], bcv[j]);
+    load_cell<T, COHERENT>(phi_in, c_in, g, bc, y0 - 1 + j, x, x_in, bp[j], bcv[j]);
 }
 
 template <typename T, int ROWS>
@@ -180,13 +184,13 @@ __device__ __forceinline__ void band_compute(const Coef<T>& k, const Geo& g,
                                              const T (&bp)[ROWS + 2], const T (&bcv)[ROWS + 2]);
 
 // One band: strip whose lane 0 sits at column xs, rows y0 .. y0+ROWS-1.
-template <typename T, int ROWS>
+template <typename T, int ROWS, bool COHERENT = false>
 __device__ __forceinline__ void band(const Coef<T>& k, const Geo& g, const Bc<T>& bc,
                                      const T* __restrict__ phi_in, const T* __restrict__ c_in,
                                      T* __restrict__ phi_out, T* __restrict__ c_out,
                                      uint64_t seed, uint64_t step, int xs, int y0) {
   T bp[ROWS + 2], bcv[ROWS + 2];
-  band_load<T, ROWS>(g, bc, phi_in, c_in, xs, y0, bp, bcv);
+  band_load<T, ROWS, COHERENT>(g, bc, phi_in, c_in, xs, y0, bp, bcv);
   band_compute<T, ROWS>(k, g, phi_out, c_out, seed, step, xs, y0, bp, bcv);
 }
 

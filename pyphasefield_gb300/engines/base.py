@@ -59,7 +59,8 @@ MAX_GRAPHS = 8
 
 _STATUS_NAMES = ((L.PPF_STATUS_TIMEOUT, "a bounded barrier wait timed out (tile not written)"),
                  (L.PPF_STATUS_NONFINITE, "a field holds NaN or Inf"),
-                 (L.PPF_STATUS_RANGE, "a value left the kernel's representable range"))
+                 (L.PPF_STATUS_RANGE, "a value left the kernel's representable range"),
+                 (L.PPF_STATUS_NOT_CONVERGED, "an iterative solve did not converge"))
 
 
 try:

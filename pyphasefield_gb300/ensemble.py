@@ -2,10 +2,12 @@
 
 The reference runs one Simulation at a time; an ensemble here is a list of
 ordinary engine instances (each with its own fields, parameters and grid
-size) whose device buffers are stepped by ONE persistent launch per time step
-(`ppf_ensemble_step_f32`), captured `graph_chunk` steps per CUDA graph.
-Afterwards each member is an ordinary engine again: retrieve_fields_from_GPU,
-save_simulation etc. work on it.
+size) whose device buffers are stepped by ONE persistent cooperative launch
+per chunk of `graph_chunk` steps (`ppf_ensemble_run_f32`: the CTAs meet at a
+bounded grid barrier between steps), captured in a CUDA graph. The rows per
+warp band are picked by the autotuner for the ensemble's mix of member
+sizes (cached per mix and device). Afterwards each member is an ordinary
+engine again: retrieve_fields_from_GPU, save_simulation etc. work on it.
 
 `make_config_ensemble` builds the benchmark ensemble: n members whose square
 sides are drawn log-uniform in [128, 1024]; even members are Warren1995 at
@@ -97,10 +99,11 @@ def partition_members(cells, world: int) -> list:
 
 class Ensemble:
     """Steps a list of 2-D float32 Warren1995GB300 / CahnAllenGB300 engines
-    together. All members must be at the same time step."""
+    together. All members must be at the same time step. rows=None picks the
+    rows per warp band with the autotuner."""
 
-    def __init__(self, sims, rows: int = 2, graph_chunk: int = 64, pdl: bool = True,
-                 bulk_shortcut: bool = True):
+    def __init__(self, sims, rows: int | None = None, graph_chunk: int = 64, pdl: bool = True,
+                 bulk_shortcut: bool = True, use_graph: bool = True):
         if not sims:
             raise ValueError("empty ensemble")
         self.sims = list(sims)
@@ -120,35 +123,87 @@ class Ensemble:
         self.step = self.sims[0].time_step_counter
         self.cur = self.sims[0]._ppf_cur
         self.graph_chunk = max(2, int(graph_chunk) // 2 * 2)
-        self.tiling = tiling_struct(1, (0, rows), pdl, 0 if bulk_shortcut else L.PPF_TILING_FULL_EVAL)
+        self.use_graph = use_graph
+        self._pdl = pdl
+        self._flags = 0 if bulk_shortcut else L.PPF_TILING_FULL_EVAL
         dev = self.sims[0]._ppf_grid.device
         self.stream = torch.cuda.Stream(dev)
         self.stepctr = torch.zeros(1, dtype=torch.int64, device=dev)
+        # grid-barrier words of the persistent launch (arrivals, generation)
+        self.sync = torch.zeros(2, dtype=torch.int32, device=dev)
+        self.status = torch.zeros(1, dtype=torch.int32, device=dev)
+        self.status_host = torch.zeros(1, dtype=torch.int32, pin_memory=True)
         self.graphs = {}
+        self.rows = int(rows) if rows else self._tune_rows()
+        self.tiling = tiling_struct(1, (0, self.rows), pdl, self._flags)
         self._build()
 
     @property
     def cells(self) -> int:
         return sum(s._ppf_grid.cells for s in self.sims)
 
-    def _member(self, s) -> L.PpfMember:
+    def _member(self, s, bufs=None) -> L.PpfMember:
         m = L.PpfMember()
         g = s._ppf_grid
+        bufs = bufs if bufs is not None else s._ppf_bufs
         m.ny, m.nx = g.kshape
         m.pitch = g.pitch
         m.bc = s._ppf_bc
-        m.phi[0] = s._ppf_bufs[0][0].data_ptr()
-        m.phi[1] = s._ppf_bufs[1][0].data_ptr()
+        m.phi[0] = bufs[0][0].data_ptr()
+        m.phi[1] = bufs[1][0].data_ptr()
         if isinstance(s, Warren1995GB300):
             m.model = L.PPF_MODEL_WARREN1995
-            m.c[0] = s._ppf_bufs[0][1].data_ptr()
-            m.c[1] = s._ppf_bufs[1][1].data_ptr()
+            m.c[0] = bufs[0][1].data_ptr()
+            m.c[1] = bufs[1][1].data_ptr()
             m.seed = int(s.user_data["seed"])
             m.w95 = s._ppf_params()
         else:
             m.model = L.PPF_MODEL_ALLEN_CAHN
             m.ac = s._ppf_params()
         return m
+
+    def _mix_key(self) -> str:
+        """The ensemble's member mix (model and grid of every member, sorted)
+        as an autotune cache key."""
+        import hashlib
+        mix = sorted((type(s).__name__, tuple(s._ppf_grid.kshape)) for s in self.sims)
+        digest = hashlib.sha1(repr(mix).encode()).hexdigest()[:16]
+        from . import autotune
+        return autotune.make_key("Ensemble", (len(mix), self.cells), torch.float32, digest)
+
+    def _tune_rows(self) -> int:
+        """Rows per warp band: each candidate times a chunk of steps on
+        scratch copies of every member's buffers (the members are untouched)."""
+        from . import autotune
+        with torch.cuda.stream(self.stream):
+            for s in self.sims:
+                self.stream.wait_stream(s._ppf_stream)
+            scratch = [[[t.clone() for t in bufs] for bufs in s._ppf_bufs] for s in self.sims]
+        sync = torch.zeros(2, dtype=torch.int32, device=self.sync.device)
+        steps = 8
+
+        def measure(cand):
+            tiling = tiling_struct(1, (0, cand["rows"]), self._pdl, self._flags)
+            members = (L.PpfMember * len(self.sims))(
+                *[self._member(s, bufs) for s, bufs in zip(self.sims, scratch)])
+            n = len(self.sims)
+            nbytes = C.c_size_t()
+            L.call("ppf_ensemble_plan_bytes", members, n, C.byref(tiling), C.byref(nbytes))
+            table = torch.empty(max(16, nbytes.value), dtype=torch.uint8, device=sync.device)
+            plan = L.PpfEnsemblePlan()
+            sp = C.c_void_p(self.stream.cuda_stream)
+            L.call("ppf_ensemble_build", members, n, C.byref(tiling), ptr(table),
+                   C.c_size_t(table.numel()), C.byref(plan), sp)
+
+            def run():
+                L.call("ppf_ensemble_run_f32", C.byref(plan), 0, C.c_uint64(0), None, steps,
+                       ptr(sync), C.byref(tiling), sp)
+
+            return autotune.time_candidate(run, self.stream, warmup=1, reps=3) / steps
+
+        best = autotune.pick(self._mix_key(), [{"rows": r} for r in (2, 4, 8)], measure)
+        del scratch
+        return int(best["rows"])
 
     def _members_key(self) -> bytes:
         """Every member's parameter struct as bytes: the plan (and so every
@@ -169,9 +224,39 @@ class Ensemble:
         L.call("ppf_ensemble_build", self.members, n, C.byref(self.tiling), ptr(self.table),
                C.c_size_t(self.table.numel()), C.byref(self.plan), C.c_void_p(self.stream.cuda_stream))
 
-    def _launch(self, parity, step, base):
-        L.call("ppf_ensemble_step_f32", C.byref(self.plan), int(parity), C.c_uint64(step), ptr(base),
-               C.byref(self.tiling), C.c_void_p(self.stream.cuda_stream))
+    def _launch(self, parity, step, base, nsteps=1):
+        sp = C.c_void_p(self.stream.cuda_stream)
+        if nsteps == 1:
+            L.call("ppf_ensemble_step_f32", C.byref(self.plan), int(parity), C.c_uint64(step),
+                   ptr(base), C.byref(self.tiling), sp)
+        else:
+            L.call("ppf_ensemble_run_f32", C.byref(self.plan), int(parity), C.c_uint64(step),
+                   ptr(base), int(nsteps), ptr(self.sync), C.byref(self.tiling), sp)
+
+    def _watch(self):
+        """Status bits of the chunk (a grid-barrier wait that gave up) moved
+        into the ensemble's word and copied to the host."""
+        sp = C.c_void_p(self.stream.cuda_stream)
+        L.call("ppf_status_collect", ptr(self.status), sp)
+        with torch.cuda.stream(self.stream):
+            self.status_host.copy_(self.status, non_blocking=True)
+
+    def check_status(self, block: bool = True):
+        """Raises EngineFault if a launch reported a fault; the barrier words
+        are reset so that the ensemble can run again."""
+        from .engines.base import EngineFault
+        if block:
+            self.synchronize()
+        bits = int(self.status_host.item())
+        if bits:
+            self.synchronize()
+            bits = int(self.status_host.item())
+            with torch.cuda.stream(self.stream):
+                self.status.zero_()
+                self.sync.zero_()
+            self.synchronize()
+            self.status_host.zero_()
+            raise EngineFault(bits, f"Ensemble of {len(self.sims)} (step {self.step})")
 
     def _graph(self):
         key = self.cur
@@ -184,9 +269,10 @@ class Ensemble:
         exec_ = C.c_void_p()
         L.call("ppf_graph_begin", sp)
         try:
-            for k in range(self.graph_chunk):
-                self._launch((self.cur + k) & 1, k, self.stepctr)
+            # one persistent launch for the whole chunk
+            self._launch(self.cur, 0, self.stepctr, self.graph_chunk)
             L.call("ppf_counter_add_u64", ptr(self.stepctr), C.c_uint64(self.graph_chunk), sp)
+            self._watch()
         finally:
             try:
                 L.call("ppf_graph_end", sp, C.byref(exec_))
@@ -196,11 +282,14 @@ class Ensemble:
         self.graphs[key] = exec_
         return exec_
 
-    def simulate(self, n: int, use_graph: bool = True):
-        """Advance every member n steps. A member whose parameters changed
+    def simulate(self, n: int, use_graph: bool | None = None):
+        """Advance every member n steps: chunks of graph_chunk steps, each one
+        persistent launch (graph-captured unless use_graph is False), and the
+        remaining steps in one more launch. A member whose parameters changed
         since the last call (user_data edited) gets a new plan: no captured
         graph replays old constants."""
         n = int(n)
+        use_graph = self.use_graph if use_graph is None else use_graph
         sp = C.c_void_p(self.stream.cuda_stream)
         if self._members_key() != self._key:
             self.synchronize()
@@ -208,18 +297,24 @@ class Ensemble:
                 L.call("ppf_graph_destroy", g)
             self.graphs = {}
             self._build()
-        if use_graph and n >= self.graph_chunk:
-            g = self._graph()
+        self.check_status(block=False)
+        if n >= self.graph_chunk:
+            g = self._graph() if use_graph else None
             with torch.cuda.stream(self.stream):
                 self.stepctr.fill_(self.step)
             while n >= self.graph_chunk:
-                L.call("ppf_graph_launch", g, sp)
-                self.step += self.graph_chunk
+                if g is not None:
+                    L.call("ppf_graph_launch", g, sp)
+                else:
+                    self._launch(self.cur, self.step, None, self.graph_chunk)
+                    self._watch()
+                self.step += self.graph_chunk  # even: the parity is unchanged
                 n -= self.graph_chunk
-        for _ in range(n):
-            self._launch(self.cur, self.step, None)
-            self.cur ^= 1
-            self.step += 1
+        if n > 0:
+            self._launch(self.cur, self.step, None, n)
+            self._watch()
+            self.cur ^= n & 1
+            self.step += n
         for s in self.sims:
             s._ppf_cur = self.cur
             s.time_step_counter = self.step
@@ -229,7 +324,7 @@ class Ensemble:
         self.stream.synchronize()
 
     def retrieve_fields_from_GPU(self):
-        self.synchronize()
+        self.check_status(block=True)
         for s in self.sims:
             s.retrieve_fields_from_GPU()
 

@@ -137,9 +137,9 @@ def main():
     # (CahnAllen.py:137-267, CahnHilliard.py:148-227)
     prng = np.random.default_rng(20240603)
     ud = dict(M=0.7, W=1.3, epsilon=1.1)
-    # the full 2-D system (the GMRES engine) runs with dt = 0.1 here: the
-    # library's Chebyshev solve needs 16 W M dt < 4 (a diagonally dominant
-    # system); the others with dt = 0.3
+    # the full 2-D system (the GMRES engine) runs with dt = 0.1 here (16 W M
+    # dt < 4: the library's Chebyshev solve) and, in phase_indefinite, with
+    # dt = 0.5 (beyond it: MINRES); the others with dt = 0.3
     for name, module, fn, shape, solver, adi, gm in [
         ("phase_implicit_ac_1d", "CahnAllen", "engine_CahnAllenImplicit1D", (40,), "implicit",
          False, False),
@@ -169,6 +169,7 @@ def main():
                     function=fn, steps=3, dt=dt, dx=dx_, solver=solver, adi=adi, gmres=gm,
                     params=ud)
         save(name, meta, c0=c0, out=out)
+    phase_indefinite()
 
     # NCGPU (Engines/NCGPU.py): the reference's numba kernels run serially
     # under a stand-in numba module, Ni-Cu ideal TDB of the reference
@@ -330,8 +331,30 @@ def ncgpu_new():
         save(name, meta, **arrays)
 
 
+def phase_indefinite():
+    """engine_CahnAllenImplicit2D_GMRES (CahnAllen.py:163-175) beyond the
+    diagonal-dominance bound: 16 W M dt = 7.28 >= 4 with half the cells at
+    phi = 0.75 (the double well's most negative slope), so the system is
+    indefinite (90 of 168 eigenvalues negative) yet well conditioned
+    (|eigenvalue| >= 0.5), and the reference's GMRES (rtol 1e-5) converges.
+    One step: beyond it the next system inherits the indefinite step's
+    overshoot."""
+    os.environ.setdefault("PPF_REFERENCE_ROOT", "/root/reference/pyphasefield")
+    prng = np.random.default_rng(0)
+    ud = dict(M=0.7, W=1.3, epsilon=1.1)
+    c0 = np.where(prng.random((14, 12)) > 0.5, 0.75, 0.2) + 0.01 * (prng.random((14, 12)) - 0.5)
+    fn = "engine_CahnAllenImplicit2D_GMRES"
+    dt, dx_ = 0.5, 3.0
+    out = refshim.run_implicit(fn, c0, 1, None, dt, dx_, module="CahnAllen", user_data=ud)
+    meta = dict(model="allen_cahn", function=fn, steps=1, dt=dt, dx=dx_, solver="implicit",
+                adi=False, gmres=True, params=ud)
+    save("phase_implicit_ac_2d_gmres_indefinite", meta, c0=c0, out=out)
+
+
 if __name__ == "__main__":
-    if sys.argv[1:] == ["ncgpu_multicomponent"]:
+    if sys.argv[1:] == ["phase_indefinite"]:
+        phase_indefinite()
+    elif sys.argv[1:] == ["ncgpu_multicomponent"]:
         ncgpu_multicomponent()
     elif sys.argv[1:] == ["ncgpu_excess"]:
         ncgpu_excess()

@@ -1,5 +1,5 @@
-"""The batched ensemble (one persistent launch per step over many engines)
-and the autotuner, on the GPU. Ensemble members must match the same engines
+"""The batched ensemble (one persistent cooperative launch per chunk of
+steps over many engines) and the autotuner, on the GPU. Ensemble members must match the same engines
 stepped one by one (fp32: within 1e-6 relative L2; the ensemble's Allen-Cahn
 band is a different kernel from the single-grid one, so rounding may differ)
 and the FP64 oracle (1e-5)."""
@@ -93,6 +93,61 @@ def test_autotune_picks_and_caches(cuda, tmp_path, monkeypatch):
     entry = next(iter(cache.values()))
     assert entry["config"]["temporal_depth"] == sim.user_data["temporal_depth"]
     from pyphasefield_gb300.engines.models import _stencil_candidates
-    assert len(entry["tried"]) == len(_stencil_candidates(sim)) == 17
+    assert len(entry["tried"]) == len(_stencil_candidates(sim)) == 20
     ref = restate.run_single("diffusion", c0, 16, "PERIODIC", 1.0, 0.2, D=1.0)
     assert rel_l2(sim.fields[0].get_cells(), ref) < 1e-5  # tuning did not change the state
+
+
+def test_persistent_chunks_equal_single_steps(cuda):
+    """One cooperative launch of 7 steps (grid barrier between steps) equals
+    7 one-step launches bit for bit, on an ensemble large enough that the
+    launch has many CTAs."""
+    from pyphasefield_gb300.ensemble import Ensemble, make_config_ensemble
+    a = make_config_ensemble(n=8, seed=4, side_range=(100, 400))
+    b = make_config_ensemble(n=8, seed=4, side_range=(100, 400))
+    ea = Ensemble(a, rows=2, graph_chunk=8)
+    ea.simulate(7, use_graph=False)  # one persistent launch
+    eb = Ensemble(b, rows=2, graph_chunk=8)
+    for _ in range(7):
+        eb.simulate(1, use_graph=False)
+    ea.retrieve_fields_from_GPU()
+    eb.retrieve_fields_from_GPU()
+    for sa, sb in zip(a, b):
+        for fa, fb in zip(sa.fields, sb.fields):
+            np.testing.assert_array_equal(fa.get_cells(), fb.get_cells())
+
+
+def test_ensemble_follows_parameter_edits(cuda):
+    """A member's T changed between simulate() calls: the graph-launched
+    ensemble equals eager launches bit for bit (no stale plan)."""
+    from pyphasefield_gb300.ensemble import Ensemble
+    runs = []
+    for use_graph in (True, False):
+        sims = _members(3)
+        ens = Ensemble(sims, rows=2, graph_chunk=4, use_graph=use_graph)
+        ens.simulate(12)
+        sims[0].user_data["T"] -= 10.0
+        ens.simulate(12)
+        ens.retrieve_fields_from_GPU()
+        runs.append(_snapshot(sims))
+    for ma, mb in zip(*runs):
+        for fa, fb in zip(ma, mb):
+            np.testing.assert_array_equal(fa, fb)
+
+
+def test_ensemble_rows_autotuned_and_cached(cuda, tmp_path, monkeypatch):
+    import json
+    from pyphasefield_gb300.ensemble import Ensemble
+    monkeypatch.setenv("PPF_AUTOTUNE_CACHE", str(tmp_path / "tune.json"))
+    sims = _members(5)
+    init = _snapshot(sims)
+    ens = Ensemble(sims, graph_chunk=4)
+    assert ens.rows in (2, 4, 8)
+    cache = json.loads((tmp_path / "tune.json").read_text())
+    entry = next(iter(cache.values()))
+    assert entry["config"] == {"rows": ens.rows} and len(entry["tried"]) == 3
+    # tuning ran on scratch copies: the members still hold their initial state
+    ens.retrieve_fields_from_GPU()
+    for m, s in zip(init, sims):
+        for f0, f in zip(m, s.fields):
+            np.testing.assert_array_equal(f0, f.get_cells())

@@ -264,7 +264,7 @@ def run_phase_gpu(model, c0, steps, solver, M, W, eps, dt, dx, adi, gmres, preci
 
 
 def test_phase_fixture_count():
-    assert len(PHASE) == 10
+    assert len(PHASE) == 11
 
 
 @pytest.mark.parametrize("name", PHASE)

@@ -77,6 +77,31 @@ def test_temporal_blocking_bit_exact(cuda, model, bc, depth):
         np.testing.assert_array_equal(a, b)
 
 
+@pytest.mark.parametrize("depth,seg", [(4, 0), (8, 0), (2, 12), (5, 4), (7, 64)])
+def test_marching_kernel_segments_bit_exact(cuda, depth, seg):
+    """The marching temporal-blocking kernel (TMA-fed windows, one register
+    stage per step) on a grid with interior TMA windows and edge windows,
+    with the default and explicit segment lengths: depth-k passes equal k
+    single steps bit for bit, and the FP64 oracle."""
+    rng = np.random.default_rng(21)
+    c0 = rng.random((517, 1003))
+    for model, params in (("diffusion", dict(D=1.0)),
+                          ("allen_cahn", dict(M=0.1, epsilon=1.0, W=1.0))):
+        for bc in ("PERIODIC", ["NEUMANN", "PERIODIC"], ["DIRCHLET", "NEUMANN"]):
+            bcs = [bc] * 2 if isinstance(bc, str) else bc
+            vals = [[[0.25, 0.5] if b == "DIRCHLET" else [0.0, 0.0] for b in bcs]]
+            for prec in ("fp32", "fp64"):
+                a = run_single_gpu(model, c0, 2 * depth + 1, bc, 1.0, 0.1, values=vals,
+                                   precision=prec, depth=1, **params)
+                b = run_single_gpu(model, c0, 2 * depth + 1, bc, 1.0, 0.1, values=vals,
+                                   precision=prec, depth=depth, tile=(0, seg) if seg else None,
+                                   **params)
+                np.testing.assert_array_equal(a, b)
+            ref = restate.run_single(model, c0, 2 * depth + 1, bc, 1.0, 0.1, values=vals,
+                                     **params)
+            assert rel_l2(b, ref) < F64_TOL
+
+
 @pytest.mark.parametrize("shape", [(1, 7), (7, 1), (5, 3), (33, 65), (129, 31)])
 def test_odd_and_tiny_shapes(cuda, shape):
     rng = np.random.default_rng(12)

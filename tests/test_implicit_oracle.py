@@ -84,7 +84,7 @@ PHASE = sorted(p.stem for p in GOLDEN.glob("phase_implicit_*.npz"))
 
 
 def test_phase_fixture_set_complete():
-    assert len(PHASE) == 10
+    assert len(PHASE) == 11
 
 
 @pytest.mark.parametrize("name", PHASE)
