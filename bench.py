@@ -419,6 +419,10 @@ SWEEP = {
     "diffusion_8192_d4": ("diffusion", (8192, 8192), 4, 200),
     "diffusion_16384_d4": ("diffusion", (16384, 16384), 4, 100),
     "diffusion_16384_d8": ("diffusion", (16384, 16384), 8, 200),
+    "diffusion_16384_d2": ("diffusion", (16384, 16384), 2, 100),
+    "diffusion_8192_d8": ("diffusion", (8192, 8192), 8, 200),
+    "allen_cahn_16384_d8": ("allen_cahn", (16384, 16384), 8, 200),
+    "diffusion_16384_d4_fp64": ("diffusion", (16384, 16384), 4, 100, {"precision": "fp64"}),
     "allen_cahn_4096": ("allen_cahn", (4096, 4096), 1, 200),
     "allen_cahn_8192": ("allen_cahn", (8192, 8192), 1, 100),
     "allen_cahn_16384": ("allen_cahn", (16384, 16384), 1, 100),

@@ -18,6 +18,10 @@ from pathlib import Path
 import torch
 
 _lock = threading.Lock()
+# choices made in this process (per cache file and key): consulted first, so
+# that a cache file that cannot be written (read-only home) does not make two
+# engines of the same key pick differently
+_memory: dict = {}
 
 
 def cache_path() -> Path:
@@ -69,10 +73,13 @@ def time_candidate(run, stream: torch.cuda.Stream, warmup: int = 2, reps: int = 
 def pick(key: str, candidates: list, measure) -> dict:
     """Return the cached best candidate for `key`, or time every candidate
     with measure(candidate) -> seconds per unit of work and cache the best."""
+    mkey = (str(cache_path()), key)
     with _lock:
-        cache = _load()
-        hit = cache.get(key)
+        hit = _memory.get(mkey)
+        if hit is None:
+            hit = _load().get(key)
         if hit is not None and hit.get("config") in candidates:
+            _memory[mkey] = hit
             return hit["config"]
     results = []
     for cand in candidates:
@@ -83,9 +90,11 @@ def pick(key: str, candidates: list, measure) -> dict:
     if not results:
         raise RuntimeError(f"no autotune candidate ran for {key}")
     best_t, best = min(results, key=lambda r: r[0])
+    entry = {"config": best, "seconds": best_t,
+             "tried": [{"config": c, "seconds": t} for t, c in results]}
     with _lock:
+        _memory[mkey] = entry
         cache = _load()
-        cache[key] = {"config": best, "seconds": best_t,
-                      "tried": [{"config": c, "seconds": t} for t, c in results]}
+        cache[key] = entry
         _store(cache)
     return best

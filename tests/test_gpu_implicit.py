@@ -328,13 +328,65 @@ def test_var_line_solve(cuda, shape, axis, alpha, variant):
         assert rel_l2(got, ref) < tol, precision
 
 
-def test_full_allen_cahn_system_outside_the_bound_rejected(cuda):
-    """16 W M dt >= 4: the Chebyshev bound of the full 2-D solve does not
-    hold; the library refuses instead of returning an unconverged field."""
+@pytest.mark.parametrize("shape,dt,dx,seed", [((14, 12), 0.5, 3.0, 0), ((64, 80), 0.6, 2.5, 1),
+                                              ((300, 257), 1.0, 3.0, 2)])
+def test_full_allen_cahn_system_beyond_the_bound_minres(cuda, shape, dt, dx, seed):
+    """16 W M dt >= 4: the full 2-D system may be indefinite (here half the
+    cells sit at phi = 0.75, the double well's most negative slope, and the
+    matrix has negative eigenvalues) and the Chebyshev bound fails; the
+    library solves it with MINRES in one persistent launch. Against the
+    exact dense solve (small grids) or the system's own residual."""
+    import torch
     from pyphasefield_gb300 import _lib as L
-    with pytest.raises(L.PpfError, match="diagonally dominant"):
-        run_phase_gpu("allen_cahn", np.full((8, 8), 0.5), 1, "implicit", 0.7, 1.3, 1.1, 0.3, 1.2,
-                      False, True)
+    rng = np.random.default_rng(seed)
+    c0 = np.where(rng.random(shape) > 0.5, 0.75, 0.2) + 0.01 * (rng.random(shape) - 0.5)
+    M, W, eps = 0.7, 1.3, 1.1
+    assert 16 * W * M * dt >= 4
+    args = ("allen_cahn", c0, 1, "implicit", M, W, eps, dt, dx, False, True)
+    a = M * dt * eps ** 2 / dx ** 2
+    d = 1 + 4 * a + 16 * W * M * dt * (4 * c0 * c0 - 6 * c0 + 2)
+
+    def residual(x):
+        ax = d * x - a * (np.roll(x, 1, 0) + np.roll(x, -1, 0) + np.roll(x, 1, 1)
+                          + np.roll(x, -1, 1))
+        return np.linalg.norm(ax - c0) / np.linalg.norm(c0)
+
+    for precision, tol in (("fp64", F64_TOL), ("fp32", F32_TOL)):
+        v = C.c_int32()
+        L.call("ppf_status_take", C.byref(v))
+        out = run_phase_gpu(*args, precision=precision)
+        L.call("ppf_status_take", C.byref(v))
+        assert v.value == 0, v.value  # converged: no status bit
+        assert residual(out) < (1e-12 if precision == "fp64" else 1e-5)
+        if c0.size <= 5000:
+            assert rel_l2(out, I.run_phase(*args)) < tol
+    assert (out < 0).any()  # the indefinite step overshoots below phi = 0
+
+
+def test_minres_reports_an_unconverged_solve(cuda):
+    """An iteration cap too small for the system: the solve sets
+    PPF_STATUS_NOT_CONVERGED instead of passing off its iterate as converged."""
+    import torch
+    from pyphasefield_gb300 import _lib as L
+    rng = np.random.default_rng(3)
+    c0 = np.where(rng.random((64, 64)) > 0.5, 0.75, 0.2)
+    g, _, kshape, pitch = make_structs(c0.shape, "PERIODIC")
+    nbytes = C.c_size_t()
+    L.call("ppf_phase_implicit_scratch_bytes", C.byref(g), 8, C.byref(nbytes))
+    scratch = torch.empty(nbytes.value, dtype=torch.uint8, device="cuda")
+    a = to_dev(c0, kshape, pitch, torch.float64, "cuda")
+    o, tmp = torch.zeros_like(a), torch.zeros_like(a)
+    # tol below what double reaches on this system within the library's cap
+    p = L.PpfImplicitPhaseParams(2.5, 0.6, 0.7, 1.3, 1.1, 1e-300, L.PPF_MODEL_ALLEN_CAHN, 1, 0, 1)
+    v = C.c_int32()
+    L.call("ppf_status_take", C.byref(v))
+    it = C.c_int32()
+    L.call("ppf_phase_implicit_step_f64", C.byref(p), C.byref(g), C.c_void_p(a.data_ptr()),
+           C.c_void_p(o.data_ptr()), C.c_void_p(tmp.data_ptr()), C.c_void_p(scratch.data_ptr()),
+           scratch.numel(), C.byref(it), C.c_void_p(torch.cuda.current_stream().cuda_stream))
+    torch.cuda.synchronize()
+    L.call("ppf_status_take", C.byref(v))
+    assert v.value & L.PPF_STATUS_NOT_CONVERGED
 
 
 def test_cahn_hilliard_1d_pentadiagonal_large(cuda):
