@@ -729,6 +729,8 @@ def profile_case(name: str):
     ch256       Cahn-Hilliard 256^3 periodic, dt 0.01, 5 steps
     diff4096    Diffusion 2-D 4096^2 periodic, 5 steps (temporal depth from PPF_DEPTH, default 1)
     diff3d384   Diffusion 3-D 384^3 periodic, 5 steps
+    diff8192    Diffusion 2-D 8192^2 periodic, 5 passes of PPF_DEPTH (default 4) steps: the
+                marching temporal-blocking kernel on 512 MiB of fields
     diff16384   Diffusion 2-D 16384^2 periodic, 5 steps (2 GiB of fields: beyond L2)
     adi4096     implicit ADI Diffusion 2-D 4096^2 (Crank-Nicolson with PPF_CN=1), D dt = 5,
                 3 steps: line solves along x and y
@@ -758,6 +760,14 @@ def profile_case(name: str):
                              user_data={"D": 1.0, "use_graph": False, "temporal_depth": depth})
         sim.initialize_fields_and_imported_data()
         sim.fields[0].data[1:-1, 1:-1] = 0.5 + 0.01 * rng.standard_normal((4096, 4096))
+        sim.simulate(5 * depth)
+    elif name == "diff8192":
+        depth = int(os.environ.get("PPF_DEPTH", "4"))
+        sim = DiffusionGB300(dimensions=[8192, 8192], dx=1.0, dt=0.2,
+                             boundary_conditions="PERIODIC",
+                             user_data={"D": 1.0, "use_graph": False, "temporal_depth": depth})
+        sim.initialize_fields_and_imported_data()
+        sim.fields[0].data[1:-1, 1:-1] = 0.5 + 0.01 * rng.standard_normal((8192, 8192))
         sim.simulate(5 * depth)
     elif name == "diff16384":
         sim = DiffusionGB300(dimensions=[16384, 16384], dx=1.0, dt=0.2,

@@ -298,6 +298,9 @@ typedef struct PpfImplicitPhaseParams {
   int32_t model;  /* PPF_MODEL_ALLEN_CAHN or PPF_MODEL_CAHN_HILLIARD */
   int32_t solver; /* PPF_SOLVER_IMPLICIT, _CRANK_NICOLSON or _IMEX */
   int32_t adi, gmres;
+  int32_t max_iter; /* MINRES iteration cap (0: 20000); past it the solve
+                       sets PPF_STATUS_NOT_CONVERGED */
+  int32_t reserved;
 } PpfImplicitPhaseParams;
 
 int32_t ppf_phase_implicit_scratch_bytes(const PpfGrid* g, int32_t elem_bytes, size_t* bytes);

@@ -85,7 +85,7 @@ PPF_MODEL_CAHN_HILLIARD = 3
 
 class PpfImplicitPhaseParams(C.Structure):
     _fields_ = [(n, C.c_double) for n in ("dx", "dt", "M", "W", "epsilon", "tol")] + [
-        (n, C.c_int32) for n in ("model", "solver", "adi", "gmres")]
+        (n, C.c_int32) for n in ("model", "solver", "adi", "gmres", "max_iter", "reserved")]
 
 
 class PpfImplicitDiffusionParams(C.Structure):

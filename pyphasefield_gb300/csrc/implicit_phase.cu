@@ -724,9 +724,10 @@ int32_t jacobi_solve(const Geo& g, double a, double dbase, double dc, double tol
 // accumulated in double from per-CTA partial sums that every CTA adds up in
 // the same order (so every CTA takes the same scalars and the same stopping
 // decision). The loop ends on the device when the residual norm (|eta|,
-// exact in exact arithmetic) reaches tol ||b|| or after max_iter
-// iterations, which sets PPF_STATUS_NOT_CONVERGED. Initial guess: b (the
-// field before the step).
+// exact in exact arithmetic) reaches tol ||b||, when the Lanczos process
+// finds an invariant subspace (solved), or, unconverged, after max_iter
+// iterations or at a singular tridiagonal (both set
+// PPF_STATUS_NOT_CONVERGED). Initial guess: b (the field before the step).
 constexpr int kMinresThreads = 256;
 constexpr int kMinresMaxCtas = 2048;
 constexpr int kMinresMaxIter = 20000;
@@ -865,6 +866,7 @@ __global__ void __launch_bounds__(kMinresThreads)
       // Givens rotations of the tridiagonal's QR factorisation
       const double a0 = c * alpha - c_prev * sg * beta;
       const double a1 = sqrt(a0 * a0 + beta_n * beta_n);
+      if (!(a1 > 0.0) || !isfinite(a1) || !isfinite(alpha)) break;  // singular: not converged
       const double a2 = sg * alpha + c_prev * c * beta;
       const double a3 = s_prev * beta;
       const double c_n = a0 / a1, s_n = beta_n / a1;
@@ -1080,8 +1082,9 @@ int32_t phase_step(const PpfImplicitPhaseParams* p, const PpfGrid* grid, const T
         return jacobi_solve<T>(g, a, dbase, dc, tol, in, out, tmp, iterations, st);
       }
       const double tol = p->tol > 0 ? p->tol : (sizeof(T) == 4 ? 1e-7 : 1e-14);
-      return minres_solve<T>(g, a, dbase, dc, tol, kMinresMaxIter, in, out, scratch, bytes,
-                             iterations, st);
+      if (p->max_iter < 0) return fail(PPF_ERR_INVALID, "max_iter must be >= 0");
+      return minres_solve<T>(g, a, dbase, dc, tol, p->max_iter ? p->max_iter : kMinresMaxIter,
+                             in, out, scratch, bytes, iterations, st);
     }
     rc = var_sweep<T>(g, 1, a, 1 + 2 * a, 8 * wm, nullptr, 0, 0.0, in, out, scratch, bytes, st);
     if (rc) return rc;

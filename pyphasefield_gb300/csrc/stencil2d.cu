@@ -461,22 +461,38 @@ int32_t plan_tile2d(const PpfTiling* t, Tile2d* out) {
   return PPF_OK;
 }
 
-// Segment rows per warp: enough warps to fill the GPU (about 28 resident
-// per SM) while the 2K halo rows re-read per segment stay a small share.
-inline int march_segment(int ny, int nstrips, int K) {
-  long want = ((long)ny * nstrips + 4095) / 4096;
-  long seg = want < 8L * K ? 8L * K : (want > 512 ? 512 : want);
+// Segment rows per warp: the launch fills exactly one wave of resident
+// CTAs (a partial second wave would leave most SMs idle at the end of the
+// pass), unless that makes segments shorter than 8K rows, where the 2K halo
+// rows re-read per segment would cost too much.
+inline int march_segment(int ny, int nstrips, int K, long resident) {
+  const long cols = (nstrips + kMWarps - 1) / kMWarps;
+  long nseg = resident / cols;
+  if (nseg < 1) nseg = 1;
+  long seg = (ny + nseg - 1) / nseg;
+  if (seg < 8L * K) seg = 8L * K;
   seg = (seg + kMRows - 1) / kMRows * kMRows;
-  return (int)(seg < ny ? seg : (ny + kMRows - 1) / kMRows * kMRows);
+  const long full = (ny + kMRows - 1) / kMRows * kMRows;
+  return (int)(seg < full ? seg : full);
 }
 
 template <typename T, typename Op, int K>
 int32_t launch_march(const CUtensorMap& map, Op op, const Geo& g, const Bc<T>& bc, const T* in,
-                     T* out, int ow, int seg, int nstrips, int* st, bool pdl, cudaStream_t s) {
+                     T* out, int ow, int seg_req, int nstrips, int* st, bool pdl,
+                     cudaStream_t s) {
   constexpr int WW = 32 * Vec16<T>::n;
   const size_t smem = (size_t)kMWarps * kMSlots * kMRows * WW * sizeof(T);
   auto kern = stencil2d_march_kernel<T, Op, K>;
   PPF_TRY_CUDA(allow_smem(kern, smem));
+  int seg = seg_req;
+  if (seg <= 0) {
+    int dev = 0, sms = 0, per_sm = 0;
+    PPF_TRY_CUDA(cudaGetDevice(&dev));
+    PPF_TRY_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    PPF_TRY_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32 * kMWarps,
+                                                               smem));
+    seg = march_segment(g.n[0], nstrips, K, (long)sms * (per_sm < 1 ? 1 : per_sm));
+  }
   const long gy = (g.n[0] + seg - 1) / seg;
   if (gy > 65535) return fail(PPF_ERR_INVALID, "too many row segments");
   dim3 grid_dim((nstrips + kMWarps - 1) / kMWarps, (unsigned)gy);
@@ -495,9 +511,7 @@ int32_t run_march(Op op, const Geo& g, const Bc<T>& bc, const T* in, T* out, int
   const int KA = (K + V - 1) / V * V;
   const int ow = WW - 2 * KA;
   const int nstrips = (g.n[1] + ow - 1) / ow;
-  int seg = seg_req > 0 ? (seg_req + kMRows - 1) / kMRows * kMRows
-                        : march_segment(g.n[0], nstrips, K);
-  if (seg < kMRows) seg = kMRows;
+  int seg = seg_req > 0 ? (seg_req + kMRows - 1) / kMRows * kMRows : 0;
   CUtensorMap map;
   const uint64_t dims[2] = {(uint64_t)g.n[1], (uint64_t)g.n[0]};
   const uint64_t strides[1] = {(uint64_t)g.pitch * sizeof(T)};

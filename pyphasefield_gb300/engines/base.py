@@ -232,6 +232,9 @@ class GB300Engine:
 
     def __del__(self):
         try:
+            if getattr(self, "_ppf_stream", None) is not None:
+                # work in flight still reads the buffers freed with the engine
+                self._ppf_stream.synchronize()
             self._ppf_checkpoint_wait()
             ck = getattr(self, "_ppf_ckpt", None)
             if ck is not None:

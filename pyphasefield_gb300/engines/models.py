@@ -41,7 +41,9 @@ class _ImplicitPhase:
     (Engines/CahnAllen.py:325-361) and CahnHilliard.simulation_loop
     (Engines/CahnHilliard.py:382-421) do; periodic, as the reference's
     matrices are. user_data["implicit_tol"] bounds the error of the full 2-D
-    solve (0: the library default)."""
+    solve (0: the library default); beyond the Chebyshev bound (16 W M dt >=
+    4) that solve is MINRES, capped at user_data["implicit_max_iter"]
+    iterations (0: 20000; an unconverged solve raises EngineFault)."""
 
     PHASE_MODEL = 0
 
@@ -81,7 +83,8 @@ class _ImplicitPhase:
                                      float(ud["W"]), float(ud["epsilon"]),
                                      float(ud.get("implicit_tol", 0.0)), self.PHASE_MODEL,
                                      self._ppf_phase_solver, 1 if ud.get("adi") else 0,
-                                     1 if ud.get("gmres") else 0)
+                                     1 if ud.get("gmres") else 0,
+                                     int(ud.get("implicit_max_iter", 0)), 0)
         it = C.c_int32()
         sc = self._ppf_scratch
         L.call(f"ppf_phase_implicit_step_{_F[self._ppf_dtype]}", C.byref(p),

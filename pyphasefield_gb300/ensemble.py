@@ -128,10 +128,13 @@ class Ensemble:
         self._flags = 0 if bulk_shortcut else L.PPF_TILING_FULL_EVAL
         dev = self.sims[0]._ppf_grid.device
         self.stream = torch.cuda.Stream(dev)
-        self.stepctr = torch.zeros(1, dtype=torch.int64, device=dev)
-        # grid-barrier words of the persistent launch (arrivals, generation)
-        self.sync = torch.zeros(2, dtype=torch.int32, device=dev)
-        self.status = torch.zeros(1, dtype=torch.int32, device=dev)
+        # the ensemble's own device words live on its stream: freed with the
+        # ensemble, their memory is reused only after the stream's work
+        with torch.cuda.stream(self.stream):
+            self.stepctr = torch.zeros(1, dtype=torch.int64, device=dev)
+            # grid-barrier words of the persistent launch (arrivals, generation)
+            self.sync = torch.zeros(2, dtype=torch.int32, device=dev)
+            self.status = torch.zeros(1, dtype=torch.int32, device=dev)
         self.status_host = torch.zeros(1, dtype=torch.int32, pin_memory=True)
         self.graphs = {}
         self.rows = int(rows) if rows else self._tune_rows()
@@ -216,8 +219,9 @@ class Ensemble:
         self._key = b"".join(bytes(m) for m in self.members)
         nbytes = C.c_size_t()
         L.call("ppf_ensemble_plan_bytes", self.members, n, C.byref(self.tiling), C.byref(nbytes))
-        self.table = torch.empty(max(16, nbytes.value), dtype=torch.uint8,
-                                 device=self.stepctr.device)
+        with torch.cuda.stream(self.stream):
+            self.table = torch.empty(max(16, nbytes.value), dtype=torch.uint8,
+                                     device=self.stepctr.device)
         self.plan = L.PpfEnsemblePlan()
         for s in self.sims:  # member uploads must land before the first step
             self.stream.wait_stream(s._ppf_stream)
@@ -330,6 +334,8 @@ class Ensemble:
 
     def __del__(self):
         try:
+            # launches still in flight read the plan table and barrier words
+            self.stream.synchronize()
             for g in self.graphs.values():
                 L.call("ppf_graph_destroy", g)
         except Exception:

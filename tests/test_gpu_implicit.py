@@ -250,7 +250,7 @@ def run_phase_gpu(model, c0, steps, solver, M, W, eps, dt, dx, adi, gmres, preci
     p = L.PpfImplicitPhaseParams(dx, dt, M, W, eps, 0.0,
                                  L.PPF_MODEL_ALLEN_CAHN if model == "allen_cahn"
                                  else L.PPF_MODEL_CAHN_HILLIARD, _PSOLVER[solver],
-                                 1 if adi else 0, 1 if gmres else 0)
+                                 1 if adi else 0, 1 if gmres else 0, 0, 0)
     it = C.c_int32()
     sfx = "f64" if precision == "fp64" else "f32"
     s = C.c_void_p(torch.cuda.current_stream().cuda_stream)
@@ -364,8 +364,9 @@ def test_full_allen_cahn_system_beyond_the_bound_minres(cuda, shape, dt, dx, see
 
 
 def test_minres_reports_an_unconverged_solve(cuda):
-    """An iteration cap too small for the system: the solve sets
-    PPF_STATUS_NOT_CONVERGED instead of passing off its iterate as converged."""
+    """An iteration cap too small for the system (3 iterations): the solve
+    sets PPF_STATUS_NOT_CONVERGED instead of passing off its iterate as
+    converged."""
     import torch
     from pyphasefield_gb300 import _lib as L
     rng = np.random.default_rng(3)
@@ -376,8 +377,8 @@ def test_minres_reports_an_unconverged_solve(cuda):
     scratch = torch.empty(nbytes.value, dtype=torch.uint8, device="cuda")
     a = to_dev(c0, kshape, pitch, torch.float64, "cuda")
     o, tmp = torch.zeros_like(a), torch.zeros_like(a)
-    # tol below what double reaches on this system within the library's cap
-    p = L.PpfImplicitPhaseParams(2.5, 0.6, 0.7, 1.3, 1.1, 1e-300, L.PPF_MODEL_ALLEN_CAHN, 1, 0, 1)
+    p = L.PpfImplicitPhaseParams(2.5, 0.6, 0.7, 1.3, 1.1, 0.0, L.PPF_MODEL_ALLEN_CAHN, 1, 0, 1,
+                                 3, 0)
     v = C.c_int32()
     L.call("ppf_status_take", C.byref(v))
     it = C.c_int32()
