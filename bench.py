@@ -423,6 +423,8 @@ SWEEP = {
     "diffusion_8192_d8": ("diffusion", (8192, 8192), 8, 200),
     "allen_cahn_16384_d8": ("allen_cahn", (16384, 16384), 8, 200),
     "diffusion_16384_d4_fp64": ("diffusion", (16384, 16384), 4, 100, {"precision": "fp64"}),
+    "diffusion_16384_d8_seg512": ("diffusion", (16384, 16384), 8, 200, {"tile": (0, 512)}),
+    "diffusion_16384_d4_seg256": ("diffusion", (16384, 16384), 4, 100, {"tile": (0, 256)}),
     "allen_cahn_4096": ("allen_cahn", (4096, 4096), 1, 200),
     "allen_cahn_8192": ("allen_cahn", (8192, 8192), 1, 100),
     "allen_cahn_16384": ("allen_cahn", (16384, 16384), 1, 100),
@@ -729,6 +731,8 @@ def profile_case(name: str):
     ch256       Cahn-Hilliard 256^3 periodic, dt 0.01, 5 steps
     diff4096    Diffusion 2-D 4096^2 periodic, 5 steps (temporal depth from PPF_DEPTH, default 1)
     diff3d384   Diffusion 3-D 384^3 periodic, 5 steps
+    ensemble64  the 64-member ensemble benchmark (1.56e7 cells), five persistent launches of
+                8 steps
     diff8192    Diffusion 2-D 8192^2 periodic, 5 passes of PPF_DEPTH (default 4) steps: the
                 marching temporal-blocking kernel on 512 MiB of fields
     diff16384   Diffusion 2-D 16384^2 periodic, 5 steps (2 GiB of fields: beyond L2)
@@ -761,6 +765,13 @@ def profile_case(name: str):
         sim.initialize_fields_and_imported_data()
         sim.fields[0].data[1:-1, 1:-1] = 0.5 + 0.01 * rng.standard_normal((4096, 4096))
         sim.simulate(5 * depth)
+    elif name == "ensemble64":
+        from pyphasefield_gb300.ensemble import Ensemble, make_config_ensemble
+        ens = Ensemble(make_config_ensemble(n=64, seed=0), rows=2, graph_chunk=8,
+                       use_graph=False)
+        ens.simulate(40)
+        ens.synchronize()
+        return
     elif name == "diff8192":
         depth = int(os.environ.get("PPF_DEPTH", "4"))
         sim = DiffusionGB300(dimensions=[8192, 8192], dx=1.0, dt=0.2,

@@ -426,7 +426,9 @@ typedef struct PpfEnsemblePlan {
   int64_t n_items;          /* warp bands over all members */
   int32_t n_members;
   int32_t rows;    /* rows per warp band (tiling->tile_y: 2, 4 or 8) */
-  int64_t n_units; /* four-band units (one CTA pass each) */
+  int64_t n_units; /* units of 4 x bands bands (one CTA pass each) */
+  int32_t bands;   /* bands per warp and unit (tiling->tile_x: 1 or 4; 0 -> 4) */
+  int32_t reserved;
 } PpfEnsemblePlan;
 
 /* Device bytes of the member table (members and unit map) for these

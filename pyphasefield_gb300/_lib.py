@@ -129,7 +129,8 @@ class PpfMember(C.Structure):
 
 class PpfEnsemblePlan(C.Structure):
     _fields_ = [("device_table", C.c_void_p), ("n_items", C.c_int64),
-                ("n_members", C.c_int32), ("rows", C.c_int32), ("n_units", C.c_int64)]
+                ("n_members", C.c_int32), ("rows", C.c_int32), ("n_units", C.c_int64),
+                ("bands", C.c_int32), ("reserved", C.c_int32)]
 
 
 class PpfSgShape(C.Structure):

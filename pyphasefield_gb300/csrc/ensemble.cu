@@ -3,8 +3,9 @@
 // persistent launch per chunk of steps.
 //
 // Work: a member's grid is cut into warp bands (a 30-column strip x ROWS
-// rows), and its bands are grouped four at a time into units, one per CTA
-// pass; a member's units are padded so that no unit spans two members. A
+// rows), and its bands are grouped sixteen at a time into units, one per CTA
+// pass (four per warp); a member's last unit is padded so that no unit spans
+// two members. A
 // unit table maps every unit to its member, so a CTA finds its member with
 // one load and stages the member's folded constants in shared memory for its
 // four warps. The launch is cooperative (every CTA resident) and persistent:
@@ -79,22 +80,29 @@ __device__ __forceinline__ void ac_band(float a, float b, const Geo& g, const Bc
   }
 }
 
-template <int ROWS>
+// A unit is BANDS bands per warp; warp w of the CTA takes bands w, w + 4,
+// ... of the unit's 4 BANDS (the CTA's warps work on neighbouring strips at
+// any moment).
+template <int ROWS, int BANDS>
 __device__ __forceinline__ void run_unit(const MemberDev& m, long long unit, int parity,
                                          uint64_t step) {
-  const long long local = (unit - m.unit_begin) * kWarpsPerCta + threadIdx.y;
-  if (local >= m.items) return;  // padding warp (whole warp)
-  const int xs = (int)(local % m.strips) * w95::kStrip - 1;
-  const int y0 = (int)(local / m.strips) * ROWS;
-  if (m.model == PPF_MODEL_WARREN1995)
-    w95::band<float, ROWS, true>(m.w, m.g, m.bc, m.phi[parity], m.c[parity], m.phi[1 - parity],
-                                 m.c[1 - parity], m.seed, step, xs, y0);
-  else
-    ac_band<ROWS>(m.ac_a, m.ac_b, m.g, m.bc, m.phi[parity], m.phi[1 - parity], xs, y0);
+  const long long first = (unit - m.unit_begin) * (kWarpsPerCta * BANDS);
+#pragma unroll 1
+  for (int j = 0; j < BANDS; ++j) {
+    const long long local = first + j * kWarpsPerCta + threadIdx.y;
+    if (local >= m.items) return;  // past the member's last band (whole warp)
+    const int xs = (int)(local % m.strips) * w95::kStrip - 1;
+    const int y0 = (int)(local / m.strips) * ROWS;
+    if (m.model == PPF_MODEL_WARREN1995)
+      w95::band<float, ROWS, true>(m.w, m.g, m.bc, m.phi[parity], m.c[parity],
+                                   m.phi[1 - parity], m.c[1 - parity], m.seed, step, xs, y0);
+    else
+      ac_band<ROWS>(m.ac_a, m.ac_b, m.g, m.bc, m.phi[parity], m.phi[1 - parity], xs, y0);
+  }
 }
 
-template <int ROWS>
-__global__ void __launch_bounds__(kCtaThreads, 7)
+template <int ROWS, int BANDS>
+__global__ void __launch_bounds__(kCtaThreads, 4)
     ensemble_kernel(const MemberDev* __restrict__ members, const int* __restrict__ unit_member,
                     long long n_units, int parity, uint64_t step,
                     const uint64_t* __restrict__ step_base, int nsteps, unsigned* sync,
@@ -117,7 +125,7 @@ __global__ void __launch_bounds__(kCtaThreads, 7)
         for (int i = tid; i < (int)(sizeof(MemberDev) / 4); i += kCtaThreads) dst[i] = src[i];
       }
       __syncthreads();
-      run_unit<ROWS>(sm, u, par, step + s);
+      run_unit<ROWS, BANDS>(sm, u, par, step + s);
     }
     if (s + 1 < nsteps && !grid_barrier(sync, gridDim.x, status, &flag)) return;
   }
@@ -125,12 +133,15 @@ __global__ void __launch_bounds__(kCtaThreads, 7)
 
 int32_t build_table(const PpfMember* members, int32_t n, const PpfTiling* tiling,
                     std::vector<MemberDev>* out, std::vector<int>* units, long long* n_items,
-                    int* rows) {
+                    int* rows, int* bands) {
   if (!members || n < 1 || n > (1 << 20))
     return fail(PPF_ERR_INVALID, "ensemble needs 1..2^20 members (got %d)", n);
   *rows = tiling && tiling->tile_y ? tiling->tile_y : 2;
   if (*rows != 2 && *rows != 4 && *rows != 8)
     return fail(PPF_ERR_INVALID, "ensemble rows per warp must be 2, 4 or 8");
+  *bands = tiling && tiling->tile_x ? tiling->tile_x : 4;
+  if (*bands != 1 && *bands != 4)
+    return fail(PPF_ERR_INVALID, "ensemble bands per warp (tile_x) must be 1 or 4");
   if (tiling && tiling->depth > 1)
     return fail(PPF_ERR_UNSUPPORTED, "ensemble steps advance one step per pass");
   const bool bulk = !(tiling && (tiling->flags & PPF_TILING_FULL_EVAL));
@@ -176,7 +187,8 @@ int32_t build_table(const PpfMember* members, int32_t n, const PpfTiling* tiling
     d.item_begin = items;
     d.items = (long long)d.strips * ((s.ny + *rows - 1) / *rows);
     d.unit_begin = (long long)units->size();
-    const long long nu = (d.items + kWarpsPerCta - 1) / kWarpsPerCta;
+    const long long per_unit = (long long)kWarpsPerCta * *bands;
+    const long long nu = (d.items + per_unit - 1) / per_unit;
     if ((long long)units->size() + nu > (1LL << 31) - 1)
       return fail(PPF_ERR_INVALID, "ensemble too large");
     units->insert(units->end(), (size_t)nu, i);
@@ -190,11 +202,11 @@ struct Occupancy {
   int sms = 0, per_sm = 0;
 };
 
-template <int ROWS>
+template <int ROWS, int BANDS>
 cudaError_t launch_ensemble(const PpfEnsemblePlan* p, int parity, uint64_t step,
                             const uint64_t* step_base, int nsteps, unsigned* sync, int* status,
                             bool pdl, cudaStream_t s) {
-  auto kern = ensemble_kernel<ROWS>;
+  auto kern = ensemble_kernel<ROWS, BANDS>;
   static Occupancy occ[SymbolCache::kMaxDevices];
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
@@ -255,12 +267,19 @@ int32_t run(const PpfEnsemblePlan* plan, int32_t parity, uint64_t step,
   cudaStream_t s = (cudaStream_t)stream;
   unsigned* sy = (unsigned*)sync;
   cudaError_t e;
-  switch (plan->rows) {
-    case 2: e = launch_ensemble<2>(plan, parity, step, step_base, nsteps, sy, status, pdl, s); break;
-    case 4: e = launch_ensemble<4>(plan, parity, step, step_base, nsteps, sy, status, pdl, s); break;
-    case 8: e = launch_ensemble<8>(plan, parity, step, step_base, nsteps, sy, status, pdl, s); break;
-    default: return fail(PPF_ERR_INVALID, "plan rows %d invalid", plan->rows);
+#define PPF_ENS(R, B) launch_ensemble<R, B>(plan, parity, step, step_base, nsteps, sy, status, pdl, s)
+  const int key = plan->rows * 10 + plan->bands;
+  switch (key) {
+    case 21: e = PPF_ENS(2, 1); break;
+    case 24: e = PPF_ENS(2, 4); break;
+    case 41: e = PPF_ENS(4, 1); break;
+    case 44: e = PPF_ENS(4, 4); break;
+    case 81: e = PPF_ENS(8, 1); break;
+    case 84: e = PPF_ENS(8, 4); break;
+    default: return fail(PPF_ERR_INVALID, "plan rows %d / bands %d invalid", plan->rows,
+                         plan->bands);
   }
+#undef PPF_ENS
   if (e != cudaSuccess) return fail(PPF_ERR_CUDA, "ensemble launch: %s", cudaGetErrorString(e));
   return PPF_OK;
 }
@@ -279,8 +298,8 @@ int32_t ppf_ensemble_plan_bytes(const PpfMember* members, int32_t n, const PpfTi
   std::vector<MemberDev> t;
   std::vector<int> units;
   long long items;
-  int rows;
-  int32_t rc = build_table(members, n, tiling, &t, &units, &items, &rows);
+  int rows, bands;
+  int32_t rc = build_table(members, n, tiling, &t, &units, &items, &rows, &bands);
   if (rc) return rc;
   *bytes = units_offset(n) + units.size() * sizeof(int);
   return PPF_OK;
@@ -294,8 +313,8 @@ int32_t ppf_ensemble_build(const PpfMember* members, int32_t n, const PpfTiling*
   std::vector<MemberDev> t;
   std::vector<int> units;
   long long items;
-  int rows;
-  int32_t rc = build_table(members, n, tiling, &t, &units, &items, &rows);
+  int rows, bands;
+  int32_t rc = build_table(members, n, tiling, &t, &units, &items, &rows, &bands);
   if (rc) return rc;
   const size_t need = units_offset(n) + units.size() * sizeof(int);
   if (bytes < need) return fail(PPF_ERR_INVALID, "table needs %zu bytes, got %zu", need, bytes);
@@ -311,6 +330,8 @@ int32_t ppf_ensemble_build(const PpfMember* members, int32_t n, const PpfTiling*
   plan->n_items = items;
   plan->n_members = n;
   plan->rows = rows;
+  plan->bands = bands;
+  plan->reserved = 0;
   plan->n_units = (int64_t)units.size();
   return PPF_OK;
 }

@@ -323,9 +323,13 @@ __global__ void __launch_bounds__(32 * kMWarps, (MarchMinBlocks<T, K>::value))
     if (bc.type[1] == PPF_BC_DIRCHLET && (unsigned)(xl + e) >= (unsigned)nx) fix_x |= 1u << e;
   const bool fix_y = bc.type[0] == PPF_BC_DIRCHLET;
 
+  // blocks whose rows lie in the grid come by TMA (a window over the left
+  // or right edge included: the columns outside the grid arrive zero-filled
+  // and are rewritten below); the few blocks of rows outside the grid are
+  // filled by the warp
   auto tma_block = [&](int b) {
     const int r0 = ylo + b * kMRows;
-    return xin && r0 >= 0 && r0 + kMRows <= ny;
+    return r0 >= 0 && r0 + kMRows <= ny;
   };
   auto issue = [&](int b) {
     const int slot = b % kMSlots;
@@ -367,9 +371,20 @@ __global__ void __launch_bounds__(32 * kMWarps, (MarchMinBlocks<T, K>::value))
         return;
       }
       phase ^= 1u << slot;
+      if (!xin) {  // the window's cells outside the grid, by the boundary rule
+        T* dst = ring + slot * SLOT;
+        const int r0 = ylo + b * kMRows;
+#pragma unroll
+        for (int e = 0; e < V; ++e)
+          if ((unsigned)(xl + e) >= (unsigned)nx)
+            for (int r = 0; r < kMRows; ++r)
+              dst[r * WW + lane * V + e] = fetch<T, 2>(in, g, bc, 0, r0 + r, xl + e);
+        __syncwarp();
+      }
     }
     const T* src = ring + slot * SLOT;
-#pragma unroll 1
+    // two rows per iteration: the pipeline registers rotate without copies
+#pragma unroll 2
     for (int r = 0; r < kMRows; ++r) {
       const int y = ylo + b * kMRows + r;  // row of step 0 entering the pipeline
       // (rows past yhi only feed outputs below the segment, never stored)

@@ -5,8 +5,8 @@ ordinary engine instances (each with its own fields, parameters and grid
 size) whose device buffers are stepped by ONE persistent cooperative launch
 per chunk of `graph_chunk` steps (`ppf_ensemble_run_f32`: the CTAs meet at a
 bounded grid barrier between steps), captured in a CUDA graph. The rows per
-warp band are picked by the autotuner for the ensemble's mix of member
-sizes (cached per mix and device). Afterwards each member is an ordinary
+warp band and the bands per warp are picked by the autotuner for the
+ensemble's mix of member sizes (cached per mix and device). Afterwards each member is an ordinary
 engine again: retrieve_fields_from_GPU, save_simulation etc. work on it.
 
 `make_config_ensemble` builds the benchmark ensemble: n members whose square
@@ -100,10 +100,10 @@ def partition_members(cells, world: int) -> list:
 class Ensemble:
     """Steps a list of 2-D float32 Warren1995GB300 / CahnAllenGB300 engines
     together. All members must be at the same time step. rows=None picks the
-    rows per warp band with the autotuner."""
+    rows per warp band and the bands per warp with the autotuner."""
 
     def __init__(self, sims, rows: int | None = None, graph_chunk: int = 64, pdl: bool = True,
-                 bulk_shortcut: bool = True, use_graph: bool = True):
+                 bulk_shortcut: bool = True, use_graph: bool = True, bands: int | None = None):
         if not sims:
             raise ValueError("empty ensemble")
         self.sims = list(sims)
@@ -137,8 +137,13 @@ class Ensemble:
             self.status = torch.zeros(1, dtype=torch.int32, device=dev)
         self.status_host = torch.zeros(1, dtype=torch.int32, pin_memory=True)
         self.graphs = {}
-        self.rows = int(rows) if rows else self._tune_rows()
-        self.tiling = tiling_struct(1, (0, self.rows), pdl, self._flags)
+        if rows and bands:
+            self.rows, self.bands = int(rows), int(bands)
+        elif rows:
+            self.rows, self.bands = int(rows), 4
+        else:
+            self.rows, self.bands = self._tune_tiling()
+        self.tiling = tiling_struct(1, (self.bands, self.rows), pdl, self._flags)
         self._build()
 
     @property
@@ -174,9 +179,10 @@ class Ensemble:
         from . import autotune
         return autotune.make_key("Ensemble", (len(mix), self.cells), torch.float32, digest)
 
-    def _tune_rows(self) -> int:
-        """Rows per warp band: each candidate times a chunk of steps on
-        scratch copies of every member's buffers (the members are untouched)."""
+    def _tune_tiling(self) -> tuple[int, int]:
+        """Rows per warp band and bands per warp: each candidate times a chunk
+        of steps on scratch copies of every member's buffers (the members are
+        untouched)."""
         from . import autotune
         with torch.cuda.stream(self.stream):
             for s in self.sims:
@@ -186,7 +192,7 @@ class Ensemble:
         steps = 8
 
         def measure(cand):
-            tiling = tiling_struct(1, (0, cand["rows"]), self._pdl, self._flags)
+            tiling = tiling_struct(1, (cand["bands"], cand["rows"]), self._pdl, self._flags)
             members = (L.PpfMember * len(self.sims))(
                 *[self._member(s, bufs) for s, bufs in zip(self.sims, scratch)])
             n = len(self.sims)
@@ -204,9 +210,10 @@ class Ensemble:
 
             return autotune.time_candidate(run, self.stream, warmup=1, reps=3) / steps
 
-        best = autotune.pick(self._mix_key(), [{"rows": r} for r in (2, 4, 8)], measure)
+        cands = [{"rows": r, "bands": b} for r in (2, 4, 8) for b in (1, 4)]
+        best = autotune.pick(self._mix_key(), cands, measure)
         del scratch
-        return int(best["rows"])
+        return int(best["rows"]), int(best["bands"])
 
     def _members_key(self) -> bytes:
         """Every member's parameter struct as bytes: the plan (and so every

@@ -21,14 +21,14 @@ def _snapshot(sims):
     return [[f.get_cells().copy() for f in s.fields] for s in sims]
 
 
-@pytest.mark.parametrize("rows", [2, 4, 8])
-def test_ensemble_matches_members_stepped_alone(cuda, rows):
+@pytest.mark.parametrize("rows,bands", [(2, 4), (4, 1), (8, 4), (2, 1)])
+def test_ensemble_matches_members_stepped_alone(cuda, rows, bands):
     from pyphasefield_gb300.ensemble import Ensemble
     a = _members()
     b = _members()
     for s in b:
         s.user_data["tile"] = (0, rows)
-    ens = Ensemble(a, rows=rows, graph_chunk=8)
+    ens = Ensemble(a, rows=rows, bands=bands, graph_chunk=8)
     ens.simulate(40)
     ens.retrieve_fields_from_GPU()
     for s in b:
@@ -142,10 +142,11 @@ def test_ensemble_rows_autotuned_and_cached(cuda, tmp_path, monkeypatch):
     sims = _members(5)
     init = _snapshot(sims)
     ens = Ensemble(sims, graph_chunk=4)
-    assert ens.rows in (2, 4, 8)
+    assert ens.rows in (2, 4, 8) and ens.bands in (1, 4)
     cache = json.loads((tmp_path / "tune.json").read_text())
     entry = next(iter(cache.values()))
-    assert entry["config"] == {"rows": ens.rows} and len(entry["tried"]) == 3
+    assert entry["config"] == {"rows": ens.rows, "bands": ens.bands}
+    assert len(entry["tried"]) == 6
     # tuning ran on scratch copies: the members still hold their initial
     # (float32-rounded) state
     ens.retrieve_fields_from_GPU()
@@ -153,4 +154,5 @@ def test_ensemble_rows_autotuned_and_cached(cuda, tmp_path, monkeypatch):
         for f0, f in zip(m, s.fields):
             np.testing.assert_array_equal(f0.astype(np.float32), f.get_cells())
     # a second ensemble of the same mix takes the cached choice
-    assert Ensemble(_members(5), graph_chunk=4).rows == ens.rows
+    again = Ensemble(_members(5), graph_chunk=4)
+    assert (again.rows, again.bands) == (ens.rows, ens.bands)
