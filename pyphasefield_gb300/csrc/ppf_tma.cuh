@@ -65,6 +65,25 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity,
   return false;
 }
 
+// Bounded wait by polling (mbarrier.test_wait: no suspension between polls),
+// for warps that wait on their own loads and have little else to hide the
+// latency with; gives up after `limit` polls.
+__device__ __forceinline__ bool mbar_wait_poll(uint64_t* bar, uint32_t parity,
+                                               uint32_t limit = kWaitLimit * 4) {
+  const uint32_t a = smem_addr(bar);
+  for (uint32_t i = 0; i < limit; ++i) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
 // 2-D / 3-D tensor tile load into shared memory, completing on `bar`.
 // The innermost coordinate times the element size must be a multiple of 16.
 __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y,

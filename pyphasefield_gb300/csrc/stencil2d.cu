@@ -359,7 +359,7 @@ __global__ void __launch_bounds__(32 * kMWarps, (MarchMinBlocks<T, K>::value))
   for (int b = 0; b < nb; ++b) {
     const int slot = b % kMSlots;
     if (tma_block(b)) {
-      if (!mbar_wait(&bar[slot], (phase >> slot) & 1u)) {
+      if (!mbar_wait_poll(&bar[slot], (phase >> slot) & 1u)) {
         if (lane == 0) {
           atomicOr(status, PPF_STATUS_TIMEOUT);
           // let every load still in flight land before the warp leaves
@@ -555,6 +555,14 @@ int32_t run2d(Op op, double dx, const PpfGrid* grid, const PpfBoundary* b,
   if (rc) return rc;
   if (!in || !out) return fail(PPF_ERR_INVALID, "NULL field pointer");
   if (in == out) return fail(PPF_ERR_INVALID, "in and out must differ");
+  const int depth = tiling && tiling->depth ? tiling->depth : 1;
+  if (depth > 1 && !(tiling && tiling->tile_x)) {
+    if (depth > 8) return fail(PPF_ERR_INVALID, "depth=%d not in [1, 8]", depth);
+    Bc<T> bcm;
+    if ((rc = make_bc<T>(b, g, dx, 1, depth, &bcm))) return rc;
+    return run_march<T, Op>(op, g, bcm, in, out, depth, tiling->tile_y, tiling->pdl != 0,
+                            (cudaStream_t)stream);
+  }
   Tile2d t;
   if ((rc = plan_tile2d<T>(tiling, &t))) return rc;
   Bc<T> bc;
@@ -571,9 +579,6 @@ int32_t run2d(Op op, double dx, const PpfGrid* grid, const PpfBoundary* b,
                         (cudaStream_t)stream, pdl, op, g, bc, in, out, vec_ok));
     return PPF_OK;
   }
-  if (!(tiling && tiling->tile_x)) return run_march<T, Op>(op, g, bc, in, out, t.k,
-                                                          tiling ? tiling->tile_y : 0, pdl,
-                                                          (cudaStream_t)stream);
   auto kern = stencil2d_tb_kernel<T, Op>;
   PPF_TRY_CUDA(allow_smem(kern, t.smem));
   dim3 grid_dim((g.n[1] + t.tx - 1) / t.tx, (g.n[0] + t.ty - 1) / t.ty);
