@@ -441,6 +441,9 @@ SWEEP = {
     "cahn_hilliard_384": ("cahn_hilliard", (384, 384, 384), 1, 100),
     "cahn_hilliard_512": ("cahn_hilliard", (512, 512, 512), 1, 100),
     "ensemble_64": ("ensemble", None, 1, 2000),
+    # the same 64 members stepped one after another, each as its own engine
+    # (its own kernel launches and CUDA graphs): what batching saves
+    "ensemble_64_solo": ("ensemble_solo", None, 1, 2000),
     # implicit / Crank-Nicolson diffusion (periodic line solves or the full
     # system), D dt / dx^2 = 5
     "implicit_adi_8192": ("diffusion", (8192, 8192), 1, 50,
@@ -565,6 +568,26 @@ def time_sweep_case(name, steps=None):
     steps = steps or case_steps
     extra = SWEEP[name][4] if len(SWEEP[name]) > 4 else None
     rng = np.random.default_rng(0)
+    if model == "ensemble_solo":
+        from pyphasefield_gb300.ensemble import make_config_ensemble
+        sims = make_config_ensemble(n=64, seed=0, graph_chunk=100)
+        for sm in sims:
+            sm.simulate(100)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for sm in sims:
+            sm.simulate(steps)
+            sm.synchronize()
+        sec = time.perf_counter() - t0
+        cells = sum(sm._ppf_grid.cells for sm in sims)
+        byts = sum(sm._ppf_grid.cells * (16 if len(sm.fields) == 2 else 8) for sm in sims)
+        del sims
+        return {"sweep": name, "model": model, "grid": "config ensemble, members alone",
+                "steps": steps, "cells": cells, "cell_updates_per_s": cells * steps / sec,
+                "ms_per_step": 1e3 * sec / steps, "algorithmic_bytes_per_step": byts,
+                "achieved_gbs": byts * steps / sec / 1e9, "peak_gbs": peak,
+                "peak_source": peak_kind, "frac": byts * steps / sec / 1e9 / peak,
+                "timing": "host wall clock, members one after another"}
     if model == "ensemble":
         from pyphasefield_gb300.ensemble import Ensemble, make_config_ensemble
         sims = make_config_ensemble(n=64, seed=0)

@@ -83,26 +83,66 @@ __device__ __forceinline__ void ac_band(float a, float b, const Geo& g, const Bc
 // A unit is BANDS bands per warp; warp w of the CTA takes bands w, w + 4,
 // ... of the unit's 4 BANDS (the CTA's warps work on neighbouring strips at
 // any moment).
+// Warren1995 members: the next band's rows are requested before the current
+// band is computed, so a warp's loads overlap its own arithmetic.
 template <int ROWS, int BANDS>
 __device__ __forceinline__ void run_unit(const MemberDev& m, long long unit, int parity,
                                          uint64_t step) {
   const long long first = (unit - m.unit_begin) * (kWarpsPerCta * BANDS);
+  if (m.model == PPF_MODEL_WARREN1995) {
+    long long local = first + threadIdx.y;
+    if (local >= m.items) return;  // whole warp
+    float bp[ROWS + 2], bcv[ROWS + 2];
+    int xs = (int)(local % m.strips) * w95::kStrip - 1;
+    int y0 = (int)(local / m.strips) * ROWS;
+    w95::band_load<float, ROWS, true>(m.g, m.bc, m.phi[parity], m.c[parity], xs, y0, bp, bcv);
+#pragma unroll 1
+    for (int j = 0; j < BANDS; ++j) {
+      const long long nxt = local + kWarpsPerCta;
+      const bool more = j + 1 < BANDS && nxt < m.items;
+      float np[ROWS + 2], ncv[ROWS + 2];
+      int nxs = 0, ny0 = 0;
+      if (more) {
+        nxs = (int)(nxt % m.strips) * w95::kStrip - 1;
+        ny0 = (int)(nxt / m.strips) * ROWS;
+        w95::band_load<float, ROWS, true>(m.g, m.bc, m.phi[parity], m.c[parity], nxs, ny0, np,
+                                          ncv);
+      }
+      w95::band_compute<float, ROWS>(m.w, m.g, m.phi[1 - parity], m.c[1 - parity], m.seed,
+                                     step, xs, y0, bp, bcv);
+      if (!more) return;
+#pragma unroll
+      for (int r = 0; r < ROWS + 2; ++r) {
+        bp[r] = np[r];
+        bcv[r] = ncv[r];
+      }
+      local = nxt;
+      xs = nxs;
+      y0 = ny0;
+    }
+    return;
+  }
 #pragma unroll 1
   for (int j = 0; j < BANDS; ++j) {
     const long long local = first + j * kWarpsPerCta + threadIdx.y;
     if (local >= m.items) return;  // past the member's last band (whole warp)
     const int xs = (int)(local % m.strips) * w95::kStrip - 1;
     const int y0 = (int)(local / m.strips) * ROWS;
-    if (m.model == PPF_MODEL_WARREN1995)
-      w95::band<float, ROWS, true>(m.w, m.g, m.bc, m.phi[parity], m.c[parity],
-                                   m.phi[1 - parity], m.c[1 - parity], m.seed, step, xs, y0);
-    else
-      ac_band<ROWS>(m.ac_a, m.ac_b, m.g, m.bc, m.phi[parity], m.phi[1 - parity], xs, y0);
+    ac_band<ROWS>(m.ac_a, m.ac_b, m.g, m.bc, m.phi[parity], m.phi[1 - parity], xs, y0);
   }
 }
 
+// Resident CTAs per SM asked of the register allocator: the member's
+// constants come from shared memory into registers (a single grid's kernel
+// takes them as kernel parameters), so the band needs 80 (two rows) to 96
+// registers a thread without spills.
+template <int ROWS>
+struct EnsMinBlocks {
+  static constexpr int value = ROWS == 2 ? 6 : 5;
+};
+
 template <int ROWS, int BANDS>
-__global__ void __launch_bounds__(kCtaThreads, 4)
+__global__ void __launch_bounds__(kCtaThreads, (EnsMinBlocks<ROWS>::value))
     ensemble_kernel(const MemberDev* __restrict__ members, const int* __restrict__ unit_member,
                     long long n_units, int parity, uint64_t step,
                     const uint64_t* __restrict__ step_base, int nsteps, unsigned* sync,

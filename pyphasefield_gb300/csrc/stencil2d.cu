@@ -476,16 +476,16 @@ int32_t plan_tile2d(const PpfTiling* t, Tile2d* out) {
   return PPF_OK;
 }
 
-// Segment rows per warp: the launch fills exactly one wave of resident
-// CTAs (a partial second wave would leave most SMs idle at the end of the
-// pass), unless that makes segments shorter than 8K rows, where the 2K halo
-// rows re-read per segment would cost too much.
+// Segment rows per warp: short enough for about four waves of CTAs, so
+// that CTAs that run slower (their rows sit in the other die's memory, or
+// they hold the grid's edges) are balanced by the scheduler; one wave of long
+// segments measured 40 % slower. Between 16K rows (the 2K halo rows re-read
+// per segment cost 12 %) and 64K rows.
 inline int march_segment(int ny, int nstrips, int K, long resident) {
   const long cols = (nstrips + kMWarps - 1) / kMWarps;
-  long nseg = resident / cols;
-  if (nseg < 1) nseg = 1;
-  long seg = (ny + nseg - 1) / nseg;
-  if (seg < 8L * K) seg = 8L * K;
+  long seg = ((long)ny * cols + 4 * resident - 1) / (4 * resident);
+  if (seg < 16L * K) seg = 16L * K;
+  if (seg > 64L * K) seg = 64L * K;
   seg = (seg + kMRows - 1) / kMRows * kMRows;
   const long full = (ny + kMRows - 1) / kMRows * kMRows;
   return (int)(seg < full ? seg : full);

@@ -101,9 +101,11 @@ def _stencil_candidates(sim) -> list:
     """Diffusion / Allen-Cahn launch shapes: temporal depth x tile (2-D),
     tile and planes per CTA along z (3-D)."""
     if len(sim._ppf_grid.kshape) == 2:
-        # depth 1: the warp-strip kernel; depth > 1 without a tile: the
-        # marching kernel; with a tile: the shared-memory tile kernel
+        # depth 1: the warp-strip kernel; depth > 1 without a tile or with
+        # (0, rows): the marching kernel (segments of `rows`); with a tile:
+        # the shared-memory tile kernel
         return [{"temporal_depth": d, "tile": None} for d in (1, 2, 4, 8)] + \
+            [{"temporal_depth": d, "tile": (0, 32 * d * f)} for d in (2, 4, 8) for f in (1, 4)] + \
             [{"temporal_depth": d, "tile": t} for d in (1, 2, 4, 8)
              for t in ((128, 32), (64, 32), (256, 16), (128, 16))]
     return [{"tile": (32, 32), "zchunk": z} for z in (8, 12, 16, 24)] + \

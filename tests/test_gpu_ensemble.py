@@ -93,7 +93,7 @@ def test_autotune_picks_and_caches(cuda, tmp_path, monkeypatch):
     entry = next(iter(cache.values()))
     assert entry["config"]["temporal_depth"] == sim.user_data["temporal_depth"]
     from pyphasefield_gb300.engines.models import _stencil_candidates
-    assert len(entry["tried"]) == len(_stencil_candidates(sim)) == 20
+    assert len(entry["tried"]) == len(_stencil_candidates(sim)) == 26
     ref = restate.run_single("diffusion", c0, 16, "PERIODIC", 1.0, 0.2, D=1.0)
     assert rel_l2(sim.fields[0].get_cells(), ref) < 1e-5  # tuning did not change the state
 
