@@ -756,6 +756,11 @@ def profile_case(name: str):
     diff3d384   Diffusion 3-D 384^3 periodic, 5 steps
     ensemble64  the 64-member ensemble benchmark (1.56e7 cells), five persistent launches of
                 8 steps
+    tb4096      Diffusion 2-D 4096^2, depth 4 on 128 x 32 shared-memory tiles, 20 steps
+    reduce4096  five FP64 sums of a 4096^2 float field (ppf_reduce_sum_f32)
+    acfull2048  implicit Allen-Cahn, full 2-D system on 2048^2 (Chebyshev), fp64, 2 steps
+    acminres1024  the same beyond the Chebyshev bound (16 W M dt = 7.3, an indefinite
+                system: MINRES in one persistent launch) on 1024^2, fp64, 2 steps
     diff8192    Diffusion 2-D 8192^2 periodic, 5 passes of PPF_DEPTH (default 4) steps: the
                 marching temporal-blocking kernel on 512 MiB of fields
     diff16384   Diffusion 2-D 16384^2 periodic, 5 steps (2 GiB of fields: beyond L2)
@@ -795,6 +800,45 @@ def profile_case(name: str):
         ens.simulate(40)
         ens.synchronize()
         return
+    elif name == "tb4096":
+        sim = DiffusionGB300(dimensions=[4096, 4096], dx=1.0, dt=0.2,
+                             boundary_conditions="PERIODIC",
+                             user_data={"D": 1.0, "use_graph": False, "temporal_depth": 4,
+                                        "tile": (128, 32)})
+        sim.initialize_fields_and_imported_data()
+        sim.fields[0].data[1:-1, 1:-1] = 0.5 + 0.01 * rng.standard_normal((4096, 4096))
+        sim.simulate(20)
+    elif name == "reduce4096":
+        import ctypes as C
+        from pyphasefield_gb300 import _lib as L
+        from pyphasefield_gb300.device import DeviceGrid
+        g = DeviceGrid((4096, 4096), torch.float32, torch.device("cuda"))
+        x = g.empty()
+        x.uniform_()
+        n = C.c_size_t()
+        L.call("ppf_reduce_scratch_bytes", C.byref(g.grid), C.byref(n))
+        scratch = torch.empty(n.value, dtype=torch.uint8, device="cuda")
+        out = torch.zeros(1, dtype=torch.float64, device="cuda")
+        sp = C.c_void_p(torch.cuda.current_stream().cuda_stream)
+        for _ in range(5):
+            L.call("ppf_reduce_sum_f32", C.c_void_p(x.data_ptr()), C.byref(g.grid),
+                   C.c_void_p(out.data_ptr()), C.c_void_p(scratch.data_ptr()), n, sp)
+    elif name in ("acfull2048", "acminres1024"):
+        from pyphasefield_gb300 import CahnAllenGB300
+        n = 2048 if name == "acfull2048" else 1024
+        full = name == "acfull2048"
+        sim = CahnAllenGB300(dimensions=[n, n], dx=1.0 if full else 3.0, dt=1.0 if full else 0.5,
+                             boundary_conditions="PERIODIC",
+                             user_data={"use_graph": False, "solver": "implicit", "adi": False,
+                                        "gmres": True, "M": 0.1 if full else 0.7,
+                                        "W": 1.0 if full else 1.3,
+                                        "epsilon": 1.0 if full else 1.1, "precision": "fp64"})
+        sim.initialize_fields_and_imported_data()
+        if full:
+            sim.fields[0].data[1:-1, 1:-1] = rng.random((n, n))
+        else:  # half the cells at phi = 0.75: an indefinite system (MINRES)
+            sim.fields[0].data[1:-1, 1:-1] = np.where(rng.random((n, n)) > 0.5, 0.75, 0.2)
+        sim.simulate(2)
     elif name == "diff8192":
         depth = int(os.environ.get("PPF_DEPTH", "4"))
         sim = DiffusionGB300(dimensions=[8192, 8192], dx=1.0, dt=0.2,

@@ -400,6 +400,15 @@ int32_t ppf_ncgpu_tables_f32(const PpfNcgpuParams* p, const PpfGrid* g, const fl
                              double* tables, void* stream);
 int32_t ppf_ncgpu_tables_f64(const PpfNcgpuParams* p, const PpfGrid* g, const double* temperature,
                              double* tables, void* stream);
+/* temperature += dT on every interior cell (stream-ordered): the
+ * per-step rise of a LINEAR_GRADIENT temperature with dT/dt, dT = dTdt * dt
+ * (update_thermal_gradient_2D_kernel, ppf_gpu_utils.py:326-334, which
+ * Simulation.simulate runs after every engine step, simulation.py:262-266).
+ * Tables from ppf_ncgpu_tables_* do not follow it: step without them. */
+int32_t ppf_ncgpu_temperature_advance_f32(const PpfGrid* g, float* temperature, double dT,
+                                          void* stream);
+int32_t ppf_ncgpu_temperature_advance_f64(const PpfGrid* g, double* temperature, double dT,
+                                          void* stream);
 
 /* ---- batched ensemble ------------------------------------------------- */
 

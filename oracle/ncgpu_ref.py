@@ -494,12 +494,20 @@ def _update(P, Q1, Q4, CC, TT, GL, GS, MC, DF, p, ebar2, eqbar2, idx, noise=None
 
 
 def run(fields, T, steps, p, tdb, seed=0, bc="PERIODIC", noise_scale=1.0, step0=0,
-        variant="NCGPU"):
+        variant="NCGPU", dT_step=0.0):
+    """`steps` steps from absolute step index step0. dT_step: the temperature
+    rise per step of a LINEAR_GRADIENT temperature with dT/dt (dTdt * dt):
+    every step reads T, then T += dT_step on every cell
+    (Simulation.simulate, simulation.py:262-266, with
+    update_thermal_gradient_2D_kernel, ppf_gpu_utils.py:326-334)."""
     f = [np.array(a, dtype=np.float64) for a in fields]
+    T = np.array(T, dtype=np.float64)
     for s in range(steps):
         if variant == "NCGPU_new":
             nz = noise_new(seed, step0 + s, f[0].shape, len(f) - 3)
         else:
             nz = noise_normal(seed, step0 + s, f[0].shape) if noise_scale else np.zeros(f[0].shape)
         f = step(f, T, p, tdb, nz, bc, noise_scale, variant)
+        if dT_step:
+            T += dT_step
     return f

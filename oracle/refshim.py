@@ -322,13 +322,17 @@ def ncgpu_module(name: str = "NCGPU"):
     return mod
 
 
-def run_ncgpu(phi, q1, q4, c, T, steps: int, p: dict, tdb, noise_fields, bc="PERIODIC"):
+def run_ncgpu(phi, q1, q4, c, T, steps: int, p: dict, tdb, noise_fields, bc="PERIODIC",
+              dT_step=0.0):
     """Drive NComponent_helper_kernel and NComponent_kernel for `steps`
     steps; c is one concentration field (binary) or a list of N - 1 of them.
     noise_fields[s] is the interior N(0,1) field of step s; ghost cells take
     the noise of the cell the boundary rule maps them to. Ghost cells of
     every field and of T follow `bc` (PERIODIC or zero-gradient NEUMANN), as
-    ppf_gpu_utils.apply_boundary_conditions fills them between steps."""
+    ppf_gpu_utils.apply_boundary_conditions fills them between steps.
+    dT_step (dTdt * dt of a LINEAR_GRADIENT temperature): after every step
+    each cell of the padded temperature array rises by it, as
+    update_thermal_gradient_2D_kernel (ppf_gpu_utils.py:326-334) does."""
     mod = ncgpu_module()
     mode = "wrap" if bc == "PERIODIC" else "symmetric"
     pad = lambda a: np.pad(np.asarray(a, dtype=np.float64), 1, mode=mode)  # noqa: E731
@@ -354,6 +358,8 @@ def run_ncgpu(phi, q1, q4, c, T, steps: int, p: dict, tdb, noise_fields, bc="PER
         _NC["queue"] = iter([0.0] * (ny * nx))
         mod.NComponent_kernel(fields, Tp, transfer, out, None, params, c_params)
         f = [out[k, 1:-1, 1:-1].copy() for k in range(len(f))]
+        if dT_step:
+            Tp += dT_step
     _NC["queue"] = None
     return f
 

@@ -167,6 +167,8 @@ SIGNATURES: dict[str, list] = {
     "ppf_ncgpu_step_f64": [C.POINTER(PpfNcgpuParams), PG, PB, P, P, P, P, P, U64, U64, P, P],
     "ppf_ncgpu_tables_f32": [C.POINTER(PpfNcgpuParams), PG, P, P, P],
     "ppf_ncgpu_tables_f64": [C.POINTER(PpfNcgpuParams), PG, P, P, P],
+    "ppf_ncgpu_temperature_advance_f32": [PG, P, C.c_double, P],
+    "ppf_ncgpu_temperature_advance_f64": [PG, P, C.c_double, P],
     "ppf_phase_implicit_scratch_bytes": [PG, I32, C.POINTER(SZ)],
     "ppf_phase_implicit_step_f32": [C.POINTER(PpfImplicitPhaseParams), PG, P, P, P, P, SZ,
                                     C.POINTER(I32), P],

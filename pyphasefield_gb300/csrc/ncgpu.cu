@@ -606,6 +606,34 @@ int32_t ncgpu_step(const PpfNcgpuParams* p, const PpfGrid* grid, const PpfBounda
   return PPF_OK;
 }
 
+// Temperature of a LINEAR_GRADIENT profile that changes in time: every cell
+// rises by dT = dTdt * dt after each step (update_thermal_gradient_2D_kernel,
+// ppf_gpu_utils.py:326-334; Simulation.simulate calls it after each engine
+// step, simulation.py:262-266).
+template <typename T>
+__global__ void __launch_bounds__(256) temperature_advance_kernel(Geo g, T* __restrict__ t, T dT) {
+  pdl_wait();
+  pdl_launch_next();
+  const int nx = g.n[1];
+  for (int r = blockIdx.y; r < g.n[0]; r += gridDim.y)
+    for (int x = blockIdx.x * blockDim.x + threadIdx.x; x < nx; x += gridDim.x * blockDim.x)
+      t[(int64_t)r * g.pitch + x] += dT;
+}
+
+template <typename T>
+int32_t temperature_advance(const PpfGrid* grid, T* t, double dT, void* stream) {
+  clear_error();
+  Geo g;
+  int32_t rc = make_geo(grid, 2, 2, &g);
+  if (rc) return rc;
+  if (!t) return fail(PPF_ERR_INVALID, "temperature is NULL");
+  if (!isfinite(dT)) return fail(PPF_ERR_INVALID, "dT must be finite");
+  const dim3 grid2((g.n[1] + 255) / 256, (unsigned)(g.n[0] < 65535 ? g.n[0] : 65535));
+  PPF_TRY_CUDA(launch(temperature_advance_kernel<T>, grid2, dim3(256), 0, (cudaStream_t)stream,
+                      true, g, t, (T)dT));
+  return PPF_OK;
+}
+
 }  // namespace
 }  // namespace ppf
 
@@ -629,6 +657,15 @@ int32_t ppf_ncgpu_step_f64(const PpfNcgpuParams* p, const PpfGrid* g, const PpfB
                            void* stream) {
   return ncgpu_step<double>(p, g, bc, fields_in, fields_out, temperature, tables, transfer, seed,
                             step, step_base, stream);
+}
+
+int32_t ppf_ncgpu_temperature_advance_f32(const PpfGrid* g, float* temperature, double dT,
+                                          void* stream) {
+  return temperature_advance<float>(g, temperature, dT, stream);
+}
+int32_t ppf_ncgpu_temperature_advance_f64(const PpfGrid* g, double* temperature, double dT,
+                                          void* stream) {
+  return temperature_advance<double>(g, temperature, dT, stream);
 }
 
 int32_t ppf_ncgpu_tables_f32(const PpfNcgpuParams* p, const PpfGrid* g, const float* temperature,

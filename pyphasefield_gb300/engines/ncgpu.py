@@ -13,8 +13,11 @@ noise_scale (1 = the reference's Langevin term on dF/dc, 0 = none).
 dt is the reference's dx^2 / 5 / D_L / 8. precision defaults to "fp64"
 (float32 runs; its threshold branches part from float64 within a few
 steps). Periodic or zero-gradient
-boundaries; the temperature field must be ISOTHERMAL or a LINEAR_GRADIENT
-without dTdt (the device copy of the field is fixed during a run).
+boundaries; the temperature field is ISOTHERMAL or a LINEAR_GRADIENT, with
+or without dTdt: the device copy rises by dTdt * dt after every step, as
+the reference's update_thermal_gradient kernels do (ppf_gpu_utils.py:
+326-334); with dTdt the pure-element energies are evaluated at every step
+instead of once per run.
 """
 from __future__ import annotations
 
@@ -218,9 +221,6 @@ class _NcgpuMixin(GB300Engine):
         t = self._temperature_type
         if self.temperature is None or t not in ("ISOTHERMAL", "LINEAR_GRADIENT"):
             raise ValueError("NCGPU needs an ISOTHERMAL or LINEAR_GRADIENT temperature field")
-        if t == "LINEAR_GRADIENT" and self._dTdt:
-            raise NotImplementedError("NCGPU: a temperature that changes in time (dTdt) is not "
-                                      "supported")
         if self._boundary_conditions_type is None:
             self._boundary_conditions_type = "PERIODIC"
 
@@ -237,14 +237,32 @@ class _NcgpuMixin(GB300Engine):
         ud = self.user_data
         noise = ud.get("noise_c", 1.0) if self.VARIANT else ud.get("noise_scale", 1.0)
         self._nc_params = params_struct(self._ppf_db, ud, self.dx, noise, self.VARIANT)
-        # the temperature is fixed during a run: the pure-element energies of
-        # every cell are evaluated once, after the upload, on the same stream
-        nplanes = 2 * ncomp + int(self._nc_params.nexcess)
-        self._nc_tables = torch.empty((nplanes,) + tuple(g.alloc_shape), dtype=torch.float64,
-                                      device=g.device)
-        L.call(f"ppf_ncgpu_tables_{_F[self._ppf_dtype]}", C.byref(self._nc_params),
-               C.byref(g.grid), ptr(self._nc_temp), ptr(self._nc_tables),
-               C.c_void_p(self._ppf_stream.cuda_stream))
+        self._nc_tables = None
+        if not self._nc_dT():
+            # a temperature fixed during the run: the pure-element energies of
+            # every cell are evaluated once, after the upload, on the same
+            # stream (with dT/dt every step evaluates them at its own T)
+            nplanes = 2 * ncomp + int(self._nc_params.nexcess)
+            self._nc_tables = torch.empty((nplanes,) + tuple(g.alloc_shape),
+                                          dtype=torch.float64, device=g.device)
+            L.call(f"ppf_ncgpu_tables_{_F[self._ppf_dtype]}", C.byref(self._nc_params),
+                   C.byref(g.grid), ptr(self._nc_temp), ptr(self._nc_tables),
+                   C.c_void_p(self._ppf_stream.cuda_stream))
+
+    def _nc_dT(self) -> float:
+        """Temperature rise per step, dTdt * dt (LINEAR_GRADIENT with dT/dt;
+        else 0)."""
+        if self._temperature_type == "LINEAR_GRADIENT" and self._dTdt:
+            return float(self._dTdt) * float(self.dt)
+        return 0.0
+
+    def _ppf_send(self, s):
+        super()._ppf_send(s)
+        # the temperature field too: the host copy is the one that advances
+        # with the step counter between runs
+        if getattr(self, "_nc_temp", None) is not None:
+            self._nc_temp_staging = self._ppf_grid.upload(self._nc_temp,
+                                                          self.temperature.get_cells(), s)
 
     def _ppf_step(self, src, dst, depth, step, step_base, sp):
         fin = (C.c_void_p * len(src))(*[ptr(t) for t in src])
@@ -254,6 +272,11 @@ class _NcgpuMixin(GB300Engine):
                ptr(self._nc_temp), ptr(self._nc_tables), ptr(self._nc_transfer),
                C.c_uint64(int(self.user_data["seed"])),
                C.c_uint64(int(step)), ptr(step_base), sp)
+        dT = self._nc_dT()
+        if dT:
+            # the step read T; then T rises (Simulation.simulate, simulation.py:262-266)
+            L.call(f"ppf_ncgpu_temperature_advance_{_F[self._ppf_dtype]}",
+                   C.byref(self._ppf_grid.grid), ptr(self._nc_temp), C.c_double(dT), sp)
 
 
 class _NcgpuNewMixin(_NcgpuMixin):

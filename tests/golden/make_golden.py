@@ -211,6 +211,7 @@ def main():
     ncgpu_multicomponent()
     ncgpu_excess()
     ncgpu_new()
+    ncgpu_cooling()
 
     dx = 4.6e-8
     prm = dict(restate.WARREN_DEFAULTS)
@@ -331,6 +332,31 @@ def ncgpu_new():
         save(name, meta, **arrays)
 
 
+def ncgpu_cooling():
+    """NCGPU (Engines/NCGPU.py) under a LINEAR_GRADIENT temperature that also
+    changes in time: 2 K per cell along x and -5 K per step (dTdt * dt), the
+    reference's kernels run serially with the temperature raised after every
+    step as update_thermal_gradient_2D_kernel (ppf_gpu_utils.py:326-334)
+    does; no-flux boundaries, Ni-Cu ideal database."""
+    os.environ.setdefault("PPF_REFERENCE_ROOT", "/root/reference/pyphasefield")
+    from oracle import ncgpu_ref
+    tdb = ncgpu_ref.Tdb(HERE / "ncgpu_nicu.tdb")
+    shape, steps, seed = (22, 20), 4, 13
+    p = ncgpu_ref.tdb_params(tdb, 4.6e-6)
+    phi0, q10, q40, c0 = ncgpu_ref.seed_fields(shape, melt_angle=0.1, seed_angle=0.4,
+                                               c0=0.40831)
+    c0 = c0 + np.random.default_rng(20240606).uniform(-1e-3, 1e-3, shape)
+    T = 1576.0 + 2.0 * np.arange(shape[1])[None, :] * np.ones(shape)
+    dT_step = -5.0
+    noise = [ncgpu_ref.noise_normal(seed, s, shape) for s in range(steps)]
+    out = refshim.run_ncgpu(phi0, q10, q40, c0, T, steps, p, tdb, noise, "NEUMANN",
+                            dT_step=dT_step)
+    meta = dict(model="ncgpu", steps=steps, bc="NEUMANN", seed=seed, dx=4.6e-6, T=1576.0,
+                dTdx_per_cell=2.0, dT_step=dT_step, dt=p["dt"], tdb="ncgpu_nicu.tdb")
+    save("ncgpu_cooling", meta, phi0=phi0, q10=q10, q40=q40, c0=c0, T0=T, phi=out[0], q1=out[1],
+         q4=out[2], c=out[3])
+
+
 def phase_indefinite():
     """engine_CahnAllenImplicit2D_GMRES (CahnAllen.py:163-175) beyond the
     diagonal-dominance bound: 16 W M dt = 7.28 >= 4 with half the cells at
@@ -354,6 +380,8 @@ def phase_indefinite():
 if __name__ == "__main__":
     if sys.argv[1:] == ["phase_indefinite"]:
         phase_indefinite()
+    elif sys.argv[1:] == ["ncgpu_cooling"]:
+        ncgpu_cooling()
     elif sys.argv[1:] == ["ncgpu_multicomponent"]:
         ncgpu_multicomponent()
     elif sys.argv[1:] == ["ncgpu_excess"]:

@@ -33,9 +33,11 @@ def params_struct(dx, noise_scale=1.0, tdb=TDB, variant=0):
 
 
 def run_gpu(fields, T, steps, dx, seed, bc, precision, noise_scale=1.0, tdb=TDB, tables=True,
-            variant=0):
+            variant=0, dT_step=0.0):
     """`steps` steps through ppf_ncgpu_step_*; tables: the pure-element
-    energies from ppf_ncgpu_tables_* (False: evaluated in every step)."""
+    energies from ppf_ncgpu_tables_* (False: evaluated in every step);
+    dT_step: the temperature rises by it after every step
+    (ppf_ncgpu_temperature_advance_*)."""
     import torch
     from pyphasefield_gb300 import _lib as L
     shape = fields[0].shape
@@ -60,6 +62,9 @@ def run_gpu(fields, T, steps, dx, seed, bc, precision, noise_scale=1.0, tdb=TDB,
         L.call(f"ppf_ncgpu_step_{sfx}", C.byref(p), C.byref(g), C.byref(b), fin, fout,
                C.c_void_p(temp.data_ptr()), C.c_void_p(None if tab is None else tab.data_ptr()),
                C.c_void_p(transfer.data_ptr()), C.c_uint64(seed), C.c_uint64(k), None, s)
+        if dT_step:
+            L.call(f"ppf_ncgpu_temperature_advance_{sfx}", C.byref(g),
+                   C.c_void_p(temp.data_ptr()), C.c_double(dT_step), s)
         a, o = o, a
     torch.cuda.synchronize()
     return [from_dev(t, kshape, shape) for t in a]
@@ -78,6 +83,45 @@ def test_reference_fixtures(cuda, name, precision, tables):
                   m["bc"], precision, tables=tables, tdb=GOLDEN / m["tdb"])
     for got, key in zip(out, ("phi", "q1", "q4", "c")):
         assert rel_l2(got, z[key]) < TOL[precision], (key, rel_l2(got, z[key]))
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_cooling_reference_fixture(cuda, precision):
+    """A LINEAR_GRADIENT temperature that falls 5 K per step (dT/dt), against
+    the reference's kernels with the temperature raised after every step as
+    its update_thermal_gradient kernel does."""
+    z = np.load(GOLDEN / "ncgpu_cooling.npz")
+    m = json.loads(str(z["meta"]))
+    out = run_gpu([z["phi0"], z["q10"], z["q40"], z["c0"]], z["T0"], m["steps"], m["dx"],
+                  m["seed"], m["bc"], precision, tables=False, dT_step=m["dT_step"])
+    for got, key in zip(out, ("phi", "q1", "q4", "c")):
+        assert rel_l2(got, z[key]) < TOL[precision], (key, rel_l2(got, z[key]))
+
+
+def test_cooling_engine_against_oracle(cuda):
+    """NCGPUGB300 with temperature_type LINEAR_GRADIENT, dTdx and dTdt,
+    through captured graphs: against the oracle with the same per-step rise,
+    and the host temperature field advanced by the same amount."""
+    from pyphasefield_gb300 import NCGPUGB300
+    shape, steps = (30, 28), 12
+    tdb = N.Tdb(TDB)
+    p = N.tdb_params(tdb, 4.6e-6)
+    dTdt = -2.0 / p["dt"]  # -2 K per step
+    sim = NCGPUGB300(dimensions=list(shape), dx=4.6e-6, tdb_path=str(TDB),
+                     temperature_type="LINEAR_GRADIENT", initial_T=1578.0, dTdx=3000.0,
+                     dTdt=dTdt, boundary_conditions="NEUMANN",
+                     user_data={"seed": 4, "sim_type": "seed", "graph_chunk": 4,
+                                "initial_concentration_array": [0.40831]})
+    sim.initialize_fields_and_imported_data()
+    T0 = sim.temperature.get_cells().copy()
+    init = [f.get_cells().copy() for f in sim.fields]
+    sim.simulate(steps)
+    sim.retrieve_fields_from_GPU()
+    ref = N.run(init, T0, steps, p, tdb, seed=4, bc="NEUMANN", dT_step=dTdt * sim.dt)
+    for f, r, key in zip(sim.fields, ref, ("phi", "q1", "q4", "c")):
+        assert rel_l2(f.get_cells(), r) < 1e-8, (key, rel_l2(f.get_cells(), r))
+    np.testing.assert_allclose(sim.temperature.get_cells(), T0 + steps * dTdt * sim.dt,
+                               rtol=1e-12)
 
 
 @pytest.fixture(scope="module")

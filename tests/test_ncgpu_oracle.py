@@ -34,6 +34,26 @@ def test_oracle_matches_reference_kernels(name):
         assert np.abs(got - ref).max() <= tol * max(1.0, np.abs(ref).max()), key
 
 
+def test_oracle_matches_reference_kernels_under_cooling():
+    """A temperature falling 5 K per step (LINEAR_GRADIENT with dT/dt): the
+    oracle raises T after every step as the reference's
+    update_thermal_gradient kernel does, and reproduces the reference's run."""
+    z = np.load(GOLDEN / "ncgpu_cooling.npz")
+    m = json.loads(str(z["meta"]))
+    tdb = N.Tdb(GOLDEN / m["tdb"])
+    p = N.tdb_params(tdb, m["dx"])
+    assert p["dt"] == m["dt"]
+    out = N.run([z["phi0"], z["q10"], z["q40"], z["c0"]], z["T0"], m["steps"], p, tdb,
+                seed=m["seed"], bc=m["bc"], dT_step=m["dT_step"])
+    for got, key, tol in zip(out, ("phi", "q1", "q4", "c"), (1e-12, 1e-12, 1e-12, 1e-8)):
+        ref = z[key]
+        assert np.abs(got - ref).max() <= tol * max(1.0, np.abs(ref).max()), key
+    # the cooling matters: without it the run parts from the reference's
+    still = N.run([z["phi0"], z["q10"], z["q40"], z["c0"]], z["T0"], m["steps"], p, tdb,
+                  seed=m["seed"], bc=m["bc"])
+    assert np.abs(still[0] - z["phi"]).max() > 1e-6
+
+
 def test_tdb_reader_matches_oracle_evaluation():
     db, tdb = Database(TDB), N.Tdb(TDB)
     assert db.elements == tdb.elements == ["CU", "NI"]
