@@ -4,6 +4,8 @@
 // shuffles into one double in caller-provided scratch; pass 2 sums the
 // partials in one CTA. The reference has no diagnostics; these are the
 // conservation and energy sums the precision split keeps in double.
+#include <type_traits>
+
 #include "ppf_common.cuh"
 
 namespace ppf {
@@ -70,16 +72,37 @@ __device__ __forceinline__ double cell_term(EnergyOp, const T* __restrict__ x,
   return k.w * f + k.half_kappa_over_dx2 * grad2;
 }
 
+// Float sums: each thread carries its running sum as an unevaluated pair of
+// floats (s, c), updated with Knuth's TwoSum (six FP32 additions, exact:
+// s + x = t + e with t = fl(s + x)), and turns it into a double once at the
+// end. The pair holds the thread's partial sum to about 2^-48 relative, as
+// a double accumulator would, without an FP64 operation per element (the
+// GB300's FP64 rate bounded the double accumulation at 0.14 of the copy
+// peak).
+struct Pair {
+  float s = 0.f, c = 0.f;
+  __device__ __forceinline__ void add(float x) {
+    const float t = s + x;
+    const float z = t - s;
+    const float e = (s - (t - z)) + (x - z);
+    s = t;
+    c += e;
+  }
+  __device__ __forceinline__ double value() const { return (double)s + (double)c; }
+};
+
 template <typename T, typename Op>
 __global__ void __launch_bounds__(kRedThreads)
     reduce_pass1(Op op, const T* __restrict__ x, Geo g, Bc<T> bc,
                  EnergyCoef<T> k, double* __restrict__ partial) {
   pdl_wait();
+  constexpr bool kPair = std::is_same<T, float>::value && std::is_same<Op, SumOp>::value;
   const int nx = g.n[g.ndim - 1];
   const int64_t rows = g.ndim == 2 ? (int64_t)g.n[0] : (int64_t)g.n[0] * g.n[1];
   const int64_t r0 = rows * blockIdx.x / gridDim.x;
   const int64_t r1 = rows * (blockIdx.x + 1) / gridDim.x;
   double acc = 0.0;
+  Pair pacc;
   for (int64_t r = r0; r < r1; ++r) {
     int i0, i1;
     int64_t off;
@@ -94,10 +117,14 @@ __global__ void __launch_bounds__(kRedThreads)
     }
     for (int c = threadIdx.x; c < nx; c += kRedThreads) {
       const T v = x[off + c];
-      acc += g.ndim == 2 ? cell_term<T>(op, x, g, bc, k, i0, c, 0, v)
-                         : cell_term<T>(op, x, g, bc, k, i0, i1, c, v);
+      if constexpr (kPair)
+        pacc.add(v);
+      else
+        acc += g.ndim == 2 ? cell_term<T>(op, x, g, bc, k, i0, c, 0, v)
+                           : cell_term<T>(op, x, g, bc, k, i0, i1, c, v);
     }
   }
+  if constexpr (kPair) acc = pacc.value();
   const double s = block_sum(acc);
   if (threadIdx.x == 0) partial[blockIdx.x] = s;
 }
