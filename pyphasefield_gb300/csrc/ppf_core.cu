@@ -165,7 +165,7 @@ namespace {
 
 struct MapKey {
   const void* base;
-  int elem, rank;
+  int elem, rank, kind;  // kind 0: float / double tiles, 1: bf16 with 128-byte swizzle
   uint64_t dims[3], strides[2];
   uint32_t box[3];
   int device;
@@ -201,13 +201,15 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
 
 }  // namespace
 
-int32_t tensor_map(CUtensorMap* out, const void* base, int elem_bytes, int rank,
-                   const uint64_t* dims, const uint64_t* strides_bytes, const uint32_t* box) {
+static int32_t tensor_map_kind(CUtensorMap* out, const void* base, int elem_bytes, int rank,
+                               const uint64_t* dims, const uint64_t* strides_bytes,
+                               const uint32_t* box, int kind) {
   MapKey key;
   std::memset(&key, 0, sizeof(key));
   key.base = base;
   key.elem = elem_bytes;
   key.rank = rank;
+  key.kind = kind;
   for (int i = 0; i < rank; ++i) {
     key.dims[i] = dims[i];
     key.box[i] = box[i];
@@ -226,17 +228,34 @@ int32_t tensor_map(CUtensorMap* out, const void* base, int elem_bytes, int rank,
   if (((uintptr_t)base) % 16) return fail(PPF_ERR_INVALID, "field base not 16-byte aligned");
   cuuint32_t estr[3] = {1, 1, 1};
   CUtensorMap m;
-  CUresult r = fn(&m, elem_bytes == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32
-                                      : CU_TENSOR_MAP_DATA_TYPE_FLOAT64,
-                  (cuuint32_t)rank, const_cast<void*>(base), (const cuuint64_t*)dims,
+  const CUtensorMapDataType dt = kind == 1 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16
+                                 : (elem_bytes == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32
+                                                    : CU_TENSOR_MAP_DATA_TYPE_FLOAT64);
+  CUresult r = fn(&m, dt, (cuuint32_t)rank, const_cast<void*>(base), (const cuuint64_t*)dims,
                   (const cuuint64_t*)strides_bytes, (const cuuint32_t*)box, estr,
-                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE,
+                  kind == 1 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_NONE,
                   CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) return fail(PPF_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
   if (cache.size() > 4096) cache.clear();
   cache.emplace(key, m);
   *out = m;
   return PPF_OK;
+}
+
+int32_t tensor_map(CUtensorMap* out, const void* base, int elem_bytes, int rank,
+                   const uint64_t* dims, const uint64_t* strides_bytes, const uint32_t* box) {
+  return tensor_map_kind(out, base, elem_bytes, rank, dims, strides_bytes, box, 0);
+}
+
+int32_t tensor_map_bf16_sw128(CUtensorMap* out, const void* base, uint64_t cols, uint64_t rows,
+                              uint64_t row_bytes, uint32_t box_cols, uint32_t box_rows) {
+  if (box_cols * 2 > 128) return fail(PPF_ERR_INVALID, "swizzled box wider than 128 bytes");
+  if (row_bytes % 16) return fail(PPF_ERR_INVALID, "row stride not a multiple of 16 bytes");
+  const uint64_t dims[2] = {cols, rows};
+  const uint64_t strides[1] = {row_bytes};
+  const uint32_t box[2] = {box_cols, box_rows};
+  return tensor_map_kind(out, base, 2, 2, dims, strides, box, 1);
 }
 
 }  // namespace ppf

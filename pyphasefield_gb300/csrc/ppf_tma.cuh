@@ -111,5 +111,11 @@ __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, i
 int32_t tensor_map(CUtensorMap* out, const void* base, int elem_bytes, int rank,
                    const uint64_t* dims, const uint64_t* strides_bytes,
                    const uint32_t* box);
+// bf16 matrix [rows][cols] (row stride row_bytes), box of box_rows x
+// box_cols (box_cols * 2 <= 128 bytes) written to shared memory with the
+// 128-byte swizzle that the tcgen05 K-major SW128 operand layout expects;
+// out-of-range rows and columns arrive as zeros.
+int32_t tensor_map_bf16_sw128(CUtensorMap* out, const void* base, uint64_t cols, uint64_t rows,
+                              uint64_t row_bytes, uint32_t box_cols, uint32_t box_rows);
 
 }  // namespace ppf

@@ -19,6 +19,7 @@
 #include <type_traits>
 
 #include "ppf_common.cuh"
+#include "ppf_tma.cuh"
 
 namespace ppf {
 namespace {
@@ -409,32 +410,37 @@ __device__ __forceinline__ bool tc_wait(uint64_t* bar, uint32_t parity, uint32_t
   return false;
 }
 
-// Stage one 128 x 64 operand tile: rows r0.. of x (row stride ld elements,
-// k contiguous), zero beyond R rows or K columns. 128-byte swizzled K-major
-// layout: row r's 16-byte chunk j sits at (r / 8) * 1024 + (r % 8) * 128 +
-// ((j ^ (r % 8)) * 16), so the 8 threads that copy one row hit 8 different
-// bank groups.
-__device__ __forceinline__ void tc_load_tile(uint8_t* dst, const __nv_bfloat16* __restrict__ x,
-                                             long long ld, long long r0, long long R,
-                                             long long k0, long long K, int tid) {
-#pragma unroll 4
-  for (int i = tid; i < 128 * (TCK / 8); i += kTcThreads) {
-    const int row = i >> 3, j = i & 7;
-    uint4 v = make_uint4(0u, 0u, 0u, 0u);
-    if (r0 + row < R && k0 + j * 8 < K)
-      v = *reinterpret_cast<const uint4*>(x + (r0 + row) * ld + k0 + j * 8);
-    *reinterpret_cast<uint4*>(dst + (row >> 3) * 1024 + (row & 7) * 128 + ((j ^ (row & 7)) << 4)) = v;
-  }
+// Pipeline: a producer thread (warp 0) streams the k-tiles of A (128 rows)
+// and B (128 columns) into kTcStages shared-memory stages with TMA tensor
+// loads (cp.async.bulk.tensor.2d, 128-byte swizzle: the K-major SW128 layout
+// the descriptors describe), completing on the stage's `full` mbarrier; an
+// MMA thread (warp 1) waits for a stage, issues its four tcgen05.mma (K = 16
+// each) into the TMEM accumulator and commits onto the stage's `empty`
+// mbarrier, which frees the stage for the producer; a final commit onto
+// `done` releases the four warps into the epilogue. With three 32 KB stages
+// two CTAs share an SM, so one CTA's epilogue overlaps the other's loads.
+// Every wait is bounded; a timeout sets PPF_STATUS_TIMEOUT, the issued MMAs
+// and loads are waited for (bounded) and the tensor memory is freed.
+constexpr int kTcStages = 3;
+
+__device__ __forceinline__ void tc_tma_load(void* dst, const CUtensorMap* map, int x, int y,
+                                            uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3}], [%4];" ::"r"(tc_smem(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(tc_smem(bar))
+      : "memory");
 }
 
 template <typename ST>
 __global__ void __launch_bounds__(kTcThreads)
-    tc_gemm_kernel(const __nv_bfloat16* __restrict__ a, long long lda,
-                   const __nv_bfloat16* __restrict__ b, long long ldb, ST st, long long M,
-                   long long N, long long K, int* __restrict__ lib_status) {
+    tc_gemm_kernel(const __grid_constant__ CUtensorMap map_a,
+                   const __grid_constant__ CUtensorMap map_b, ST st, long long M, long long N,
+                   long long K, int* __restrict__ lib_status) {
   extern __shared__ __align__(1024) uint8_t tc_stage[];
-  __shared__ __align__(8) uint64_t bars[2];
+  __shared__ __align__(8) uint64_t full[kTcStages], empty[kTcStages], done;
   __shared__ uint32_t tmem_base;
+  __shared__ int abort_flag, consumed;
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const long long m0 = (long long)blockIdx.y * TCM, n0 = (long long)blockIdx.x * TCN;
   uint8_t* const base = tc_stage + ((1024 - (tc_smem(tc_stage) & 1023)) & 1023);
@@ -446,28 +452,52 @@ __global__ void __launch_bounds__(kTcThreads)
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
   if (tid == 0) {
-    for (int i = 0; i < 2; ++i)
-      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(tc_smem(&bars[i])) : "memory");
+    for (int i = 0; i < kTcStages; ++i) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(tc_smem(&full[i])) : "memory");
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(tc_smem(&empty[i])) : "memory");
+    }
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(tc_smem(&done)) : "memory");
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    abort_flag = 0;
+    consumed = 0;
   }
-  pdl_wait();
-  pdl_launch_next();
-  const int nk = (int)((K + TCK - 1) / TCK);
-  tc_load_tile(sa(0), a, lda, m0, M, 0, K, tid);
-  tc_load_tile(sb(0), b, ldb, n0, N, 0, K, tid);
-  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = tmem_base;
-  bool ok = true;
-  for (int kt = 0; kt < nk; ++kt) {
-    const int cur = kt & 1;
-    if (tid == 0) {
+  pdl_wait();
+  pdl_launch_next();
+  const int nk = (int)((K + TCK - 1) / TCK);
+  constexpr uint32_t kLimit = 1u << 15;
+  int issued = 0;
+  if (warp == 0 && lane == 0) {  // producer
+    for (int kt = 0; kt < nk; ++kt) {
+      const int s = kt % kTcStages;
+      if (kt >= kTcStages &&
+          !tc_wait(&empty[s], (uint32_t)((kt / kTcStages - 1) & 1), kLimit)) {
+        atomicExch(&abort_flag, 1);
+        break;
+      }
+      if (*(volatile int*)&abort_flag) break;
+      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
+                   ::"r"(tc_smem(&full[s])), "r"((uint32_t)kTcStage) : "memory");
+      tc_tma_load(sa(s), &map_a, kt * TCK, (int)m0, &full[s]);
+      tc_tma_load(sb(s), &map_b, kt * TCK, (int)n0, &full[s]);
+      issued = kt + 1;
+    }
+  } else if (warp == 1 && lane == 0) {  // MMA issuer
+    int kt = 0;
+    for (; kt < nk; ++kt) {
+      const int s = kt % kTcStages;
+      if (!tc_wait(&full[s], (uint32_t)((kt / kTcStages) & 1), kLimit)) {
+        atomicExch(&abort_flag, 1);
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
 #pragma unroll
       for (int kk = 0; kk < TCK / 16; ++kk) {
-        const uint64_t da = tc_desc(tc_smem(sa(cur)) + kk * 32);
-        const uint64_t db = tc_desc(tc_smem(sb(cur)) + kk * 32);
+        const uint64_t da = tc_desc(tc_smem(sa(s)) + kk * 32);
+        const uint64_t db = tc_desc(tc_smem(sb(s)) + kk * 32);
         const uint32_t acc = (kt > 0 || kk > 0) ? 1u : 0u;
         asm volatile(
             "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
@@ -476,22 +506,16 @@ __global__ void __launch_bounds__(kTcThreads)
       }
       asm volatile(
           "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
-          ::"r"(tc_smem(&bars[cur])) : "memory");
+          ::"r"(tc_smem(&empty[s])) : "memory");
     }
-    if (kt + 1 < nk) {
-      const int nxt = cur ^ 1;
-      // stage nxt was read by the MMAs of tile kt - 1
-      if (kt >= 1 && !tc_wait(&bars[nxt], (uint32_t)(((kt - 1) >> 1) & 1), 1u << 15)) ok = false;
-      tc_load_tile(sa(nxt), a, lda, m0, M, (long long)(kt + 1) * TCK, K, tid);
-      tc_load_tile(sb(nxt), b, ldb, n0, N, (long long)(kt + 1) * TCK, K, tid);
-      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    }
-    __syncthreads();
-    if (__syncthreads_or(!ok)) break;
+    consumed = kt;
+    // completes once every MMA issued above has (also after an abort)
+    asm volatile(
+        "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];"
+        ::"r"(tc_smem(&done)) : "memory");
   }
-  // the last commit (tile nk - 1) covers every MMA issued before it
-  if (ok && !tc_wait(&bars[(nk - 1) & 1], (uint32_t)(((nk - 1) >> 1) & 1), 1u << 15)) ok = false;
-  ok = !__syncthreads_or(!ok);
+  bool ok = tc_wait(&done, 0u, kLimit);
+  ok = !__syncthreads_or(!ok || abort_flag);
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   if (ok) {
     // lane = row of the accumulator; 32 columns per round go through a
@@ -527,10 +551,12 @@ __global__ void __launch_bounds__(kTcThreads)
     }
   } else {
     if (tid == 0) atomicOr(lib_status, PPF_STATUS_TIMEOUT);
-    // let every issued MMA complete before the accumulator is freed
-    if (tid == 0)
-      for (int i = 0; i < 2; ++i)
-        for (int ph = 0; ph < 2; ++ph) tc_wait(&bars[i], (uint32_t)ph, 1u << 10);
+    // the MMAs: `done` completes when they have; the loads issued but not
+    // consumed: their stages' `full` phases
+    if (tid == 0) tc_wait(&done, 0u, kLimit);
+    if (warp == 0 && lane == 0)
+      for (int kt = consumed; kt < issued; ++kt)
+        tc_wait(&full[kt % kTcStages], (uint32_t)((kt / kTcStages) & 1), kLimit);
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
@@ -553,13 +579,21 @@ int32_t tc_gemm(const StridedBf16& la, const StridedBf16& lb, ST st, long long M
                 long long K, cudaStream_t s) {
   int* status = status_ptr();
   if (!status) return fail(PPF_ERR_CUDA, "status word unavailable");
-  const size_t smem = 2 * (size_t)kTcStage + 1024;
+  if (M > (1LL << 31) - 1 || N > (1LL << 31) - 1 || K > (1LL << 31) - 1)
+    return fail(PPF_ERR_INVALID, "GEMM too large");
+  CUtensorMap ma, mb;
+  int32_t rc = tensor_map_bf16_sw128(&ma, la.x, (uint64_t)K, (uint64_t)M,
+                                     (uint64_t)la.si * 2, TCK, TCM);
+  if (rc) return rc;
+  if ((rc = tensor_map_bf16_sw128(&mb, lb.x, (uint64_t)K, (uint64_t)N, (uint64_t)lb.sj * 2, TCK,
+                                  TCN)))
+    return rc;
+  const size_t smem = (size_t)kTcStages * kTcStage + 1024;
   auto kern = tc_gemm_kernel<ST>;
   PPF_TRY_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   dim3 grid((unsigned)((N + TCN - 1) / TCN), (unsigned)((M + TCM - 1) / TCM));
   if (grid.y > 65535) return fail(PPF_ERR_INVALID, "GEMM too large");
-  PPF_TRY_CUDA(launch(kern, grid, dim3(kTcThreads), smem, s, false, la.x, la.si, lb.x, lb.sj, st,
-                      M, N, K, status));
+  PPF_TRY_CUDA(launch(kern, grid, dim3(kTcThreads), smem, s, false, ma, mb, st, M, N, K, status));
   return PPF_OK;
 }
 
