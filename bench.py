@@ -761,6 +761,9 @@ def profile_case(name: str):
     acfull2048  implicit Allen-Cahn, full 2-D system on 2048^2 (Chebyshev), fp64, 2 steps
     acminres1024  the same beyond the Chebyshev bound (16 W M dt = 7.3, an indefinite
                 system: MINRES in one persistent launch) on 1024^2, fp64, 2 steps
+    surrogate_train  six Adam steps of the default surrogate network on 512^2 stencil
+                snapshots, batch 8 (8192 tokens): the tcgen05 and mma.sync GEMMs, the
+                depthwise convolutions
     diff8192    Diffusion 2-D 8192^2 periodic, 5 passes of PPF_DEPTH (default 4) steps: the
                 marching temporal-blocking kernel on 512 MiB of fields
     diff16384   Diffusion 2-D 16384^2 periodic, 5 steps (2 GiB of fields: beyond L2)
@@ -839,6 +842,12 @@ def profile_case(name: str):
         else:  # half the cells at phi = 0.75: an indefinite system (MINRES)
             sim.fields[0].data[1:-1, 1:-1] = np.where(rng.random((n, n)) > 0.5, 0.75, 0.2)
         sim.simulate(2)
+    elif name == "surrogate_train":
+        from pyphasefield_gb300 import surrogate as S
+        data = S.generate_trajectories(2, 512, 64, 16, seed=1, warm_steps=16)
+        net = S.SurrogateNet(seed=0)
+        net.fit_normalisation(data, 512)
+        S.train(net, data, 512, iters=6, batch=8, log_every=1000)
     elif name == "diff8192":
         depth = int(os.environ.get("PPF_DEPTH", "4"))
         sim = DiffusionGB300(dimensions=[8192, 8192], dx=1.0, dt=0.2,
