@@ -556,6 +556,44 @@ def time_predict(net, H, reps=50):
         L.call("ppf_graph_destroy", exec_)
 
 
+def gemm_table(shapes=((1024, 384, 192), (8192, 384, 192), (8192, 512, 192), (65536, 384, 192),
+                       (65536, 192, 384), (65536, 512, 512), (131072, 384, 192)), reps=20):
+    """TFLOP/s of ppf_sg_gemm (K-contiguous bf16 operands, fp32 output) on
+    the tcgen05 path and on mma.sync, CUDA events over `reps` launches after
+    three warm-up launches; one dict per shape."""
+    dev = torch.device("cuda")
+    s = torch.cuda.current_stream()
+    sp = _sp(s)
+    rows = []
+    try:
+        for M, N, K in shapes:
+            a = torch.randn(M, K, device=dev).to(BF)
+            b = torch.randn(N, K, device=dev).to(BF)
+            y = torch.zeros(M, N, device=dev)
+            row = {"M": M, "N": N, "K": K}
+            for path, name in ((1, "tcgen05"), (0, "mma_sync")):
+                L.call("ppf_sg_set_tensor_path", path)
+
+                def run():
+                    L.call("ppf_sg_gemm", ptr(a), K, 1, ptr(b), 1, K, ptr(y), N, None, 0, M, N, K,
+                           1, sp)
+
+                for _ in range(3):
+                    run()
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(s)
+                for _ in range(reps):
+                    run()
+                e1.record(s)
+                e1.synchronize()
+                row[name] = 2 * M * N * K / (e0.elapsed_time(e1) / reps / 1e3) / 1e12
+            rows.append(row)
+    finally:
+        L.call("ppf_sg_set_tensor_path", 1)
+    return rows
+
+
 def held_out_error_ratio(net, held) -> float:
     """Sum over held-out windows of the network's squared phi error against
     the stencil, over the same for predicting no change."""
@@ -596,7 +634,13 @@ def main(argv=None):
     ap.add_argument("--mma-sync", action="store_true",
                     help="run every GEMM on mma.sync (default: tcgen05 for the large "
                          "K-contiguous ones)")
+    ap.add_argument("--gemm-table", action="store_true",
+                    help="time the GEMM kernels at the network's shapes instead")
     a = ap.parse_args(argv)
+    if a.gemm_table:
+        for row in gemm_table():
+            print(json.dumps(row), flush=True)
+        return
     L.call("ppf_sg_set_tensor_path", 0 if a.mma_sync else 1)
     H, k = a.grid, a.k
     t0 = time.perf_counter()
