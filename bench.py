@@ -120,6 +120,15 @@ class ClockSampler:
                 stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
+            return self
+        # nvidia-smi takes a moment to start: wait (bounded) for its first
+        # sample so that a short timed region is still covered by samples
+        t_end = time.perf_counter() + 5.0
+        while time.perf_counter() < t_end and self.proc.poll() is None:
+            self.f.flush()
+            if self.path.stat().st_size > 0:
+                break
+            time.sleep(0.05)
         return self
 
     def __exit__(self, *exc):
@@ -385,7 +394,7 @@ def run_gb300(args):
                          "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": cap.get("dram_bytes_per_launch"),
                          "peak_source": peak_kind,
-                         "kernel": "warren1995_kernel<float, 2>",
+                         "kernel": cap.get("kernel", "warren1995_f2_kernel"),
                          "per_launch_us": step_launch_s * 1e6},
             "gpu_launches": launches,
             "wall_s": wall,

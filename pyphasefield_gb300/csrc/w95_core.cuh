@@ -102,12 +102,15 @@ __device__ __forceinline__ void load_cell(const T* __restrict__ phi, const T* __
 }
 
 // Noise words of a band, computed once per Philox block. Cell (row, x)
-// takes word x % 4 of the block with counter (x / 4, row, step): the band's
-// owned columns x0 .. x0 + 29 span at most kGroups blocks per row, so the
+// takes word x % 4 of the block with counter (x / 4, row, step). A band's
+// owned columns x0 .. x0 + 29 start at a multiple of kStrip, an even column,
+// so x0 % 4 is 0 or 2 and they span at most kGroups = 8 blocks per row. The
 // ROWS * kGroups blocks of a band are spread over the lanes (one block per
-// lane and pass) and each cell fetches its word from the computing lane by
-// shuffles, instead of every lane evaluating the block of its own column.
-constexpr int kGroups = 9;
+// lane and pass: four rows in one pass) and each cell fetches its word from
+// the computing lane by shuffles, instead of every lane evaluating the block
+// of its own column.
+static_assert(kStrip % 2 == 0 && kStrip <= 30, "owned columns must span at most 8 blocks");
+constexpr int kGroups = 8;
 
 template <int ROWS>
 struct BandNoise {
@@ -162,15 +165,27 @@ __device__ __forceinline__ T shfl_e(T v) { return __shfl_down_sync(0xffffffffu, 
 namespace ppf {
 namespace w95 {
 
-// Loads of one band (rows y0 - 1 .. y0 + ROWS, this lane's column). Only
-// the lanes whose column lies outside the grid (the edge strips' halo
-// lanes) take the boundary rule.
+// Loads of one band (rows y0 - 1 .. y0 + ROWS, this lane's column). A band
+// whose rows and 32 columns all lie inside the grid (warp-uniform test) reads
+// straight from one base pointer; otherwise only the cells outside the grid
+// take the boundary rule.
 template <typename T, int ROWS, bool COHERENT = false>
 __device__ __forceinline__ void band_load(const Geo& g, const Bc<T>& bc,
                                           const T* __restrict__ phi_in,
                                           const T* __restrict__ c_in, int xs, int y0,
                                           T (&bp)[ROWS + 2], T (&bcv)[ROWS + 2]) {
   const int x = xs + (int)threadIdx.x;
+  if (xs >= 0 && xs + 32 <= g.n[1] && y0 >= 1 && y0 + ROWS + 1 <= g.n[0]) {
+    const int64_t o = (int64_t)(y0 - 1) * g.pitch + x;
+    const T* p = phi_in + o;
+    const T* c = c_in + o;
+#pragma unroll
+    for (int j = 0; j < ROWS + 2; ++j) {
+      bp[j] = ldf<COHERENT>(p + (int64_t)j * g.pitch);
+      bcv[j] = ldf<COHERENT>(c + (int64_t)j * g.pitch);
+    }
+    return;
+  }
   const bool x_in = (unsigned)x < (unsigned)g.n[1];
 #pragma unroll
   for (int j = 0; j < ROWS + 2; ++j)
@@ -199,12 +214,10 @@ __device__ __forceinline__ void band_compute(const Coef<T>& k, const Geo& g,
                                              T* __restrict__ phi_out, T* __restrict__ c_out,
                                              uint64_t seed, uint64_t step, int xs, int y0,
                                              const T (&bp)[ROWS + 2], const T (&bcv)[ROWS + 2]) {
-#ifndef PPF_W95_SCALAR
-  if constexpr (std::is_same<T, float>::value && ROWS == 2) {
-    band_compute_f2(k, g, phi_out, c_out, seed, step, xs, y0, bp, bcv);
+  if constexpr (std::is_same<T, float>::value && (ROWS == 2 || ROWS == 4 || ROWS == 8)) {
+    band_compute_pk<ROWS / 2>(k, g, phi_out, c_out, seed, step, xs, y0, bp, bcv);
     return;
   }
-#endif
   const int lane = threadIdx.x;
   const int ny = g.n[0], nx = g.n[1];
   const int x = xs + lane;

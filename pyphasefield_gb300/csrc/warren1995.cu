@@ -9,6 +9,7 @@
 //
 // Reference: engine_Warren1995 (Engines/Warren1995.py:50-92).
 #include <cmath>
+#include <type_traits>
 
 #include "ppf_common.cuh"
 #include "w95_core.cuh"
@@ -19,12 +20,12 @@ namespace {
 constexpr int kWarpsPerCta = 4;
 constexpr int kCtaThreads = 32 * kWarpsPerCta;
 
-// Resident CTAs per SM asked of the register allocator: ten 128-thread CTAs
-// (48 registers a thread) for the float two-row band, the benchmark's
-// kernel; the others take what they need.
+// Resident CTAs per SM asked of the register allocator for the generic
+// band kernel: none (each takes what it needs); the float two-row kernel
+// below asks for ten 128-thread CTAs (48 registers a thread).
 template <typename T, int ROWS>
 struct W95MinBlocks {
-  static constexpr int value = (sizeof(T) == 4 && ROWS == 2) ? 10 : 0;
+  static constexpr int value = 0;
 };
 
 template <typename T, int ROWS>
@@ -42,6 +43,49 @@ __global__ void __launch_bounds__(kCtaThreads, (W95MinBlocks<T, ROWS>::value))
                      blockIdx.x * w95::kStrip - 1, y0);
 }
 
+// The benchmark's instantiation (float, two rows per warp). The CTA's four
+// warps own four consecutive bands of one strip (a group of eight rows). The
+// Philox blocks of the group's rows (4 bands x 2 rows x kGroups = 64 blocks)
+// are drawn by two warps, one block per lane, while the bands' loads are in
+// flight, into a shared-memory table that every band reads its words from,
+// instead of each warp drawing its own 16 blocks with half its lanes idle and
+// fetching words by shuffles.
+constexpr int kTableJobs = kWarpsPerCta * 2 * w95::kGroups;
+static_assert(kTableJobs == 64, "two warps draw a group's noise blocks");
+
+__global__ void __launch_bounds__(kCtaThreads, 10)
+    warren1995_f2_kernel(w95::Coef<float> k, Geo g, Bc<float> bc,
+                         const float* __restrict__ phi_in, const float* __restrict__ c_in,
+                         float* __restrict__ phi_out, float* __restrict__ c_out, uint64_t seed,
+                         uint64_t step, const uint64_t* __restrict__ step_base) {
+  __shared__ U4 table[kTableJobs];
+  const int w = threadIdx.y, lane = threadIdx.x;
+  const int band0 = blockIdx.y * (kWarpsPerCta * 2);  // first row of the group
+  const int y0 = band0 + 2 * w;
+  const int xs = blockIdx.x * w95::kStrip - 1;
+  const uint32_t gbase = (uint32_t)(xs + 1) / 4u;  // first owned column's Philox block
+  pdl_wait();
+  pdl_launch_next();
+  if (step_base) step += *step_base;
+  const bool live = y0 < g.n[0];  // warp-uniform; dead warps still meet the barrier
+  float bp[4], bcv[4], v = 0.f;
+  if (live) w95::band_load<float, 2>(g, bc, phi_in, c_in, xs, y0, bp, bcv);
+  if (k.alpha != 0.f && w < 2) {
+    const int job = w * 32 + lane;  // (band b, row r, block i)
+    const int b = job / (2 * w95::kGroups), r = (job / w95::kGroups) & 1;
+    const int i = job % w95::kGroups;
+    table[job] = noise_group(seed, step, (uint32_t)(band0 + 2 * b + r), gbase + (uint32_t)i);
+  }
+  __syncthreads();
+  if (!live) return;
+  if (k.bulk && w95::band_is_bulk(bp, v)) {
+    w95::band_bulk_pk<1>(k, g, phi_out, c_out, xs, y0, bp, bcv, v);
+    return;
+  }
+  w95::TableNoise noise{reinterpret_cast<const uint32_t*>(table + w * 2 * w95::kGroups), gbase};
+  w95::band_full_pk<1>(k, g, phi_out, c_out, noise, xs, y0, bp, bcv);
+}
+
 template <typename T, int ROWS>
 cudaError_t launch_rows(const w95::Coef<T>& k, const Geo& g, const Bc<T>& bc, const T* phi_in,
                         const T* c_in, T* phi_out, T* c_out, uint64_t seed, uint64_t step,
@@ -50,9 +94,14 @@ cudaError_t launch_rows(const w95::Coef<T>& k, const Geo& g, const Bc<T>& bc, co
   const long bands = (g.n[0] + ROWS - 1) / ROWS;
   const long gy = (bands + kWarpsPerCta - 1) / kWarpsPerCta;
   if (strips > (1L << 30) || gy > 65535) return cudaErrorInvalidConfiguration;
-  return launch(warren1995_kernel<T, ROWS>, dim3((unsigned)strips, (unsigned)gy),
-                dim3(32, kWarpsPerCta), 0, s, pdl, k, g, bc, phi_in, c_in, phi_out, c_out, seed,
-                step, step_base);
+  if constexpr (std::is_same<T, float>::value && ROWS == 2)
+    return launch(warren1995_f2_kernel, dim3((unsigned)strips, (unsigned)gy),
+                  dim3(32, kWarpsPerCta), 0, s, pdl, k, g, bc, phi_in, c_in, phi_out, c_out,
+                  seed, step, step_base);
+  else
+    return launch(warren1995_kernel<T, ROWS>, dim3((unsigned)strips, (unsigned)gy),
+                  dim3(32, kWarpsPerCta), 0, s, pdl, k, g, bc, phi_in, c_in, phi_out, c_out,
+                  seed, step, step_base);
 }
 
 template <typename T>
