@@ -763,8 +763,8 @@ def profile_case(name: str):
     ch256       Cahn-Hilliard 256^3 periodic, dt 0.01, 5 steps
     diff4096    Diffusion 2-D 4096^2 periodic, 5 steps (temporal depth from PPF_DEPTH, default 1)
     diff3d384   Diffusion 3-D 384^3 periodic, 5 steps
-    ensemble64  the 64-member ensemble benchmark (1.56e7 cells), five persistent launches of
-                8 steps
+    ensemble64  the 64-member ensemble benchmark (1.56e7 cells), two rows and four bands per
+                warp: 40 steps, one launch each
     tb4096      Diffusion 2-D 4096^2, depth 4 on 128 x 32 shared-memory tiles, 20 steps
     reduce4096  five FP64 sums of a 4096^2 float field (ppf_reduce_sum_f32)
     acfull2048  implicit Allen-Cahn, full 2-D system on 2048^2 (Chebyshev), fp64, 2 steps
@@ -807,7 +807,7 @@ def profile_case(name: str):
         sim.simulate(5 * depth)
     elif name == "ensemble64":
         from pyphasefield_gb300.ensemble import Ensemble, make_config_ensemble
-        ens = Ensemble(make_config_ensemble(n=64, seed=0), rows=2, graph_chunk=8,
+        ens = Ensemble(make_config_ensemble(n=64, seed=0), rows=2, bands=4, graph_chunk=8,
                        use_graph=False)
         ens.simulate(40)
         ens.synchronize()

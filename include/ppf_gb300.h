@@ -436,7 +436,8 @@ typedef struct PpfEnsemblePlan {
   int32_t n_members;
   int32_t rows;    /* rows per warp band (tiling->tile_y: 2, 4 or 8) */
   int64_t n_units; /* units of 4 x bands bands (one CTA pass each) */
-  int32_t bands;   /* bands per warp and unit (tiling->tile_x: 1 or 4; 0 -> 4) */
+  int32_t bands;   /* bands per warp and unit (tiling->tile_x: 1 or 4, with two
+                      rows also 8 or 16; 0 -> 4) */
   int32_t reserved;
 } PpfEnsemblePlan;
 
@@ -456,11 +457,13 @@ int32_t ppf_ensemble_build(const PpfMember* members, int32_t n,
 int32_t ppf_ensemble_step_f32(const PpfEnsemblePlan* plan, int32_t parity,
                               uint64_t step, const uint64_t* step_base,
                               const PpfTiling* tiling, void* stream);
-/* nsteps time steps of every member in ONE persistent cooperative launch:
- * the CTAs meet at a grid barrier between steps (waits bounded; a timeout
- * sets PPF_STATUS_TIMEOUT in the status word and ends the launch early).
- * `sync` is caller device memory of 8 bytes, zeroed once before its first
- * use and used by one launch at a time; after a timeout zero it again. The
+/* nsteps time steps of every member. Two-row plans: one launch per step
+ * (programmatic dependent launch when tiling->pdl), `sync` unused. Four- and
+ * eight-row plans: ONE persistent cooperative launch: the CTAs meet at a
+ * grid barrier between steps (waits bounded; a timeout sets
+ * PPF_STATUS_TIMEOUT in the status word and ends the launch early). `sync`
+ * is then caller device memory of 8 bytes, zeroed once before its first use
+ * and used by one launch at a time; after a timeout zero it again. The
  * member buffers swap by step parity, starting from `parity`. */
 int32_t ppf_ensemble_run_f32(const PpfEnsemblePlan* plan, int32_t parity,
                              uint64_t step, const uint64_t* step_base,

@@ -1,19 +1,22 @@
 // Batched ensemble: many Warren1995 and Allen-Cahn instances with uneven 2-D
-// grids and per-instance parameters, advanced together by one cooperative,
-// persistent launch per chunk of steps.
+// grids and per-instance parameters, advanced together.
 //
 // Work: a member's grid is cut into warp bands (a 30-column strip x ROWS
-// rows), and its bands are grouped sixteen at a time into units, one per CTA
-// pass (four per warp); a member's last unit is padded so that no unit spans
-// two members. A
-// unit table maps every unit to its member, so a CTA finds its member with
-// one load and stages the member's folded constants in shared memory for its
-// four warps. The launch is cooperative (every CTA resident) and persistent:
-// each CTA walks the units grid-stride, then all CTAs meet at a grid barrier
-// before the next step (each member's ping-pong buffers swap by step
-// parity). The barrier's waits are bounded: a CTA that waits too long sets
-// PPF_STATUS_TIMEOUT and the launch ends early. Reads of the fields use
-// plain (coherent) loads, since other CTAs of the same launch wrote them.
+// rows), and its bands are grouped 4 x BANDS at a time into units, one per
+// CTA (BANDS per warp); a member's last unit is padded so that no unit spans
+// two members. A unit table maps every unit to its member, so a CTA finds
+// its member with one load and stages the member's folded constants in
+// shared memory for its four warps.
+//
+// Two-row tilings: ensemble_f2_kernel, one plain launch per step over every
+// unit (the single-grid float kernel's band code and register budget).
+// Four- and eight-row tilings: ensemble_kernel, one cooperative, persistent
+// launch per chunk of steps: each CTA walks the units grid-stride, then all
+// CTAs meet at a grid barrier before the next step (each member's ping-pong
+// buffers swap by step parity). The barrier's waits are bounded: a CTA that
+// waits too long sets PPF_STATUS_TIMEOUT and the launch ends early. Reads of
+// the fields use plain (coherent) loads there, since other CTAs of the same
+// launch wrote them.
 //
 // Reference: engine_Warren1995 (Engines/Warren1995.py:50-92) and
 // engine_CahnAllenExplicit (Engines/CahnAllen.py:128-135), one instance per
@@ -35,6 +38,7 @@ constexpr int kCtaThreads = 32 * kWarpsPerCta;
 struct MemberDev {
   int model;
   int strips;
+  unsigned long long strips_magic;  // ceil(2^64 / strips): band / strips by one multiply
   long long item_begin;  // first band (items of a member are [begin, begin + items))
   long long items;
   long long unit_begin;  // first unit
@@ -50,25 +54,51 @@ struct MemberDev {
 // Device table layout: MemberDev[n_members], then int unit_member[n_units].
 inline size_t units_offset(int n) { return ((size_t)n * sizeof(MemberDev) + 15) / 16 * 16; }
 
+// Band b of a member (b < 2^32) as strip and row band: b / strips through the
+// member's 64-bit reciprocal (exact for 32-bit dividends: the error of the
+// rounded-up reciprocal, b / 2^64, stays below 1 / strips), instead of a
+// 64-bit division.
+__device__ __forceinline__ void band_coords(const MemberDev& m, unsigned b, int& strip,
+                                            int& rowband) {
+  const unsigned q = m.strips == 1 ? b : (unsigned)__umul64hi((unsigned long long)b, m.strips_magic);
+  rowband = (int)q;
+  strip = (int)(b - q * (unsigned)m.strips);
+}
+
 // Allen-Cahn band in the warp-strip layout: phi + a lap - b (4phi^3 - 6phi^2
 // + 2phi), neighbour sum grouped ((w + e) + (n + s)) as in the single-grid
-// kernel.
+// kernel. ac_load requests rows y0 - 1 .. y0 + ROWS of this lane's column
+// (straight from one base pointer for an interior band), ac_compute writes
+// rows y0 .. y0 + ROWS - 1.
 template <int ROWS>
-__device__ __forceinline__ void ac_band(float a, float b, const Geo& g, const Bc<float>& bc,
-                                        const float* __restrict__ in, float* __restrict__ out,
-                                        int xs, int y0) {
-  const int lane = threadIdx.x;
+__device__ __forceinline__ void ac_load(const Geo& g, const Bc<float>& bc,
+                                        const float* __restrict__ in, int xs, int y0,
+                                        float (&v)[ROWS + 2]) {
   const int ny = g.n[0], nx = g.n[1];
-  const int x = xs + lane;
+  const int x = xs + (int)threadIdx.x;
+  if (xs >= 0 && xs + 32 <= nx && y0 >= 1 && y0 + ROWS + 1 <= ny) {  // warp-uniform
+    const float* p = in + (int64_t)(y0 - 1) * g.pitch + x;
+#pragma unroll
+    for (int j = 0; j < ROWS + 2; ++j) v[j] = p[(int64_t)j * g.pitch];
+    return;
+  }
   const bool x_in = (unsigned)x < (unsigned)nx;
-  const bool owner = lane >= 1 && lane <= w95::kStrip && x < nx;
-  float v[ROWS + 2];
 #pragma unroll
   for (int j = 0; j < ROWS + 2; ++j) {
     const int row = y0 - 1 + j;
     v[j] = (x_in && (unsigned)row < (unsigned)ny) ? in[(int64_t)row * g.pitch + x]
                                                    : fetch<float, 2, true>(in, g, bc, 0, row, x);
   }
+}
+
+template <int ROWS>
+__device__ __forceinline__ void ac_compute(float a, float b, const Geo& g,
+                                           float* __restrict__ out, int xs, int y0,
+                                           const float (&v)[ROWS + 2]) {
+  const int lane = threadIdx.x;
+  const int ny = g.n[0], nx = g.n[1];
+  const int x = xs + lane;
+  const bool owner = lane >= 1 && lane <= w95::kStrip && x < nx;
 #pragma unroll
   for (int r = 0; r < ROWS; ++r) {
     const float c = v[r + 1];
@@ -78,6 +108,15 @@ __device__ __forceinline__ void ac_band(float a, float b, const Geo& g, const Bc
     const int row = y0 + r;
     if (owner && row < ny) out[(int64_t)row * g.pitch + x] = c + (a * lap - b * fp);
   }
+}
+
+template <int ROWS>
+__device__ __forceinline__ void ac_band(float a, float b, const Geo& g, const Bc<float>& bc,
+                                        const float* __restrict__ in, float* __restrict__ out,
+                                        int xs, int y0) {
+  float v[ROWS + 2];
+  ac_load<ROWS>(g, bc, in, xs, y0, v);
+  ac_compute<ROWS>(a, b, g, out, xs, y0, v);
 }
 
 // A unit is BANDS bands per warp; warp w of the CTA takes bands w, w + 4,
@@ -93,8 +132,10 @@ __device__ __forceinline__ void run_unit(const MemberDev& m, long long unit, int
     long long local = first + threadIdx.y;
     if (local >= m.items) return;  // whole warp
     float bp[ROWS + 2], bcv[ROWS + 2];
-    int xs = (int)(local % m.strips) * w95::kStrip - 1;
-    int y0 = (int)(local / m.strips) * ROWS;
+    int strip, rowband;
+    band_coords(m, (unsigned)local, strip, rowband);
+    int xs = strip * w95::kStrip - 1;
+    int y0 = rowband * ROWS;
     w95::band_load<float, ROWS, true>(m.g, m.bc, m.phi[parity], m.c[parity], xs, y0, bp, bcv);
 #pragma unroll 1
     for (int j = 0; j < BANDS; ++j) {
@@ -103,8 +144,9 @@ __device__ __forceinline__ void run_unit(const MemberDev& m, long long unit, int
       float np[ROWS + 2], ncv[ROWS + 2];
       int nxs = 0, ny0 = 0;
       if (more) {
-        nxs = (int)(nxt % m.strips) * w95::kStrip - 1;
-        ny0 = (int)(nxt / m.strips) * ROWS;
+        band_coords(m, (unsigned)nxt, strip, rowband);
+        nxs = strip * w95::kStrip - 1;
+        ny0 = rowband * ROWS;
         w95::band_load<float, ROWS, true>(m.g, m.bc, m.phi[parity], m.c[parity], nxs, ny0, np,
                                           ncv);
       }
@@ -126,19 +168,21 @@ __device__ __forceinline__ void run_unit(const MemberDev& m, long long unit, int
   for (int j = 0; j < BANDS; ++j) {
     const long long local = first + j * kWarpsPerCta + threadIdx.y;
     if (local >= m.items) return;  // past the member's last band (whole warp)
-    const int xs = (int)(local % m.strips) * w95::kStrip - 1;
-    const int y0 = (int)(local / m.strips) * ROWS;
+    int strip, rowband;
+    band_coords(m, (unsigned)local, strip, rowband);
+    const int xs = strip * w95::kStrip - 1;
+    const int y0 = rowband * ROWS;
     ac_band<ROWS>(m.ac_a, m.ac_b, m.g, m.bc, m.phi[parity], m.phi[1 - parity], xs, y0);
   }
 }
 
-// Resident CTAs per SM asked of the register allocator: the member's
-// constants come from shared memory into registers (a single grid's kernel
-// takes them as kernel parameters), so the band needs 80 (two rows) to 96
-// registers a thread without spills.
+// Resident CTAs per SM asked of the register allocator for the persistent
+// kernel: the member's constants come from shared memory into registers and
+// the next band is prefetched, so a band of two or four rows needs up to
+// 126 registers a thread and eight rows 151 without spills.
 template <int ROWS>
 struct EnsMinBlocks {
-  static constexpr int value = ROWS == 2 ? 6 : 5;
+  static constexpr int value = ROWS <= 4 ? 4 : 3;
 };
 
 template <int ROWS, int BANDS>
@@ -171,6 +215,57 @@ __global__ void __launch_bounds__(kCtaThreads, (EnsMinBlocks<ROWS>::value))
   }
 }
 
+// One step over every unit of two-row tilings, one CTA per unit (4 BANDS
+// bands of one member; warp w takes bands w, w + 4, ...): the ensemble
+// counterpart of the single-grid float kernel (warren1995.cu). A plain launch
+// per step (no grid barrier), at that kernel's register budget. The member's
+// record is staged in shared memory once per CTA, before waiting on the
+// previous step (the plan table is written before the first launch and never
+// by a step, so with programmatic dependent launch these loads overlap that
+// step's tail), and a band's strip and row band come from the member's
+// reciprocal of its strip count. A Warren1995 band that takes the full update
+// draws its own Philox blocks: members early in a run are mostly bulk, and a
+// bulk band draws none.
+template <int BANDS>
+__global__ void __launch_bounds__(kCtaThreads, 10)
+    ensemble_f2_kernel(const MemberDev* __restrict__ members,
+                       const int* __restrict__ unit_member, int parity, uint64_t step,
+                       const uint64_t* __restrict__ step_base) {
+  __shared__ MemberDev m;
+  const int w = threadIdx.y;
+  const int tid = threadIdx.x + 32 * w;
+  {
+    const int* src = reinterpret_cast<const int*>(members + unit_member[blockIdx.x]);
+    int* dst = reinterpret_cast<int*>(&m);
+    for (int i = tid; i < (int)(sizeof(MemberDev) / 4); i += kCtaThreads) dst[i] = src[i];
+  }
+  __syncthreads();
+  pdl_wait();
+  pdl_launch_next();
+  if (step_base) step += *step_base;
+  // the member's bands are < 2^32 (checked when the plan is built)
+  const unsigned first = (blockIdx.x - (unsigned)m.unit_begin) * (kWarpsPerCta * BANDS);
+  const unsigned items = (unsigned)m.items;
+  const bool warren = m.model == PPF_MODEL_WARREN1995;
+#pragma unroll 1
+  for (int j = 0; j < BANDS; ++j) {
+    const unsigned local = first + (unsigned)(w + kWarpsPerCta * j);
+    if (local >= items) return;  // whole warp
+    int strip, rowband;
+    band_coords(m, local, strip, rowband);
+    const int xs = strip * w95::kStrip - 1;
+    const int y0 = rowband * 2;
+    if (!warren) {
+      ac_band<2>(m.ac_a, m.ac_b, m.g, m.bc, m.phi[parity], m.phi[1 - parity], xs, y0);
+      continue;
+    }
+    float bp[4], bcv[4];
+    w95::band_load<float, 2>(m.g, m.bc, m.phi[parity], m.c[parity], xs, y0, bp, bcv);
+    w95::band_compute_pk<1>(m.w, m.g, m.phi[1 - parity], m.c[1 - parity], m.seed, step, xs, y0,
+                            bp, bcv);
+  }
+}
+
 int32_t build_table(const PpfMember* members, int32_t n, const PpfTiling* tiling,
                     std::vector<MemberDev>* out, std::vector<int>* units, long long* n_items,
                     int* rows, int* bands) {
@@ -180,8 +275,9 @@ int32_t build_table(const PpfMember* members, int32_t n, const PpfTiling* tiling
   if (*rows != 2 && *rows != 4 && *rows != 8)
     return fail(PPF_ERR_INVALID, "ensemble rows per warp must be 2, 4 or 8");
   *bands = tiling && tiling->tile_x ? tiling->tile_x : 4;
-  if (*bands != 1 && *bands != 4)
-    return fail(PPF_ERR_INVALID, "ensemble bands per warp (tile_x) must be 1 or 4");
+  if (*bands != 1 && *bands != 4 && !(*rows == 2 && (*bands == 8 || *bands == 16)))
+    return fail(PPF_ERR_INVALID,
+                "ensemble bands per warp (tile_x) must be 1 or 4 (or 8, 16 with two rows)");
   if (tiling && tiling->depth > 1)
     return fail(PPF_ERR_UNSUPPORTED, "ensemble steps advance one step per pass");
   const bool bulk = !(tiling && (tiling->flags & PPF_TILING_FULL_EVAL));
@@ -224,8 +320,10 @@ int32_t build_table(const PpfMember* members, int32_t n, const PpfTiling* tiling
       d.ac_b = (float)(s.ac.dt * s.ac.M * 16.0 * s.ac.W);
     }
     d.strips = (int)((s.nx + w95::kStrip - 1) / w95::kStrip);
+    d.strips_magic = d.strips > 1 ? ~0ULL / (unsigned long long)d.strips + 1 : 0;
     d.item_begin = items;
     d.items = (long long)d.strips * ((s.ny + *rows - 1) / *rows);
+    if (d.items >= (1LL << 32)) return fail(PPF_ERR_INVALID, "member %d: too many bands", i);
     d.unit_begin = (long long)units->size();
     const long long per_unit = (long long)kWarpsPerCta * *bands;
     const long long nu = (d.items + per_unit - 1) / per_unit;
@@ -292,6 +390,23 @@ cudaError_t launch_ensemble(const PpfEnsemblePlan* p, int parity, uint64_t step,
                             step_base, nsteps, sync, status);
 }
 
+// nsteps launches of ensemble_f2_kernel, each over every unit.
+template <int BANDS>
+cudaError_t launch_f2_steps(const PpfEnsemblePlan* p, int parity, uint64_t step,
+                            const uint64_t* step_base, int nsteps, bool pdl, cudaStream_t s) {
+  if (p->n_units > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
+  const char* base = reinterpret_cast<const char*>(p->device_table);
+  const MemberDev* members = reinterpret_cast<const MemberDev*>(base);
+  const int* units = reinterpret_cast<const int*>(base + units_offset(p->n_members));
+  for (int i = 0; i < nsteps; ++i) {
+    const cudaError_t e =
+        launch(ensemble_f2_kernel<BANDS>, dim3((unsigned)p->n_units), dim3(32, kWarpsPerCta), 0, s, pdl,
+               members, units, (parity + i) & 1, step + (uint64_t)i, step_base);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
 int32_t run(const PpfEnsemblePlan* plan, int32_t parity, uint64_t step,
             const uint64_t* step_base, int32_t nsteps, void* sync, const PpfTiling* tiling,
             void* stream) {
@@ -299,7 +414,7 @@ int32_t run(const PpfEnsemblePlan* plan, int32_t parity, uint64_t step,
   if (parity != 0 && parity != 1) return fail(PPF_ERR_INVALID, "parity must be 0 or 1");
   if (plan->n_items < 1 || plan->n_units < 1) return fail(PPF_ERR_INVALID, "empty plan");
   if (nsteps < 1) return fail(PPF_ERR_INVALID, "nsteps must be >= 1");
-  if (nsteps > 1 && (!sync || ((uintptr_t)sync) % 8))
+  if (plan->rows != 2 && nsteps > 1 && (!sync || ((uintptr_t)sync) % 8))
     return fail(PPF_ERR_INVALID, "several steps per launch need an 8-byte aligned sync buffer");
   int* status = status_ptr();
   if (!status) return fail(PPF_ERR_CUDA, "status word unavailable");
@@ -308,14 +423,16 @@ int32_t run(const PpfEnsemblePlan* plan, int32_t parity, uint64_t step,
   unsigned* sy = (unsigned*)sync;
   cudaError_t e;
 #define PPF_ENS(R, B) launch_ensemble<R, B>(plan, parity, step, step_base, nsteps, sy, status, pdl, s)
-  const int key = plan->rows * 10 + plan->bands;
+  const int key = plan->rows * 100 + plan->bands;
   switch (key) {
-    case 21: e = PPF_ENS(2, 1); break;
-    case 24: e = PPF_ENS(2, 4); break;
-    case 41: e = PPF_ENS(4, 1); break;
-    case 44: e = PPF_ENS(4, 4); break;
-    case 81: e = PPF_ENS(8, 1); break;
-    case 84: e = PPF_ENS(8, 4); break;
+    case 201: e = launch_f2_steps<1>(plan, parity, step, step_base, nsteps, pdl, s); break;
+    case 204: e = launch_f2_steps<4>(plan, parity, step, step_base, nsteps, pdl, s); break;
+    case 208: e = launch_f2_steps<8>(plan, parity, step, step_base, nsteps, pdl, s); break;
+    case 216: e = launch_f2_steps<16>(plan, parity, step, step_base, nsteps, pdl, s); break;
+    case 401: e = PPF_ENS(4, 1); break;
+    case 404: e = PPF_ENS(4, 4); break;
+    case 801: e = PPF_ENS(8, 1); break;
+    case 804: e = PPF_ENS(8, 4); break;
     default: return fail(PPF_ERR_INVALID, "plan rows %d / bands %d invalid", plan->rows,
                          plan->bands);
   }

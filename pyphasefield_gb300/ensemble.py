@@ -2,11 +2,13 @@
 
 The reference runs one Simulation at a time; an ensemble here is a list of
 ordinary engine instances (each with its own fields, parameters and grid
-size) whose device buffers are stepped by ONE persistent cooperative launch
-per chunk of `graph_chunk` steps (`ppf_ensemble_run_f32`: the CTAs meet at a
-bounded grid barrier between steps), captured in a CUDA graph. The rows per
-warp band and the bands per warp are picked by the autotuner for the
-ensemble's mix of member sizes (cached per mix and device). Afterwards each member is an ordinary
+size) whose device buffers are stepped together, a chunk of `graph_chunk`
+steps per `ppf_ensemble_run_f32` call captured in a CUDA graph: one launch
+per step over every member for two-row bands, or one persistent cooperative
+launch per chunk for four- and eight-row bands (the CTAs meet at a bounded
+grid barrier between steps). The rows per warp band and the bands per warp
+are picked by the autotuner for the ensemble's mix of member sizes (cached
+per mix and device). Afterwards each member is an ordinary
 engine again: retrieve_fields_from_GPU, save_simulation etc. work on it.
 
 `make_config_ensemble` builds the benchmark ensemble: n members whose square
