@@ -70,7 +70,7 @@ __device__ __forceinline__ void band_coords(const MemberDev& m, unsigned b, int&
 // kernel. ac_load requests rows y0 - 1 .. y0 + ROWS of this lane's column
 // (straight from one base pointer for an interior band), ac_compute writes
 // rows y0 .. y0 + ROWS - 1.
-template <int ROWS>
+template <int ROWS, bool COHERENT>
 __device__ __forceinline__ void ac_load(const Geo& g, const Bc<float>& bc,
                                         const float* __restrict__ in, int xs, int y0,
                                         float (&v)[ROWS + 2]) {
@@ -79,15 +79,16 @@ __device__ __forceinline__ void ac_load(const Geo& g, const Bc<float>& bc,
   if (xs >= 0 && xs + 32 <= nx && y0 >= 1 && y0 + ROWS + 1 <= ny) {  // warp-uniform
     const float* p = in + (int64_t)(y0 - 1) * g.pitch + x;
 #pragma unroll
-    for (int j = 0; j < ROWS + 2; ++j) v[j] = p[(int64_t)j * g.pitch];
+    for (int j = 0; j < ROWS + 2; ++j) v[j] = ldf<COHERENT>(p + (int64_t)j * g.pitch);
     return;
   }
   const bool x_in = (unsigned)x < (unsigned)nx;
 #pragma unroll
   for (int j = 0; j < ROWS + 2; ++j) {
     const int row = y0 - 1 + j;
-    v[j] = (x_in && (unsigned)row < (unsigned)ny) ? in[(int64_t)row * g.pitch + x]
-                                                   : fetch<float, 2, true>(in, g, bc, 0, row, x);
+    v[j] = (x_in && (unsigned)row < (unsigned)ny)
+               ? ldf<COHERENT>(in + (int64_t)row * g.pitch + x)
+               : fetch<float, 2, COHERENT>(in, g, bc, 0, row, x);
   }
 }
 
@@ -110,12 +111,12 @@ __device__ __forceinline__ void ac_compute(float a, float b, const Geo& g,
   }
 }
 
-template <int ROWS>
+template <int ROWS, bool COHERENT>
 __device__ __forceinline__ void ac_band(float a, float b, const Geo& g, const Bc<float>& bc,
                                         const float* __restrict__ in, float* __restrict__ out,
                                         int xs, int y0) {
   float v[ROWS + 2];
-  ac_load<ROWS>(g, bc, in, xs, y0, v);
+  ac_load<ROWS, COHERENT>(g, bc, in, xs, y0, v);
   ac_compute<ROWS>(a, b, g, out, xs, y0, v);
 }
 
@@ -172,7 +173,7 @@ __device__ __forceinline__ void run_unit(const MemberDev& m, long long unit, int
     band_coords(m, (unsigned)local, strip, rowband);
     const int xs = strip * w95::kStrip - 1;
     const int y0 = rowband * ROWS;
-    ac_band<ROWS>(m.ac_a, m.ac_b, m.g, m.bc, m.phi[parity], m.phi[1 - parity], xs, y0);
+    ac_band<ROWS, true>(m.ac_a, m.ac_b, m.g, m.bc, m.phi[parity], m.phi[1 - parity], xs, y0);
   }
 }
 
@@ -218,7 +219,8 @@ __global__ void __launch_bounds__(kCtaThreads, (EnsMinBlocks<ROWS>::value))
 // One step over every unit of two-row tilings, one CTA per unit (4 BANDS
 // bands of one member; warp w takes bands w, w + 4, ...): the ensemble
 // counterpart of the single-grid float kernel (warren1995.cu). A plain launch
-// per step (no grid barrier), at that kernel's register budget. The member's
+// per step (no grid barrier), twelve CTAs per SM (40 registers a thread with
+// a few spilled: measured faster than ten CTAs without spills). The member's
 // record is staged in shared memory once per CTA, before waiting on the
 // previous step (the plan table is written before the first launch and never
 // by a step, so with programmatic dependent launch these loads overlap that
@@ -227,7 +229,7 @@ __global__ void __launch_bounds__(kCtaThreads, (EnsMinBlocks<ROWS>::value))
 // draws its own Philox blocks: members early in a run are mostly bulk, and a
 // bulk band draws none.
 template <int BANDS>
-__global__ void __launch_bounds__(kCtaThreads, 10)
+__global__ void __launch_bounds__(kCtaThreads, 12)
     ensemble_f2_kernel(const MemberDev* __restrict__ members,
                        const int* __restrict__ unit_member, int parity, uint64_t step,
                        const uint64_t* __restrict__ step_base) {
@@ -256,7 +258,7 @@ __global__ void __launch_bounds__(kCtaThreads, 10)
     const int xs = strip * w95::kStrip - 1;
     const int y0 = rowband * 2;
     if (!warren) {
-      ac_band<2>(m.ac_a, m.ac_b, m.g, m.bc, m.phi[parity], m.phi[1 - parity], xs, y0);
+      ac_band<2, false>(m.ac_a, m.ac_b, m.g, m.bc, m.phi[parity], m.phi[1 - parity], xs, y0);
       continue;
     }
     float bp[4], bcv[4];

@@ -122,11 +122,12 @@ __host__ __device__ __forceinline__ int mirror_index(int i, int n) {
 // Field load: through the read-only (non-coherent) path by default, which
 // is valid when the field was written by an earlier kernel; COHERENT = true
 // for kernels that read what other CTAs of the same launch wrote before a
-// grid barrier (plain ld.global, ordered by the barrier's acquire).
+// barrier or an arrival flag (ordered by its acquire): cached in L2 only
+// (ld.global.cg), so no line this SM's L1 holds from before can be read.
 template <bool COHERENT, typename T>
 __device__ __forceinline__ T ldf(const T* p) {
   if constexpr (COHERENT)
-    return *p;
+    return __ldcg(p);
   else
     return __ldg(p);
 }
