@@ -46,8 +46,8 @@ __global__ void __launch_bounds__(kCtaThreads, (W95MinBlocks<T, ROWS>::value))
 // The benchmark's instantiation (float, two rows per warp). The CTA's four
 // warps own four consecutive bands of one strip (a group of eight rows). The
 // Philox blocks of the group's rows (4 bands x 2 rows x kGroups = 64 blocks)
-// are drawn by two warps, one block per lane, while the bands' loads are in
-// flight, into a shared-memory table that every band reads its words from,
+// are drawn by two warps, one block per lane, before the bands' loads, into a
+// shared-memory table that every band reads its words from,
 // instead of each warp drawing its own 16 blocks with half its lanes idle and
 // fetching words by shuffles.
 constexpr int kTableJobs = kWarpsPerCta * 2 * w95::kGroups;
@@ -64,18 +64,23 @@ __global__ void __launch_bounds__(kCtaThreads, 10)
   const int y0 = band0 + 2 * w;
   const int xs = blockIdx.x * w95::kStrip - 1;
   const uint32_t gbase = (uint32_t)(xs + 1) / 4u;  // first owned column's Philox block
-  pdl_wait();
-  pdl_launch_next();
+  // The noise blocks depend on the step and indices only, not on the fields,
+  // so they are drawn before waiting on the previous step (with programmatic
+  // dependent launch, during its tail). The step offset *step_base is written
+  // only between graph replays (ppf_counter_add_u64), never by the previous
+  // step of the same replay.
   if (step_base) step += *step_base;
-  const bool live = y0 < g.n[0];  // warp-uniform; dead warps still meet the barrier
-  float bp[4], bcv[4], v = 0.f;
-  if (live) w95::band_load<float, 2>(g, bc, phi_in, c_in, xs, y0, bp, bcv);
   if (k.alpha != 0.f && w < 2) {
     const int job = w * 32 + lane;  // (band b, row r, block i)
     const int b = job / (2 * w95::kGroups), r = (job / w95::kGroups) & 1;
     const int i = job % w95::kGroups;
     table[job] = noise_group(seed, step, (uint32_t)(band0 + 2 * b + r), gbase + (uint32_t)i);
   }
+  pdl_wait();
+  pdl_launch_next();
+  const bool live = y0 < g.n[0];  // warp-uniform; dead warps still meet the barrier
+  float bp[4], bcv[4], v = 0.f;
+  if (live) w95::band_load<float, 2>(g, bc, phi_in, c_in, xs, y0, bp, bcv);
   __syncthreads();
   if (!live) return;
   if (k.bulk && w95::band_is_bulk(bp, v)) {
