@@ -20,16 +20,11 @@ namespace {
 constexpr int kWarpsPerCta = 4;
 constexpr int kCtaThreads = 32 * kWarpsPerCta;
 
-// Resident CTAs per SM asked of the register allocator for the generic
-// band kernel: none (each takes what it needs); the float two-row kernel
-// below asks for ten 128-thread CTAs (48 registers a thread).
+// The generic band kernel (float64, and float with 4 / 8 / 16 rows) takes
+// the registers it needs; the float two-row kernel below asks for ten
+// 128-thread CTAs per SM (48 registers a thread).
 template <typename T, int ROWS>
-struct W95MinBlocks {
-  static constexpr int value = 0;
-};
-
-template <typename T, int ROWS>
-__global__ void __launch_bounds__(kCtaThreads, (W95MinBlocks<T, ROWS>::value))
+__global__ void __launch_bounds__(kCtaThreads)
     warren1995_kernel(w95::Coef<T> k, Geo g, Bc<T> bc, const T* __restrict__ phi_in,
                       const T* __restrict__ c_in, T* __restrict__ phi_out,
                       T* __restrict__ c_out, uint64_t seed, uint64_t step,
