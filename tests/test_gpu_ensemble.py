@@ -1,5 +1,6 @@
-"""The batched ensemble (one persistent cooperative launch per chunk of
-steps over many engines) and the autotuner, on the GPU. Ensemble members must match the same engines
+"""The batched ensemble (many engines stepped together: one launch per step
+for two-row bands, one persistent cooperative launch per chunk of steps for
+four- and eight-row bands) and the autotuner, on the GPU. Ensemble members must match the same engines
 stepped one by one (fp32: within 1e-6 relative L2; the ensemble's Allen-Cahn
 band is a different kernel from the single-grid one, so rounding may differ)
 and the FP64 oracle (1e-5)."""
@@ -21,7 +22,7 @@ def _snapshot(sims):
     return [[f.get_cells().copy() for f in s.fields] for s in sims]
 
 
-@pytest.mark.parametrize("rows,bands", [(2, 4), (4, 1), (8, 4), (2, 1)])
+@pytest.mark.parametrize("rows,bands", [(2, 4), (4, 1), (8, 4), (2, 1), (2, 8), (2, 16)])
 def test_ensemble_matches_members_stepped_alone(cuda, rows, bands):
     from pyphasefield_gb300.ensemble import Ensemble
     a = _members()
