@@ -24,6 +24,7 @@
 // or zero-gradient), for the fields, the temperature and the per-cell
 // thermodynamic terms alike.
 #include <math.h>
+#include <type_traits>
 #include <string.h>
 
 #include "ppf_common.cuh"
@@ -144,6 +145,161 @@ __global__ void __launch_bounds__(256)
   for (int e = 0; e < gb.nex; ++e) tab[(2 * N + e) * plane + i] = l_excess(gb, e, t, lnT);
 }
 
+// 1e7 (f(x + d) - f(x)) for f(x) = x ln x (0 at x <= 0) and d = s 1e-7,
+// s = +1 or -1: the reference's forward difference of the ideal mixing term
+// at step 1e-7, in a form without cancellation: d ln x + (x + d) log1p(d / x)
+// in float while |d / x| <= 0.01, in double below that (a nearly absent
+// component).
+__device__ __forceinline__ float dxlogx(float x, float s) {
+  if (x >= 1e-5f) {
+    const float r = s * 1e-7f / x;
+    return s * logf(x) + (x * 1e7f + s) * log1pf(r);
+  }
+  const double xd = (double)x, xp = xd + (double)s * 0.0000001;
+  const double a = xp > 0 ? xp * log(xp) : 0.0, b = xd > 0 ? xd * log(xd) : 0.0;
+  return (float)(10000000.0 * (a - b));
+}
+
+// The float path of the thermodynamics kernel: the pure-element energies
+// (and their differences) in double, everything else in float, and the
+// forward differences of the reference taken as sums of per-term
+// differences, so that no difference of two Gibbs energies of ~1e4 J/mol is
+// formed in float. Up (component `up` by +1e-7) and down (the last
+// component by -1e-7) steps, as in the reference.
+template <int N>
+struct NcF32Thermo {
+  float x[N];
+  float gdiff[N];        // G_solid,l - G_liquid,l
+  float dls[N], dll[N];  // G_phase,l - G_phase,N-1 (solid, liquid)
+  float L[kMaxExcess];
+  float rt;
+
+  // 1e7 (E(x + 1e-7 e_up - 1e-7 e_last) - E(x)) of the solid (es) and the
+  // liquid (el) molar Gibbs energy
+  __device__ __forceinline__ void fd(const NcGibbs& gb, int up, float& es, float& el) const {
+    const float dmix = dxlogx(x[up], 1.f) + dxlogx(x[N - 1], -1.f);
+    float xs = dls[up], xl = dll[up];
+    for (int e = 0; e < gb.nex; ++e) {
+      const int a = gb.ex_meta[e][1], b = gb.ex_meta[e][2], ord = gb.ex_meta[e][3];
+      const float sa = a == up ? 1.f : (a == N - 1 ? -1.f : 0.f);
+      const float sb = b == up ? 1.f : (b == N - 1 ? -1.f : 0.f);
+      if (sa == 0.f && sb == 0.f) continue;
+      float xa = 0.f, xb = 0.f;
+#pragma unroll
+      for (int l = 0; l < N; ++l) {
+        xa = l == a ? x[l] : xa;
+        xb = l == b ? x[l] : xb;
+      }
+      // term = L xa xb u^k, u = xa - xb: 1e7 dterm = L (dP' (u + du)^k + P dU')
+      // with P = xa xb, dP' = 1e7 dP, dU' = 1e7 ((u + du)^k - u^k)
+      const float u = xa - xb, su = sa - sb, du = su * 1e-7f;
+      const float P = xa * xb;
+      const float dP = sa * xb + xa * sb + 1e-7f * sa * sb;
+      float upow = 1.f, dU = 0.f;  // (u + du)^k and its difference, term by term
+      float binom = 1.f;
+      // (u + du)^k - u^k = sum_{j >= 1} C(k, j) u^(k-j) du^j
+      // scaled: su sum_j C(k, j) u^(k-j) du^(j-1)
+      float upk[8];
+      upk[0] = 1.f;
+      for (int j = 1; j <= ord && j < 8; ++j) upk[j] = upk[j - 1] * u;
+      for (int j = 0; j < ord; ++j) upow *= u + du;
+      float dup = 1.f;  // du^(j-1)
+      for (int j = 1; j <= ord && j < 8; ++j) {
+        binom = binom * (float)(ord - j + 1) / (float)j;
+        dU += binom * upk[ord - j] * dup;
+        dup *= du;
+      }
+      const float dterm = L[e] * (dP * upow + P * su * dU);
+      if (gb.ex_meta[e][0] == 0)
+        xs += dterm;
+      else
+        xl += dterm;
+    }
+    es = xs + rt * dmix;
+    el = xl + rt * dmix;
+  }
+};
+
+template <int NC>
+__device__ __forceinline__ void ncgpu_thermo_f32(const Geo& g, const NcCoef<float>& k,
+                                                 const NcGibbs& gb, const float* __restrict__ phi,
+                                                 NcPtrs<float> cp, const float* __restrict__ temp,
+                                                 const double* __restrict__ tab,
+                                                 float* __restrict__ dG, uint64_t seed,
+                                                 uint64_t st, int x, int y, int64_t i) {
+  constexpr int N = NC + 1;
+  const int64_t plane = (int64_t)g.n[0] * g.pitch;
+  const float tf = temp[i];
+  const double t = (double)tf;
+  NcF32Thermo<N> th;
+  double last = 1.0;
+#pragma unroll
+  for (int l = 0; l < NC; ++l) {
+    th.x[l] = cp.c[l][i];
+    last -= (double)th.x[l];
+  }
+  th.x[NC] = (float)last;
+  double G[2 * N];
+  const double lnT = tab ? 0.0 : log(t);
+  if (tab) {
+#pragma unroll
+    for (int l = 0; l < 2 * N; ++l) G[l] = __ldg(tab + l * plane + i);
+  } else {
+    pure_energies<N>(gb, t, lnT, G);
+  }
+#pragma unroll
+  for (int l = 0; l < N; ++l) {
+    th.gdiff[l] = (float)(G[l] - G[N + l]);
+    th.dls[l] = (float)(G[l] - G[N - 1]);
+    th.dll[l] = (float)(G[N + l] - G[2 * N - 1]);
+  }
+  for (int e = 0; e < gb.nex; ++e)
+    th.L[e] = (float)(tab ? __ldg(tab + (2 * N + e) * plane + i) : l_excess(gb, e, t, lnT));
+  th.rt = 8.3145f * tf;
+  // G_S - G_L: the mixing term is the same in both phases and cancels
+  float dg = 0.f;
+#pragma unroll
+  for (int l = 0; l < N; ++l) dg += th.x[l] * th.gdiff[l];
+  for (int e = 0; e < gb.nex; ++e) {
+    const int a = gb.ex_meta[e][1], b = gb.ex_meta[e][2], ord = gb.ex_meta[e][3];
+    float xa = 0.f, xb = 0.f;
+#pragma unroll
+    for (int l = 0; l < N; ++l) {
+      xa = l == a ? th.x[l] : xa;
+      xb = l == b ? th.x[l] : xb;
+    }
+    float term = xa * xb * th.L[e];
+    for (int j = 0; j < ord; ++j) term *= xa - xb;
+    dg += gb.ex_meta[e][0] == 0 ? term : -term;
+  }
+  const float p = phi[i];
+  const float gg = p * p * (1.f - p) * (1.f - p);
+  const float h = p * p * p * (6.f * p * p - 15.f * p + 10.f);
+  const float namp = k.noise * sqrtf(2.f * 8.314f * tf / k.v_m);
+  dG[i] = dg;
+  const float mob = k.v_m * (k.D_L + h * (k.D_S - k.D_L)) / (8.314f * tf);
+  if (k.variant == 0) {
+    float es, el;
+    th.fd(gb, 0, es, el);
+    const float nz = k.noise > 0.f ? namp * noise_normal<float>(seed, st, y, x, 0) : 0.f;
+    const float dfc = (el + h * (es - el)) / k.v_m;
+#pragma unroll
+    for (int l = 0; l < NC; ++l) {
+      cp.Mc[l][i] = th.x[l] * mob;
+      cp.dF[l][i] = dfc + (k.W[l] - k.W[NC]) * gg * tf + nz;
+    }
+  } else {
+#pragma unroll
+    for (int l = 0; l < NC; ++l) {
+      float es, el;
+      th.fd(gb, l, es, el);
+      const float nz = k.noise > 0.f ? namp * noise_normal<float>(seed, st, y, x, l) : 0.f;
+      cp.Mc[l][i] = th.x[l] * mob;
+      cp.dF[l][i] = (el + h * (es - el)) / k.v_m + (k.W[l] - k.W[NC]) * gg * tf + nz;
+    }
+  }
+}
+
 template <typename T, int NC>
 __global__ void __launch_bounds__(256)
     ncgpu_thermo_kernel(Geo g, NcCoef<T> k, const __grid_constant__ NcGibbs gb,
@@ -159,6 +315,10 @@ __global__ void __launch_bounds__(256)
   if (x >= g.n[1]) return;
   const int64_t i = (int64_t)y * g.pitch + x;
   const uint64_t st = step + (step_base ? *step_base : 0);
+  if constexpr (std::is_same<T, float>::value) {
+    ncgpu_thermo_f32<NC>(g, k, gb, phi, cp, temp, tab, dG, seed, st, x, y, i);
+    return;
+  }
   const double t = (double)temp[i];
   double xs[N], xp[N], G[2 * N];
   double last = 1.0;
