@@ -390,10 +390,15 @@ int32_t ppf_ncgpu_step_f64(const PpfNcgpuParams* p, const PpfGrid* g, const PpfB
 
 /* The pure-element Gibbs energies of both phases and the interaction
  * parameters at every cell's temperature, for a temperature field that
- * stays fixed over many steps: tables = 2 ncomp + nexcess planes of doubles
- * in the grid's layout (rows x pitch each), plane l = G(solid, component l),
- * plane ncomp + l = G(liquid, l), plane 2 ncomp + e = L of excess[e].
- * Passed as `tables` to ppf_ncgpu_step_*, the step reads them instead of
+ * stays fixed over many steps. The caller allocates 2 ncomp + nexcess
+ * planes of doubles in the grid's layout (rows x pitch each). _f64 fills
+ * them: plane l = G(solid, component l), plane ncomp + l = G(liquid, l),
+ * plane 2 ncomp + e = L of excess[e]. _f32 fills the same memory with
+ * 3 ncomp - 2 + nexcess planes of floats (each rows x pitch floats):
+ * G(solid, l) - G(liquid, l) for l < ncomp, then G(solid, l) - G(solid,
+ * last) and G(liquid, l) - G(liquid, last) for l < ncomp - 1, then L of
+ * excess[e] (the differences formed in double). Passed as `tables` to
+ * ppf_ncgpu_step_* of the same precision, the step reads them instead of
  * evaluating the piecewise polynomials (NULL: evaluated every step, the
  * same values). Recompute them whenever the temperature changes. */
 int32_t ppf_ncgpu_tables_f32(const PpfNcgpuParams* p, const PpfGrid* g, const float* temperature,

@@ -125,7 +125,10 @@ __device__ __forceinline__ void pure_energies(const NcGibbs& gb, double t, doubl
 // (2 ncomp + nex planes of doubles in the grid's layout) for a temperature
 // field that stays fixed over many steps: the thermodynamics kernel then
 // reads them instead of evaluating the piecewise polynomials and a
-// logarithm.
+// logarithm. For float fields the same memory holds 3 ncomp - 2 + nex float
+// planes: G_solid,l - G_liquid,l (l < ncomp), then G_solid,l - G_solid,last
+// and G_liquid,l - G_liquid,last (l < ncomp - 1), then the L of each excess
+// term.
 template <typename T, int N>
 __global__ void __launch_bounds__(256)
     ncgpu_table_kernel(Geo g, const __grid_constant__ NcGibbs gb, const T* __restrict__ temp,
@@ -140,9 +143,24 @@ __global__ void __launch_bounds__(256)
   const double t = (double)temp[i], lnT = log(t);
   double v[2 * N];
   pure_energies<N>(gb, t, lnT, v);
+  if constexpr (std::is_same<T, float>::value) {
+    // the float path's layout (float planes in the same memory): the
+    // differences it uses, formed here in double once per run
+    float* ft = reinterpret_cast<float*>(tab);
 #pragma unroll
-  for (int l = 0; l < 2 * N; ++l) tab[l * plane + i] = v[l];
-  for (int e = 0; e < gb.nex; ++e) tab[(2 * N + e) * plane + i] = l_excess(gb, e, t, lnT);
+    for (int l = 0; l < N; ++l) ft[l * plane + i] = (float)(v[l] - v[N + l]);
+#pragma unroll
+    for (int l = 0; l < N - 1; ++l) {
+      ft[(N + l) * plane + i] = (float)(v[l] - v[N - 1]);
+      ft[(2 * N - 1 + l) * plane + i] = (float)(v[N + l] - v[2 * N - 1]);
+    }
+    for (int e = 0; e < gb.nex; ++e)
+      ft[(3 * N - 2 + e) * plane + i] = (float)l_excess(gb, e, t, lnT);
+  } else {
+#pragma unroll
+    for (int l = 0; l < 2 * N; ++l) tab[l * plane + i] = v[l];
+    for (int e = 0; e < gb.nex; ++e) tab[(2 * N + e) * plane + i] = l_excess(gb, e, t, lnT);
+  }
 }
 
 // 1e7 (f(x + d) - f(x)) for f(x) = x ln x (0 at x <= 0) and d = s 1e-7,
@@ -170,7 +188,7 @@ template <int N>
 struct NcF32Thermo {
   float x[N];
   float gdiff[N];        // G_solid,l - G_liquid,l
-  float dls[N], dll[N];  // G_phase,l - G_phase,N-1 (solid, liquid)
+  float dls[N - 1], dll[N - 1];  // G_phase,l - G_phase,N-1 (solid, liquid), l < N - 1
   float L[kMaxExcess];
   float rt;
 
@@ -239,22 +257,30 @@ __device__ __forceinline__ void ncgpu_thermo_f32(const Geo& g, const NcCoef<floa
     last -= (double)th.x[l];
   }
   th.x[NC] = (float)last;
-  double G[2 * N];
-  const double lnT = tab ? 0.0 : log(t);
   if (tab) {
+    // float planes written by ncgpu_table_kernel<float>
+    const float* ft = reinterpret_cast<const float*>(tab);
 #pragma unroll
-    for (int l = 0; l < 2 * N; ++l) G[l] = __ldg(tab + l * plane + i);
+    for (int l = 0; l < N; ++l) th.gdiff[l] = __ldg(ft + l * plane + i);
+#pragma unroll
+    for (int l = 0; l < N - 1; ++l) {
+      th.dls[l] = __ldg(ft + (N + l) * plane + i);
+      th.dll[l] = __ldg(ft + (2 * N - 1 + l) * plane + i);
+    }
+    for (int e = 0; e < gb.nex; ++e) th.L[e] = __ldg(ft + (3 * N - 2 + e) * plane + i);
   } else {
+    double G[2 * N];
+    const double lnT = log(t);
     pure_energies<N>(gb, t, lnT, G);
-  }
 #pragma unroll
-  for (int l = 0; l < N; ++l) {
-    th.gdiff[l] = (float)(G[l] - G[N + l]);
-    th.dls[l] = (float)(G[l] - G[N - 1]);
-    th.dll[l] = (float)(G[N + l] - G[2 * N - 1]);
+    for (int l = 0; l < N; ++l) th.gdiff[l] = (float)(G[l] - G[N + l]);
+#pragma unroll
+    for (int l = 0; l < N - 1; ++l) {
+      th.dls[l] = (float)(G[l] - G[N - 1]);
+      th.dll[l] = (float)(G[N + l] - G[2 * N - 1]);
+    }
+    for (int e = 0; e < gb.nex; ++e) th.L[e] = (float)l_excess(gb, e, t, lnT);
   }
-  for (int e = 0; e < gb.nex; ++e)
-    th.L[e] = (float)(tab ? __ldg(tab + (2 * N + e) * plane + i) : l_excess(gb, e, t, lnT));
   th.rt = 8.3145f * tf;
   // G_S - G_L: the mixing term is the same in both phases and cancels
   float dg = 0.f;
