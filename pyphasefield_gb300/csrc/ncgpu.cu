@@ -467,7 +467,13 @@ __global__ void __launch_bounds__(256)
   const int y = blockIdx.y;
   if (x >= g.n[1]) return;
   const int64_t i = (int64_t)y * g.pitch + x;
-  auto F = [&](const T* f, int dy, int dx) { return fetch<T, 2>(f, g, bc, 0, y + dy, x + dx); };
+  // a cell whose 3 x 3 neighbourhood lies inside the grid reads its
+  // neighbours directly; the others through the boundary rule
+  const bool inner = x >= 1 && x + 1 < g.n[1] && y >= 1 && y + 1 < g.n[0];
+  auto F = [&](const T* f, int dy, int dx) {
+    return inner ? __ldg(f + i + (int64_t)dy * g.pitch + dx)
+                 : fetch<T, 2>(f, g, bc, 0, y + dy, x + dx);
+  };
   const T idx = k.idx;
   const T ph = phi[i];
   const T gg = ph * ph * (T(1) - ph) * (T(1) - ph);
