@@ -68,8 +68,9 @@ __device__ __forceinline__ void band_coords(const MemberDev& m, unsigned b, int&
 // Allen-Cahn band in the warp-strip layout: phi + a lap - b (4phi^3 - 6phi^2
 // + 2phi), neighbour sum grouped ((w + e) + (n + s)) as in the single-grid
 // kernel. ac_load requests rows y0 - 1 .. y0 + ROWS of this lane's column
-// (straight from one base pointer for an interior band), ac_compute writes
-// rows y0 .. y0 + ROWS - 1.
+// (straight from one base pointer for an interior band, from the lane's
+// source column when only the x edge is crossed), ac_compute writes rows
+// y0 .. y0 + ROWS - 1.
 template <int ROWS, bool COHERENT>
 __device__ __forceinline__ void ac_load(const Geo& g, const Bc<float>& bc,
                                         const float* __restrict__ in, int xs, int y0,
@@ -80,6 +81,15 @@ __device__ __forceinline__ void ac_load(const Geo& g, const Bc<float>& bc,
     const float* p = in + (int64_t)(y0 - 1) * g.pitch + x;
 #pragma unroll
     for (int j = 0; j < ROWS + 2; ++j) v[j] = ldf<COHERENT>(p + (int64_t)j * g.pitch);
+    return;
+  }
+  if (y0 >= 1 && y0 + ROWS + 1 <= ny) {  // rows inside, strip across the x edge
+    const ColumnRule<float, 1> cr(g, bc, x);
+    const float* p = in + (int64_t)(y0 - 1) * g.pitch + cr.xi;
+#pragma unroll
+    for (int j = 0; j < ROWS + 2; ++j) v[j] = ldf<COHERENT>(p + (int64_t)j * g.pitch);
+#pragma unroll
+    for (int j = 0; j < ROWS + 2; ++j) v[j] = cr.value(0, v[j]);
     return;
   }
   const bool x_in = (unsigned)x < (unsigned)nx;

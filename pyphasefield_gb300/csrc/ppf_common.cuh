@@ -166,6 +166,46 @@ __device__ __forceinline__ T fetch(const T* __restrict__ f, const Geo& g,
   return ldf<COHERENT>(f + off) + extra;
 }
 
+// fetch's rule for a 2-D cell whose row lies inside the grid, split into a
+// per-lane part taken once per column (source column xi; for a ghost
+// column the DIRCHLET value or the shift added to the loaded value, each
+// formed with the same additions as fetch) and a per-row part (value(f,
+// loaded)). A strip that crosses the x edge then loads every row straight
+// from one column and fixes its ghost lanes afterwards, instead of a
+// divergent fetch per row. Field f of shift: 0 phi, 1 c (as fetch's fld).
+template <typename T, int NF>
+struct ColumnRule {
+  int xi;
+  bool ghost, fixed;
+  T add[NF];
+  __device__ __forceinline__ ColumnRule(const Geo& g, const Bc<T>& bc, int x) {
+    const int n = g.n[1];
+    xi = x;
+    ghost = (unsigned)x >= (unsigned)n;
+    fixed = false;
+#pragma unroll
+    for (int f = 0; f < NF; ++f) add[f] = T(0);
+    if (!ghost) return;
+    const int side = x < 0 ? 0 : 1;
+    const int t = bc.type[1];
+    if (t == PPF_BC_PERIODIC) {
+      xi = wrap_index(x, n);
+    } else if (t == PPF_BC_NEUMANN) {
+      xi = mirror_index(x, n);
+#pragma unroll
+      for (int f = 0; f < NF; ++f) add[f] = T(0) + bc.shift[f][1][side];
+    } else {
+      xi = x < 0 ? 0 : n - 1;
+      fixed = true;
+#pragma unroll
+      for (int f = 0; f < NF; ++f) add[f] = bc.shift[f][1][side] + T(0);
+    }
+  }
+  __device__ __forceinline__ T value(int f, T loaded) const {
+    return !ghost ? loaded : (fixed ? add[f] : loaded + add[f]);
+  }
+};
+
 // True when the cell lies outside the grid along a DIRCHLET axis: such a
 // ghost keeps its fixed value in every sub-step of a temporally blocked tile.
 template <typename T, int ND>

@@ -167,8 +167,10 @@ namespace w95 {
 
 // Loads of one band (rows y0 - 1 .. y0 + ROWS, this lane's column). A band
 // whose rows and 32 columns all lie inside the grid (warp-uniform test) reads
-// straight from one base pointer; otherwise only the cells outside the grid
-// take the boundary rule.
+// straight from one base pointer; one whose rows lie inside but whose strip
+// crosses the x edge reads every row from its lane's source column and fixes
+// the ghost lanes after the loads (ColumnRule); the first and last row bands
+// take the boundary rule per cell outside the grid.
 template <typename T, int ROWS, bool COHERENT = false>
 __device__ __forceinline__ void band_load(const Geo& g, const Bc<T>& bc,
                                           const T* __restrict__ phi_in,
@@ -183,6 +185,23 @@ __device__ __forceinline__ void band_load(const Geo& g, const Bc<T>& bc,
     for (int j = 0; j < ROWS + 2; ++j) {
       bp[j] = ldf<COHERENT>(p + (int64_t)j * g.pitch);
       bcv[j] = ldf<COHERENT>(c + (int64_t)j * g.pitch);
+    }
+    return;
+  }
+  if (y0 >= 1 && y0 + ROWS + 1 <= g.n[0]) {
+    const ColumnRule<T, 2> cr(g, bc, x);
+    const int64_t o = (int64_t)(y0 - 1) * g.pitch + cr.xi;
+    const T* p = phi_in + o;
+    const T* c = c_in + o;
+#pragma unroll
+    for (int j = 0; j < ROWS + 2; ++j) {
+      bp[j] = ldf<COHERENT>(p + (int64_t)j * g.pitch);
+      bcv[j] = ldf<COHERENT>(c + (int64_t)j * g.pitch);
+    }
+#pragma unroll
+    for (int j = 0; j < ROWS + 2; ++j) {
+      bp[j] = cr.value(0, bp[j]);
+      bcv[j] = cr.value(1, bcv[j]);
     }
     return;
   }
