@@ -433,6 +433,19 @@ class _Warren1995Mixin(GB300Engine):
     def _ppf_tune_candidates(self):
         return [{"tile": (0, rows)} for rows in (2, 4, 8)]
 
+    def _ppf_tiling(self, depth: int):
+        t = super()._ppf_tiling(depth)
+        if self.user_data.get("tile") is None and self._ppf_dtype == torch.float32:
+            # rows per warp when neither the user nor the autotuner chose:
+            # eight from 2^22 cells up, where each warp then keeps more loads
+            # in flight and the grid still fills several waves of CTAs
+            # (per step: 2048^2 22.5 -> 21.0 us, 3072^2 45.7 -> 36.9 us,
+            # 4096^2 77.4 -> 55.3 us, every cell on the full update 122 -> 96
+            # us), two below (1024^2: 10.9 us against 12.9 with four rows:
+            # about one wave of the larger bands)
+            t.tile_y = 8 if self._ppf_grid.cells >= 1 << 22 else 2
+        return t
+
     def _ppf_params(self):
         ud = self.user_data
         vals = dict(ud, dx=float(self.dx), dt=float(self.dt))
