@@ -462,14 +462,16 @@ int32_t ppf_ensemble_build(const PpfMember* members, int32_t n,
 int32_t ppf_ensemble_step_f32(const PpfEnsemblePlan* plan, int32_t parity,
                               uint64_t step, const uint64_t* step_base,
                               const PpfTiling* tiling, void* stream);
-/* nsteps time steps of every member. Two-row plans: one launch per step
- * (programmatic dependent launch when tiling->pdl), `sync` unused. Four- and
- * eight-row plans: ONE persistent cooperative launch: the CTAs meet at a
- * grid barrier between steps (waits bounded; a timeout sets
- * PPF_STATUS_TIMEOUT in the status word and ends the launch early). `sync`
- * is then caller device memory of 8 bytes, zeroed once before its first use
- * and used by one launch at a time; after a timeout zero it again. The
- * member buffers swap by step parity, starting from `parity`. */
+/* nsteps time steps of every member. Two-row plans, and four- and
+ * eight-row plans given no `sync` (NULL): one launch per step (programmatic
+ * dependent launch when tiling->pdl). Four- and eight-row plans given a
+ * `sync` buffer: ONE persistent cooperative launch: the CTAs meet at a grid
+ * barrier between steps (waits bounded; a timeout sets PPF_STATUS_TIMEOUT in
+ * the status word and ends the launch early). `sync` is then caller device
+ * memory of 8 bytes (8-byte aligned), zeroed once before its first use and
+ * used by one launch at a time; after a timeout zero it again. Both ways give
+ * the same results bit for bit. The member buffers swap by step parity,
+ * starting from `parity`. */
 int32_t ppf_ensemble_run_f32(const PpfEnsemblePlan* plan, int32_t parity,
                              uint64_t step, const uint64_t* step_base,
                              int32_t nsteps, void* sync, const PpfTiling* tiling,

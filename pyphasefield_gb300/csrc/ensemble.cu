@@ -226,24 +226,21 @@ __global__ void __launch_bounds__(kCtaThreads, (EnsMinBlocks<ROWS>::value))
   }
 }
 
-// One step over every unit of two-row tilings, one CTA per unit (4 BANDS
-// bands of one member; warp w takes bands w, w + 4, ...): the ensemble
-// counterpart of the single-grid float kernel (warren1995.cu). A plain launch
-// per step (no grid barrier), twelve CTAs per SM (40 registers a thread with
-// a few spilled: measured faster than ten CTAs without spills). The member's
-// record is staged in shared memory once per CTA, before waiting on the
-// previous step (the plan table is written before the first launch and never
-// by a step, so with programmatic dependent launch these loads overlap that
-// step's tail), and a band's strip and row band come from the member's
-// reciprocal of its strip count. A Warren1995 band that takes the full update
-// draws its own Philox blocks: members early in a run are mostly bulk, and a
-// bulk band draws none.
-template <int BANDS>
-__global__ void __launch_bounds__(kCtaThreads, 12)
-    ensemble_f2_kernel(const MemberDev* __restrict__ members,
-                       const int* __restrict__ unit_member, int parity, uint64_t step,
-                       const uint64_t* __restrict__ step_base) {
-  __shared__ MemberDev m;
+// One step over every unit, one CTA per unit (4 BANDS bands of one member;
+// warp w takes bands w, w + 4, ...): the ensemble counterpart of the
+// single-grid float kernels (warren1995.cu). A plain launch per step (no grid
+// barrier). The member's record is staged in shared memory once per CTA,
+// before waiting on the previous step (the plan table is written before the
+// first launch and never by a step, so with programmatic dependent launch
+// these loads overlap that step's tail), and a band's strip and row band come
+// from the member's reciprocal of its strip count. A Warren1995 band that
+// takes the full update draws its own Philox blocks: members early in a run
+// are mostly bulk, and a bulk band draws none.
+template <int ROWS, int BANDS>
+__device__ __forceinline__ void step_units(const MemberDev* __restrict__ members,
+                                           const int* __restrict__ unit_member, int parity,
+                                           uint64_t step, const uint64_t* __restrict__ step_base,
+                                           MemberDev& m) {
   const int w = threadIdx.y;
   const int tid = threadIdx.x + 32 * w;
   {
@@ -266,16 +263,39 @@ __global__ void __launch_bounds__(kCtaThreads, 12)
     int strip, rowband;
     band_coords(m, local, strip, rowband);
     const int xs = strip * w95::kStrip - 1;
-    const int y0 = rowband * 2;
+    const int y0 = rowband * ROWS;
     if (!warren) {
-      ac_band<2, false>(m.ac_a, m.ac_b, m.g, m.bc, m.phi[parity], m.phi[1 - parity], xs, y0);
+      ac_band<ROWS, false>(m.ac_a, m.ac_b, m.g, m.bc, m.phi[parity], m.phi[1 - parity], xs, y0);
       continue;
     }
-    float bp[4], bcv[4];
-    w95::band_load<float, 2>(m.g, m.bc, m.phi[parity], m.c[parity], xs, y0, bp, bcv);
-    w95::band_compute_pk<1>(m.w, m.g, m.phi[1 - parity], m.c[1 - parity], m.seed, step, xs, y0,
-                            bp, bcv);
+    float bp[ROWS + 2], bcv[ROWS + 2];
+    w95::band_load<float, ROWS>(m.g, m.bc, m.phi[parity], m.c[parity], xs, y0, bp, bcv);
+    w95::band_compute_pk<ROWS / 2>(m.w, m.g, m.phi[1 - parity], m.c[1 - parity], m.seed, step,
+                                   xs, y0, bp, bcv);
   }
+}
+
+// Two-row bands: twelve CTAs per SM (40 registers a thread with a few
+// spilled: measured faster than ten CTAs without spills).
+template <int BANDS>
+__global__ void __launch_bounds__(kCtaThreads, 12)
+    ensemble_f2_kernel(const MemberDev* __restrict__ members,
+                       const int* __restrict__ unit_member, int parity, uint64_t step,
+                       const uint64_t* __restrict__ step_base) {
+  __shared__ MemberDev m;
+  step_units<2, BANDS>(members, unit_member, parity, step, step_base, m);
+}
+
+// Four- and eight-row bands stepped the same way (plans of those heights run
+// without a grid-barrier buffer): eight CTAs per SM at four rows (64
+// registers), six at eight rows (80).
+template <int ROWS, int BANDS>
+__global__ void __launch_bounds__(kCtaThreads, ROWS == 4 ? 8 : 6)
+    ensemble_tall_kernel(const MemberDev* __restrict__ members,
+                         const int* __restrict__ unit_member, int parity, uint64_t step,
+                         const uint64_t* __restrict__ step_base) {
+  __shared__ MemberDev m;
+  step_units<ROWS, BANDS>(members, unit_member, parity, step, step_base, m);
 }
 
 int32_t build_table(const PpfMember* members, int32_t n, const PpfTiling* tiling,
@@ -402,18 +422,19 @@ cudaError_t launch_ensemble(const PpfEnsemblePlan* p, int parity, uint64_t step,
                             step_base, nsteps, sync, status);
 }
 
-// nsteps launches of ensemble_f2_kernel, each over every unit.
-template <int BANDS>
-cudaError_t launch_f2_steps(const PpfEnsemblePlan* p, int parity, uint64_t step,
-                            const uint64_t* step_base, int nsteps, bool pdl, cudaStream_t s) {
+// nsteps launches of a per-step kernel (ensemble_f2_kernel or
+// ensemble_tall_kernel), each over every unit.
+template <typename Kernel>
+cudaError_t launch_plain_steps(Kernel kern, const PpfEnsemblePlan* p, int parity, uint64_t step,
+                               const uint64_t* step_base, int nsteps, bool pdl, cudaStream_t s) {
   if (p->n_units > 0x7fffffffLL) return cudaErrorInvalidConfiguration;
   const char* base = reinterpret_cast<const char*>(p->device_table);
   const MemberDev* members = reinterpret_cast<const MemberDev*>(base);
   const int* units = reinterpret_cast<const int*>(base + units_offset(p->n_members));
   for (int i = 0; i < nsteps; ++i) {
     const cudaError_t e =
-        launch(ensemble_f2_kernel<BANDS>, dim3((unsigned)p->n_units), dim3(32, kWarpsPerCta), 0, s, pdl,
-               members, units, (parity + i) & 1, step + (uint64_t)i, step_base);
+        launch(kern, dim3((unsigned)p->n_units), dim3(32, kWarpsPerCta), 0, s, pdl, members,
+               units, (parity + i) & 1, step + (uint64_t)i, step_base);
     if (e != cudaSuccess) return e;
   }
   return cudaSuccess;
@@ -426,8 +447,8 @@ int32_t run(const PpfEnsemblePlan* plan, int32_t parity, uint64_t step,
   if (parity != 0 && parity != 1) return fail(PPF_ERR_INVALID, "parity must be 0 or 1");
   if (plan->n_items < 1 || plan->n_units < 1) return fail(PPF_ERR_INVALID, "empty plan");
   if (nsteps < 1) return fail(PPF_ERR_INVALID, "nsteps must be >= 1");
-  if (plan->rows != 2 && nsteps > 1 && (!sync || ((uintptr_t)sync) % 8))
-    return fail(PPF_ERR_INVALID, "several steps per launch need an 8-byte aligned sync buffer");
+  if (plan->rows != 2 && sync && ((uintptr_t)sync) % 8)
+    return fail(PPF_ERR_INVALID, "the grid-barrier sync buffer must be 8-byte aligned");
   int* status = status_ptr();
   if (!status) return fail(PPF_ERR_CUDA, "status word unavailable");
   const bool pdl = tiling && tiling->pdl;
@@ -435,19 +456,27 @@ int32_t run(const PpfEnsemblePlan* plan, int32_t parity, uint64_t step,
   unsigned* sy = (unsigned*)sync;
   cudaError_t e;
 #define PPF_ENS(R, B) launch_ensemble<R, B>(plan, parity, step, step_base, nsteps, sy, status, pdl, s)
-  const int key = plan->rows * 100 + plan->bands;
+#define PPF_PLAIN(K) launch_plain_steps(K, plan, parity, step, step_base, nsteps, pdl, s)
+  // four- and eight-row plans: the persistent kernel when given a barrier
+  // buffer, per-step launches without one
+  const int key = plan->rows * 100 + plan->bands + (plan->rows != 2 && sy ? 10000 : 0);
   switch (key) {
-    case 201: e = launch_f2_steps<1>(plan, parity, step, step_base, nsteps, pdl, s); break;
-    case 204: e = launch_f2_steps<4>(plan, parity, step, step_base, nsteps, pdl, s); break;
-    case 208: e = launch_f2_steps<8>(plan, parity, step, step_base, nsteps, pdl, s); break;
-    case 216: e = launch_f2_steps<16>(plan, parity, step, step_base, nsteps, pdl, s); break;
-    case 401: e = PPF_ENS(4, 1); break;
-    case 404: e = PPF_ENS(4, 4); break;
-    case 801: e = PPF_ENS(8, 1); break;
-    case 804: e = PPF_ENS(8, 4); break;
+    case 201: e = PPF_PLAIN(ensemble_f2_kernel<1>); break;
+    case 204: e = PPF_PLAIN(ensemble_f2_kernel<4>); break;
+    case 208: e = PPF_PLAIN(ensemble_f2_kernel<8>); break;
+    case 216: e = PPF_PLAIN(ensemble_f2_kernel<16>); break;
+    case 401: e = PPF_PLAIN((ensemble_tall_kernel<4, 1>)); break;
+    case 404: e = PPF_PLAIN((ensemble_tall_kernel<4, 4>)); break;
+    case 801: e = PPF_PLAIN((ensemble_tall_kernel<8, 1>)); break;
+    case 804: e = PPF_PLAIN((ensemble_tall_kernel<8, 4>)); break;
+    case 10401: e = PPF_ENS(4, 1); break;
+    case 10404: e = PPF_ENS(4, 4); break;
+    case 10801: e = PPF_ENS(8, 1); break;
+    case 10804: e = PPF_ENS(8, 4); break;
     default: return fail(PPF_ERR_INVALID, "plan rows %d / bands %d invalid", plan->rows,
                          plan->bands);
   }
+#undef PPF_PLAIN
 #undef PPF_ENS
   if (e != cudaSuccess) return fail(PPF_ERR_CUDA, "ensemble launch: %s", cudaGetErrorString(e));
   return PPF_OK;

@@ -4,11 +4,11 @@ The reference runs one Simulation at a time; an ensemble here is a list of
 ordinary engine instances (each with its own fields, parameters and grid
 size) whose device buffers are stepped together, a chunk of `graph_chunk`
 steps per `ppf_ensemble_run_f32` call captured in a CUDA graph: one launch
-per step over every member for two-row bands, or one persistent cooperative
-launch per chunk for four- and eight-row bands (the CTAs meet at a bounded
-grid barrier between steps). The rows per warp band and the bands per warp
-are picked by the autotuner for the ensemble's mix of member sizes (cached
-per mix and device). Afterwards each member is an ordinary
+per step over every member, or for four- and eight-row bands one persistent
+cooperative launch per chunk (the CTAs meet at a bounded grid barrier
+between steps). The rows per warp band, the bands per warp and the launch
+kind are picked by the autotuner for the ensemble's mix of member sizes
+(cached per mix and device). Afterwards each member is an ordinary
 engine again: retrieve_fields_from_GPU, save_simulation etc. work on it.
 
 `make_config_ensemble` builds the benchmark ensemble: n members whose square
@@ -102,10 +102,14 @@ def partition_members(cells, world: int) -> list:
 class Ensemble:
     """Steps a list of 2-D float32 Warren1995GB300 / CahnAllenGB300 engines
     together. All members must be at the same time step. rows=None picks the
-    rows per warp band and the bands per warp with the autotuner."""
+    rows per warp band, the bands per warp and, for four- or eight-row bands,
+    persistent or per-step launches with the autotuner. persistent (four- and
+    eight-row bands only): each graph chunk of steps is one cooperative launch
+    with a grid barrier between steps (default), else one launch per step."""
 
     def __init__(self, sims, rows: int | None = None, graph_chunk: int = 64, pdl: bool = True,
-                 bulk_shortcut: bool = True, use_graph: bool = True, bands: int | None = None):
+                 bulk_shortcut: bool = True, use_graph: bool = True, bands: int | None = None,
+                 persistent: bool = True):
         if not sims:
             raise ValueError("empty ensemble")
         self.sims = list(sims)
@@ -139,12 +143,13 @@ class Ensemble:
             self.status = torch.zeros(1, dtype=torch.int32, device=dev)
         self.status_host = torch.zeros(1, dtype=torch.int32, pin_memory=True)
         self.graphs = {}
+        self.persistent = bool(persistent)
         if rows and bands:
             self.rows, self.bands = int(rows), int(bands)
         elif rows:
             self.rows, self.bands = int(rows), 4
         else:
-            self.rows, self.bands = self._tune_tiling()
+            self.rows, self.bands, self.persistent = self._tune_tiling()
         self.tiling = tiling_struct(1, (self.bands, self.rows), pdl, self._flags)
         self._build()
 
@@ -181,10 +186,10 @@ class Ensemble:
         from . import autotune
         return autotune.make_key("Ensemble", (len(mix), self.cells), torch.float32, digest)
 
-    def _tune_tiling(self) -> tuple[int, int]:
-        """Rows per warp band and bands per warp: each candidate times a chunk
-        of steps on scratch copies of every member's buffers (the members are
-        untouched)."""
+    def _tune_tiling(self) -> tuple[int, int, bool]:
+        """Rows per warp band, bands per warp and persistent launches: each
+        candidate times a chunk of steps on scratch copies of every member's
+        buffers (the members are untouched)."""
         from . import autotune
         with torch.cuda.stream(self.stream):
             for s in self.sims:
@@ -206,16 +211,20 @@ class Ensemble:
             L.call("ppf_ensemble_build", members, n, C.byref(tiling), ptr(table),
                    C.c_size_t(table.numel()), C.byref(plan), sp)
 
+            barrier = ptr(sync) if cand["persistent"] else None
+
             def run():
                 L.call("ppf_ensemble_run_f32", C.byref(plan), 0, C.c_uint64(0), None, steps,
-                       ptr(sync), C.byref(tiling), sp)
+                       barrier, C.byref(tiling), sp)
 
             return autotune.time_candidate(run, self.stream, warmup=1, reps=3) / steps
 
-        cands = [{"rows": r, "bands": b} for r in (2, 4, 8) for b in (1, 4)]
+        cands = [{"rows": 2, "bands": b, "persistent": False} for b in (1, 4)] + \
+            [{"rows": r, "bands": b, "persistent": p} for r in (4, 8) for b in (1, 4)
+             for p in (False, True)]
         best = autotune.pick(self._mix_key(), cands, measure)
         del scratch
-        return int(best["rows"]), int(best["bands"])
+        return int(best["rows"]), int(best["bands"]), bool(best["persistent"])
 
     def _members_key(self) -> bytes:
         """Every member's parameter struct as bytes: the plan (and so every
@@ -243,8 +252,9 @@ class Ensemble:
             L.call("ppf_ensemble_step_f32", C.byref(self.plan), int(parity), C.c_uint64(step),
                    ptr(base), C.byref(self.tiling), sp)
         else:
+            barrier = ptr(self.sync) if self.persistent and self.rows != 2 else None
             L.call("ppf_ensemble_run_f32", C.byref(self.plan), int(parity), C.c_uint64(step),
-                   ptr(base), int(nsteps), ptr(self.sync), C.byref(self.tiling), sp)
+                   ptr(base), int(nsteps), barrier, C.byref(self.tiling), sp)
 
     def _watch(self):
         """Status bits of the chunk (a grid-barrier wait that gave up) moved

@@ -1,6 +1,6 @@
-"""The batched ensemble (many engines stepped together: one launch per step
-for two-row bands, one persistent cooperative launch per chunk of steps for
-four- and eight-row bands) and the autotuner, on the GPU. Ensemble members must match the same engines
+"""The batched ensemble (many engines stepped together: one launch per step,
+or for four- and eight-row bands one persistent cooperative launch per chunk
+of steps) and the autotuner, on the GPU. Ensemble members must match the same engines
 stepped one by one (fp32: within 1e-6 relative L2; the ensemble's Allen-Cahn
 band is a different kernel from the single-grid one, so rounding may differ)
 and the FP64 oracle (1e-5)."""
@@ -22,14 +22,16 @@ def _snapshot(sims):
     return [[f.get_cells().copy() for f in s.fields] for s in sims]
 
 
-@pytest.mark.parametrize("rows,bands", [(2, 4), (4, 1), (8, 4), (2, 1), (2, 8), (2, 16)])
-def test_ensemble_matches_members_stepped_alone(cuda, rows, bands):
+@pytest.mark.parametrize("rows,bands,persistent", [
+    (2, 4, False), (4, 1, True), (8, 4, True), (2, 1, False), (2, 8, False), (2, 16, False),
+    (4, 4, False), (8, 1, False), (8, 4, False)])
+def test_ensemble_matches_members_stepped_alone(cuda, rows, bands, persistent):
     from pyphasefield_gb300.ensemble import Ensemble
     a = _members()
     b = _members()
     for s in b:
         s.user_data["tile"] = (0, rows)
-    ens = Ensemble(a, rows=rows, bands=bands, graph_chunk=8)
+    ens = Ensemble(a, rows=rows, bands=bands, graph_chunk=8, persistent=persistent)
     ens.simulate(40)
     ens.retrieve_fields_from_GPU()
     for s in b:
@@ -118,6 +120,25 @@ def test_persistent_chunks_equal_single_steps(cuda):
             np.testing.assert_array_equal(fa.get_cells(), fb.get_cells())
 
 
+@pytest.mark.parametrize("rows,bands", [(4, 4), (8, 1)])
+def test_persistent_equals_per_step_launches(cuda, rows, bands):
+    """Four- and eight-row plans: the persistent cooperative launch (grid
+    barrier between steps) and one launch per step give the same fields bit
+    for bit, graph-launched chunks included."""
+    from pyphasefield_gb300.ensemble import Ensemble, make_config_ensemble
+    runs = []
+    for persistent in (True, False):
+        sims = make_config_ensemble(n=8, seed=4, side_range=(100, 400))
+        ens = Ensemble(sims, rows=rows, bands=bands, graph_chunk=6, persistent=persistent)
+        ens.simulate(7, use_graph=False)
+        ens.simulate(12)
+        ens.retrieve_fields_from_GPU()
+        runs.append(_snapshot(sims))
+    for ma, mb in zip(*runs):
+        for fa, fb in zip(ma, mb):
+            np.testing.assert_array_equal(fa, fb)
+
+
 def test_ensemble_follows_parameter_edits(cuda):
     """A member's T changed between simulate() calls: the graph-launched
     ensemble equals eager launches bit for bit (no stale plan)."""
@@ -144,10 +165,11 @@ def test_ensemble_rows_autotuned_and_cached(cuda, tmp_path, monkeypatch):
     init = _snapshot(sims)
     ens = Ensemble(sims, graph_chunk=4)
     assert ens.rows in (2, 4, 8) and ens.bands in (1, 4)
+    assert ens.persistent in (True, False) and (ens.rows != 2 or not ens.persistent)
     cache = json.loads((tmp_path / "tune.json").read_text())
     entry = next(iter(cache.values()))
-    assert entry["config"] == {"rows": ens.rows, "bands": ens.bands}
-    assert len(entry["tried"]) == 6
+    assert entry["config"] == {"rows": ens.rows, "bands": ens.bands, "persistent": ens.persistent}
+    assert len(entry["tried"]) == 10
     # tuning ran on scratch copies: the members still hold their initial
     # (float32-rounded) state
     ens.retrieve_fields_from_GPU()
@@ -156,4 +178,4 @@ def test_ensemble_rows_autotuned_and_cached(cuda, tmp_path, monkeypatch):
             np.testing.assert_array_equal(f0.astype(np.float32), f.get_cells())
     # a second ensemble of the same mix takes the cached choice
     again = Ensemble(_members(5), graph_chunk=4)
-    assert (again.rows, again.bands) == (ens.rows, ens.bands)
+    assert (again.rows, again.bands, again.persistent) == (ens.rows, ens.bands, ens.persistent)
