@@ -765,6 +765,10 @@ def profile_case(name: str):
     diff3d384   Diffusion 3-D 384^3 periodic, 5 steps
     ensemble64  the 64-member ensemble benchmark (1.56e7 cells), two rows and four bands per
                 warp: 40 steps, one launch each
+    ensemble64_tall  the same with four rows and four bands per warp, per-step launches (the
+                autotuner's choice for this mix): 40 steps
+    warren4096  Warren1995 4096^2 from the sweep's seeded state, 5 steps (the engines' default
+                of eight rows per warp at this size)
     tb4096      Diffusion 2-D 4096^2, depth 4 on 128 x 32 shared-memory tiles, 20 steps
     reduce4096  five FP64 sums of a 4096^2 float field (ppf_reduce_sum_f32)
     acfull2048  implicit Allen-Cahn, full 2-D system on 2048^2 (Chebyshev), fp64, 2 steps
@@ -805,13 +809,17 @@ def profile_case(name: str):
         sim.initialize_fields_and_imported_data()
         sim.fields[0].data[1:-1, 1:-1] = 0.5 + 0.01 * rng.standard_normal((4096, 4096))
         sim.simulate(5 * depth)
-    elif name == "ensemble64":
+    elif name in ("ensemble64", "ensemble64_tall"):
         from pyphasefield_gb300.ensemble import Ensemble, make_config_ensemble
-        ens = Ensemble(make_config_ensemble(n=64, seed=0), rows=2, bands=4, graph_chunk=8,
-                       use_graph=False)
+        rows = 2 if name == "ensemble64" else 4
+        ens = Ensemble(make_config_ensemble(n=64, seed=0), rows=rows, bands=4, graph_chunk=8,
+                       use_graph=False, persistent=False)
         ens.simulate(40)
         ens.synchronize()
         return
+    elif name == "warren4096":
+        sim = sweep_engine("warren1995", (4096, 4096), 1, 5, rng, {"use_graph": False})
+        sim.simulate(5)
     elif name == "tb4096":
         sim = DiffusionGB300(dimensions=[4096, 4096], dx=1.0, dt=0.2,
                              boundary_conditions="PERIODIC",
