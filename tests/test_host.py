@@ -93,6 +93,27 @@ def test_make_engines_builds_every_engine_on_a_given_base():
         assert issubclass(cls, Host)
 
 
+def test_warren_rows_per_warp_default():
+    """Float Warren1995 engines take eight rows per warp band from 2^22 cells
+    up and two below; an explicit tile (the user's or the autotuner's) and
+    float64 keep the library default or the given rows."""
+    from types import SimpleNamespace
+
+    from pyphasefield_gb300 import Warren1995GB300
+
+    def rows(cells, **ud):
+        sim = Warren1995GB300(dimensions=[8, 8], dx=4.6e-8, user_data=ud)
+        sim._ppf_grid = SimpleNamespace(cells=cells)
+        return sim._ppf_tiling(1).tile_y
+
+    assert rows(1024 * 1024) == 2
+    assert rows((1 << 22) - 1) == 2
+    assert rows(2048 * 2048) == 8
+    assert rows(4096 * 4096) == 8
+    assert rows(4096 * 4096, tile=(0, 4)) == 4
+    assert rows(4096 * 4096, precision="fp64") == 0
+
+
 def test_boundary_struct_from_simulation():
     from pyphasefield_gb300 import DiffusionGB300
     from pyphasefield_gb300.device import DeviceGrid, boundary_struct
