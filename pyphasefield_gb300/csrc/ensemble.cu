@@ -9,9 +9,11 @@
 // shared memory for its four warps.
 //
 // Two-row tilings: ensemble_f2_kernel, one plain launch per step over every
-// unit (the single-grid float kernel's band code and register budget).
-// Four- and eight-row tilings: ensemble_kernel, one cooperative, persistent
-// launch per chunk of steps: each CTA walks the units grid-stride, then all
+// unit (the single-grid float kernel's band code and register budget); four-
+// and eight-row tilings run without a grid-barrier buffer the same way
+// (ensemble_tall_kernel). Four- and eight-row tilings given one:
+// ensemble_kernel, one cooperative, persistent launch per chunk of steps
+// (same results bit for bit): each CTA walks the units grid-stride, then all
 // CTAs meet at a grid barrier before the next step (each member's ping-pong
 // buffers swap by step parity). The barrier's waits are bounded: a CTA that
 // waits too long sets PPF_STATUS_TIMEOUT and the launch ends early. Reads of
