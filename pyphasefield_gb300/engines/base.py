@@ -19,7 +19,10 @@ retrieve_fields_from_GPU / apply_boundary_conditions, ppf_gpu_utils.py:
 
 User-data keys added to the reference's: precision ("fp32" | "fp64"),
 temporal_depth (steps per HBM pass, 2-D Diffusion/Allen-Cahn), tile
-((tile_x, tile_y) or None), pdl (bool), use_graph (bool), graph_chunk (int),
+((tile_x, tile_y) or None; Warren1995: (0, rows per warp band), chosen by
+grid size when None), zchunk (planes per CTA, 3-D), autotune (bool: time the
+launch shapes on scratch copies and cache the fastest), bulk_shortcut
+(bool, Warren1995), pdl (bool), use_graph (bool), graph_chunk (int),
 check_status (bool, default True).
 
 Failure detection: after every chunk of steps (inside the captured graph)
