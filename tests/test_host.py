@@ -194,6 +194,28 @@ def test_library_rejects_bad_arguments_without_gpu(built_lib):
         L.call("ppf_diffusion_step_f32", None, C.byref(g), C.byref(b), None, None, None, None)
 
 
+def test_ensemble_run_validates_without_gpu(built_lib):
+    """ppf_ensemble_run_f32 checks its arguments on the host before any
+    launch: a NULL plan, a parity other than 0/1, no steps, and (four- and
+    eight-row plans) a grid-barrier buffer that is not 8-byte aligned."""
+    from pyphasefield_gb300 import _lib as L
+    lib = L.load()
+    plan = L.PpfEnsemblePlan()
+    plan.device_table = 0x1000  # never dereferenced by the host checks
+    plan.n_items, plan.n_members, plan.rows, plan.n_units, plan.bands = 4, 1, 4, 1, 1
+    t = L.PpfTiling()
+
+    def run(pl, parity=0, nsteps=2, sync=None):
+        return lib.ppf_ensemble_run_f32(pl, parity, C.c_uint64(0), None, nsteps,
+                                        C.c_void_p(sync) if sync else None, C.byref(t), None)
+
+    assert run(None) == L.PPF_ERR_INVALID
+    assert run(C.byref(plan), parity=2) == L.PPF_ERR_INVALID
+    assert run(C.byref(plan), nsteps=0) == L.PPF_ERR_INVALID
+    assert run(C.byref(plan), sync=0x2004) == L.PPF_ERR_INVALID
+    assert "aligned" in L.last_error()
+
+
 def test_ncgpu_entry_points_validate_without_gpu(built_lib):
     """NCGPU parameter checks run on the host before any launch: component
     count, interaction-term count and indices, NULL buffers."""
